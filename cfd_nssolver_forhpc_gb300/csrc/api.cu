@@ -1,0 +1,1180 @@
+// api.cu -- the C ABI of include/cfdgpu.h: context, device memory, metric
+// tables, and the host orchestration of the time step and of the iterative
+// solvers (BiCGSTAB with device-resident scalars replayed from a CUDA graph,
+// red-black SOR, mixed-precision defect correction).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/cfdgpu.h"
+#include "kernels.h"
+
+using namespace cfd;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(...)                                                                            \
+    do {                                                                                   \
+        cudaError_t e_ = (__VA_ARGS__);                                                    \
+        if (e_ != cudaSuccess)                                                             \
+            return fail(CFD_ERR_CUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define CKS(...)                        \
+    do {                                \
+        int st_ = (__VA_ARGS__);        \
+        if (st_ != CFD_OK) return st_;  \
+    } while (0)
+
+template <class T>
+struct Tag {
+    using type = T;
+};
+
+}  // namespace
+
+struct cfd_ctx {
+    cfd_config cfg{};
+    Geo g{};
+    bool fp32 = false;
+    cudaStream_t s = nullptr;
+    cfd_launch_ctx lc{};
+    std::vector<void *> allocs;
+
+    // state (velocity type T = double or float)
+    void *vel[3][3] = {};  // [slot 0/1/2 = T0/T1/T3][component]
+    void *eta = nullptr, *f = nullptr, *src = nullptr;
+    double *p = nullptr, *x = nullptr, *b = nullptr, *jp = nullptr;
+    double *staging = nullptr;  // FP64 staging for conversions (mixed precision)
+
+    // metrics: raw arrays (X,Y,Z,Dx,Dy,Dz,Dxs,Dys,Dzs) and per-axis tables
+    double *raw = nullptr;
+    double *rawp[9] = {};
+    double *tab64[3] = {};
+    float *tab32[3] = {};
+    bool metrics = false;
+    std::vector<double> hraw[9];
+
+    // Poisson operators
+    double *spe_c[3] = {};
+    float *spe_c32[3] = {};
+    float *jp32 = nullptr;
+    int *ell_cols = nullptr;
+    double *ell_vals = nullptr;
+    float *ell_vals32 = nullptr;
+
+    // BiCGSTAB work
+    BicgVecs<double> w64{};
+    BicgVecs<float> w32{};
+    double *px1 = nullptr, *px2 = nullptr;
+    float *r32 = nullptr, *e32 = nullptr;
+    BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [0] FP64 outer, [1] FP32 inner
+    int graph_batch[2] = {0, 0};
+
+    // SOR
+    double *cf6 = nullptr, *cf7 = nullptr;
+    unsigned long long *sor_res = nullptr;
+    int *sor_state = nullptr, *h_sor_state = nullptr;
+
+    // scalars: [0] rhs mean, [1..2] cd/cl, [3] residual norm^2, [4] dot
+    double *dscal = nullptr, *h_scal = nullptr;
+    unsigned long long *dmax = nullptr, *h_max = nullptr;
+
+    long long loop = 1;
+    double time = 0.0;
+    bool use_graphs = true;
+};
+
+namespace {
+
+template <class T>
+T *dv(cfd_ctx *c, int slot, int comp)
+{
+    return static_cast<T *>(c->vel[slot][comp]);
+}
+
+int slot_index(int slot)
+{
+    return slot == CFD_SLOT_T0 ? 0 : slot == CFD_SLOT_T1 ? 1 : slot == CFD_SLOT_T3 ? 2 : -1;
+}
+
+int dalloc(cfd_ctx *c, void **p, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(CFD_ERR_NOMEM, std::string("cudaMalloc(") + std::to_string(bytes) +
+                                       "): " + cudaGetErrorString(e));
+    }
+    c->allocs.push_back(*p);
+    return CFD_OK;
+}
+
+template <class P>
+int dalloc_t(cfd_ctx *c, P **p, size_t count)
+{
+    return dalloc(c, reinterpret_cast<void **>(p), count * sizeof(P));
+}
+
+template <class Fn>
+auto dispatch(cfd_ctx *c, Fn &&fn)
+{
+    if (c->fp32) return fn(Tag<float>{});
+    return fn(Tag<double>{});
+}
+
+template <class T>
+Metrics<T> metrics_of(cfd_ctx *c);
+template <>
+Metrics<double> metrics_of<double>(cfd_ctx *c)
+{
+    return {{c->tab64[0], c->g.nx}, {c->tab64[1], c->g.ny}, {c->tab64[2], c->g.nz}};
+}
+template <>
+Metrics<float> metrics_of<float>(cfd_ctx *c)
+{
+    return {{c->tab32[0], c->g.nx}, {c->tab32[1], c->g.ny}, {c->tab32[2], c->g.nz}};
+}
+
+SpeOp<double> spe64(cfd_ctx *c)
+{
+    const Geo &g = c->g;
+    return {c->spe_c[0], c->spe_c[0] + g.nxc, c->spe_c[1], c->spe_c[1] + g.nyc, c->spe_c[2],
+            c->spe_c[2] + g.nzc, c->jp, g.nxc, g.nyc, g.nzc, g.sxc, g.n};
+}
+SpeOp<float> spe32(cfd_ctx *c)
+{
+    const Geo &g = c->g;
+    return {c->spe_c32[0], c->spe_c32[0] + g.nxc, c->spe_c32[1], c->spe_c32[1] + g.nyc, c->spe_c32[2],
+            c->spe_c32[2] + g.nzc, c->jp32, g.nxc, g.nyc, g.nzc, g.sxc, g.n};
+}
+EllOp<double> ell64(cfd_ctx *c) { return {c->ell_cols, c->ell_vals, c->g.n}; }
+EllOp<float> ell32(cfd_ctx *c) { return {c->ell_cols, c->ell_vals32, c->g.n}; }
+
+// Per-axis tables (row-major [AX_ROWS][n]) from the cell and staggered
+// widths, with the reference's evaluation order for every factor.
+std::vector<double> axis_table(const std::vector<double> &D, const std::vector<double> &Ds)
+{
+    const int n = (int)D.size();
+    std::vector<double> t((size_t)AX_ROWS * n, 0.0);
+    auto T = [&](int r, int i) -> double & { return t[(size_t)r * n + i]; };
+    for (int i = 0; i < n; ++i) {
+        T(AX_D, i) = D[i];
+        T(AX_DS, i) = Ds[i];
+        T(AX_RD, i) = 1.0 / D[i];
+        T(AX_RDS, i) = 1.0 / Ds[i];
+        T(AX_IT, i) = (Ds[i] * 0.5) / D[i];
+        if (i + 1 < n) {
+            T(AX_CAPP, i) = 0.125 * D[i + 1] * D[i + 1] / Ds[i];
+            T(AX_CAPN, i) = 0.125 * D[i + 1] * D[i + 1] / Ds[i + 1];
+            T(AX_CBPN, i) = 0.125 * Ds[i] * Ds[i] / D[i + 1];
+            T(AX_PP, i) = 1.0 / D[i] / Ds[i];
+        }
+        if (i >= 1) {
+            T(AX_CANP, i) = 0.125 * D[i] * D[i] / Ds[i - 1];
+            T(AX_CBNP, i) = 0.125 * Ds[i - 1] * Ds[i - 1] / D[i - 1];
+            T(AX_CBNN, i) = 0.125 * Ds[i - 1] * Ds[i - 1] / D[i];
+            T(AX_PM, i) = 1.0 / D[i] / Ds[i - 1];
+        }
+        T(AX_CANN, i) = 0.125 * D[i] * D[i] / Ds[i];
+        T(AX_CBPP, i) = 0.125 * Ds[i] * Ds[i] / D[i];
+    }
+    return t;
+}
+
+int check_ctx(cfd_ctx *c)
+{
+    if (!c) return fail(CFD_ERR_ARG, "null context");
+    return CFD_OK;
+}
+
+int need_metrics(cfd_ctx *c)
+{
+    CKS(check_ctx(c));
+    if (!c->metrics) return fail(CFD_ERR_STATE, "grid metrics not set (cfd_grid_uniform / cfd_set_metrics)");
+    return CFD_OK;
+}
+
+int check_slot(int slot)
+{
+    if (slot_index(slot) < 0) return fail(CFD_ERR_ARG, "velocity slot must be 0 (T0), 1 (T1) or 3 (T3)");
+    return CFD_OK;
+}
+
+size_t field_count(const cfd_ctx *c, int field)
+{
+    if (field >= CFD_FIELD_U0 && field <= CFD_FIELD_ETA) return (size_t)c->g.ng;
+    if (field == CFD_FIELD_F || field == CFD_FIELD_SRC) return (size_t)(3 * c->g.n);
+    if (field >= CFD_FIELD_X && field <= CFD_FIELD_JP) return (size_t)c->g.n;
+    return 0;
+}
+
+// device pointer and whether it holds velocity-type (T) data
+void *field_ptr(cfd_ctx *c, int field, bool &is_t)
+{
+    is_t = false;
+    if (field <= CFD_FIELD_W3) {
+        is_t = true;
+        return c->vel[field / 3][field % 3];
+    }
+    switch (field) {
+    case CFD_FIELD_P: return c->p;
+    case CFD_FIELD_ETA: is_t = true; return c->eta;
+    case CFD_FIELD_F: is_t = true; return c->f;
+    case CFD_FIELD_SRC: is_t = true; return c->src;
+    case CFD_FIELD_X: return c->x;
+    case CFD_FIELD_B: return c->b;
+    case CFD_FIELD_JP: return c->jp;
+    default: return nullptr;
+    }
+}
+
+// ---- solvers ----------------------------------------------------------------
+
+template <class Op, class V>
+int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V *px1, V *px2,
+             BicgScal *sc, int which_graph)
+{
+    launch_bicg_init<Op, V>(c->lc, A, b, x, w, px1, px2, sc);
+    CK(cudaGetLastError());
+    const int batch = c->cfg.check_every;
+    cudaGraphExec_t &ge = c->graph[which_graph];
+    if (c->use_graphs && (!ge || c->graph_batch[which_graph] != batch)) {
+        if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+        cudaGraph_t gr = nullptr;
+        CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc);
+        cudaError_t e = cudaStreamEndCapture(c->s, &gr);
+        if (e != cudaSuccess) return fail(CFD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ge, gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) { ge = nullptr; return fail(CFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+        c->graph_batch[which_graph] = batch;
+    }
+    const long long cap_batches = (long long)c->cfg.p_iter_max / batch + 3;
+    for (long long nb = 0;; ++nb) {
+        if (c->use_graphs) {
+            CK(cudaGraphLaunch(ge, c->s));
+        } else {
+            for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc);
+            CK(cudaGetLastError());
+        }
+        CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
+        CK(cudaStreamSynchronize(c->s));
+        if (c->h_sc->done != BICG_RUNNING) break;
+        if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "BiCGSTAB did not report completion");
+    }
+    return CFD_OK;
+}
+
+// The graphs bake in the buffers and operator of the context; they are
+// captured for the configured operator only.
+template <class Op>
+int solve64(cfd_ctx *c, const Op &A, int *iters, double *relres)
+{
+    CKS(bicg_run<Op, double>(c, A, c->b, c->x, c->w64, c->px1, c->px2, c->sc, 0));
+    int st = CFD_OK;
+    if (c->h_sc->done == BICG_CAPPED) {
+        launch_bicg_nan_reset<double>(c->lc, c->g.n, c->x, c->px1, c->px2, c->sc);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(c->h_sc, c->sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
+        CK(cudaStreamSynchronize(c->s));
+        st = fail(CFD_ERR_NOCONV, "BiCGSTAB reached its iteration cap");
+    }
+    if (iters) *iters = c->h_sc->iter;
+    if (relres) *relres = c->h_sc->relres;
+    return st;
+}
+
+void residual64(cfd_ctx *c, const SpeOp<double> &A, const double *b, const double *x, float *r32, double *out)
+{
+    launch_residual64<float>(c->lc, A, b, x, r32, out);
+}
+void residual64(cfd_ctx *c, const EllOp<double> &A, const double *b, const double *x, float *r32, double *out)
+{
+    launch_residual64_ell<float>(c->lc, A, b, x, r32, out);
+}
+
+// Mixed precision: FP64 defect correction around FP32 BiCGSTAB solves.
+//   r = b - A x (FP64, written as FP32);  stop when |r|/|b| < tol
+//   solve A e = r in FP32 to inner_tol (e from 0);  x += e (FP64)
+template <class Op64, class Op32>
+int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double *relres, int *outer)
+{
+    const long long n = c->g.n;
+    // |b|^2 via the residual kernel with x = 0 would need a zero vector; the
+    // dot of b with itself is taken by the same FP64 reduction instead.
+    // |b|^2 from the residual kernel with x = 0 (w64.r0 is an FP64 zero
+    // vector in mixed-precision contexts)
+    double norm0 = 0.0;
+    residual64(c, A64, c->b, c->w64.r0, c->r32, c->dscal + 4);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    norm0 = std::sqrt(c->h_scal[4]);
+    int total = 0, sweeps = 0;
+    double rel = 0.0;
+    if (norm0 == 0.0) {
+        if (iters) *iters = 0;
+        if (relres) *relres = 0.0;
+        if (outer) *outer = 0;
+        return CFD_OK;
+    }
+    int st = CFD_OK;
+    for (;;) {
+        residual64(c, A64, c->b, c->x, c->r32, c->dscal + 3);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+        CK(cudaStreamSynchronize(c->s));
+        rel = std::sqrt(c->h_scal[3]) / norm0;
+        if (rel < c->cfg.p_criteria || !std::isfinite(rel)) break;
+        if (sweeps >= c->cfg.max_outer) { st = fail(CFD_ERR_NOCONV, "defect correction reached its sweep cap"); break; }
+        CK(cudaMemsetAsync(c->e32, 0, (size_t)n * sizeof(float), c->s));
+        CKS((bicg_run<Op32, float>(c, A32, c->r32, c->e32, c->w32, nullptr, nullptr, c->sc_in, 1)));
+        total += c->h_sc->iter;
+        launch_correct<float>(c->lc, n, c->x, c->e32);
+        CK(cudaGetLastError());
+        ++sweeps;
+    }
+    if (!std::isfinite(rel)) st = fail(CFD_ERR_NAN, "non-finite Poisson residual");
+    if (iters) *iters = total;
+    if (relres) *relres = rel;
+    if (outer) *outer = sweeps;
+    return st;
+}
+
+int poisson_solve(cfd_ctx *c, int *iters, double *relres, int *outer)
+{
+    if (outer) *outer = 0;
+    const bool ell = c->cfg.solver == CFD_SOLVER_BICG_ELL;
+    if (c->cfg.precision == CFD_PREC_MIXED) {
+        if (ell) return solve_mixed(c, ell64(c), ell32(c), iters, relres, outer);
+        return solve_mixed(c, spe64(c), spe32(c), iters, relres, outer);
+    }
+    if (ell) return solve64(c, ell64(c), iters, relres);
+    return solve64(c, spe64(c), iters, relres);
+}
+
+template <class T>
+int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
+{
+    const Geo &g = c->g;
+    const Metrics<double> m = metrics_of<double>(c);
+    launch_sor_rhs<T>(c->s, g, m, 1.0 / c->cfg.dt, dv<T>(c, si, 0), dv<T>(c, si, 1), dv<T>(c, si, 2),
+                      c->cf6);
+    const int itmax = c->cfg.p_sor_iter_max;
+    CK(cudaMemsetAsync(c->sor_res, 0, (size_t)(itmax + 1) * sizeof(unsigned long long), c->s));
+    CK(cudaMemsetAsync(c->sor_state, 0, 2 * sizeof(int), c->s));
+    const int batch = c->cfg.check_every;
+    int sweep = 0;
+    for (;;) {
+        for (int q = 0; q < batch && sweep <= itmax; ++q, ++sweep)
+            launch_sor_sweep(c->s, g, m, c->cf6, c->cf7, c->p, c->cfg.p_sor_omega, c->cfg.p_criteria,
+                             itmax, sweep, c->sor_res, c->sor_state);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(c->h_sor_state, c->sor_state, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->s));
+        CK(cudaStreamSynchronize(c->s));
+        if (c->h_sor_state[0] || sweep > itmax) break;
+    }
+    const int run = c->h_sor_state[1];
+    unsigned long long last = 0;
+    if (run > 0)
+        CK(cudaMemcpy(&last, c->sor_res + (run - 1), sizeof(last), cudaMemcpyDeviceToHost));
+    double e;
+    std::memcpy(&e, &last, sizeof(e));
+    if (iters) *iters = run - 1;
+    if (err) *err = e;
+    return CFD_OK;
+}
+
+template <class T>
+int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer)
+{
+    const Geo &g = c->g;
+    if (c->cfg.solver == CFD_SOLVER_SOR_RB) {
+        if (outer) *outer = 0;
+        return sor_solve_t<T>(c, si, iters, relres);
+    }
+    launch_rhs<T>(c->lc, g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, si, 0),
+                  dv<T>(c, si, 1), dv<T>(c, si, 2), c->b, c->cfg.compat_rhs != 0, c->dscal + 0);
+    CK(cudaGetLastError());
+    int st = poisson_solve(c, iters, relres, outer);
+    if (st != CFD_OK && st != CFD_ERR_NOCONV) return st;
+    launch_transform(c->s, g, c->x, c->p);
+    CK(cudaGetLastError());
+    return st;
+}
+
+template <class T>
+int step_t(cfd_ctx *c, cfd_step_info *info)
+{
+    const Geo &g = c->g;
+    const Metrics<T> m = metrics_of<T>(c);
+    const bool pc = c->cfg.method == CFD_METHOD_PC;
+    const bool aligned = c->cfg.aligned_source != 0;
+    const T dt = (T)c->cfg.dt, nudt = (T)((1.0 / c->cfg.re) * c->cfg.dt);
+    T *u0 = dv<T>(c, 0, 0), *v0 = dv<T>(c, 0, 1), *w0 = dv<T>(c, 0, 2);
+    T *u1 = dv<T>(c, 1, 0), *v1 = dv<T>(c, 1, 1), *w1 = dv<T>(c, 1, 2);
+    T *u3 = dv<T>(c, 2, 0), *v3 = dv<T>(c, 2, 1), *w3 = dv<T>(c, 2, 2);
+    T *src = static_cast<T *>(c->src), *f = static_cast<T *>(c->f);
+    const int npass = pc ? 4 : 1;
+    int st = CFD_OK;
+    cfd_step_info loc{};
+    if (pc) CK(cudaMemsetAsync(src, 0, (size_t)(3 * g.n) * sizeof(T), c->s));
+    for (int pass = 0; pass < npass; ++pass) {
+        launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, u1, v1, w1,
+                           (pc && aligned && pass > 0) ? src : nullptr);
+        if (pc && !aligned) launch_src_add<T>(c->lc, g, 0, u1, v1, w1, src);
+        CK(cudaGetLastError());
+        if (c->loop > 1) {
+            int s2 = pressure_step<T>(c, 1, &loc.iters[pass], &loc.relres[pass], &loc.outer[pass]);
+            if (s2 != CFD_OK && s2 != CFD_ERR_NOCONV) return s2;
+            if (s2 != CFD_OK) st = s2;
+        }
+        launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
+                            u1, v1, w1, u3, v3, w3, f);
+        if (pc && pass < 3) launch_src_accumulate<T>(c->lc, 3 * g.n, dt, src, f);
+        CK(cudaGetLastError());
+    }
+    const size_t bytes = (size_t)g.ng * sizeof(T);
+    for (int q = 0; q < 3; ++q)
+        CK(cudaMemcpyAsync(c->vel[0][q], c->vel[2][q], bytes, cudaMemcpyDeviceToDevice, c->s));
+    BcTab bc;
+    std::memcpy(bc.dir, c->cfg.bc_dir, sizeof(bc.dir));
+    std::memcpy(bc.num, c->cfg.bc_num, sizeof(bc.num));
+    launch_bc_main<T>(c->s, g, bc, u0, v0, w0, c->p);
+    launch_bc_copy<T>(c->s, g, u0, v0, w0, u1, v1, w1);
+    launch_cdcl<T>(c->lc, g, metrics_of<double>(c), c->cfg.lz, f, c->dscal + 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    loc.cd = c->h_scal[1];
+    loc.cl = c->h_scal[2];
+    c->loop += 1;
+    c->time += c->cfg.dt;
+    loc.loop = c->loop;
+    loc.time = c->time;
+    if (info) *info = loc;
+    return st;
+}
+
+int build_tables(cfd_ctx *c)
+{
+    const Geo &g = c->g;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; ++a) {
+        std::vector<double> t = axis_table(c->hraw[3 + a], c->hraw[6 + a]);
+        CK(cudaMemcpyAsync(c->tab64[a], t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, c->s));
+        std::vector<float> t32(t.begin(), t.end());
+        CK(cudaMemcpyAsync(c->tab32[a], t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, c->s));
+        CK(cudaStreamSynchronize(c->s));
+        (void)n;
+    }
+    for (int q = 0; q < 9; ++q)
+        CK(cudaMemcpyAsync(c->rawp[q], c->hraw[q].data(), c->hraw[q].size() * sizeof(double),
+                           cudaMemcpyHostToDevice, c->s));
+    // operators
+    launch_spe_setup(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7], c->rawp[8],
+                     c->spe_c[0], c->spe_c[1], c->spe_c[2], c->jp);
+    if (c->cfg.solver == CFD_SOLVER_BICG_ELL)
+        launch_ell_assemble(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7],
+                            c->rawp[8], c->ell_cols, c->ell_vals, c->jp);
+    if (c->cfg.solver == CFD_SOLVER_SOR_RB)
+        launch_sor_setup(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7], c->rawp[8],
+                         c->cf7);
+    if (c->fp32) {
+        for (int a = 0; a < 3; ++a) {
+            const int na = a == 0 ? g.nxc : a == 1 ? g.nyc : g.nzc;
+            launch_convert<double, float>(c->lc, 2LL * na, c->spe_c[a], c->spe_c32[a]);
+        }
+        launch_convert<double, float>(c->lc, g.n, c->jp, c->jp32);
+        if (c->cfg.solver == CFD_SOLVER_BICG_ELL)
+            launch_convert<double, float>(c->lc, 7 * g.n, c->ell_vals, c->ell_vals32);
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    c->metrics = true;
+    return CFD_OK;
+}
+
+void free_ctx(cfd_ctx *c)
+{
+    if (!c) return;
+    for (auto &ge : c->graph)
+        if (ge) cudaGraphExecDestroy(ge);
+    if (c->s) cudaStreamSynchronize(c->s);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->h_sc) cudaFreeHost(c->h_sc);
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->h_sor_state) cudaFreeHost(c->h_sor_state);
+    if (c->h_max) cudaFreeHost(c->h_max);
+    if (c->s) cudaStreamDestroy(c->s);
+    delete c;
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+int cfd_abi_version(void) { return CFDGPU_ABI_VERSION; }
+
+const char *cfd_last_error(void) { return g_err.c_str(); }
+
+int cfd_config_default(cfd_config *cfg, int nx, int ny, int nz)
+{
+    if (!cfg) return fail(CFD_ERR_ARG, "null config");
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->nx_cal = nx;
+    cfg->ny_cal = ny;
+    cfg->nz_cal = nz;
+    cfg->lx = 1.0;
+    cfg->ly = 1.0;
+    cfg->lz = 1.0;
+    cfg->re = 40.0;      // src/CFD_MX.cpp:39
+    cfg->dt = 0.002;     // src/CFD_MX.cpp:37
+    cfg->method = CFD_METHOD_PC;
+    cfg->solver = CFD_SOLVER_BICG_SPE;
+    cfg->precision = CFD_PREC_FP64;
+    cfg->p_criteria = 1e-3;   // simuClass.hpp:74
+    cfg->p_iter_max = 5000;   // bicgstabRe2.hpp:57
+    cfg->p_sor_omega = 1.8;   // simuClass.hpp:78
+    cfg->p_sor_iter_max = 5000;
+    cfg->aligned_source = 0;
+    cfg->compat_rhs = 0;
+    cfg->check_every = 16;
+    cfg->inner_tol = 1e-4;
+    cfg->max_outer = 30;
+    return CFD_OK;
+}
+
+int cfd_create(const cfd_config *cfg, cfd_ctx **out)
+{
+    if (!cfg || !out) return fail(CFD_ERR_ARG, "null argument");
+    *out = nullptr;
+    const cfd_config &k = *cfg;
+    if (k.nx_cal < 4 || k.ny_cal < 4 || k.nz_cal < 4)
+        return fail(CFD_ERR_ARG, "every interior dimension must be at least 4");
+    const long long n = (long long)k.nx_cal * k.ny_cal * k.nz_cal;
+    if (n >= (1LL << 31) - 1) return fail(CFD_ERR_ARG, "grid too large for 32-bit ELL column indices");
+    if (!(k.lx > 0 && k.ly > 0 && k.lz > 0)) return fail(CFD_ERR_ARG, "domain lengths must be positive");
+    if (!(k.dt > 0) || !(k.re > 0)) return fail(CFD_ERR_ARG, "dt and re must be positive");
+    if (!(k.p_criteria > 0) || k.p_iter_max < 1 || k.p_sor_iter_max < 1)
+        return fail(CFD_ERR_ARG, "solver tolerance and iteration caps must be positive");
+    if (k.solver != CFD_SOLVER_BICG_SPE && k.solver != CFD_SOLVER_BICG_ELL && k.solver != CFD_SOLVER_SOR_RB)
+        return fail(CFD_ERR_ARG, "unknown solver");
+    if (k.method != CFD_METHOD_PC && k.method != CFD_METHOD_PLAIN) return fail(CFD_ERR_ARG, "unknown method");
+    if (k.precision != CFD_PREC_FP64 && k.precision != CFD_PREC_MIXED)
+        return fail(CFD_ERR_ARG, "unknown precision");
+    if (k.check_every < 1 || k.check_every > 4096) return fail(CFD_ERR_ARG, "check_every out of range");
+    if (k.precision == CFD_PREC_MIXED && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
+        return fail(CFD_ERR_ARG, "mixed precision needs 0 < inner_tol < 1 and max_outer >= 1");
+
+    cfd_ctx *c = new cfd_ctx();
+    c->cfg = k;
+    c->fp32 = k.precision == CFD_PREC_MIXED;
+    Geo &g = c->g;
+    g.nxc = k.nx_cal; g.nyc = k.ny_cal; g.nzc = k.nz_cal;
+    g.nx = g.nxc + 2 * GC; g.ny = g.nyc + 2 * GC; g.nz = g.nzc + 2 * GC;
+    g.sx = (long long)g.ny * g.nz; g.sy = g.nz;
+    g.sxc = (long long)g.nyc * g.nzc; g.syc = g.nzc;
+    g.ng = (long long)g.nx * g.ny * g.nz;
+    g.n = n;
+    if (const char *e = std::getenv("CFDGPU_NO_GRAPH")) c->use_graphs = !(e[0] == '1');
+
+    int st = CFD_OK;
+    auto bail = [&](int code) { free_ctx(c); return code; };
+    cudaError_t e = cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail(CFD_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+    const size_t ts = c->fp32 ? sizeof(float) : sizeof(double);
+#define AL(ptr, bytes) \
+    if ((st = dalloc(c, reinterpret_cast<void **>(&(ptr)), (bytes))) != CFD_OK) return bail(st)
+    for (int sl = 0; sl < 3; ++sl)
+        for (int q = 0; q < 3; ++q) AL(c->vel[sl][q], (size_t)g.ng * ts);
+    AL(c->eta, (size_t)g.ng * ts);
+    AL(c->f, (size_t)(3 * n) * ts);
+    AL(c->src, (size_t)(3 * n) * ts);
+    AL(c->p, (size_t)g.ng * sizeof(double));
+    AL(c->x, (size_t)n * sizeof(double));
+    AL(c->b, (size_t)n * sizeof(double));
+    AL(c->jp, (size_t)n * sizeof(double));
+    AL(c->raw, (size_t)(3 * (g.nx + g.ny + g.nz) + 3) * sizeof(double));
+    {
+        double *q = c->raw;
+        const int len[9] = {g.nx + 1, g.ny + 1, g.nz + 1, g.nx, g.ny, g.nz, g.nx, g.ny, g.nz};
+        for (int a = 0; a < 9; ++a) { c->rawp[a] = q; q += len[a]; c->hraw[a].assign(len[a], 0.0); }
+    }
+    const int na[3] = {g.nx, g.ny, g.nz};
+    const int nc[3] = {g.nxc, g.nyc, g.nzc};
+    for (int a = 0; a < 3; ++a) {
+        AL(c->tab64[a], (size_t)AX_ROWS * na[a] * sizeof(double));
+        AL(c->tab32[a], (size_t)AX_ROWS * na[a] * sizeof(float));
+        AL(c->spe_c[a], (size_t)2 * nc[a] * sizeof(double));
+    }
+    const bool bicg = k.solver != CFD_SOLVER_SOR_RB;
+    if (k.solver == CFD_SOLVER_BICG_ELL) {
+        AL(c->ell_cols, (size_t)(7 * n) * sizeof(int));
+        AL(c->ell_vals, (size_t)(7 * n) * sizeof(double));
+    }
+    if (bicg && !c->fp32) {
+        AL(c->w64.r0, n * 8); AL(c->w64.r1, n * 8); AL(c->w64.p1, n * 8);
+        AL(c->w64.s1, n * 8); AL(c->w64.ap, n * 8); AL(c->w64.as, n * 8);
+        AL(c->px1, n * 8); AL(c->px2, n * 8);
+    }
+    if (bicg && c->fp32) {
+        AL(c->w64.r0, n * 8);  // FP64 zero vector for |b| in the defect correction
+        AL(c->w32.r0, n * 4); AL(c->w32.r1, n * 4); AL(c->w32.p1, n * 4);
+        AL(c->w32.s1, n * 4); AL(c->w32.ap, n * 4); AL(c->w32.as, n * 4);
+        AL(c->r32, n * 4); AL(c->e32, n * 4);
+        for (int a = 0; a < 3; ++a) AL(c->spe_c32[a], (size_t)2 * nc[a] * sizeof(float));
+        AL(c->jp32, n * 4);
+        if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
+    }
+    if (!bicg) {
+        AL(c->cf6, n * 8);
+        AL(c->cf7, n * 8);
+        AL(c->sor_res, (size_t)(k.p_sor_iter_max + 2) * sizeof(unsigned long long));
+        AL(c->sor_state, 4 * sizeof(int));
+    }
+    AL(c->sc, sizeof(BicgScal));
+    AL(c->sc_in, sizeof(BicgScal));
+    AL(c->sc_t, sizeof(BicgScal));
+    AL(c->dscal, 8 * sizeof(double));
+    AL(c->dmax, sizeof(unsigned long long));
+    const int red_blocks = blocks_for(n, sms * 8);
+    AL(c->lc.partials, (size_t)4 * red_blocks * sizeof(double));
+    AL(c->lc.counter, sizeof(unsigned int));
+    if (c->fp32) AL(c->staging, (size_t)g.ng * sizeof(double));
+#undef AL
+    if (cudaMallocHost(reinterpret_cast<void **>(&c->h_sc), sizeof(BicgScal)) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void **>(&c->h_scal), 8 * sizeof(double)) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void **>(&c->h_sor_state), 4 * sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void **>(&c->h_max), sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(CFD_ERR_NOMEM, "pinned host allocation failed"));
+    }
+    c->lc.s = c->s;
+    c->lc.red_blocks = red_blocks;
+    c->lc.grid_cap = sms * 16;
+
+    // zero everything, then the reference's initial values
+    e = cudaMemsetAsync(c->lc.counter, 0, sizeof(unsigned int), c->s);
+    BicgScal h{};
+    h.tol = k.p_criteria;
+    h.restart_tol = 1e-7 * k.p_criteria;  // pRestartFactor_ (bicgstabRe2.hpp:39-42)
+    h.maxit = k.p_iter_max;
+    BicgScal hin{};
+    hin.tol = k.inner_tol;
+    hin.restart_tol = 1e-7 * k.inner_tol;
+    hin.maxit = k.p_iter_max;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice, c->s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->sc_in, &hin, sizeof(hin), cudaMemcpyHostToDevice, c->s);
+    const size_t zero_bytes[] = {(size_t)g.ng * ts, (size_t)(3 * n) * ts, (size_t)n * 8};
+    for (int sl = 0; sl < 3 && e == cudaSuccess; ++sl)
+        for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaMemsetAsync(c->vel[sl][q], 0, zero_bytes[0], c->s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->eta, 0, zero_bytes[0], c->s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->f, 0, zero_bytes[1], c->s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->src, 0, zero_bytes[1], c->s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->p, 0, (size_t)g.ng * 8, c->s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->x, 0, zero_bytes[2], c->s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->b, 0, zero_bytes[2], c->s);
+    if (e == cudaSuccess && c->px1) e = cudaMemsetAsync(c->px1, 0, zero_bytes[2], c->s);
+    if (e == cudaSuccess && c->px2) e = cudaMemsetAsync(c->px2, 0, zero_bytes[2], c->s);
+    if (e == cudaSuccess && c->w64.r0) e = cudaMemsetAsync(c->w64.r0, 0, zero_bytes[2], c->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->s);
+    if (e != cudaSuccess) return bail(fail(CFD_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e)));
+    *out = c;
+    return CFD_OK;
+}
+
+int cfd_destroy(cfd_ctx *c)
+{
+    if (!c) return CFD_OK;
+    free_ctx(c);
+    return CFD_OK;
+}
+
+int cfd_sync(cfd_ctx *c)
+{
+    CKS(check_ctx(c));
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_grid_uniform(cfd_ctx *c)
+{
+    CKS(check_ctx(c));
+    const Geo &g = c->g;
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const double L[3] = {c->cfg.lx, c->cfg.ly, c->cfg.lz};
+    // grid::init_uniform (structureGrid.hpp:409-440)
+    for (int a = 0; a < 3; ++a) {
+        const double d = L[a] / (n[a] - 2.0 * GC);
+        std::vector<double> &P = c->hraw[a];
+        P[0] = 0.0 - 2.0 * d;
+        for (int i = 1; i < n[a] + 1; ++i) P[i] = P[i - 1] + d;
+        c->hraw[3 + a].assign(n[a], d);
+        c->hraw[6 + a].assign(n[a], d);
+    }
+    return build_tables(c);
+}
+
+int cfd_set_metrics(cfd_ctx *c, const double *X, const double *Y, const double *Z, const double *Dx,
+                    const double *Dy, const double *Dz, const double *Dxs, const double *Dys,
+                    const double *Dzs)
+{
+    CKS(check_ctx(c));
+    const double *in[9] = {X, Y, Z, Dx, Dy, Dz, Dxs, Dys, Dzs};
+    for (int q = 0; q < 9; ++q) {
+        if (!in[q]) return fail(CFD_ERR_ARG, "null metric array");
+        std::memcpy(c->hraw[q].data(), in[q], c->hraw[q].size() * sizeof(double));
+    }
+    for (int q = 3; q < 9; ++q)
+        for (double v : c->hraw[q])
+            if (!(v > 0) || !std::isfinite(v)) return fail(CFD_ERR_ARG, "cell widths must be positive and finite");
+    return build_tables(c);
+}
+
+size_t cfd_field_count(cfd_ctx *c, int field)
+{
+    if (!c) return 0;
+    return field_count(c, field);
+}
+
+int cfd_upload(cfd_ctx *c, int field, const double *host, size_t count)
+{
+    CKS(check_ctx(c));
+    if (field < 0 || field >= CFD_FIELD_COUNT) return fail(CFD_ERR_ARG, "unknown field");
+    if (!host) return fail(CFD_ERR_ARG, "null host pointer");
+    const size_t want = field_count(c, field);
+    if (count != want)
+        return fail(CFD_ERR_ARG, "element count " + std::to_string(count) + " != " + std::to_string(want));
+    bool is_t;
+    void *d = field_ptr(c, field, is_t);
+    if (is_t && c->fp32) {
+        CK(cudaMemcpyAsync(c->staging, host, count * sizeof(double), cudaMemcpyHostToDevice, c->s));
+        launch_convert<double, float>(c->lc, (long long)count, c->staging, static_cast<float *>(d));
+        CK(cudaGetLastError());
+    } else {
+        CK(cudaMemcpyAsync(d, host, count * sizeof(double), cudaMemcpyHostToDevice, c->s));
+    }
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_download(cfd_ctx *c, int field, double *host, size_t count)
+{
+    CKS(check_ctx(c));
+    if (field < 0 || field >= CFD_FIELD_COUNT) return fail(CFD_ERR_ARG, "unknown field");
+    if (!host) return fail(CFD_ERR_ARG, "null host pointer");
+    const size_t want = field_count(c, field);
+    if (count != want)
+        return fail(CFD_ERR_ARG, "element count " + std::to_string(count) + " != " + std::to_string(want));
+    bool is_t;
+    void *d = field_ptr(c, field, is_t);
+    if (is_t && c->fp32) {
+        launch_convert<float, double>(c->lc, (long long)count, static_cast<float *>(d), c->staging);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(host, c->staging, count * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    } else {
+        CK(cudaMemcpyAsync(host, d, count * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    }
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_host_register(void *host, size_t bytes)
+{
+    if (!host || !bytes) return fail(CFD_ERR_ARG, "null or empty host buffer");
+    CK(cudaHostRegister(host, bytes, cudaHostRegisterDefault));
+    return CFD_OK;
+}
+
+int cfd_host_unregister(void *host)
+{
+    if (!host) return fail(CFD_ERR_ARG, "null host buffer");
+    CK(cudaHostUnregister(host));
+    return CFD_OK;
+}
+
+int cfd_init_uniform(cfd_ctx *c, double ui, double vi, double wi)
+{
+    CKS(check_ctx(c));
+    const double val[3] = {ui, vi, wi};
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        for (int sl = 0; sl < 3; ++sl)
+            for (int q = 0; q < 3; ++q) launch_fill<T>(c->lc, c->g.ng, dv<T>(c, sl, q), (T)val[q]);
+        return 0;
+    });
+    CK(cudaMemsetAsync(c->p, 0, (size_t)c->g.ng * sizeof(double), c->s));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_start(cfd_ctx *c)
+{
+    CKS(need_metrics(c));
+    const size_t ts = c->fp32 ? 4 : 8;
+    for (int sl = 1; sl < 3; ++sl)
+        for (int q = 0; q < 3; ++q)
+            CK(cudaMemcpyAsync(c->vel[sl][q], c->vel[0][q], (size_t)c->g.ng * ts, cudaMemcpyDeviceToDevice, c->s));
+    CKS(cfd_bc_main(c, CFD_SLOT_T0));
+    CKS(cfd_bc_copy(c, CFD_SLOT_T0, CFD_SLOT_T1));
+    c->loop = 1;
+    c->time = 0.0;
+    return CFD_OK;
+}
+
+int cfd_convection_diffusion(cfd_ctx *c, int src_slot, int dst_slot)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(src_slot));
+    CKS(check_slot(dst_slot));
+    if (src_slot == dst_slot) return fail(CFD_ERR_ARG, "source and destination slots must differ");
+    const int a = slot_index(src_slot), b = slot_index(dst_slot);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_convdiff<T>(c->s, c->g, metrics_of<T>(c), (T)c->cfg.dt, (T)((1.0 / c->cfg.re) * c->cfg.dt),
+                           dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), dv<T>(c, b, 0), dv<T>(c, b, 1),
+                           dv<T>(c, b, 2), nullptr);
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_add_source(cfd_ctx *c, int slot)
+{
+    CKS(check_ctx(c));
+    CKS(check_slot(slot));
+    const int a = slot_index(slot);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_src_add<T>(c->lc, c->g, c->cfg.aligned_source, dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2),
+                          static_cast<T *>(c->src));
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_accumulate_source(cfd_ctx *c)
+{
+    CKS(check_ctx(c));
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_src_accumulate<T>(c->lc, 3 * c->g.n, (T)c->cfg.dt, static_cast<T *>(c->src),
+                                 static_cast<T *>(c->f));
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_clear_source(cfd_ctx *c)
+{
+    CKS(check_ctx(c));
+    CK(cudaMemsetAsync(c->src, 0, (size_t)(3 * c->g.n) * (c->fp32 ? 4 : 8), c->s));
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_create_b(cfd_ctx *c, int slot, double *mean)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot));
+    const int a = slot_index(slot);
+    const bool compat = c->cfg.compat_rhs != 0;
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_rhs<T>(c->lc, c->g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, a, 0),
+                      dv<T>(c, a, 1), dv<T>(c, a, 2), c->b, compat, c->dscal + 0);
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    if (mean) *mean = compat ? c->h_scal[0] : 0.0;
+    return CFD_OK;
+}
+
+int cfd_bicgstab(cfd_ctx *c, int *iters, double *relres)
+{
+    CKS(need_metrics(c));
+    if (c->cfg.solver == CFD_SOLVER_SOR_RB) return fail(CFD_ERR_STATE, "context was created for SOR");
+    return poisson_solve(c, iters, relres, nullptr);
+}
+
+int cfd_apply_operator(cfd_ctx *c)
+{
+    CKS(need_metrics(c));
+    if (c->cfg.solver == CFD_SOLVER_BICG_ELL) launch_apply(c->lc, ell64(c), c->x, c->b);
+    else launch_apply(c->lc, spe64(c), c->x, c->b);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_pressure_transform(cfd_ctx *c)
+{
+    CKS(check_ctx(c));
+    launch_transform(c->s, c->g, c->x, c->p);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_sor(cfd_ctx *c, int slot, int *iters, double *err)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot));
+    if (c->cfg.solver != CFD_SOLVER_SOR_RB) return fail(CFD_ERR_STATE, "context was not created for SOR");
+    const int a = slot_index(slot);
+    return dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        return sor_solve_t<T>(c, a, iters, err);
+    });
+}
+
+int cfd_update_uf(cfd_ctx *c, int src_slot, int dst_slot)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(src_slot));
+    CKS(check_slot(dst_slot));
+    const int a = slot_index(src_slot), b = slot_index(dst_slot);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_update_uf<T>(c->s, c->g, metrics_of<T>(c), c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p,
+                            static_cast<T *>(c->eta), dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2),
+                            dv<T>(c, b, 0), dv<T>(c, b, 1), dv<T>(c, b, 2), static_cast<T *>(c->f));
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_cdcl(cfd_ctx *c, double *cd, double *cl)
+{
+    CKS(need_metrics(c));
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_cdcl<T>(c->lc, c->g, metrics_of<double>(c), c->cfg.lz, static_cast<T *>(c->f), c->dscal + 1);
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    if (cd) *cd = c->h_scal[1];
+    if (cl) *cl = c->h_scal[2];
+    return CFD_OK;
+}
+
+int cfd_bc_main(cfd_ctx *c, int slot)
+{
+    CKS(check_ctx(c));
+    CKS(check_slot(slot));
+    const int a = slot_index(slot);
+    BcTab bc;
+    std::memcpy(bc.dir, c->cfg.bc_dir, sizeof(bc.dir));
+    std::memcpy(bc.num, c->cfg.bc_num, sizeof(bc.num));
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_bc_main<T>(c->s, c->g, bc, dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), c->p);
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_bc_copy(cfd_ctx *c, int from_slot, int to_slot)
+{
+    CKS(check_ctx(c));
+    CKS(check_slot(from_slot));
+    CKS(check_slot(to_slot));
+    const int a = slot_index(from_slot), b = slot_index(to_slot);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_bc_copy<T>(c->s, c->g, dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), dv<T>(c, b, 0),
+                          dv<T>(c, b, 1), dv<T>(c, b, 2));
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_copy_velocity(cfd_ctx *c, int from_slot, int to_slot)
+{
+    CKS(check_ctx(c));
+    CKS(check_slot(from_slot));
+    CKS(check_slot(to_slot));
+    const int a = slot_index(from_slot), b = slot_index(to_slot);
+    const size_t bytes = (size_t)c->g.ng * (c->fp32 ? 4 : 8);
+    for (int q = 0; q < 3; ++q)
+        CK(cudaMemcpyAsync(c->vel[b][q], c->vel[a][q], bytes, cudaMemcpyDeviceToDevice, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_eta_cylinder_z(cfd_ctx *c, double cx, double cy, double radius, int nsub)
+{
+    CKS(need_metrics(c));
+    if (nsub < 1 || nsub > 4096 || !(radius > 0)) return fail(CFD_ERR_ARG, "bad cylinder parameters");
+    double *eta64 = c->fp32 ? c->staging : static_cast<double *>(c->eta);
+    CK(cudaMemsetAsync(eta64, 0, (size_t)c->g.ng * sizeof(double), c->s));
+    launch_eta_cylinder_z(c->s, c->g, c->rawp[0], c->rawp[1], c->rawp[3], c->rawp[4], cx, cy, radius, nsub,
+                          std::pow((double)nsub, -2.0), eta64);
+    if (c->fp32) launch_convert<double, float>(c->lc, c->g.ng, eta64, static_cast<float *>(c->eta));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_step(cfd_ctx *c, cfd_step_info *info)
+{
+    CKS(need_metrics(c));
+    return dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        return step_t<T>(c, info);
+    });
+}
+
+int cfd_div_inf(cfd_ctx *c, int slot, double *out)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot));
+    if (!out) return fail(CFD_ERR_ARG, "null output");
+    const int a = slot_index(slot);
+    CK(cudaMemsetAsync(c->dmax, 0, sizeof(unsigned long long), c->s));
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_div_inf<T>(c->lc, c->g, metrics_of<double>(c), dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2),
+                          c->dmax);
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_max, c->dmax, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    std::memcpy(out, c->h_max, sizeof(double));
+    return CFD_OK;
+}
+
+int cfd_stream(cfd_ctx *c, void **stream)
+{
+    CKS(check_ctx(c));
+    if (!stream) return fail(CFD_ERR_ARG, "null output");
+    *stream = (void *)c->s;
+    return CFD_OK;
+}
+
+int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
+{
+    CKS(need_metrics(c));
+    if (!ms || nms < 1 || reps < 1) return fail(CFD_ERR_ARG, "bad arguments");
+    for (int k = 0; k < nms && k < CFD_KERNEL_COUNT; ++k) ms[k] = -1.0;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    auto timed = [&](int id, auto &&launch) -> int {
+        launch();  // warm-up launch
+        CK(cudaEventRecord(e0, c->s));
+        for (int r = 0; r < reps; ++r) launch();
+        CK(cudaEventRecord(e1, c->s));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaGetLastError());
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, e0, e1));
+        if (id < nms) ms[id] = (double)t / reps;
+        return CFD_OK;
+    };
+    // scratch scalars: never converge, never cap
+    BicgScal hs{};
+    hs.norm0 = 1.0; hs.rho = 1.0; hs.alpha = 0.5; hs.omega = 0.5; hs.beta = 0.5;
+    hs.tol = 0.0; hs.restart_tol = 0.0; hs.maxit = 0x7fffffff; hs.timestep = 1;
+    CK(cudaMemcpyAsync(c->sc_t, &hs, sizeof(hs), cudaMemcpyHostToDevice, c->s));
+    int st = CFD_OK;
+    const Geo &g = c->g;
+    const int G = c->lc.red_blocks;
+    if (c->cfg.solver != CFD_SOLVER_SOR_RB) {
+        auto run = [&](auto A, auto *x, auto &w) -> int {
+            using V = std::remove_pointer_t<decltype(x)>;
+            cfd_launch_ctx &lc = c->lc;
+            int s2 = CFD_OK;
+            if ((s2 = timed(CFD_KERNEL_BICG_AP, [&] { launch_bicg_iteration_part<decltype(A), V>(lc, A, x, w, c->sc_t, 0); })) != CFD_OK) return s2;
+            if ((s2 = timed(CFD_KERNEL_BICG_S, [&] { launch_bicg_iteration_part<decltype(A), V>(lc, A, x, w, c->sc_t, 1); })) != CFD_OK) return s2;
+            if ((s2 = timed(CFD_KERNEL_BICG_AS, [&] { launch_bicg_iteration_part<decltype(A), V>(lc, A, x, w, c->sc_t, 2); })) != CFD_OK) return s2;
+            if ((s2 = timed(CFD_KERNEL_BICG_XR, [&] { launch_bicg_iteration_part<decltype(A), V>(lc, A, x, w, c->sc_t, 3); })) != CFD_OK) return s2;
+            return timed(CFD_KERNEL_BICG_P, [&] { launch_bicg_iteration_part<decltype(A), V>(lc, A, x, w, c->sc_t, 4); });
+        };
+        (void)G;
+        if (c->fp32) {
+            float *xs = c->e32;
+            CK(cudaMemsetAsync(xs, 0, (size_t)g.n * sizeof(float), c->s));
+            st = c->cfg.solver == CFD_SOLVER_BICG_ELL ? run(ell32(c), xs, c->w32) : run(spe32(c), xs, c->w32);
+        } else {
+            double *xs = c->px2;
+            CK(cudaMemcpyAsync(xs, c->x, (size_t)g.n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+            st = c->cfg.solver == CFD_SOLVER_BICG_ELL ? run(ell64(c), xs, c->w64) : run(spe64(c), xs, c->w64);
+            CK(cudaMemcpyAsync(c->px2, c->px1, (size_t)g.n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+        }
+        if (st != CFD_OK) return st;
+    }
+    st = dispatch(c, [&](auto tag) -> int {
+        using T = typename decltype(tag)::type;
+        const Metrics<T> m = metrics_of<T>(c);
+        int s2;
+        // T3 is scratch here: convection-diffusion T0 -> T3, projection T1 -> T3
+        if ((s2 = timed(CFD_KERNEL_CONVDIFF, [&] {
+                 launch_convdiff<T>(c->s, g, m, (T)c->cfg.dt, (T)((1.0 / c->cfg.re) * c->cfg.dt), dv<T>(c, 0, 0),
+                                    dv<T>(c, 0, 1), dv<T>(c, 0, 2), dv<T>(c, 2, 0), dv<T>(c, 2, 1), dv<T>(c, 2, 2),
+                                    nullptr);
+             })) != CFD_OK)
+            return s2;
+        if ((s2 = timed(CFD_KERNEL_UPDATE_UF, [&] {
+                 launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
+                                     dv<T>(c, 1, 0), dv<T>(c, 1, 1), dv<T>(c, 1, 2), dv<T>(c, 2, 0),
+                                     dv<T>(c, 2, 1), dv<T>(c, 2, 2), static_cast<T *>(c->f));
+             })) != CFD_OK)
+            return s2;
+        if (c->cfg.solver != CFD_SOLVER_SOR_RB) {
+            if ((s2 = timed(CFD_KERNEL_RHS, [&] {
+                     launch_rhs<T>(c->lc, g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, 1, 0),
+                                   dv<T>(c, 1, 1), dv<T>(c, 1, 2), c->b, c->cfg.compat_rhs != 0, c->dscal + 0);
+                 })) != CFD_OK)
+                return s2;
+        }
+        return CFD_OK;
+    });
+    if (st != CFD_OK) return st;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return CFD_OK;
+}
+
+}  // extern "C"

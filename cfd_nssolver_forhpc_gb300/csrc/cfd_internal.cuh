@@ -1,0 +1,184 @@
+// cfd_internal.cuh -- device-side building blocks shared by the kernels.
+//
+// Layout: every field keeps the reference's layout (k fastest).  Ghosted
+// fields are nx*ny*nz with nx = nx_cal + 4 (two ghost layers, gC = 2,
+// inc/grid/structureGrid.hpp:40); compact fields are nx_cal*ny_cal*nz_cal.
+//
+// Metrics live in per-axis tables of FieldCount rows; every division by a
+// cell or staggered width of the reference becomes a multiplication by a
+// reciprocal read from these tables (FP64 divides are slow on GB300), and the
+// QUICK curvature factors 0.125*D*D/Ds of QuickUnitA/B
+// (inc/source/convection_and_difussion.hpp:20-84) are tabulated with the
+// reference's own evaluation order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cfd {
+
+constexpr int GC = 2;
+constexpr int kBlock = 256;
+
+struct Geo {
+    int nx, ny, nz;       // ghosted
+    int nxc, nyc, nzc;    // interior
+    long long sx;         // ghosted i stride = ny*nz
+    int sy;               // ghosted j stride = nz
+    long long sxc;        // compact i stride = nyc*nzc
+    int syc;              // compact j stride = nzc
+    long long ng, n;      // ghosted and compact element counts
+};
+
+__host__ __device__ __forceinline__ long long icel(const Geo &g, int i, int j, int k)
+{
+    return (long long)i * g.sx + (long long)j * g.sy + k;
+}
+__host__ __device__ __forceinline__ long long icelcal(const Geo &g, int i, int j, int k)
+{
+    return (long long)(i - GC) * g.sxc + (long long)(j - GC) * g.syc + (k - GC);
+}
+
+// Per-axis metric table rows (table[row * n + index], n = ghosted length).
+enum AxRow {
+    AX_D = 0,   // cell width Dx
+    AX_DS,      // staggered width Dxs
+    AX_RD,      // 1 / Dx
+    AX_RDS,     // 1 / Dxs
+    AX_IT,      // face interpolation factor (Dxs*0.5)/Dx  (x_INTRPL, structureGrid.hpp:442)
+    AX_CAPP,    // QuickUnitA, Up > 0:  0.125*D[i+1]*D[i+1]/Ds[i]
+    AX_CAPN,    //             Up <= 0: 0.125*D[i+1]*D[i+1]/Ds[i+1]
+    AX_CANP,    //             Un > 0:  0.125*D[i]*D[i]/Ds[i-1]
+    AX_CANN,    //             Un <= 0: 0.125*D[i]*D[i]/Ds[i]
+    AX_CBPP,    // QuickUnitB, Up > 0:  0.125*Ds[i]*Ds[i]/D[i]
+    AX_CBPN,    //             Up <= 0: 0.125*Ds[i]*Ds[i]/D[i+1]
+    AX_CBNP,    //             Un > 0:  0.125*Ds[i-1]*Ds[i-1]/D[i-1]
+    AX_CBNN,    //             Un <= 0: 0.125*Ds[i-1]*Ds[i-1]/D[i]
+    AX_PM,      // Poisson -face coefficient 1/D[i]/Ds[i-1], zero on the first cell
+    AX_PP,      // Poisson +face coefficient 1/D[i]/Ds[i],   zero on the last cell
+    AX_ROWS
+};
+
+template <class T>
+struct Axis {
+    const T *t;
+    int n;
+    __device__ __forceinline__ T operator()(int row, int i) const { return __ldg(t + row * n + i); }
+};
+
+template <class T>
+struct Metrics {
+    Axis<T> x, y, z;
+};
+
+// ---- deterministic grid reductions --------------------------------------
+// Each block reduces NV values (warp shuffles, then warps in index order),
+// writes them to partials[q * gridDim.x + blockIdx.x], and takes a ticket.
+// The last block to arrive sums the partials in block order and returns
+// true with the totals in tot[] (valid in every thread of that block).  The
+// result does not depend on which block finishes last, so for a fixed launch
+// shape the sums are bitwise reproducible.
+template <int NV>
+__device__ __forceinline__ void warp_sum(double (&v)[NV])
+{
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
+}
+
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials,
+                                            unsigned int *counter, double (&tot)[NV])
+{
+    __shared__ double sm[32][NV];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    warp_sum<NV>(v);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sm[warp][q] = v[q];
+    __syncthreads();
+    if (warp == 0) {
+        double w[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? sm[lane][q] : 0.0;
+        warp_sum<NV>(w);
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) partials[q * gridDim.x + blockIdx.x] = w[q];
+            __threadfence();
+            unsigned int t = atomicAdd(counter, 1u);
+            last = (t == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        s[q] = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            s[q] += __ldcg(partials + q * gridDim.x + b);
+    }
+    warp_sum<NV>(s);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sm[warp][q] = s[q];
+    __syncthreads();
+    if (warp == 0) {
+        double w[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? sm[lane][q] : 0.0;
+        warp_sum<NV>(w);
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) sm[0][q] = w[q];
+            *counter = 0u;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) tot[q] = sm[0][q];
+    return true;
+}
+
+// Block-level max of a non-negative double folded into a global slot with an
+// order-independent atomicMax on the bit pattern (non-negative IEEE doubles
+// order like their unsigned bit patterns).  NaN propagates as the largest.
+__device__ __forceinline__ void grid_max_nonneg(double v, unsigned long long *slot)
+{
+    __shared__ double sm[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    unsigned long long b = (v != v) ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long o = __shfl_down_sync(0xffffffffu, b, off);
+        b = o > b ? o : b;
+    }
+    if (lane == 0) sm[warp] = __longlong_as_double((long long)b);
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long w = lane < nwarps ? (unsigned long long)__double_as_longlong(sm[lane]) : 0ull;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            unsigned long long o = __shfl_down_sync(0xffffffffu, w, off);
+            w = o > w ? o : w;
+        }
+        if (lane == 0 && w) atomicMax(slot, w);
+    }
+}
+
+// ---- launch helpers ------------------------------------------------------
+inline int blocks_for(long long n, int cap)
+{
+    long long b = (n + kBlock - 1) / kBlock;
+    if (b < 1) b = 1;
+    return (int)(b < cap ? b : cap);
+}
+
+}  // namespace cfd

@@ -1,0 +1,626 @@
+// flow.cu -- velocity-side kernels of the time step: QUICK convection-
+// diffusion, predictor-corrector source coupling, Poisson right-hand side,
+// projection + direct forcing, drag/lift, boundary conditions, immersed-body
+// volume fraction and the divergence check.  Templates on the velocity type
+// T (double for the FP64 path, float for the mixed-precision path); the
+// pressure, Poisson vectors and all reductions stay FP64.
+#include "cfd_internal.cuh"
+#include "kernels.h"
+
+namespace cfd {
+
+// ---------------------------------------------------------------------------
+// QUICK face values.  quick_a follows QuickUnitA and quick_b QuickUnitB
+// (inc/source/convection_and_difussion.hpp:20-84): the upwind choice picks
+// the curvature factor and the two one-sided gradients, then one formula
+// evaluates the face value.
+template <class T>
+__device__ __forceinline__ void quick_a(T Up, T Un, T pp, T p, T c, T n, T nn, const Axis<T> &a,
+                                        int I, T &phiP, T &phiN)
+{
+    const T pc = p - c, cn = c - n;
+    T cf, g1, r1, g2, r2;
+    if (Up > T(0)) { cf = a(AX_CAPP, I); g1 = pc;     r1 = a(AX_RD, I + 1); g2 = cn; r2 = a(AX_RD, I); }
+    else           { cf = a(AX_CAPN, I); g1 = pp - p; r1 = a(AX_RD, I + 2); g2 = pc; r2 = a(AX_RD, I + 1); }
+    phiP = T(0.5) * (c + p) - cf * (g1 * r1 - g2 * r2);
+    if (Un > T(0)) { cf = a(AX_CANP, I); g1 = cn; r1 = a(AX_RD, I);     g2 = n - nn; r2 = a(AX_RD, I - 1); }
+    else           { cf = a(AX_CANN, I); g1 = pc; r1 = a(AX_RD, I + 1); g2 = cn;     r2 = a(AX_RD, I); }
+    phiN = T(0.5) * (n + c) - cf * (g1 * r1 - g2 * r2);
+}
+
+template <class T>
+__device__ __forceinline__ void quick_b(T Up, T Un, T pp, T p, T c, T n, T nn, const Axis<T> &a,
+                                        int I, T &phiP, T &phiN)
+{
+    const T pc = p - c, cn = c - n;
+    T cf, g1, r1, g2, r2;
+    if (Up > T(0)) { cf = a(AX_CBPP, I); g1 = pc;     r1 = a(AX_RDS, I);     g2 = cn; r2 = a(AX_RDS, I - 1); }
+    else           { cf = a(AX_CBPN, I); g1 = pp - p; r1 = a(AX_RDS, I + 1); g2 = pc; r2 = a(AX_RDS, I); }
+    phiP = T(0.5) * (c + p) - cf * (g1 * r1 - g2 * r2);
+    if (Un > T(0)) { cf = a(AX_CBNP, I); g1 = cn; r1 = a(AX_RDS, I - 1); g2 = n - nn; r2 = a(AX_RDS, I - 2); }
+    else           { cf = a(AX_CBNN, I); g1 = pc; r1 = a(AX_RDS, I);     g2 = cn;     r2 = a(AX_RDS, I - 1); }
+    phiN = T(0.5) * (n + c) - cf * (g1 * r1 - g2 * r2);
+}
+
+__device__ __forceinline__ void cell_of(const Geo &g, long long t, int &i, int &j, int &k)
+{
+    const long long ii = t / g.sxc;
+    const long long rem = t - ii * g.sxc;
+    const int jj = (int)(rem / g.syc);
+    i = (int)ii + GC;
+    j = jj + GC;
+    k = (int)(rem - (long long)jj * g.syc) + GC;
+}
+
+// ConvectionDifussion (convection_and_difussion.hpp:168-446): explicit Euler
+// u* = u + dt(-div(u u) + nu lap u) for the three staggered components of
+// one cell per thread.  The normal component skips the domain's last face
+// (d = 1, lines 193, 274, 357).  With src != nullptr the PC source is added
+// at the same cell (aligned convention).
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_convdiff(Geo g, Metrics<T> m, T dt, T nudt, const T *__restrict__ u0, const T *__restrict__ v0,
+           const T *__restrict__ w0, T *__restrict__ u1, T *__restrict__ v1, T *__restrict__ w1,
+           const T *__restrict__ src)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const long long sx = g.sx, sy = g.sy;
+    const long long ic = icel(g, i, j, k);
+    const Axis<T> &X = m.x, &Y = m.y, &Z = m.z;
+    const T uc = __ldg(u0 + ic), vc = __ldg(v0 + ic), wc = __ldg(w0 + ic);
+    const T u_xp = __ldg(u0 + ic + sx), u_xm = __ldg(u0 + ic - sx);
+    const T v_yp = __ldg(v0 + ic + sy), v_ym = __ldg(v0 + ic - sy);
+    const T w_zp = __ldg(w0 + ic + 1), w_zm = __ldg(w0 + ic - 1);
+
+    if (i < g.nx - GC - 1) {  // ---- u, lines 196-269
+        const T IT = X(AX_IT, i);
+        const T Up = T(0.5) * (u_xp + uc), Un = T(0.5) * (u_xm + uc);
+        const T Vp = vc + (__ldg(v0 + ic + sx) - vc) * IT;
+        const T Vn = v_ym + (__ldg(v0 + ic - sy + sx) - v_ym) * IT;
+        const T Wp = wc + (__ldg(w0 + ic + sx) - wc) * IT;
+        const T Wn = w_zm + (__ldg(w0 + ic - 1 + sx) - w_zm) * IT;
+        const T u_yp = __ldg(u0 + ic + sy), u_ym = __ldg(u0 + ic - sy);
+        const T u_zp = __ldg(u0 + ic + 1), u_zm = __ldg(u0 + ic - 1);
+        T uPx, uNx, uPy, uNy, uPz, uNz;
+        quick_a(Up, Un, __ldg(u0 + ic + 2 * sx), u_xp, uc, u_xm, __ldg(u0 + ic - 2 * sx), X, i, uPx, uNx);
+        quick_b(Vp, Vn, __ldg(u0 + ic + 2 * sy), u_yp, uc, u_ym, __ldg(u0 + ic - 2 * sy), Y, j, uPy, uNy);
+        quick_b(Wp, Wn, __ldg(u0 + ic + 2), u_zp, uc, u_zm, __ldg(u0 + ic - 2), Z, k, uPz, uNz);
+        const T conv = -dt * ((uPx * uPx - uNx * uNx) * X(AX_RDS, i) + (uPy * Vp - uNy * Vn) * Y(AX_RD, j)
+                              + (uPz * Wp - uNz * Wn) * Z(AX_RD, k));
+        const T diff = nudt * (((u_xp - uc) * X(AX_RD, i + 1) - (uc - u_xm) * X(AX_RD, i)) * X(AX_RDS, i)
+                               + ((u_yp - uc) * Y(AX_RDS, j) - (uc - u_ym) * Y(AX_RDS, j - 1)) * Y(AX_RD, j)
+                               + ((u_zp - uc) * Z(AX_RDS, k) - (uc - u_zm) * Z(AX_RDS, k - 1)) * Z(AX_RD, k));
+        T r = uc + conv + diff;
+        if (src) r += src[t];
+        u1[ic] = r;
+    }
+    if (j < g.ny - GC - 1) {  // ---- v, lines 278-351
+        const T IT = Y(AX_IT, j);
+        const T Vp = T(0.5) * (v_yp + vc), Vn = T(0.5) * (v_ym + vc);
+        const T Up = uc + (__ldg(u0 + ic + sy) - uc) * IT;
+        const T Un = u_xm + (__ldg(u0 + ic - sx + sy) - u_xm) * IT;
+        const T Wp = wc + (__ldg(w0 + ic + sy) - wc) * IT;
+        const T Wn = w_zm + (__ldg(w0 + ic - 1 + sy) - w_zm) * IT;
+        const T v_xp = __ldg(v0 + ic + sx), v_xm = __ldg(v0 + ic - sx);
+        const T v_zp = __ldg(v0 + ic + 1), v_zm = __ldg(v0 + ic - 1);
+        T vPx, vNx, vPy, vNy, vPz, vNz;
+        quick_b(Up, Un, __ldg(v0 + ic + 2 * sx), v_xp, vc, v_xm, __ldg(v0 + ic - 2 * sx), X, i, vPx, vNx);
+        quick_a(Vp, Vn, __ldg(v0 + ic + 2 * sy), v_yp, vc, v_ym, __ldg(v0 + ic - 2 * sy), Y, j, vPy, vNy);
+        quick_b(Wp, Wn, __ldg(v0 + ic + 2), v_zp, vc, v_zm, __ldg(v0 + ic - 2), Z, k, vPz, vNz);
+        const T conv = -dt * ((Up * vPx - Un * vNx) * X(AX_RD, i) + (vPy * vPy - vNy * vNy) * Y(AX_RDS, j)
+                              + (Wp * vPz - Wn * vNz) * Z(AX_RD, k));
+        const T diff = nudt * (((v_xp - vc) * X(AX_RDS, i) - (vc - v_xm) * X(AX_RDS, i - 1)) * X(AX_RD, i)
+                               + ((v_yp - vc) * Y(AX_RD, j + 1) - (vc - v_ym) * Y(AX_RD, j)) * Y(AX_RDS, j)
+                               + ((v_zp - vc) * Z(AX_RDS, k) - (vc - v_zm) * Z(AX_RDS, k - 1)) * Z(AX_RD, k));
+        T r = vc + conv + diff;
+        if (src) r += src[g.n + t];
+        v1[ic] = r;
+    }
+    if (k < g.nz - GC - 1) {  // ---- w, lines 360-434
+        const T IT = Z(AX_IT, k);
+        const T Wp = T(0.5) * (w_zp + wc), Wn = T(0.5) * (w_zm + wc);
+        const T Up = uc + (__ldg(u0 + ic + 1) - uc) * IT;
+        const T Un = u_xm + (__ldg(u0 + ic - sx + 1) - u_xm) * IT;
+        const T Vp = vc + (__ldg(v0 + ic + 1) - vc) * IT;
+        const T Vn = v_ym + (__ldg(v0 + ic - sy + 1) - v_ym) * IT;
+        const T w_xp = __ldg(w0 + ic + sx), w_xm = __ldg(w0 + ic - sx);
+        const T w_yp = __ldg(w0 + ic + sy), w_ym = __ldg(w0 + ic - sy);
+        T wPx, wNx, wPy, wNy, wPz, wNz;
+        quick_b(Up, Un, __ldg(w0 + ic + 2 * sx), w_xp, wc, w_xm, __ldg(w0 + ic - 2 * sx), X, i, wPx, wNx);
+        quick_b(Vp, Vn, __ldg(w0 + ic + 2 * sy), w_yp, wc, w_ym, __ldg(w0 + ic - 2 * sy), Y, j, wPy, wNy);
+        quick_a(Wp, Wn, __ldg(w0 + ic + 2), w_zp, wc, w_zm, __ldg(w0 + ic - 2), Z, k, wPz, wNz);
+        const T conv = -dt * ((Up * wPx - Un * wNx) * X(AX_RD, i) + (Vp * wPy - Vn * wNy) * Y(AX_RD, j)
+                              + (wPz * wPz - wNz * wNz) * Z(AX_RDS, k));
+        const T diff = nudt * (((w_xp - wc) * X(AX_RDS, i) - (wc - w_xm) * X(AX_RDS, i - 1)) * X(AX_RD, i)
+                               + ((w_yp - wc) * Y(AX_RDS, j) - (wc - w_ym) * Y(AX_RDS, j - 1)) * Y(AX_RD, j)
+                               + ((w_zp - wc) * Z(AX_RD, k + 1) - (wc - w_zm) * Z(AX_RD, k)) * Z(AX_RDS, k));
+        T r = wc + conv + diff;
+        if (src) r += src[2 * g.n + t];
+        w1[ic] = r;
+    }
+}
+
+// Source coupling with the reference's index convention
+// (RUN_CPU_PC_METHOD.hpp:309-316): element m of the ghosted array gets
+// src[m] for m < N.
+template <class T>
+__global__ void k_src_add_ref(long long n, T *__restrict__ u1, T *__restrict__ v1, T *__restrict__ w1,
+                              const T *__restrict__ src)
+{
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n;
+         m += (long long)gridDim.x * blockDim.x) {
+        u1[m] += src[m];
+        v1[m] += src[n + m];
+        w1[m] += src[2 * n + m];
+    }
+}
+
+template <class T>
+__global__ void k_src_add_aligned(Geo g, T *__restrict__ u1, T *__restrict__ v1, T *__restrict__ w1,
+                                  const T *__restrict__ src)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const long long ic = icel(g, i, j, k);
+    u1[ic] += src[t];
+    v1[ic] += src[g.n + t];
+    w1[ic] += src[2 * g.n + t];
+}
+
+// source_termF += dt * f (RUN_CPU_PC_METHOD.hpp:393-401)
+template <class T>
+__global__ void k_src_accumulate(long long n3, T dt, T *__restrict__ src, const T *__restrict__ f)
+{
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n3;
+         m += (long long)gridDim.x * blockDim.x)
+        src[m] += dt * f[m];
+}
+
+// createBMatrix_omp (b_matrix.hpp:76-79): b = -jp (1/dt) div u*.  With
+// partials != nullptr it also reduces sum(dV * d) and sum(dV) with
+// d = -(1/dt) div u* for the compatibility projection; the last block stores
+// mean = sum(dV d)/sum(dV) in *mean.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_rhs(Geo g, Metrics<double> m, double ddt, const double *__restrict__ jp, const T *__restrict__ u1,
+      const T *__restrict__ v1, const T *__restrict__ w1, double *__restrict__ b, double *partials,
+      unsigned int *counter, double *mean)
+{
+    double acc[2] = {0.0, 0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        const double div = ((double)u1[ic] - (double)u1[ic - g.sx]) * m.x(AX_RD, i)
+                         + ((double)v1[ic] - (double)v1[ic - g.sy]) * m.y(AX_RD, j)
+                         + ((double)w1[ic] - (double)w1[ic - 1]) * m.z(AX_RD, k);
+        b[t] = -jp[t] * ddt * div;
+        if (partials) {
+            const double vol = m.x(AX_D, i) * m.y(AX_D, j) * m.z(AX_D, k);
+            acc[0] += vol * (-ddt * div);
+            acc[1] += vol;
+        }
+    }
+    if (!partials) return;
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) *mean = tot[0] / tot[1];
+}
+
+// b -= jp * mean
+__global__ void k_rhs_compat(long long n, const double *__restrict__ jp, const double *__restrict__ mean,
+                             double *__restrict__ b)
+{
+    const double mu = *mean;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x)
+        b[t] = b[t] - jp[t] * mu;
+}
+
+// Pressure_transform_X_result (Transform.hpp:8-24)
+__global__ void k_transform(Geo g, const double *__restrict__ x, double *__restrict__ p)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    p[icel(g, i, j, k)] = x[t];
+}
+
+// update_UandF_omp (updateUandF.hpp:95-190): T2 = u* - dt grad p;
+// u = eta*uS + (1 - eta_face) T2 with uS = 0; f = (u - T2)/dt.  One cell per
+// thread, all three components; the last normal face is skipped.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_update_uf(Geo g, Metrics<T> m, double dt, T rdt, const double *__restrict__ p,
+            const T *__restrict__ eta, const T *__restrict__ u1, const T *__restrict__ v1,
+            const T *__restrict__ w1, T *__restrict__ u3, T *__restrict__ v3, T *__restrict__ w3,
+            T *__restrict__ f)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const long long ic = icel(g, i, j, k);
+    const double pc = p[ic];
+    const T ec = eta[ic];
+    if (i < g.nx - GC - 1) {
+        const T T2 = u1[ic] - (T)(dt * (p[ic + g.sx] - pc)) * m.x(AX_RDS, i);
+        const T ef = ec + (eta[ic + g.sx] - ec) * m.x(AX_IT, i);
+        const T un = (T(1) - ef) * T2;
+        u3[ic] = un;
+        f[t] = (un - T2) * rdt;
+    }
+    if (j < g.ny - GC - 1) {
+        const T T2 = v1[ic] - (T)(dt * (p[ic + g.sy] - pc)) * m.y(AX_RDS, j);
+        const T ef = ec + (eta[ic + g.sy] - ec) * m.y(AX_IT, j);
+        const T vn = (T(1) - ef) * T2;
+        v3[ic] = vn;
+        f[g.n + t] = (vn - T2) * rdt;
+    }
+    if (k < g.nz - GC - 1) {
+        const T T2 = w1[ic] - (T)(dt * (p[ic + 1] - pc)) * m.z(AX_RDS, k);
+        const T ef = ec + (eta[ic + 1] - ec) * m.z(AX_IT, k);
+        const T wn = (T(1) - ef) * T2;
+        w3[ic] = wn;
+        f[2 * g.n + t] = (wn - T2) * rdt;
+    }
+}
+
+// virtualF_Int (virtualForceIntergrator.hpp:26-32) for x and y at once:
+// out[0] = Cd = -2 sum(f_x dV)/lz, out[1] = Cl = -2 sum(f_y dV)/lz.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_cdcl(Geo g, Metrics<double> m, double lz, const T *__restrict__ f, double *partials,
+       unsigned int *counter, double *out)
+{
+    double acc[2] = {0.0, 0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const double vol = m.x(AX_D, i) * m.y(AX_D, j) * m.z(AX_D, k);
+        acc[0] += (double)f[t] * vol;
+        acc[1] += (double)f[g.n + t] * vol;
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        out[0] = -2.0 * tot[0] / lz;
+        out[1] = -2.0 * tot[1] / lz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BC_staggered_main (Boundary_Condition.hpp:37-175).  The faces depend on
+// each other through the interior faces that faces 1, 3 and 5 overwrite, so
+// the update runs as three launches in the reference's single-thread order:
+// phase 0 = faces 0/1, phase 1 = faces 2/3, phase 2 = faces 4/5.  Products
+// and sums use explicit round-to-nearest intrinsics (no fused multiply-add),
+// which makes the ghost values bitwise equal to the reference's.
+template <class T> __device__ __forceinline__ T mul_rn(T a, T b);
+template <class T> __device__ __forceinline__ T add_rn(T a, T b);
+template <> __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
+template <class T>
+__device__ __forceinline__ T bc_norm(const BcTab &bc, int b, int c, T x)
+{   // normal component: Dir + Num * interior
+    return add_rn((T)bc.dir[b * 3 + c], mul_rn((T)bc.num[b * 3 + c], x));
+}
+template <class T>
+__device__ __forceinline__ T bc_tan(const BcTab &bc, int b, int c, T x)
+{   // tangential component: 2 Dir + (2 Num - 1) * interior
+    return add_rn((T)(bc.dir[b * 3 + c] * 2.), mul_rn((T)(2.0 * bc.num[b * 3 + c] - 1.0), x));
+}
+
+template <class T>
+__global__ void k_bc_main(Geo g, BcTab bc, int phase, T *__restrict__ u, T *__restrict__ v,
+                          T *__restrict__ w, double *__restrict__ p)
+{
+    // phase 0: (a,b) = (j,k); phase 1: (i,k); phase 2: (i,j); all interior
+    const int na = phase == 0 ? g.nyc : g.nxc;
+    const int nb = phase == 2 ? g.nyc : g.nzc;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)na * nb) return;
+    const int a = (int)(t / nb) + GC, b = (int)(t % nb) + GC;
+    if (phase == 0) {
+        const int j = a, k = b, nx = g.nx;
+        auto I = [&](int i) { return icel(g, i, j, k); };
+        T x = bc_norm<T>(bc, 0, 0, u[I(2)]); u[I(1)] = x; u[I(0)] = x;
+        x = bc_tan<T>(bc, 0, 1, v[I(2)]); v[I(1)] = x; v[I(0)] = x;
+        x = bc_tan<T>(bc, 0, 2, w[I(2)]); w[I(1)] = x; w[I(0)] = x;
+        x = bc_norm<T>(bc, 1, 0, u[I(nx - 4)]); u[I(nx - 3)] = x; u[I(nx - 2)] = x; u[I(nx - 1)] = x;
+        x = bc_tan<T>(bc, 1, 1, v[I(nx - 3)]); v[I(nx - 2)] = x; v[I(nx - 1)] = x;
+        x = bc_tan<T>(bc, 1, 2, w[I(nx - 3)]); w[I(nx - 2)] = x; w[I(nx - 1)] = x;
+        double q = p[I(2)]; p[I(1)] = q; p[I(0)] = q;
+        q = p[I(nx - 3)]; p[I(nx - 2)] = q; p[I(nx - 1)] = q;
+    } else if (phase == 1) {
+        const int i = a, k = b, ny = g.ny;
+        auto J = [&](int j) { return icel(g, i, j, k); };
+        T x = bc_tan<T>(bc, 2, 0, u[J(2)]); u[J(1)] = x; u[J(0)] = x;
+        x = bc_norm<T>(bc, 2, 1, v[J(2)]); v[J(1)] = x; v[J(0)] = x;
+        x = bc_tan<T>(bc, 2, 2, w[J(2)]); w[J(1)] = x; w[J(0)] = x;
+        x = bc_norm<T>(bc, 3, 1, v[J(ny - 4)]); v[J(ny - 3)] = x; v[J(ny - 2)] = x; v[J(ny - 1)] = x;
+        x = bc_tan<T>(bc, 3, 0, u[J(ny - 3)]); u[J(ny - 2)] = x; u[J(ny - 1)] = x;
+        x = bc_tan<T>(bc, 3, 2, w[J(ny - 3)]); w[J(ny - 2)] = x; w[J(ny - 1)] = x;
+        double q = p[J(2)]; p[J(1)] = q; p[J(0)] = q;
+        q = p[J(ny - 3)]; p[J(ny - 2)] = q; p[J(ny - 1)] = q;
+    } else {
+        const int i = a, j = b, nz = g.nz;
+        auto K = [&](int k) { return icel(g, i, j, k); };
+        T x = bc_tan<T>(bc, 4, 0, u[K(2)]); u[K(1)] = x; u[K(0)] = x;
+        x = bc_tan<T>(bc, 4, 1, v[K(2)]); v[K(1)] = x; v[K(0)] = x;
+        x = bc_norm<T>(bc, 4, 2, w[K(2)]); w[K(1)] = x; w[K(0)] = x;
+        x = bc_norm<T>(bc, 5, 2, w[K(nz - 4)]); w[K(nz - 3)] = x; w[K(nz - 2)] = x; w[K(nz - 1)] = x;
+        x = bc_tan<T>(bc, 5, 0, u[K(nz - 3)]); u[K(nz - 2)] = x; u[K(nz - 1)] = x;
+        x = bc_tan<T>(bc, 5, 1, v[K(nz - 3)]); v[K(nz - 2)] = x; v[K(nz - 1)] = x;
+        double q = p[K(2)]; p[K(1)] = q; p[K(0)] = q;
+        q = p[K(nz - 3)]; p[K(nz - 2)] = q; p[K(nz - 1)] = q;
+    }
+}
+
+// BC_staggered_copy (updateBC.hpp:6-111): the three face sets are disjoint,
+// so one launch covers them (blockIdx.y = face pair).
+template <class T>
+__global__ void k_bc_copy(Geo g, const T *__restrict__ uo, const T *__restrict__ vo,
+                          const T *__restrict__ wo, T *__restrict__ u, T *__restrict__ v,
+                          T *__restrict__ w)
+{
+    const int phase = blockIdx.y;
+    const int na = phase == 0 ? g.nyc : g.nxc;
+    const int nb = phase == 2 ? g.nyc : g.nzc;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)na * nb) return;
+    const int a = (int)(t / nb) + GC, b = (int)(t % nb) + GC;
+    long long s[8];  // ghost / boundary positions along the face normal
+    int e;           // last index along the normal axis (n - 1)
+    long long stride, base;
+    if (phase == 0) { e = g.nx - 1; stride = g.sx; base = icel(g, 0, a, b); }
+    else if (phase == 1) { e = g.ny - 1; stride = g.sy; base = icel(g, a, 0, b); }
+    else { e = g.nz - 1; stride = 1; base = icel(g, a, b, 0); }
+    s[0] = base;
+    s[1] = base + stride;
+    s[2] = base + (long long)(e - 1) * stride;
+    s[3] = base + (long long)e * stride;
+    s[4] = base + (long long)(e - 2) * stride;  // last interior normal face
+    for (int q = 0; q < 4; ++q) { u[s[q]] = uo[s[q]]; v[s[q]] = vo[s[q]]; w[s[q]] = wo[s[q]]; }
+    if (phase == 0) u[s[4]] = uo[s[4]];
+    else if (phase == 1) v[s[4]] = vo[s[4]];
+    else w[s[4]] = wo[s[4]];
+}
+
+// ---------------------------------------------------------------------------
+// DFIB_CylinderZ (setEta.hpp:136-204).  One block per (i, j) column of the
+// k = 0 plane; the cut-cell sub-sampling is spread over the block and the
+// inside count is an exact integer sum.  All arithmetic uses explicit
+// round-to-nearest operations, so eta is bitwise the reference's.
+__global__ void k_eta_plane(Geo g, const double *__restrict__ X, const double *__restrict__ Y,
+                            const double *__restrict__ Dx, const double *__restrict__ Dy, double cx,
+                            double cy, double radius, int nsub, double scale, double *__restrict__ eta)
+{
+    const int i = blockIdx.x + GC, j = blockIdx.y + GC;
+    const long long ic = icel(g, i, j, 0);
+    const double diag = __dmul_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(Dx[i], Dx[i]), __dmul_rn(Dy[j], Dy[j]))), 0.5);
+    const double ex = __dsub_rn(__dmul_rn(__dadd_rn(X[i], X[i + 1]), 0.5), cx);
+    const double ey = __dsub_rn(__dmul_rn(__dadd_rn(Y[j], Y[j + 1]), 0.5), cy);
+    const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)));
+    if (!(fabs(__dsub_rn(dist, radius)) < diag)) {
+        if (threadIdx.x == 0) eta[ic] = dist > radius ? 0.0 : 1.0;
+        return;
+    }
+    const double dxg = __ddiv_rn(Dx[i], (double)nsub), dyg = __ddiv_rn(Dy[j], (double)nsub);
+    unsigned int cnt = 0;
+    const int total = nsub * nsub;
+    for (int s = threadIdx.x; s < total; s += blockDim.x) {
+        const int ii = s / nsub, jj = s - ii * nsub;
+        const double x0 = __dadd_rn(X[i], __dmul_rn((double)ii, dxg));
+        const double x1 = __dadd_rn(X[i], __dmul_rn((double)(ii + 1), dxg));
+        const double y0 = __dadd_rn(Y[j], __dmul_rn((double)jj, dyg));
+        const double y1 = __dadd_rn(Y[j], __dmul_rn((double)(jj + 1), dyg));
+        const double a = __dsub_rn(__dmul_rn(__dadd_rn(x0, x1), 0.5), cx);
+        const double b = __dsub_rn(__dmul_rn(__dadd_rn(y0, y1), 0.5), cy);
+        if (__dsqrt_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b))) <= radius) ++cnt;
+    }
+    __shared__ unsigned int sm[32];
+    for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int c = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) c += sm[q];
+        eta[ic] = __dmul_rn((double)c, scale);
+    }
+}
+
+// eta(i,j,k) = eta(i,j,0) for i < nx-1, j < ny-1, 1 <= k < nz-1 (setEta.hpp:200-203)
+__global__ void k_eta_extrude(Geo g, double *__restrict__ eta)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nij = (long long)(g.nx - 1) * (g.ny - 1);
+    if (t >= nij * (g.nz - 2)) return;
+    const int k = (int)(t / nij) + 1;
+    const long long ij = t % nij;
+    const int i = (int)(ij / (g.ny - 1)), j = (int)(ij % (g.ny - 1));
+    eta[icel(g, i, j, k)] = eta[icel(g, i, j, 0)];
+}
+
+// max |div u| over interior cells in FP64
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_div_inf(Geo g, Metrics<double> m, const T *__restrict__ u, const T *__restrict__ v,
+          const T *__restrict__ w, unsigned long long *slot)
+{
+    double mx = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        const double d = ((double)u[ic] - (double)u[ic - g.sx]) * m.x(AX_RD, i)
+                       + ((double)v[ic] - (double)v[ic - g.sy]) * m.y(AX_RD, j)
+                       + ((double)w[ic] - (double)w[ic - 1]) * m.z(AX_RD, k);
+        const double a = fabs(d);
+        mx = (a > mx || a != a) ? a : mx;
+    }
+    grid_max_nonneg(mx, slot);
+}
+
+template <class T>
+__global__ void k_fill(long long n, T *__restrict__ a, T val)
+{
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n;
+         m += (long long)gridDim.x * blockDim.x)
+        a[m] = val;
+}
+
+template <class A, class B>
+__global__ void k_convert(long long n, const A *__restrict__ a, B *__restrict__ b)
+{
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n;
+         m += (long long)gridDim.x * blockDim.x)
+        b[m] = (B)a[m];
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+static inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
+
+template <class T>
+void launch_convdiff(cudaStream_t s, const Geo &g, const Metrics<T> &m, T dt, T nudt, const T *u0,
+                     const T *v0, const T *w0, T *u1, T *v1, T *w1, const T *src_aligned)
+{
+    k_convdiff<T><<<nblk(g.n), kBlock, 0, s>>>(g, m, dt, nudt, u0, v0, w0, u1, v1, w1, src_aligned);
+}
+
+template <class T>
+void launch_src_add(cfd_launch_ctx &c, const Geo &g, int aligned, T *u1, T *v1, T *w1, const T *src)
+{
+    if (aligned)
+        k_src_add_aligned<T><<<nblk(g.n), kBlock, 0, c.s>>>(g, u1, v1, w1, src);
+    else
+        k_src_add_ref<T><<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g.n, u1, v1, w1, src);
+}
+
+template <class T>
+void launch_src_accumulate(cfd_launch_ctx &c, long long n3, T dt, T *src, const T *f)
+{
+    k_src_accumulate<T><<<blocks_for(n3, c.grid_cap), kBlock, 0, c.s>>>(n3, dt, src, f);
+}
+
+template <class T>
+void launch_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double ddt,
+                const double *jp, const T *u1, const T *v1, const T *w1, double *b, bool compat,
+                double *mean)
+{
+    if (compat) {
+        k_rhs<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, ddt, jp, u1, v1, w1, b, c.partials,
+                                                     c.counter, mean);
+        k_rhs_compat<<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g.n, jp, mean, b);
+    } else {
+        k_rhs<T><<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g, m, ddt, jp, u1, v1, w1, b, nullptr,
+                                                                   nullptr, nullptr);
+    }
+}
+
+void launch_transform(cudaStream_t s, const Geo &g, const double *x, double *p)
+{
+    k_transform<<<nblk(g.n), kBlock, 0, s>>>(g, x, p);
+}
+
+template <class T>
+void launch_update_uf(cudaStream_t s, const Geo &g, const Metrics<T> &m, double dt, T rdt,
+                      const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3,
+                      T *v3, T *w3, T *f)
+{
+    k_update_uf<T><<<nblk(g.n), kBlock, 0, s>>>(g, m, dt, rdt, p, eta, u1, v1, w1, u3, v3, w3, f);
+}
+
+template <class T>
+void launch_cdcl(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double lz, const T *f,
+                 double *out2)
+{
+    k_cdcl<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, lz, f, c.partials, c.counter, out2);
+}
+
+template <class T>
+void launch_bc_main(cudaStream_t s, const Geo &g, const BcTab &bc, T *u, T *v, T *w, double *p)
+{
+    k_bc_main<T><<<nblk((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, bc, 0, u, v, w, p);
+    k_bc_main<T><<<nblk((long long)g.nxc * g.nzc), kBlock, 0, s>>>(g, bc, 1, u, v, w, p);
+    k_bc_main<T><<<nblk((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, bc, 2, u, v, w, p);
+}
+
+template <class T>
+void launch_bc_copy(cudaStream_t s, const Geo &g, const T *uo, const T *vo, const T *wo, T *u, T *v,
+                    T *w)
+{
+    long long mx = (long long)g.nyc * g.nzc;
+    if ((long long)g.nxc * g.nzc > mx) mx = (long long)g.nxc * g.nzc;
+    if ((long long)g.nxc * g.nyc > mx) mx = (long long)g.nxc * g.nyc;
+    dim3 grid(nblk(mx), 3);
+    k_bc_copy<T><<<grid, kBlock, 0, s>>>(g, uo, vo, wo, u, v, w);
+}
+
+void launch_eta_cylinder_z(cudaStream_t s, const Geo &g, const double *X, const double *Y,
+                           const double *Dx, const double *Dy, double cx, double cy, double radius,
+                           int nsub, double scale, double *eta)
+{
+    dim3 grid(g.nxc, g.nyc);
+    k_eta_plane<<<grid, kBlock, 0, s>>>(g, X, Y, Dx, Dy, cx, cy, radius, nsub, scale, eta);
+    const long long n = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 2);
+    k_eta_extrude<<<nblk(n), kBlock, 0, s>>>(g, eta);
+}
+
+template <class T>
+void launch_div_inf(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const T *u,
+                    const T *v, const T *w, unsigned long long *slot)
+{
+    k_div_inf<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, u, v, w, slot);
+}
+
+template <class T>
+void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val)
+{
+    k_fill<T><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, val);
+}
+
+template <class A, class B>
+void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b)
+{
+    k_convert<A, B><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, b);
+}
+
+#define CFD_FLOW_INSTANTIATE(T)                                                                   \
+    template void launch_convdiff<T>(cudaStream_t, const Geo &, const Metrics<T> &, T, T,        \
+                                     const T *, const T *, const T *, T *, T *, T *, const T *); \
+    template void launch_src_add<T>(cfd_launch_ctx &, const Geo &, int, T *, T *, T *, const T *); \
+    template void launch_src_accumulate<T>(cfd_launch_ctx &, long long, T, T *, const T *);      \
+    template void launch_rhs<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double,  \
+                                const double *, const T *, const T *, const T *, double *, bool, \
+                                double *);                                                       \
+    template void launch_update_uf<T>(cudaStream_t, const Geo &, const Metrics<T> &, double, T,  \
+                                      const double *, const T *, const T *, const T *, const T *, \
+                                      T *, T *, T *, T *);                                       \
+    template void launch_cdcl<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double, \
+                                 const T *, double *);                                           \
+    template void launch_bc_main<T>(cudaStream_t, const Geo &, const BcTab &, T *, T *, T *,     \
+                                    double *);                                                   \
+    template void launch_bc_copy<T>(cudaStream_t, const Geo &, const T *, const T *, const T *,  \
+                                    T *, T *, T *);                                              \
+    template void launch_div_inf<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,      \
+                                    const T *, const T *, const T *, unsigned long long *);      \
+    template void launch_fill<T>(cfd_launch_ctx &, long long, T *, T);
+
+CFD_FLOW_INSTANTIATE(double)
+CFD_FLOW_INSTANTIATE(float)
+template void launch_convert<double, float>(cfd_launch_ctx &, long long, const double *, float *);
+template void launch_convert<float, double>(cfd_launch_ctx &, long long, const float *, double *);
+
+}  // namespace cfd

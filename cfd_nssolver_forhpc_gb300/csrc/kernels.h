@@ -1,0 +1,143 @@
+// kernels.h -- host-side launch interface of the kernels (flow.cu, poisson.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cfd_internal.cuh"
+
+namespace cfd {
+
+struct BcTab {
+    double dir[18];
+    double num[18];
+};
+
+// What a launcher needs besides its arguments: the stream, the fixed shape
+// of reduction launches (so sums are reproducible) and their scratch.
+struct cfd_launch_ctx {
+    cudaStream_t s;
+    int red_blocks;         // grid size of every reducing launch
+    int grid_cap;           // cap for grid-stride elementwise launches
+    double *partials;       // >= 4 * red_blocks doubles
+    unsigned int *counter;  // last-block ticket, zero between launches
+};
+
+// ---- flow.cu ----
+template <class T>
+void launch_convdiff(cudaStream_t s, const Geo &g, const Metrics<T> &m, T dt, T nudt, const T *u0,
+                     const T *v0, const T *w0, T *u1, T *v1, T *w1, const T *src_aligned);
+template <class T>
+void launch_src_add(cfd_launch_ctx &c, const Geo &g, int aligned, T *u1, T *v1, T *w1, const T *src);
+template <class T>
+void launch_src_accumulate(cfd_launch_ctx &c, long long n3, T dt, T *src, const T *f);
+template <class T>
+void launch_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double ddt,
+                const double *jp, const T *u1, const T *v1, const T *w1, double *b, bool compat,
+                double *mean);
+void launch_transform(cudaStream_t s, const Geo &g, const double *x, double *p);
+template <class T>
+void launch_update_uf(cudaStream_t s, const Geo &g, const Metrics<T> &m, double dt, T rdt,
+                      const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3,
+                      T *v3, T *w3, T *f);
+template <class T>
+void launch_cdcl(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double lz, const T *f,
+                 double *out2);
+template <class T>
+void launch_bc_main(cudaStream_t s, const Geo &g, const BcTab &bc, T *u, T *v, T *w, double *p);
+template <class T>
+void launch_bc_copy(cudaStream_t s, const Geo &g, const T *uo, const T *vo, const T *wo, T *u, T *v,
+                    T *w);
+void launch_eta_cylinder_z(cudaStream_t s, const Geo &g, const double *X, const double *Y,
+                           const double *Dx, const double *Dy, double cx, double cy, double radius,
+                           int nsub, double scale, double *eta);
+template <class T>
+void launch_div_inf(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const T *u,
+                    const T *v, const T *w, unsigned long long *slot);
+template <class T>
+void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val);
+template <class A, class B>
+void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b);
+
+// ---- poisson.cu ----
+
+// Matrix-free Jacobi-scaled 7-point operator (SPE_matrix1 with jp_on_):
+// (A x)_r = x_r - jp_r * (sum over the six neighbours of c_nb x_nb), with the
+// per-axis coefficients zeroed on the faces where the neighbour does not
+// exist (SPE_sparseMatrix1.hpp:126-144).
+template <class V>
+struct SpeOp {
+    const V *cxm, *cxp, *cym, *cyp, *czm, *czp;  // interior-length axes
+    const V *jp;                                  // compact
+    int nxc, nyc, nzc;
+    long long sxc;
+    long long n;
+};
+
+// ELL operator, slot-major: vals[s * n + row], cols[s * n + row], s < 7
+template <class V>
+struct EllOp {
+    const int *cols;
+    const V *vals;
+    long long n;
+};
+
+// Device scalars of one BiCGSTAB solve (the locals of bicgstabRe2::solve
+// plus its persistent counters).
+struct BicgScal {
+    double norm0, rho, alpha, omega, beta, relres, tol, restart_tol;
+    int iter, done, restart, timestep, maxit, restarts, total_iters, nonfinite;
+};
+enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
+
+// Work vectors of one BiCGSTAB instance (precision V).
+template <class V>
+struct BicgVecs {
+    V *r0, *r1, *p1, *s1, *ap, *as;
+};
+
+void launch_spe_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
+                      const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
+                      double *cx, double *cy, double *cz, double *jp);
+void launch_ell_assemble(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
+                         const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
+                         int *cols, double *vals, double *jp);
+
+template <class Op>
+void launch_apply(cfd_launch_ctx &c, const Op &A, const double *x, double *r);
+
+// one BiCGSTAB solve: init kernel then the iteration kernels (bicgstabRe2.hpp:93-189)
+template <class Op, class V>
+void launch_bicg_init(cfd_launch_ctx &c, const Op &A, const V *b, V *x, const BicgVecs<V> &w,
+                      V *px1, V *px2, BicgScal *sc);
+template <class Op, class V>
+void launch_bicg_iteration(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc);
+// one kernel of the iteration (0 ap, 1 s, 2 as, 3 xr, 4 p), for timing
+template <class Op, class V>
+void launch_bicg_iteration_part(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc,
+                                int part);
+template <class V>
+void launch_bicg_nan_reset(cfd_launch_ctx &c, long long n, V *x, const V *px1, const V *px2,
+                           BicgScal *sc);
+
+// SorPipeLine (SorPipeLine.seq.hpp), red-black ordered
+void launch_sor_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
+                      const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
+                      double *cf7);
+template <class T>
+void launch_sor_rhs(cudaStream_t s, const Geo &g, const Metrics<double> &m, double rdt, const T *u1,
+                    const T *v1, const T *w1, double *cf6);
+void launch_sor_sweep(cudaStream_t s, const Geo &g, const Metrics<double> &m, const double *cf6,
+                      const double *cf7, double *p, double omega, double tol, int itmax, int sweep,
+                      unsigned long long *res, int *state);
+
+// mixed precision pieces
+template <class V>
+void launch_residual64(cfd_launch_ctx &c, const SpeOp<double> &A, const double *b, const double *x,
+                       V *r32, double *norm2_out);
+template <class V>
+void launch_residual64_ell(cfd_launch_ctx &c, const EllOp<double> &A, const double *b,
+                           const double *x, V *r32, double *norm2_out);
+template <class V>
+void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e);
+
+}  // namespace cfd

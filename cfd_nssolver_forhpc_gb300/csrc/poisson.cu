@@ -1,0 +1,605 @@
+// poisson.cu -- pressure Poisson solve on the device: operator assembly
+// (matrix-free SPE_matrix1 and device-resident ELL), SpMV, the BiCGSTAB of
+// bicgstabRe2 split into fused kernels with device-resident scalars, the
+// red-black SOR of SorPipeLine, and the FP64 residual / correction kernels of
+// the mixed-precision defect correction.
+//
+// Every reducing kernel uses the deterministic last-block reduction of
+// cfd_internal.cuh and a fixed launch shape, so a solve is bitwise
+// reproducible run to run.  Kernels of an iteration return at once when the
+// solve has finished (BicgScal::done), so the host may queue iterations
+// ahead of the convergence test.
+#include "cfd_internal.cuh"
+#include "kernels.h"
+
+namespace cfd {
+
+// ---------------------------------------------------------------------------
+// operator application
+template <class V>
+__device__ __forceinline__ V apply_row(const SpeOp<V> &A, const V *__restrict__ x, long long row)
+{
+    const int i = (int)(row / A.sxc);
+    const long long rem = row - (long long)i * A.sxc;
+    const int j = (int)(rem / A.nzc);
+    const int k = (int)(rem - (long long)j * A.nzc);
+    const long long xw = i > 0 ? row - A.sxc : row;
+    const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
+    const long long ys = j > 0 ? row - A.nzc : row;
+    const long long yn = j < A.nyc - 1 ? row + A.nzc : row;
+    const long long zb = k > 0 ? row - 1 : row;
+    const long long zt = k < A.nzc - 1 ? row + 1 : row;
+    V s = __ldg(A.cxm + i) * x[xw];
+    s = fma(__ldg(A.cym + j), x[ys], s);
+    s = fma(__ldg(A.czm + k), x[zb], s);
+    s = fma(__ldg(A.czp + k), x[zt], s);
+    s = fma(__ldg(A.cyp + j), x[yn], s);
+    s = fma(__ldg(A.cxp + i), x[xe], s);
+    return fma(-A.jp[row], s, x[row]);
+}
+
+template <class V>
+__device__ __forceinline__ V apply_row(const EllOp<V> &A, const V *__restrict__ x, long long row)
+{
+    V s = V(0);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const long long o = (long long)q * A.n + row;
+        s = fma(__ldg(A.vals + o), x[__ldg(A.cols + o)], s);
+    }
+    return s;
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kBlock) k_apply(Op A, const double *__restrict__ x, double *__restrict__ r)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x)
+        r[row] = apply_row(A, x, row);
+}
+
+// ---------------------------------------------------------------------------
+// SPE_matrix1::setupPressure + set_Jp_pc (SPE_sparseMatrix1.hpp:40-121).
+// c{x,y,z} hold [minus-face | plus-face] coefficients of interior length,
+// zeroed where the neighbour does not exist; jp = 1/diag with the
+// reference's summation order, so it is bitwise the reference's jp.
+__device__ __forceinline__ double inv2(double a, double b) { return __ddiv_rn(__ddiv_rn(1.0, a), b); }
+
+__global__ void k_spe_axes(int n, const double *__restrict__ D, const double *__restrict__ Ds,
+                           double *__restrict__ c)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    c[i] = i == 0 ? 0.0 : inv2(D[i + GC], Ds[i + GC - 1]);
+    c[n + i] = i == n - 1 ? 0.0 : inv2(D[i + GC], Ds[i + GC]);
+}
+
+__global__ void k_spe_jp(Geo g, const double *__restrict__ Dx, const double *__restrict__ Dy,
+                         const double *__restrict__ Dz, const double *__restrict__ Dxs,
+                         const double *__restrict__ Dys, const double *__restrict__ Dzs,
+                         double *__restrict__ jp)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < g.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(row / g.sxc);
+        const long long rem = row - (long long)i * g.sxc;
+        const int j = (int)(rem / g.nzc), k = (int)(rem - (long long)j * g.nzc);
+        const double xm = inv2(Dx[i + GC], Dxs[i + GC - 1]), xp = inv2(Dx[i + GC], Dxs[i + GC]);
+        const double ym = inv2(Dy[j + GC], Dys[j + GC - 1]), yp = inv2(Dy[j + GC], Dys[j + GC]);
+        const double zm = inv2(Dz[k + GC], Dzs[k + GC - 1]), zp = inv2(Dz[k + GC], Dzs[k + GC]);
+        double v = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(xm, ym), zm), xp), yp), zp);
+        if (i == 0) v = __dsub_rn(v, xm);
+        if (i == g.nxc - 1) v = __dsub_rn(v, xp);
+        if (j == 0) v = __dsub_rn(v, ym);
+        if (j == g.nyc - 1) v = __dsub_rn(v, yp);
+        if (k == 0) v = __dsub_rn(v, zm);
+        if (k == g.nzc - 1) v = __dsub_rn(v, zp);
+        jp[row] = __ddiv_rn(1.0, v);
+    }
+}
+
+void launch_spe_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
+                      const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
+                      double *cx, double *cy, double *cz, double *jp)
+{
+    k_spe_axes<<<(g.nxc + 127) / 128, 128, 0, s>>>(g.nxc, Dx, Dxs, cx);
+    k_spe_axes<<<(g.nyc + 127) / 128, 128, 0, s>>>(g.nyc, Dy, Dys, cy);
+    k_spe_axes<<<(g.nzc + 127) / 128, 128, 0, s>>>(g.nzc, Dz, Dzs, cz);
+    k_spe_jp<<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, Dx, Dy, Dz, Dxs, Dys, Dzs, jp);
+}
+
+// createPressureMatrix (PressureMatrix.hpp:5-117) + ELL_matrix::set
+// (ELL_sparseMatrix.hpp:246-320) assembled on the device, one row per
+// thread: slot 0 = diagonal val*jp, then the -x,+x,-y,+y,-z,+z neighbours
+// that exist, then padding (col = N-1, val = 0).  Stored slot-major.
+__global__ void k_ell_assemble(Geo g, const double *__restrict__ Dx, const double *__restrict__ Dy,
+                               const double *__restrict__ Dz, const double *__restrict__ Dxs,
+                               const double *__restrict__ Dys, const double *__restrict__ Dzs,
+                               int *__restrict__ cols, double *__restrict__ vals, double *__restrict__ jp)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < g.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const int ic = (int)(row / g.sxc);
+        const long long rem = row - (long long)ic * g.sxc;
+        const int jc = (int)(rem / g.nzc), kc = (int)(rem - (long long)jc * g.nzc);
+        const int i = ic + GC, j = jc + GC, k = kc + GC;
+        const double xp = inv2(Dx[i], Dxs[i]), yp = inv2(Dy[j], Dys[j]), zp = inv2(Dz[k], Dzs[k]);
+        const double xm = inv2(Dx[i], Dxs[i - 1]), ym = inv2(Dy[j], Dys[j - 1]), zm = inv2(Dz[k], Dzs[k - 1]);
+        double aa = 0.0, bb = 0.0, cc = 0.0;
+        if (ic == 0) aa = -xm;
+        if (ic == g.nxc - 1) aa = -xp;
+        if (jc == 0) bb = -ym;
+        if (jc == g.nyc - 1) bb = -yp;
+        if (kc == 0) cc = -zm;
+        if (kc == g.nzc - 1) cc = -zp;
+        double v = __dadd_rn(xm, xp);
+        v = __dadd_rn(v, ym); v = __dadd_rn(v, yp); v = __dadd_rn(v, zm); v = __dadd_rn(v, zp);
+        v = __dadd_rn(v, aa); v = __dadd_rn(v, bb); v = __dadd_rn(v, cc);
+        const double jr = __ddiv_rn(1., v);
+        jp[row] = jr;
+        int c[7];
+        double w[7];
+        int s = 0;
+        c[s] = (int)row; w[s++] = __dmul_rn(v, jr);
+        if (ic != 0) { c[s] = (int)(row - g.sxc); w[s++] = __dmul_rn(-xm, jr); }
+        if (ic != g.nxc - 1) { c[s] = (int)(row + g.sxc); w[s++] = __dmul_rn(-xp, jr); }
+        if (jc != 0) { c[s] = (int)(row - g.nzc); w[s++] = __dmul_rn(-ym, jr); }
+        if (jc != g.nyc - 1) { c[s] = (int)(row + g.nzc); w[s++] = __dmul_rn(-yp, jr); }
+        if (kc != 0) { c[s] = (int)(row - 1); w[s++] = __dmul_rn(-zm, jr); }
+        if (kc != g.nzc - 1) { c[s] = (int)(row + 1); w[s++] = __dmul_rn(-zp, jr); }
+        for (; s < 7; ++s) { c[s] = (int)(g.n - 1); w[s] = 0.0; }
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            cols[(long long)q * g.n + row] = c[q];
+            vals[(long long)q * g.n + row] = w[q];
+        }
+    }
+}
+
+void launch_ell_assemble(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
+                         const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
+                         int *cols, double *vals, double *jp)
+{
+    k_ell_assemble<<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, Dx, Dy, Dz, Dxs, Dys, Dzs, cols, vals, jp);
+}
+
+template <class Op>
+void launch_apply(cfd_launch_ctx &c, const Op &A, const double *x, double *r)
+{
+    k_apply<Op><<<blocks_for(A.n, c.grid_cap), kBlock, 0, c.s>>>(A, x, r);
+}
+template void launch_apply<SpeOp<double>>(cfd_launch_ctx &, const SpeOp<double> &, const double *, double *);
+template void launch_apply<EllOp<double>>(cfd_launch_ctx &, const EllOp<double> &, const double *, double *);
+
+// ---------------------------------------------------------------------------
+// BiCGSTAB (bicgstabRe2.hpp:93-189).
+//
+// init      r0 = b - A x; px2 = px1; px1 = x; r1 = p1 = r0;
+//           norm0 = |b|, rho = r1.r0                              (lines 98-115)
+// per iteration
+//   ap      ap = A p1; alpha = rho / (ap.r0)                      (120-121)
+//   s       s = r1 - alpha ap                                     (122-124)
+//   as      as = A s;  omega = (as.s)/(as.as)                     (126-128)
+//   xr      x += alpha p1 + omega s; r1 = s - omega as;
+//           stop if |r1|/norm0 < tol; cap at maxit;
+//           rho' = r1.r0; beta = (alpha/omega)(rho'/rho);
+//           restart decision                                      (130-171)
+//   p       p1 = r1 + beta (p1 - omega ap)  or restart r0=p1=r1   (172-182)
+template <class Op, class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_init(Op A, const V *__restrict__ b, V *__restrict__ x, V *__restrict__ r0, V *__restrict__ r1,
+            V *__restrict__ p1, V *__restrict__ px1, V *__restrict__ px2, BicgScal *sc,
+            double *partials, unsigned int *counter)
+{
+    double acc[2] = {0.0, 0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V bb = b[row];
+        const V r = bb - apply_row(A, x, row);
+        r0[row] = r;
+        r1[row] = r;
+        p1[row] = r;
+        if (px1) {
+            px2[row] = px1[row];
+            px1[row] = x[row];
+        }
+        acc[0] += (double)bb * (double)bb;
+        acc[1] += (double)r * (double)r;
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        sc->norm0 = sqrt(tot[0]);
+        sc->rho = tot[1];
+        sc->iter = 0;
+        sc->restart = 0;
+        sc->nonfinite = 0;
+        sc->timestep += 1;
+        sc->done = tot[0] == 0.0 ? BICG_ZERO_RHS : BICG_RUNNING;
+        sc->relres = tot[0] == 0.0 ? 0.0 : sqrt(tot[1]) / sc->norm0;
+    }
+}
+
+template <class Op, class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_ap(Op A, const V *__restrict__ p1, const V *__restrict__ r0, V *__restrict__ ap, BicgScal *sc,
+          double *partials, unsigned int *counter)
+{
+    if (sc->done) return;
+    double acc[1] = {0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V a = apply_row(A, p1, row);
+        ap[row] = a;
+        acc[0] += (double)a * (double)r0[row];
+    }
+    double tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+}
+
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_s(long long n, const V *__restrict__ r1, const V *__restrict__ ap, V *__restrict__ s1,
+         const BicgScal *sc)
+{
+    if (sc->done) return;
+    const V alpha = (V)sc->alpha;
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x)
+        s1[row] = fma(-alpha, ap[row], r1[row]);
+}
+
+template <class Op, class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_as(Op A, const V *__restrict__ s1, V *__restrict__ as, BicgScal *sc, double *partials,
+          unsigned int *counter)
+{
+    if (sc->done) return;
+    double acc[2] = {0.0, 0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V a = apply_row(A, s1, row);
+        as[row] = a;
+        const double ad = (double)a;
+        acc[0] += ad * (double)s1[row];
+        acc[1] += ad * ad;
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) sc->omega = tot[0] / tot[1];
+}
+
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_xr(long long n, V *__restrict__ x, const V *__restrict__ p1, const V *__restrict__ s1,
+          const V *__restrict__ as, const V *__restrict__ r0, V *__restrict__ r1, BicgScal *sc,
+          double *partials, unsigned int *counter)
+{
+    if (sc->done) return;
+    const V alpha = (V)sc->alpha, omega = (V)sc->omega;
+    double acc[2] = {0.0, 0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V s = s1[row];
+        x[row] += fma(alpha, p1[row], omega * s);
+        const V r = fma(-omega, as[row], s);
+        r1[row] = r;
+        const double rd = (double)r;
+        acc[0] += rd * rd;
+        acc[1] += rd * (double)r0[row];
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        const double rel = sqrt(tot[0]) / sc->norm0;
+        sc->relres = rel;
+        if (rel < sc->tol) {
+            sc->done = BICG_CONVERGED;
+        } else if (sc->iter >= sc->maxit) {
+            sc->done = BICG_CAPPED;
+        } else {
+            const double pre = sc->rho;
+            sc->rho = tot[1];
+            sc->beta = (sc->alpha / sc->omega) * (tot[1] / pre);
+            const int restart = !(sc->timestep < 10 || fabs(pre) > sc->restart_tol);
+            sc->restart = restart;
+            sc->restarts += restart;
+            sc->iter += 1;
+            sc->total_iters += 1;
+        }
+    }
+}
+
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_p(long long n, V *__restrict__ r0, const V *__restrict__ r1, V *__restrict__ p1,
+         const V *__restrict__ ap, const BicgScal *sc)
+{
+    if (sc->done) return;
+    if (sc->restart) {
+        for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+             row += (long long)gridDim.x * blockDim.x) {
+            const V r = r1[row];
+            r0[row] = r;
+            p1[row] = r;
+        }
+        return;
+    }
+    const V beta = (V)sc->beta, omega = (V)sc->omega;
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x)
+        p1[row] = fma(beta, fma(-omega, ap[row], p1[row]), r1[row]);
+}
+
+// NaN/Inf reset at the iteration cap (bicgstabRe2.hpp:143-163): non-finite
+// entries of x take the previous initial guess px1; if more than 10% were
+// reset, x becomes the guess before that (px2).
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_nonfinite(long long n, V *__restrict__ x, const V *__restrict__ px1, BicgScal *sc,
+                 double *partials, unsigned int *counter)
+{
+    double acc[1] = {0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V v = x[row];
+        if (!isfinite((double)v)) {
+            x[row] = px1[row];
+            acc[0] += 1.0;
+        }
+    }
+    double tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->nonfinite = (int)tot[0];
+}
+
+template <class V>
+__global__ void k_bicg_px2(long long n, V *__restrict__ x, const V *__restrict__ px2, const BicgScal *sc)
+{
+    if (!((double)sc->nonfinite > (double)n * 0.1)) return;
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x)
+        x[row] = px2[row];
+}
+
+template <class Op, class V>
+void launch_bicg_init(cfd_launch_ctx &c, const Op &A, const V *b, V *x, const BicgVecs<V> &w,
+                      V *px1, V *px2, BicgScal *sc)
+{
+    k_bicg_init<Op, V><<<c.red_blocks, kBlock, 0, c.s>>>(A, b, x, w.r0, w.r1, w.p1, px1, px2, sc,
+                                                         c.partials, c.counter);
+}
+
+template <class Op, class V>
+void launch_bicg_iteration(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc)
+{
+    const int G = c.red_blocks;
+    k_bicg_ap<Op, V><<<G, kBlock, 0, c.s>>>(A, w.p1, w.r0, w.ap, sc, c.partials, c.counter);
+    k_bicg_s<V><<<G, kBlock, 0, c.s>>>(A.n, w.r1, w.ap, w.s1, sc);
+    k_bicg_as<Op, V><<<G, kBlock, 0, c.s>>>(A, w.s1, w.as, sc, c.partials, c.counter);
+    k_bicg_xr<V><<<G, kBlock, 0, c.s>>>(A.n, x, w.p1, w.s1, w.as, w.r0, w.r1, sc, c.partials, c.counter);
+    k_bicg_p<V><<<G, kBlock, 0, c.s>>>(A.n, w.r0, w.r1, w.p1, w.ap, sc);
+}
+
+template <class Op, class V>
+void launch_bicg_iteration_part(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc,
+                                int part)
+{
+    const int G = c.red_blocks;
+    switch (part) {
+    case 0: k_bicg_ap<Op, V><<<G, kBlock, 0, c.s>>>(A, w.p1, w.r0, w.ap, sc, c.partials, c.counter); break;
+    case 1: k_bicg_s<V><<<G, kBlock, 0, c.s>>>(A.n, w.r1, w.ap, w.s1, sc); break;
+    case 2: k_bicg_as<Op, V><<<G, kBlock, 0, c.s>>>(A, w.s1, w.as, sc, c.partials, c.counter); break;
+    case 3: k_bicg_xr<V><<<G, kBlock, 0, c.s>>>(A.n, x, w.p1, w.s1, w.as, w.r0, w.r1, sc, c.partials, c.counter); break;
+    default: k_bicg_p<V><<<G, kBlock, 0, c.s>>>(A.n, w.r0, w.r1, w.p1, w.ap, sc); break;
+    }
+}
+#define CFD_PART_INST(OP, V)                                                                        \
+    template void launch_bicg_iteration_part<OP, V>(cfd_launch_ctx &, const OP &, V *, const BicgVecs<V> &, \
+                                                    BicgScal *, int);
+CFD_PART_INST(SpeOp<double>, double)
+CFD_PART_INST(EllOp<double>, double)
+CFD_PART_INST(SpeOp<float>, float)
+CFD_PART_INST(EllOp<float>, float)
+
+template <class V>
+void launch_bicg_nan_reset(cfd_launch_ctx &c, long long n, V *x, const V *px1, const V *px2,
+                           BicgScal *sc)
+{
+    k_bicg_nonfinite<V><<<c.red_blocks, kBlock, 0, c.s>>>(n, x, px1, sc, c.partials, c.counter);
+    k_bicg_px2<V><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, px2, sc);
+}
+
+template void launch_bicg_init<SpeOp<double>, double>(cfd_launch_ctx &, const SpeOp<double> &,
+    const double *, double *, const BicgVecs<double> &, double *, double *, BicgScal *);
+template void launch_bicg_init<EllOp<double>, double>(cfd_launch_ctx &, const EllOp<double> &,
+    const double *, double *, const BicgVecs<double> &, double *, double *, BicgScal *);
+template void launch_bicg_init<SpeOp<float>, float>(cfd_launch_ctx &, const SpeOp<float> &,
+    const float *, float *, const BicgVecs<float> &, float *, float *, BicgScal *);
+template void launch_bicg_init<EllOp<float>, float>(cfd_launch_ctx &, const EllOp<float> &,
+    const float *, float *, const BicgVecs<float> &, float *, float *, BicgScal *);
+template void launch_bicg_iteration<SpeOp<double>, double>(cfd_launch_ctx &, const SpeOp<double> &,
+    double *, const BicgVecs<double> &, BicgScal *);
+template void launch_bicg_iteration<EllOp<double>, double>(cfd_launch_ctx &, const EllOp<double> &,
+    double *, const BicgVecs<double> &, BicgScal *);
+template void launch_bicg_iteration<SpeOp<float>, float>(cfd_launch_ctx &, const SpeOp<float> &,
+    float *, const BicgVecs<float> &, BicgScal *);
+template void launch_bicg_iteration<EllOp<float>, float>(cfd_launch_ctx &, const EllOp<float> &,
+    float *, const BicgVecs<float> &, BicgScal *);
+template void launch_bicg_nan_reset<double>(cfd_launch_ctx &, long long, double *, const double *,
+                                            const double *, BicgScal *);
+
+// ---------------------------------------------------------------------------
+// SOR (SorPipeLine.seq.hpp:30-117) in red-black order.
+// cf7 = -1/coef with the reference's operation order (bitwise equal).
+__global__ void k_sor_setup(Geo g, const double *__restrict__ Dx, const double *__restrict__ Dy,
+                            const double *__restrict__ Dz, const double *__restrict__ Dxs,
+                            const double *__restrict__ Dys, const double *__restrict__ Dzs,
+                            double *__restrict__ cf7)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < g.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(row / g.sxc) + GC;
+        const long long rem = row - (long long)(i - GC) * g.sxc;
+        const int j = (int)(rem / g.nzc) + GC, k = (int)(rem % g.nzc) + GC;
+        const double yz = __dmul_rn(Dy[j], Dz[k]), xz = __dmul_rn(Dx[i], Dz[k]), xy = __dmul_rn(Dx[i], Dy[j]);
+        double c = __ddiv_rn(yz, Dxs[i]);
+        c = __dadd_rn(c, __ddiv_rn(yz, Dxs[i - 1]));
+        c = __dadd_rn(c, __ddiv_rn(xz, Dys[j]));
+        c = __dadd_rn(c, __ddiv_rn(xz, Dys[j - 1]));
+        c = __dadd_rn(c, __ddiv_rn(xy, Dzs[k]));
+        c = __dadd_rn(c, __ddiv_rn(xy, Dzs[k - 1]));
+        cf7[row] = __ddiv_rn(-1.0, c);
+    }
+}
+
+void launch_sor_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
+                      const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
+                      double *cf7)
+{
+    k_sor_setup<<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, Dx, Dy, Dz, Dxs, Dys, Dzs, cf7);
+}
+
+// cf6 = mass change / dt (SorPipeLine.seq.hpp:48-60)
+template <class T>
+__global__ void k_sor_rhs(Geo g, Metrics<double> m, double rdt, const T *__restrict__ u1,
+                          const T *__restrict__ v1, const T *__restrict__ w1, double *__restrict__ cf6)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < g.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(row / g.sxc) + GC;
+        const long long rem = row - (long long)(i - GC) * g.sxc;
+        const int j = (int)(rem / g.nzc) + GC, k = (int)(rem % g.nzc) + GC;
+        const long long ic = icel(g, i, j, k);
+        const double Dx = m.x(AX_D, i), Dy = m.y(AX_D, j), Dz = m.z(AX_D, k);
+        const double mc = ((double)u1[ic] - (double)u1[ic - g.sx]) * Dy * Dz
+                        + ((double)v1[ic] - (double)v1[ic - g.sy]) * Dx * Dz
+                        + ((double)w1[ic] - (double)w1[ic - 1]) * Dx * Dy;
+        cf6[row] = mc * rdt;
+    }
+}
+
+template <class T>
+void launch_sor_rhs(cudaStream_t s, const Geo &g, const Metrics<double> &m, double rdt, const T *u1,
+                    const T *v1, const T *w1, double *cf6)
+{
+    k_sor_rhs<T><<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, m, rdt, u1, v1, w1, cf6);
+}
+template void launch_sor_rhs<double>(cudaStream_t, const Geo &, const Metrics<double> &, double,
+                                     const double *, const double *, const double *, double *);
+template void launch_sor_rhs<float>(cudaStream_t, const Geo &, const Metrics<double> &, double,
+                                    const float *, const float *, const float *, double *);
+
+// One colour of one sweep.  state[0] = done flag, state[1] = sweeps run.
+// The do-while test of the reference (residual > tol && iters < itmax,
+// SorPipeLine.seq.hpp:112) is evaluated at the start of the next sweep's
+// first colour from the previous sweep's max change, so sweeps queued past
+// convergence do nothing.
+__global__ void __launch_bounds__(kBlock)
+k_sor_sweep(Geo g, Metrics<double> m, const double *__restrict__ cf6, const double *__restrict__ cf7,
+            double *__restrict__ p, double omega, double tol, int itmax, int sweep, int color,
+            unsigned long long *__restrict__ res, int *state)
+{
+    if (state[0]) return;
+    if (color == 0 && sweep > 0) {
+        const double prev = __longlong_as_double((long long)res[sweep - 1]);
+        if (!(prev > tol && sweep < itmax)) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                state[0] = 1;
+                state[1] = sweep;
+            }
+            return;
+        }
+    }
+    const int nzh = (g.nzc + 1) >> 1;
+    const long long total = (long long)g.nxc * g.nyc * nzh;
+    double mx = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long ij = t / nzh;
+        const int kk = (int)(t - ij * nzh);
+        const int i = (int)(ij / g.nyc) + GC, j = (int)(ij % g.nyc) + GC;
+        const int k = GC + ((i + j + GC + color) & 1) + 2 * kk;
+        if (k >= g.nz - GC) continue;
+        const long long ic = icel(g, i, j, k);
+        const long long row = icelcal(g, i, j, k);
+        const double yz = m.y(AX_D, j) * m.z(AX_D, k), xz = m.x(AX_D, i) * m.z(AX_D, k),
+                     xy = m.x(AX_D, i) * m.y(AX_D, j);
+        double s = -p[ic + g.sx] * (yz * m.x(AX_RDS, i));
+        s = fma(-p[ic - g.sx], yz * m.x(AX_RDS, i - 1), s);
+        s = fma(-p[ic + g.sy], xz * m.y(AX_RDS, j), s);
+        s = fma(-p[ic - g.sy], xz * m.y(AX_RDS, j - 1), s);
+        s = fma(-p[ic + 1], xy * m.z(AX_RDS, k), s);
+        s = fma(-p[ic - 1], xy * m.z(AX_RDS, k - 1), s);
+        const double pnew = (s + cf6[row]) * cf7[row];
+        const double pc = p[ic];
+        const double d = pnew - pc;
+        p[ic] = fma(omega, d, pc);
+        const double a = fabs(d);
+        mx = (a > mx || a != a) ? a : mx;
+    }
+    grid_max_nonneg(mx, res + sweep);
+    if (color == 1 && blockIdx.x == 0 && threadIdx.x == 0) state[1] = sweep + 1;
+}
+
+void launch_sor_sweep(cudaStream_t s, const Geo &g, const Metrics<double> &m, const double *cf6,
+                      const double *cf7, double *p, double omega, double tol, int itmax, int sweep,
+                      unsigned long long *res, int *state)
+{
+    const long long total = (long long)g.nxc * g.nyc * ((g.nzc + 1) / 2);
+    const int G = blocks_for(total, 4096);
+    k_sor_sweep<<<G, kBlock, 0, s>>>(g, m, cf6, cf7, p, omega, tol, itmax, sweep, 0, res, state);
+    k_sor_sweep<<<G, kBlock, 0, s>>>(g, m, cf6, cf7, p, omega, tol, itmax, sweep, 1, res, state);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP64 residual of the scaled system, written as the
+// FP32 right-hand side of the next inner solve, and the FP64 correction.
+template <class Op, class V>
+__global__ void __launch_bounds__(kBlock)
+k_residual64(Op A, const double *__restrict__ b, const double *__restrict__ x, V *__restrict__ r32,
+             double *partials, unsigned int *counter, double *out)
+{
+    double acc[1] = {0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const double r = b[row] - apply_row(A, x, row);
+        r32[row] = (V)r;
+        acc[0] += r * r;
+    }
+    double tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) *out = tot[0];
+}
+
+template <class V>
+void launch_residual64(cfd_launch_ctx &c, const SpeOp<double> &A, const double *b, const double *x,
+                       V *r32, double *norm2_out)
+{
+    k_residual64<SpeOp<double>, V><<<c.red_blocks, kBlock, 0, c.s>>>(A, b, x, r32, c.partials,
+                                                                     c.counter, norm2_out);
+}
+template <class V>
+void launch_residual64_ell(cfd_launch_ctx &c, const EllOp<double> &A, const double *b,
+                           const double *x, V *r32, double *norm2_out)
+{
+    k_residual64<EllOp<double>, V><<<c.red_blocks, kBlock, 0, c.s>>>(A, b, x, r32, c.partials,
+                                                                     c.counter, norm2_out);
+}
+template void launch_residual64<float>(cfd_launch_ctx &, const SpeOp<double> &, const double *,
+                                       const double *, float *, double *);
+template void launch_residual64_ell<float>(cfd_launch_ctx &, const EllOp<double> &, const double *,
+                                           const double *, float *, double *);
+
+// x += e (FP64 accumulation of an FP32 correction)
+template <class V>
+__global__ void k_correct(long long n, double *__restrict__ x, const V *__restrict__ e)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x)
+        x[row] += (double)e[row];
+}
+
+template <class V>
+void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e)
+{
+    k_correct<V><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, e);
+}
+template void launch_correct<float>(cfd_launch_ctx &, long long, double *, const float *);
+
+}  // namespace cfd

@@ -1,0 +1,217 @@
+"""Host-side mirror of the reference's call surface over the C ABI.
+
+`Simulation` owns one device context (`cfd_ctx`).  Its methods carry the
+names of the reference functions they replace and take the same slot
+arguments (T0 / T1 / T3 are the reference's velocity objects, p, eta, f,
+source_termF and Mx live in the context):
+
+    ConvectionDifussion(T0, T1)       convection_and_difussion.hpp:168
+    add_source(T1)                    RUN_CPU_PC_METHOD.hpp:309-316
+    accumulate_source()               RUN_CPU_PC_METHOD.hpp:393-401
+    createBMatrix(T1)                 b_matrix.hpp:51
+    pSolver()                         bicgstabRe2.hpp:46 (operator())
+    Pressure_transform_X_result()     Transform.hpp:8
+    SorPipeLine(T1)                   SorPipeLine.seq.hpp:4 (red-black)
+    update_UandF(T1, T3)              updateUandF.hpp:95
+    Delay_IO_CD_CL()                  virtualForceIntergrator.hpp:108
+    BC_staggered_main(T0)             Boundary_Condition.hpp:37
+    BC_staggered_copy(T0, T1)         updateBC.hpp:6
+    DFIB_CylinderZ(cx, cy, r, nsub)   setEta.hpp:136
+    step()                            one iteration of the driver's main loop
+
+Fields move in the reference's own layouts (ghosted k-fastest, compact
+icelCal), as float64 numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import FIELD, check, dptr, lib
+from .configs import Workload
+
+
+def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi.SOLVER_BICG_SPE,
+                precision: int = capi.PREC_FP64, tol: float | None = None, maxit: int = 5000,
+                omega: float | None = None, sor_maxit: int = 5000, aligned_source: bool = False,
+                compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-4,
+                max_outer: int = 30) -> capi.CfdConfig:
+    cfg = capi.CfdConfig()
+    check(lib().cfd_config_default(C.byref(cfg), w.nxc, w.nyc, w.nzc))
+    cfg.lx, cfg.ly, cfg.lz = w.lx, w.ly, w.lz
+    cfg.re, cfg.dt = w.re, w.dt
+    cfg.method, cfg.solver, cfg.precision = method, solver, precision
+    cfg.p_criteria = w.tol if tol is None else tol
+    cfg.p_iter_max = maxit
+    cfg.p_sor_omega = w.omega if omega is None else omega
+    cfg.p_sor_iter_max = sor_maxit
+    cfg.aligned_source = int(aligned_source)
+    cfg.compat_rhs = int(compat_rhs)
+    for b in range(6):
+        for c in range(3):
+            cfg.bc_dir[b][c] = w.bc_dir[b][c]
+            cfg.bc_num[b][c] = w.bc_num[b][c]
+    cfg.check_every = check_every
+    cfg.inner_tol = inner_tol
+    cfg.max_outer = max_outer
+    return cfg
+
+
+class Simulation:
+    T0, T1, T3 = capi.T0, capi.T1, capi.T3
+
+    def __init__(self, w: Workload, **cfg_kw):
+        self.w = w
+        self.cfg = make_config(w, **cfg_kw)
+        self._h = C.c_void_p()
+        check(lib().cfd_create(C.byref(self.cfg), C.byref(self._h)))
+        self.ng = w.n_ghosted
+        self.n = w.n_cells
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if self._h:
+            lib().cfd_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- grid and state ---------------------------------------------------
+    def grid_uniform(self):
+        check(lib().cfd_grid_uniform(self._h))
+
+    def set_metrics(self, m: dict):
+        arrs = [np.ascontiguousarray(m[k], dtype=np.float64) for k in
+                ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")]
+        check(lib().cfd_set_metrics(self._h, *[dptr(a) for a in arrs]))
+
+    def count(self, field: str) -> int:
+        return int(lib().cfd_field_count(self._h, FIELD[field]))
+
+    def upload(self, field: str, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        check(lib().cfd_upload(self._h, FIELD[field], dptr(a), a.size))
+
+    def download(self, field: str, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.count(field))
+        check(lib().cfd_download(self._h, FIELD[field], dptr(out), out.size))
+        return out
+
+    def init_uniform(self, ui=1.0, vi=0.0, wi=0.0):
+        check(lib().cfd_init_uniform(self._h, ui, vi, wi))
+
+    def start(self):
+        check(lib().cfd_start(self._h))
+
+    def setup_cylinder(self, u0=None, v0=None, w0=None, eta=True):
+        """Uniform grid, eta of the workload's cylinder, initial state and the
+        first boundary update (RUN_CPU_PC_METHOD.hpp:75-119, 257-266)."""
+        self.grid_uniform()
+        self.init_uniform(1.0, 0.0, 0.0)
+        if eta:
+            self.DFIB_CylinderZ(self.w.cx, self.w.center_y, self.w.radius, self.w.nsub)
+        for name, a in (("U0", u0), ("V0", v0), ("W0", w0)):
+            if a is not None:
+                self.upload(name, a)
+        self.start()
+
+    # -- the reference's operators ----------------------------------------
+    def ConvectionDifussion(self, src=T0, dst=T1):
+        check(lib().cfd_convection_diffusion(self._h, src, dst))
+
+    def add_source(self, slot=T1):
+        check(lib().cfd_add_source(self._h, slot))
+
+    def accumulate_source(self):
+        check(lib().cfd_accumulate_source(self._h))
+
+    def clear_source(self):
+        check(lib().cfd_clear_source(self._h))
+
+    def createBMatrix(self, slot=T1) -> float:
+        mean = C.c_double()
+        check(lib().cfd_create_b(self._h, slot, C.byref(mean)))
+        return mean.value
+
+    def pSolver(self, allow_noconv=False):
+        """bicgstabRe2::operator()(Mx.matB, Mx.X_result) -> (iters, relres)."""
+        it, res = C.c_int(), C.c_double()
+        check(lib().cfd_bicgstab(self._h, C.byref(it), C.byref(res)),
+              allow=(-4,) if allow_noconv else ())
+        return it.value, res.value
+
+    def multiply(self):
+        """Mx.B = A Mx.X with the configured operator."""
+        check(lib().cfd_apply_operator(self._h))
+
+    def Pressure_transform_X_result(self):
+        check(lib().cfd_pressure_transform(self._h))
+
+    def SorPipeLine(self, slot=T1):
+        it, err = C.c_int(), C.c_double()
+        check(lib().cfd_sor(self._h, slot, C.byref(it), C.byref(err)))
+        return it.value, err.value
+
+    def update_UandF(self, src=T1, dst=T3):
+        check(lib().cfd_update_uf(self._h, src, dst))
+
+    def Delay_IO_CD_CL(self):
+        cd, cl = C.c_double(), C.c_double()
+        check(lib().cfd_cdcl(self._h, C.byref(cd), C.byref(cl)))
+        return cd.value, cl.value
+
+    def BC_staggered_main(self, slot=T0):
+        check(lib().cfd_bc_main(self._h, slot))
+
+    def BC_staggered_copy(self, src=T0, dst=T1):
+        check(lib().cfd_bc_copy(self._h, src, dst))
+
+    def copy_velocity(self, src=T3, dst=T0):
+        check(lib().cfd_copy_velocity(self._h, src, dst))
+
+    def DFIB_CylinderZ(self, cx, cy, radius=0.5, nsub=100):
+        check(lib().cfd_eta_cylinder_z(self._h, cx, cy, radius, nsub))
+
+    def div_inf(self, slot=T0) -> float:
+        out = C.c_double()
+        check(lib().cfd_div_inf(self._h, slot, C.byref(out)))
+        return out.value
+
+    def step(self, allow_noconv=False) -> dict:
+        info = capi.CfdStepInfo()
+        check(lib().cfd_step(self._h, C.byref(info)), allow=(-4,) if allow_noconv else ())
+        return {"loop": info.loop, "time": info.time, "iters": list(info.iters),
+                "relres": list(info.relres), "outer": list(info.outer), "cd": info.cd, "cl": info.cl}
+
+    def stream(self) -> int:
+        """cudaStream_t of the context (an integer handle)."""
+        out = C.c_void_p()
+        check(lib().cfd_stream(self._h, C.byref(out)))
+        return out.value or 0
+
+    def time_kernels(self, reps: int = 20) -> dict:
+        """Mean ms per launch of each hot kernel (CUDA events on the context
+        stream); kernels the context does not use are omitted."""
+        ms = (C.c_double * len(capi.KERNELS))()
+        check(lib().cfd_time_kernels(self._h, reps, ms, len(capi.KERNELS)))
+        return {k: v for k, v in zip(capi.KERNELS, ms) if v >= 0}
+
+    def sync(self):
+        check(lib().cfd_sync(self._h))

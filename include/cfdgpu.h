@@ -1,0 +1,224 @@
+/*
+ * cfdgpu.h -- C ABI of the GB300 time step for the CFD_NSsolver_forHPC
+ * staggered-grid Navier-Stokes / direct-forcing immersed-boundary solver.
+ *
+ * One context owns one device-resident simulation: the velocity triplets T0,
+ * T1, T3, the pressure p, the volume fraction eta, the forcing f, the
+ * predictor-corrector source, and the Poisson system (b, x, jp and the
+ * operator).  Arrays cross this boundary in the reference's own layouts:
+ *
+ *   ghosted   icel(i,j,k)    = i*ny*nz + j*nz + k, nx = nx_cal + 4, ...
+ *             (inc/grid/structureGrid.hpp:159)
+ *   compact   icelCal(i,j,k) = (i-2)*ny_cal*nz_cal + (j-2)*nz_cal + (k-2)
+ *             (inc/grid/structureGrid.hpp:182)
+ *   f, src    three compact components back to back (u, v, w)
+ *
+ * so a host array of the reference (std::vector<double>::data()) is uploaded
+ * or downloaded with one copy.  Every call returns CFD_OK (0) or a negative
+ * cfd_status; cfd_last_error() describes the last failure of the calling
+ * thread.  A context is used by one host thread at a time; all its work is
+ * ordered on one CUDA stream.
+ *
+ * Each entry point names the reference function (file:line) it replaces.
+ */
+#ifndef CFDGPU_H
+#define CFDGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CFDGPU_ABI_VERSION 1
+
+typedef struct cfd_ctx cfd_ctx;
+
+typedef enum {
+    CFD_OK = 0,
+    CFD_ERR_ARG = -1,     /* invalid argument (null pointer, size, slot, enum) */
+    CFD_ERR_CUDA = -2,    /* a CUDA runtime call failed */
+    CFD_ERR_NOMEM = -3,   /* device allocation failed */
+    CFD_ERR_NOCONV = -4,  /* iterative solver hit its iteration cap */
+    CFD_ERR_NAN = -5,     /* non-finite values found */
+    CFD_ERR_TIMEOUT = -6, /* a bounded device wait gave up */
+    CFD_ERR_STATE = -7    /* call not valid in the context's current state */
+} cfd_status;
+
+/* Poisson solver (inc/controlPanel.hpp:17-23 selects these at compile time) */
+typedef enum {
+    CFD_SOLVER_BICG_SPE = 0, /* bicgstabRe2 over the matrix-free SPE_matrix1 operator */
+    CFD_SOLVER_BICG_ELL = 1, /* bicgstabRe2 over the ELL matrix of createPressureMatrix */
+    CFD_SOLVER_SOR_RB = 3    /* SorPipeLine finite-volume SOR, red-black ordered */
+} cfd_solver_kind;
+
+typedef enum {
+    CFD_METHOD_PC = 0,   /* runSeqOmp_predictionMethod (inc/run/RUN_CPU_PC_METHOD.hpp:9) */
+    CFD_METHOD_PLAIN = 1 /* runSeqOmp (inc/run/RUN_CPU.hpp:11) */
+} cfd_method;
+
+typedef enum {
+    CFD_PREC_FP64 = 0,  /* everything in FP64, as the reference */
+    CFD_PREC_MIXED = 1  /* FP32 fields, FP32 convection-diffusion and inner Krylov
+                           iterations; FP64 defect correction of the Poisson
+                           residual, FP64 dots and FP64 divergence check */
+} cfd_precision;
+
+/* Velocity slots: the reference's T0 (old), T1 (predicted u*), T3 (new). */
+enum { CFD_SLOT_T0 = 0, CFD_SLOT_T1 = 1, CFD_SLOT_T3 = 3 };
+
+/* Field handles for upload/download. */
+typedef enum {
+    CFD_FIELD_U0 = 0, CFD_FIELD_V0, CFD_FIELD_W0, /* T0 (ghosted) */
+    CFD_FIELD_U1, CFD_FIELD_V1, CFD_FIELD_W1,     /* T1 (ghosted) */
+    CFD_FIELD_U3, CFD_FIELD_V3, CFD_FIELD_W3,     /* T3 (ghosted) */
+    CFD_FIELD_P,                                  /* pressure::p (ghosted) */
+    CFD_FIELD_ETA,                                /* DfibArray::eta (ghosted) */
+    CFD_FIELD_F,                                  /* DfibArray::f (3 x compact) */
+    CFD_FIELD_SRC,                                /* PC source_termF (3 x compact) */
+    CFD_FIELD_X,                                  /* MxClass::X_result (compact) */
+    CFD_FIELD_B,                                  /* MxClass::matB (compact) */
+    CFD_FIELD_JP,                                 /* grid::jp Jacobi scaling (compact) */
+    CFD_FIELD_COUNT
+} cfd_field;
+
+typedef struct {
+    int nx_cal, ny_cal, nz_cal; /* interior cells, grid::nxCal.. (structureGrid.hpp:44-46) */
+    double lx, ly, lz;          /* domain lengths (structureGrid.hpp:34) */
+    double re;                  /* simuClass::set_Re (simuClass.hpp:39) */
+    double dt;                  /* simuClass::set_dt (simuClass.hpp:108) */
+    int method;                 /* cfd_method */
+    int solver;                 /* cfd_solver_kind */
+    int precision;              /* cfd_precision */
+    double p_criteria;          /* simuClass::p_criteria, solver tolerance (simuClass.hpp:74) */
+    int p_iter_max;             /* bicgstabRe2 iters_max_ (bicgstabRe2.hpp:57) */
+    double p_sor_omega;         /* simuClass::p_sor_omega (simuClass.hpp:78) */
+    int p_sor_iter_max;         /* simuClass::p_sor_iter_max (simuClass.hpp:80) */
+    int aligned_source;         /* 0: add the PC source with the reference's compact
+                                   index into the ghosted array (RUN_CPU_PC_METHOD.hpp:314);
+                                   1: add it at the cell it belongs to */
+    int compat_rhs;             /* 1: subtract the volume-weighted mean of the unscaled
+                                   Poisson RHS (makes the singular Neumann system
+                                   consistent; needed for tolerances below ~1e-6) */
+    double bc_dir[6][3];        /* Dirichlet table Dir[face][component] */
+    double bc_num[6][3];        /* Neumann table Num[face][component]
+                                   (Boundary_Condition.hpp:4-31) */
+    int check_every;            /* iterations between host convergence polls (>= 1) */
+    double inner_tol;           /* mixed precision: relative tolerance of each FP32
+                                   inner solve inside the FP64 defect correction */
+    int max_outer;              /* mixed precision: defect-correction sweeps cap */
+} cfd_config;
+
+typedef struct {
+    long long loop;      /* simuClass::loop after the step */
+    double time;         /* simuClass::time after the step */
+    int iters[4];        /* per pass: solver iterations (simuClass::iters) */
+    double relres[4];    /* per pass: relative residual / SOR change (simuClass::error) */
+    int outer[4];        /* per pass: defect-correction sweeps (mixed precision) */
+    double cd, cl;       /* drag and lift of the final pass (Delay_IO_CD_CL) */
+} cfd_step_info;
+
+/* ---- lifetime ---------------------------------------------------------- */
+int cfd_abi_version(void);
+const char *cfd_last_error(void);
+/* Fill *cfg with the reference defaults for an nx x ny x nz interior grid. */
+int cfd_config_default(cfd_config *cfg, int nx_cal, int ny_cal, int nz_cal);
+int cfd_create(const cfd_config *cfg, cfd_ctx **out);
+int cfd_destroy(cfd_ctx *ctx);
+int cfd_sync(cfd_ctx *ctx);
+
+/* ---- grid and state ---------------------------------------------------- */
+/* grid::init_uniform (structureGrid.hpp:409-440) computed on the host */
+int cfd_grid_uniform(cfd_ctx *ctx);
+/* Metrics of any staggered grid: X,Y,Z have n+1 nodes, the rest n (ghosted). */
+int cfd_set_metrics(cfd_ctx *ctx, const double *X, const double *Y, const double *Z,
+                    const double *Dx, const double *Dy, const double *Dz,
+                    const double *Dxs, const double *Dys, const double *Dzs);
+/* count must equal the field's element count (ghosted, compact or 3 x compact). */
+int cfd_upload(cfd_ctx *ctx, int field, const double *host, size_t count);
+int cfd_download(cfd_ctx *ctx, int field, double *host, size_t count);
+size_t cfd_field_count(cfd_ctx *ctx, int field);
+/* Page-lock a host buffer for faster uploads/downloads (cudaHostRegister). */
+int cfd_host_register(void *host, size_t bytes);
+int cfd_host_unregister(void *host);
+/* velocity::iniU (physicalVariables.hpp:53) on T0, T1, T3 and p = 0
+   (RUN_CPU_PC_METHOD.hpp:84-89) */
+int cfd_init_uniform(cfd_ctx *ctx, double ui, double vi, double wi);
+/* First boundary update: T1 = T3 = T0, BC_staggered_main(T0, p),
+   BC_staggered_copy(T0 -> T1)  (RUN_CPU_PC_METHOD.hpp:114-119) */
+int cfd_start(cfd_ctx *ctx);
+
+/* ---- the hot-path operators --------------------------------------------- */
+/* ConvectionDifussion(simu, T[src], T[dst]) (convection_and_difussion.hpp:168) */
+int cfd_convection_diffusion(cfd_ctx *ctx, int src_slot, int dst_slot);
+/* T[slot] += source_termF (RUN_CPU_PC_METHOD.hpp:309-316) */
+int cfd_add_source(cfd_ctx *ctx, int slot);
+/* source_termF += dt * Dfib.f (RUN_CPU_PC_METHOD.hpp:393-401) */
+int cfd_accumulate_source(cfd_ctx *ctx);
+/* source_termF = 0 (RUN_CPU_PC_METHOD.hpp:290) */
+int cfd_clear_source(cfd_ctx *ctx);
+/* createBMatrix_omp(T[slot], Mx) (b_matrix.hpp:51), plus the compatibility
+   projection when cfg.compat_rhs is set; *mean receives the removed mean
+   (may be NULL) */
+int cfd_create_b(cfd_ctx *ctx, int slot, double *mean);
+/* bicgstabRe2::operator()(Mx.matB, Mx.X_result) (bicgstabRe2.hpp:46, 93-189);
+   returns CFD_ERR_NOCONV when the cap was hit (x then got the NaN reset of
+   lines 143-163).  In mixed precision this is the FP64 defect correction. */
+int cfd_bicgstab(cfd_ctx *ctx, int *iters, double *relres);
+/* B = A X with the configured operator (SPE_matrix1::multiply_omp,
+   SPE_sparseMatrix1.hpp:259, or ELL_matrix::multiply_omp, ELL_sparseMatrix.hpp:478) */
+int cfd_apply_operator(cfd_ctx *ctx);
+/* Pressure_transform_X_result (Transform.hpp:8-24) */
+int cfd_pressure_transform(cfd_ctx *ctx);
+/* SorPipeLine (SorPipeLine.seq.hpp:4-122) on T[slot], red-black ordered */
+int cfd_sor(cfd_ctx *ctx, int slot, int *iters, double *err);
+/* update_UandF_omp(Dfib, simu, p, T[src], T[dst]) (updateUandF.hpp:95-190) */
+int cfd_update_uf(cfd_ctx *ctx, int src_slot, int dst_slot);
+/* virtualF_Int + Delay_IO_CD_CL's coefficients (virtualForceIntergrator.hpp:5-37,
+   120-127) from the current f */
+int cfd_cdcl(cfd_ctx *ctx, double *cd, double *cl);
+/* BC_staggered_main(T[slot], p) (Boundary_Condition.hpp:37-175) */
+int cfd_bc_main(cfd_ctx *ctx, int slot);
+/* BC_staggered_copy(T[from] -> T[to]) (updateBC.hpp:6-111) */
+int cfd_bc_copy(cfd_ctx *ctx, int from_slot, int to_slot);
+/* velocity::copy_omp (physicalVariables.hpp:84-102) */
+int cfd_copy_velocity(cfd_ctx *ctx, int from_slot, int to_slot);
+/* DFIB_CylinderZ (setEta.hpp:136-204) with explicit centre and radius */
+int cfd_eta_cylinder_z(cfd_ctx *ctx, double cx, double cy, double radius, int nsub);
+/* One iteration of the main loop of the configured driver
+   (RUN_CPU_PC_METHOD.hpp:287-627 or RUN_CPU.hpp:290-462, without IO). */
+int cfd_step(cfd_ctx *ctx, cfd_step_info *info);
+/* max |div T[slot]| over interior cells, FP64 */
+int cfd_div_inf(cfd_ctx *ctx, int slot, double *out);
+
+/* ---- instrumentation ---------------------------------------------------- */
+/* The context's CUDA stream (a cudaStream_t), for callers that record events
+   or order their own work on it. */
+int cfd_stream(cfd_ctx *ctx, void **stream);
+
+/* Kernels timed by cfd_time_kernels, in ms[] order. */
+typedef enum {
+    CFD_KERNEL_BICG_AP = 0,  /* ap = A p1 and ap.r0            (bicgstabRe2.hpp:120-121) */
+    CFD_KERNEL_BICG_S,       /* s = r1 - alpha ap              (:122-124) */
+    CFD_KERNEL_BICG_AS,      /* as = A s, as.s and as.as       (:126-128) */
+    CFD_KERNEL_BICG_XR,      /* x, r1 update, |r1|^2 and r1.r0 (:130-138, 167) */
+    CFD_KERNEL_BICG_P,       /* p1 = r1 + beta (p1 - omega ap) (:172-176) */
+    CFD_KERNEL_CONVDIFF,     /* ConvectionDifussion */
+    CFD_KERNEL_UPDATE_UF,    /* update_UandF_omp */
+    CFD_KERNEL_RHS,          /* createBMatrix_omp (+ compatibility mean) */
+    CFD_KERNEL_SOR_SWEEP,    /* one red + one black SOR sweep */
+    CFD_KERNEL_COUNT
+} cfd_kernel_id;
+
+/* Mean device time (ms) of one launch of each hot kernel, measured with CUDA
+   events around `reps` back-to-back launches on the context stream.  The
+   Krylov kernels run on the solver's scratch vectors and a scratch copy of
+   x, so the simulation state is left as it was; ms[k] < 0 marks a kernel the
+   context does not use.  nms is the length of ms (at most CFD_KERNEL_COUNT
+   entries are written). */
+int cfd_time_kernels(cfd_ctx *ctx, int reps, double *ms, int nms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFDGPU_H */

@@ -1,0 +1,160 @@
+"""Poisson solvers on the GPU against the oracle.
+
+BiCGSTAB: the GPU and the oracle run the same algorithm (bicgstabRe2) on
+the same system with different summation orders, so the iteration count
+agrees to a few iterations and both solutions satisfy the tolerance; the
+solutions themselves agree to tol x (condition number), checked after
+removing the constant null-space component of the Neumann operator.
+SOR: the GPU and the oracle run the same red-black sweeps; the iterates
+agree to rounding, and both agree with the reference's lexicographic SOR at
+the converged fixed point."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from cfd_nssolver_forhpc_gb300 import capi
+from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+from cfd_nssolver_forhpc_gb300.simulation import Simulation
+from oracle.oracle import Grid
+from tests.helpers import kernel_inputs, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _centered(a):
+    return a - a.mean()
+
+
+def _consistent_rhs(oracle, g, solver):
+    x_true = kernel_inputs(g.ng, g.n)["x"]
+    b = np.zeros(g.n)
+    if solver == capi.SOLVER_BICG_SPE:
+        co, _, jp = oracle.spe_setup(g)
+        oracle.spe_spmv(g, co, jp, x_true, b)
+        op = dict(spe=(co, jp))
+    else:
+        cols, vals, _ = oracle.ell_assemble(g)
+        oracle.ell_spmv(g.n, cols, vals, x_true, b)
+        op = dict(ell=(cols, vals))
+    return b, op
+
+
+def _residual(oracle, g, op, x, b):
+    r = np.zeros(g.n)
+    if "spe" in op:
+        co, jp = op["spe"]
+        oracle.spe_spmv(g, co, jp, x, r)
+    else:
+        cols, vals = op["ell"]
+        oracle.ell_spmv(g.n, cols, vals, x, r)
+    return np.linalg.norm(b - r) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("name", ["g1", "c1"])
+@pytest.mark.parametrize("solver", [capi.SOLVER_BICG_SPE, capi.SOLVER_BICG_ELL])
+def test_bicgstab_matches_oracle(oracle, name, solver):
+    w = WORKLOADS[name]
+    g = Grid.of(w, oracle)
+    b, op = _consistent_rhs(oracle, g, solver)
+    tol = 1e-10
+    ref = oracle.bicg(g, tol, **op)
+    x_ref = np.zeros(g.n)
+    it_ref, res_ref, _ = ref.solve(b, x_ref)
+    with Simulation(w, solver=solver, tol=tol) as S:
+        S.grid_uniform()
+        S.upload("B", b)
+        S.upload("X", np.zeros(g.n))
+        it, res = S.pSolver()
+        x = S.download("X")
+    assert res < tol
+    assert _residual(oracle, g, op, x, b) < 2 * tol
+    assert abs(it - it_ref) <= max(3, 0.1 * it_ref)
+    assert rel_err(_centered(x), _centered(x_ref)) < 1e-6
+
+
+def test_bicgstab_warm_start_and_counters(oracle):
+    """Solves warm-start from the previous solution (Mx.X_result is never
+    reset, RUN_CPU_PC_METHOD.hpp:130,354): a second solve of the same system
+    takes zero iterations beyond the first check."""
+    w = WORKLOADS["g1"]
+    g = Grid.of(w, oracle)
+    b, _ = _consistent_rhs(oracle, g, capi.SOLVER_BICG_SPE)
+    with Simulation(w, tol=1e-10) as S:
+        S.grid_uniform()
+        S.upload("B", b)
+        it1, _ = S.pSolver()
+        it2, res2 = S.pSolver()
+    assert it1 > 10
+    assert it2 <= 1 and res2 < 1e-10
+
+
+def test_bicgstab_iteration_cap_reports_noconv(oracle):
+    """The cap path (bicgstabRe2.hpp:143-163) returns CFD_ERR_NOCONV with a
+    finite x (no NaN/Inf were present, so nothing is reset)."""
+    w = WORKLOADS["g1"]
+    g = Grid.of(w, oracle)
+    b, _ = _consistent_rhs(oracle, g, capi.SOLVER_BICG_SPE)
+    with Simulation(w, tol=1e-14, maxit=3) as S:
+        S.grid_uniform()
+        S.upload("B", b)
+        with pytest.raises(capi.CfdError) as e:
+            S.pSolver()
+        assert e.value.status == -4
+        it, res = S.pSolver(allow_noconv=True)
+        assert it == 3 and res > 1e-14
+        assert np.all(np.isfinite(S.download("X")))
+
+
+def test_zero_rhs_returns_immediately():
+    w = WORKLOADS["g0"]
+    with Simulation(w, tol=1e-10) as S:
+        S.grid_uniform()
+        S.upload("B", np.zeros(w.n_cells))
+        it, res = S.pSolver()
+        assert it == 0 and res == 0.0
+
+
+@pytest.mark.parametrize("solver", [capi.SOLVER_BICG_SPE, capi.SOLVER_BICG_ELL])
+def test_mixed_precision_defect_correction(oracle, solver):
+    """FP32 inner BiCGSTAB + FP64 defect correction reaches the FP64
+    tolerance on the FP64 residual."""
+    w = WORKLOADS["c1"]
+    g = Grid.of(w, oracle)
+    b, op = _consistent_rhs(oracle, g, solver)
+    tol = 1e-10
+    with Simulation(w, solver=solver, tol=tol, precision=capi.PREC_MIXED, inner_tol=1e-4) as S:
+        S.grid_uniform()
+        S.upload("B", b)
+        it, res = S.pSolver()
+        x = S.download("X")
+    assert res < tol
+    assert _residual(oracle, g, op, x, b) < 2 * tol
+    assert it > 0
+
+
+@pytest.mark.parametrize("name", ["g1", "c1"])
+def test_sor_redblack_matches_oracle(oracle, name):
+    w = WORKLOADS[name]
+    g = Grid.of(w, oracle)
+    I = kernel_inputs(g.ng, g.n)
+    u1, v1, w1 = (0.01 * I[k] for k in ("u1", "v1", "w1"))
+    p0 = I["sor_p"]
+    cf = oracle.sor_coef(g)
+    oracle.sor_rhs(g, w.dt, u1, v1, w1, cf)
+    p_ref = p0.copy()
+    it_ref, err_ref = oracle.sor(g, 1.7, 1e-9, 400, cf, p_ref, redblack=True)
+    with Simulation(w, solver=capi.SOLVER_SOR_RB, tol=1e-9, omega=1.7, sor_maxit=400,
+                    check_every=7) as S:
+        S.grid_uniform()
+        S.upload("P", p0)
+        for k, a in (("U1", u1), ("V1", v1), ("W1", w1)):
+            S.upload(k, a)
+        it, err = S.SorPipeLine(S.T1)
+        p = S.download("P")
+    assert abs(it - it_ref) <= 1
+    assert rel_err(g.interior(p), g.interior(p_ref)) < 1e-10
+    # ghost pressures are not touched by the sweeps (SorPipeLine.seq.hpp:74-104)
+    ghost = np.ones(g.ng, dtype=bool)
+    g.interior(ghost.view())[...] = False
+    np.testing.assert_array_equal(p[ghost], p0[ghost])

@@ -1,0 +1,162 @@
+"""Whole time steps on the GPU against the oracle and the reference's golden
+runs: predictor-corrector and plain drivers, SPE / ELL BiCGSTAB and
+red-black SOR, both source-index conventions, FP64 and mixed precision.
+
+Tolerances: Cd agrees with the oracle to 1e-7 relative and fields to 1e-7
+relative after several steps at solver tolerance 1e-10 (the two sides sum
+dot products in different orders, so their Krylov iterates differ at the
+tolerance level); mixed precision is compared with the FP64 GPU run."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from cfd_nssolver_forhpc_gb300 import capi
+from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+from cfd_nssolver_forhpc_gb300.initial import initial_velocity
+from cfd_nssolver_forhpc_gb300.simulation import Simulation
+from oracle.oracle import Grid
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_run(oracle, w, steps, *, method=0, solver=0, aligned=False, tol=1e-10):
+    g = Grid.of(w, oracle)
+    eta = oracle.eta_cylinder_z(g, w.cx, w.center_y)
+    S = oracle.sim(g, method=method, solver=solver, aligned_src=aligned, compat=True, dt=w.dt,
+                   nu=1.0 / w.re, tol=tol, omega=w.omega, bc_dir=w.bc_dir, bc_num=w.bc_num, eta=eta)
+    S.init()
+    u0, v0, w0 = initial_velocity(w.nxc, w.nyc, w.nzc)
+    S.field("u0")[:] = u0
+    S.field("v0")[:] = v0
+    S.field("w0")[:] = w0
+    S.start()
+    hist = [S.step() for _ in range(steps)]
+    return S, hist
+
+
+def gpu_run(w, steps, **kw):
+    S = Simulation(w, **kw)
+    S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+    hist = [S.step() for _ in range(steps)]
+    return S, hist
+
+
+@pytest.mark.parametrize("name,steps", [("g1", 6), ("c1", 4)])
+@pytest.mark.parametrize("solver", [capi.SOLVER_BICG_SPE, capi.SOLVER_BICG_ELL])
+def test_pc_steps_match_oracle(oracle, name, steps, solver):
+    w = WORKLOADS[name]
+    O, ohist = oracle_run(oracle, w, steps, solver=solver)
+    S, hist = gpu_run(w, steps, solver=solver, tol=1e-10)
+    cd = np.array([h["cd"] for h in hist])
+    ocd = np.array([h[0] for h in ohist])
+    np.testing.assert_allclose(cd, ocd, rtol=1e-7)
+    assert hist[0]["iters"] == [0, 0, 0, 0]
+    for k, f in (("U0", "u0"), ("V0", "v0"), ("W0", "w0")):
+        assert rel_err(S.download(k), O.field(f)) < 1e-7, k
+    assert rel_err(S.download("P"), O.field("p")) < 1e-6
+    for h, oh in zip(hist[1:], ohist[1:]):
+        assert all(abs(a - b) <= max(3, 0.1 * b) for a, b in zip(h["iters"], oh[2]))
+    S.close()
+
+
+def test_pc_steps_match_reference_golden(golden):
+    """20 steps of the 128x64x8 cylinder against the reference's own run."""
+    w = WORKLOADS["c1"]
+    G = golden("c1_run")
+    S, hist = gpu_run(w, 20, tol=1e-8)
+    cd = np.array([h["cd"] for h in hist])
+    cl = np.array([h["cl"] for h in hist])
+    np.testing.assert_allclose(cd, G["spe_cd"], rtol=1e-6)
+    np.testing.assert_allclose(cl, G["spe_cl"], rtol=1e-3, atol=1e-4)
+    u = S.download("U0")
+    ref = G["spe_u_summary"]
+    np.testing.assert_allclose([u.sum(), np.abs(u).sum(), np.abs(u).max()], ref[:3], rtol=1e-7)
+    S.close()
+
+
+def test_golden_g0_fields(golden):
+    G = golden("g0_run")
+    w = WORKLOADS["g0"]
+    S, hist = gpu_run(w, 5, tol=1e-10)
+    for k, f in (("U0", "spe_u"), ("V0", "spe_v"), ("W0", "spe_w")):
+        assert rel_err(S.download(k), G[f]) < 1e-8, k
+    np.testing.assert_allclose([h["cd"] for h in hist], G["spe_cd"], rtol=1e-8)
+    S.close()
+
+
+@pytest.mark.parametrize("aligned", [False, True])
+def test_plain_and_aligned_variants(oracle, aligned):
+    w = WORKLOADS["g1"]
+    for method in (capi.METHOD_PC, capi.METHOD_PLAIN):
+        O, ohist = oracle_run(oracle, w, 4, method=method, aligned=aligned)
+        S, hist = gpu_run(w, 4, method=method, aligned_source=aligned, tol=1e-10)
+        np.testing.assert_allclose([h["cd"] for h in hist], [h[0] for h in ohist], rtol=1e-7)
+        assert rel_err(S.download("U0"), O.field("u0")) < 1e-7
+        S.close()
+
+
+def test_sor_steps_match_oracle(oracle):
+    w = WORKLOADS["g1"]
+    O, ohist = oracle_run(oracle, w, 4, solver=3, tol=1e-9)
+    S, hist = gpu_run(w, 4, solver=capi.SOLVER_SOR_RB, tol=1e-9, omega=w.omega)
+    np.testing.assert_allclose([h["cd"] for h in hist], [h[0] for h in ohist], rtol=1e-8)
+    for h, oh in zip(hist, ohist):
+        assert all(abs(a - b) <= 1 for a, b in zip(h["iters"], oh[2]))
+    assert rel_err(S.download("P"), O.field("p")) < 1e-8
+    S.close()
+
+
+def test_steps_are_bitwise_reproducible():
+    w = WORKLOADS["g1"]
+    a, ha = gpu_run(w, 4, tol=1e-10)
+    b, hb = gpu_run(w, 4, tol=1e-10)
+    assert [h["cd"] for h in ha] == [h["cd"] for h in hb]
+    np.testing.assert_array_equal(a.download("P"), b.download("P"))
+    a.close()
+    b.close()
+
+
+def test_mixed_precision_step_close_to_fp64():
+    w = WORKLOADS["c1"]
+    S64, h64 = gpu_run(w, 4, tol=1e-10)
+    S32, h32 = gpu_run(w, 4, tol=1e-10, precision=capi.PREC_MIXED)
+    cd64 = np.array([h["cd"] for h in h64])
+    cd32 = np.array([h["cd"] for h in h32])
+    np.testing.assert_allclose(cd32, cd64, rtol=1e-4)
+    assert rel_err(S32.download("U0"), S64.download("U0")) < 1e-5
+    assert all(r < 1e-10 for h in h32[1:] for r in h["relres"])
+    S64.close()
+    S32.close()
+
+
+def test_divergence_of_projected_field(oracle):
+    """After a converged solve the projected field T2 = u* - dt grad p has a
+    divergence equal to the removed RHS mean (zero-gradient outflow lets mass
+    leave), so the deviation from that uniform value is at solver level."""
+    w = WORKLOADS["g1"]
+    with Simulation(w, tol=1e-12) as S:
+        S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+        S.step()
+        S.ConvectionDifussion(S.T0, S.T1)
+        mean = S.createBMatrix(S.T1)
+        S.pSolver()
+        S.Pressure_transform_X_result()
+        S.upload("ETA", np.zeros(w.n_ghosted))
+        S.update_UandF(S.T1, S.T3)
+        u, v, ww = S.download("U3"), S.download("V3"), S.download("W3")
+    g = Grid.of(w, oracle)
+    d = np.zeros(g.n)
+    shp = (g.nx, g.ny, g.nz)
+    U, V, W = u.reshape(shp), v.reshape(shp), ww.reshape(shp)
+    dx = w.lx / w.nxc
+    dy = w.ly / w.nyc
+    dz = w.lz / w.nzc
+    s = slice(2, -2)
+    div = ((U[2:-2, s, s] - U[1:-3, s, s]) / dx + (V[s, 2:-2, s] - V[s, 1:-3, s]) / dy
+           + (W[s, s, 2:-2] - W[s, s, 1:-3]) / dz)
+    # interior cells away from the skipped last faces
+    core = div[:-1, :-1, :-1]
+    assert np.max(np.abs(core - core.mean())) < 1e-6 * max(1.0, abs(mean) * w.dt)
+    del d
