@@ -1,0 +1,450 @@
+"""Benchmark of the GB300 time step: Mcell-steps/s of the predictor-corrector
+step of the flow-past-a-cylinder workload at 512x256x32 (4.19 M cells), FP64,
+BiCGSTAB (matrix-free Jacobi-scaled operator) to relative residual 1e-10.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0.  A "step" is one iteration of the reference's main
+loop (three predictor passes and the final pass, four Poisson solves).
+
+* value      -- device time: K steps bracketed by CUDA events on the library's
+                stream, inputs resident in HBM; the working set (~1.5 GB) is far
+                larger than L2, so no flush is needed between steps.
+* e2e        -- the same K steps through the C ABI with the state crossing the
+                boundary every step: upload of T0 (u, v, w) and p from pinned
+                host buffers, the step, download of T0 and p.
+* roofline   -- the dominant kernel (largest share of the step's device time),
+                timed alone with CUDA events on the library stream; bytes are
+                the algorithmic bytes of one launch.
+* cpu_baseline / --impl reference -- the reference's own CPU code for the step
+                (oracle/_ref/<workload>/libref.so, its headers compiled from a
+                patched copy), else the oracle's C restatement, on the host's
+                cores; see the `sample` field for what was timed.
+
+With --gpus N under torchrun each rank runs an independent replica (the step
+is not sharded); value is the sum over ranks, time the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mcell-steps/s mixed vs FP64 on GPU at ||div u||<1e-10; adjoint/forward time ratio"
+UNIT = "Mcell-steps/s"
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic bytes per row (compact cell) of one launch of each kernel, FP64
+# fields (8 B); the FP32 inner kernels of the mixed path move half of the
+# vector bytes (jp included).
+KERNEL_BYTES_PER_ROW = {
+    "bicg_ap": 4,   # read p1, r0, jp; write ap
+    "bicg_s": 3,    # read r1, ap; write s
+    "bicg_as": 3,   # read s, jp; write as
+    "bicg_xr": 7,   # read x, p1, s, as, r0; write x, r1
+    "bicg_p": 4,    # read r1, p1, ap; write p1
+}
+KERNEL_BYTES_PER_CELL_FLOW = {
+    "convdiff": 6,   # read u, v, w; write u*, v*, w*
+    "update_uf": 13,  # read u*, v*, w*, p, eta; write u, v, w, f (3)
+    "rhs": 6,        # read u*, v*, w*, jp; write b (+ mean pass reads jp, b, writes b)
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2")
+    ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison leg")
+    ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        d = json.loads(PEAKS_FILE.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(workload: str, kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_traffic.json"
+    try:
+        d = json.loads(f.read_text())
+        return d[workload][kernel]["dram_bytes_per_launch"]
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+def build_sim(args, w, precision):
+    from cfd_nssolver_forhpc_gb300 import capi
+    from cfd_nssolver_forhpc_gb300.initial import initial_velocity
+    from cfd_nssolver_forhpc_gb300.simulation import Simulation
+    solver = {"spe": capi.SOLVER_BICG_SPE, "ell": capi.SOLVER_BICG_ELL, "sor": capi.SOLVER_SOR_RB}[args.solver]
+    prec = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
+    S = Simulation(w, solver=solver, precision=prec, tol=w.tol, check_every=16)
+    S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+    return S
+
+
+def timed_steps(S, K, dist):
+    """K steps bracketed by barrier + synchronize; CUDA events on the
+    library's stream.  Returns (seconds, step infos)."""
+    import torch
+    stream = torch.cuda.ExternalStream(S.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    torch.cuda.synchronize()
+    S.sync()
+    n0 = S.launch_count()
+    e0.record(stream)
+    infos = [S.step(allow_noconv=True) for _ in range(K)]
+    e1.record(stream)
+    S.sync()
+    torch.cuda.synchronize()
+    dist.barrier()
+    return e0.elapsed_time(e1) / 1e3, infos, S.launch_count() - n0
+
+
+def e2e_steps(S, K, dist):
+    """K steps through the C ABI with the state crossing the host boundary."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from cfd_nssolver_forhpc_gb300.capi import check, lib
+    bufs = {k: np.empty(S.count(k)) for k in ("U0", "V0", "W0", "P")}
+    for k, a in bufs.items():
+        S.download(k, a)
+        check(lib().cfd_host_register(a.ctypes.data_as(C.c_void_p), a.nbytes))
+    stream = torch.cuda.ExternalStream(S.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist.barrier()
+    S.sync()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(K):
+        for k, a in bufs.items():
+            S.upload(k, a)
+        S.step(allow_noconv=True)
+        for k, a in bufs.items():
+            S.download(k, a)
+    e1.record(stream)
+    S.sync()
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    for a in bufs.values():
+        lib().cfd_host_unregister(a.ctypes.data_as(C.c_void_p))
+    nbytes = sum(a.nbytes for a in bufs.values())
+    return max(e0.elapsed_time(e1) / 1e3, 0.0), wall, nbytes
+
+
+def roofline(S, w, infos, precision):
+    """Dominant kernel by share of device time, its achieved GB/s."""
+    ms = S.time_kernels(reps=20)
+    iters = sum(sum(i["iters"]) for i in infos) / len(infos)
+    npass = 4
+    counts = {k: iters for k in KERNEL_BYTES_PER_ROW}
+    counts.update({"convdiff": npass, "update_uf": npass, "rhs": npass})
+    shares = {k: ms[k] * counts.get(k, 0) for k in ms}
+    total = sum(shares.values()) or 1.0
+    top = max(shares, key=shares.get)
+    word = 4 if precision == "mixed" else 8
+    per_row = KERNEL_BYTES_PER_ROW.get(top, KERNEL_BYTES_PER_CELL_FLOW.get(top, 0))
+    bytes_launch = per_row * word * w.n_cells
+    peak, how = peaks()
+    achieved = bytes_launch / (ms[top] * 1e-3) / 1e9
+    return {
+        "kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+        "frac": round(achieved / peak, 4), "peak_source": f"{how} hbm_gbs",
+        "traffic": ncu_traffic(w.name, top),
+        "algorithmic_bytes_per_launch": bytes_launch,
+        "ms_per_launch": round(ms[top], 5),
+        "share_of_step": round(shares[top] / total, 3),
+        "kernels_ms": {k: round(v, 5) for k, v in ms.items()},
+        "shares": {k: round(v / total, 3) for k, v in shares.items()},
+    }
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's own functions (or the oracle restatement)
+def cpu_worker(spec: str):
+    """Runs in a subprocess (its own OpenMP runtime and thread count)."""
+    d = json.loads(spec)
+    from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+    from cfd_nssolver_forhpc_gb300.initial import initial_velocity
+    w = WORKLOADS[d["workload"]]
+    solver = {"spe": 0, "ell": 1, "sor": 2}[d["solver"]]
+    warm, steps = d["warmup"], d["steps"]
+    u0, v0, w0 = initial_velocity(w.nxc, w.nyc, w.nzc)
+    kind = None
+    try:
+        from oracle.oracle import RefHarness
+        R = RefHarness(w.name, build=False)
+        R.setup(w.dt, w.re, w.tol, True)
+        R.pc_start(u0, v0, w0)
+        kind = "reference"
+
+        def run(n):
+            cd, cl, it, wall = R.pc_run(n, 0, solver, True)
+            return list(wall), it.tolist()
+    except (FileNotFoundError, OSError):
+        from oracle.oracle import Grid, Oracle
+        O = Oracle()
+        g = Grid.of(w, O)
+        eta = O.eta_cylinder_z(g, w.cx, w.center_y)
+        sim = O.sim(g, method=0, solver=solver if solver < 2 else 3, compat=True, dt=w.dt, nu=1.0 / w.re,
+                    tol=w.tol, omega=w.omega, bc_dir=w.bc_dir, bc_num=w.bc_num, eta=eta)
+        sim.init()
+        sim.field("u0")[:] = u0
+        sim.field("v0")[:] = v0
+        sim.field("w0")[:] = w0
+        sim.start()
+        kind = "port"
+
+        def run(n):
+            walls, its = [], []
+            for _ in range(n):
+                t = time.perf_counter()
+                r = sim.step()
+                walls.append(time.perf_counter() - t)
+                its.append(r[2])
+            return walls, its
+    run(warm)
+    walls, its = run(steps)
+    print(json.dumps({"kind": kind, "walls": walls, "iters": its}))
+
+
+def cpu_baseline(args, w, warmup, steps, budget_s=600):
+    threads = os.cpu_count() or 1
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PLACES="cores", OMP_PROC_BIND="close",
+               OMP_SCHEDULE="STATIC")
+    spec = json.dumps({"workload": w.name, "solver": args.solver, "warmup": warmup, "steps": steps})
+    try:
+        r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--cpu-worker", spec], env=env,
+                           capture_output=True, text=True, timeout=budget_s)
+        line = [x for x in r.stdout.splitlines() if x.startswith("{")][-1]
+        d = json.loads(line)
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unit": UNIT, "cores": threads, "kind": "unavailable",
+                "sample": f"CPU run failed: {type(e).__name__}"}
+    t = sum(d["walls"])
+    value = w.n_cells * len(d["walls"]) / t / 1e6
+    its = [sum(x) for x in d["iters"]]
+    return {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": d["kind"],
+            "sample": (f"{w.name} {w.nxc}x{w.nyc}x{w.nzc} predictor-corrector steps "
+                       f"{warmup + 1}..{warmup + steps} (after {warmup} untimed), BiCGSTAB tol {w.tol:g}, "
+                       f"{its} solver iterations per step, {t:.1f} s"),
+            "s_per_step": round(t / len(d["walls"]), 3)}
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.cpu_worker:
+        cpu_worker(args.cpu_worker)
+        return
+    from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+    w = WORKLOADS[args.workload]
+    dist = Dist()
+    K, W = args.steps, max(args.warmup, 0)
+
+    if args.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        # each step of the reference arm is one full reference step; the
+        # number of steps is bounded so the run ends within a few minutes
+        k_ref = max(1, min(K, 2))
+        w_ref = max(1, min(W, 3))
+        cb = cpu_baseline(args, w, w_ref, k_ref, budget_s=1500)
+        v = cb["value"]
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": k_ref, "warmup": w_ref, "ms_per_step": (cb.get("s_per_step") or 0) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded 1e-3 perturbation of u=1, v=w=0)",
+                "config": {"workload": f"{w.name}: cylinder wake {w.nxc}x{w.nyc}x{w.nzc}, Re {w.re:g}, "
+                                       f"dt {w.dt:g}, PC step, BiCGSTAB {args.solver} tol {w.tol:g}"},
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if cb["value"] is None:
+            line = {"impl": "reference", "unavailable": cb["sample"]}
+        print(json.dumps(line))
+        dist.close()
+        return
+
+    from cfd_nssolver_forhpc_gb300.build import build
+    build()
+    import torch
+    torch.cuda.init()
+    S = build_sim(args, w, args.precision)
+    for _ in range(W):
+        S.step(allow_noconv=True)
+    with ClockSampler(dist.local) as clk:
+        sec, infos, launches = timed_steps(S, K, dist)
+    clocks = clk.summary()
+    sec_max = dist.max(sec)
+    value = w.n_cells * K * dist.world / sec_max / 1e6
+    mixed = args.precision == "mixed"
+    rl = roofline(S, w, infos, args.precision)
+    div = S.div_inf(0)
+    e2e = None
+    if not args.no_e2e:
+        dev_s, wall_s, nbytes = e2e_steps(S, K, dist)
+        wall_s = dist.max(wall_s)
+        e2e = {"value": round(w.n_cells * K * dist.world / wall_s / 1e6, 4), "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "seconds": round(wall_s, 4)}
+    S.close()
+    mixed_leg = None
+    if not args.no_mixed and not mixed and args.solver != "sor":
+        M = build_sim(args, w, "mixed")
+        for _ in range(W):
+            M.step(allow_noconv=True)
+        msec, minfos, _ = timed_steps(M, K, dist)
+        msec = dist.max(msec)
+        mval = w.n_cells * K * dist.world / msec / 1e6
+        mixed_leg = {"value": round(mval, 4), "unit": UNIT, "ratio_vs_fp64": round(mval / value, 3),
+                     "iters_per_step": [sum(i["iters"]) for i in minfos],
+                     "outer_per_step": [sum(i["outer"]) for i in minfos],
+                     "cd_last": minfos[-1]["cd"]}
+        M.close()
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, w, 1, 1, budget_s=300)
+    if dist.rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world, "steps": K,
+            "warmup": W, "ms_per_step": round(sec_max / K * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
+            "data": "synthetic (seeded 1e-3 perturbation of u=1, v=w=0)",
+            "config": {"workload": f"{w.name}: cylinder wake {w.nxc}x{w.nyc}x{w.nzc} ({w.n_cells} cells), "
+                                   f"Re {w.re:g}, dt {w.dt:g}, predictor-corrector step",
+                       "solver": f"BiCGSTAB {args.solver}" if args.solver != "sor" else "red-black SOR",
+                       "tol": w.tol, "precision": args.precision, "parallelism": f"replicas x{dist.world}",
+                       "l2": "working set larger than L2 (no flush needed)"},
+            "iters_per_step": [sum(i["iters"]) for i in infos],
+            "cd_last": infos[-1]["cd"], "div_inf_T0": div,
+            "roofline": rl, "cpu_baseline": cpu, "clocks": clocks, "e2e": e2e,
+            "gpu_launches": launches,
+        }
+        if mixed_leg:
+            line["mixed"] = mixed_leg
+        print(json.dumps(line))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -96,7 +96,9 @@ def lib() -> C.CDLL:
         "cfd_eta_cylinder_z": ([vp, d, d, d, i], i),
         "cfd_step": ([vp, C.POINTER(CfdStepInfo)], i),
         "cfd_div_inf": ([vp, i, dp], i),
+        "cfd_div_projected": ([vp, i, dp, dp], i),
         "cfd_stream": ([vp, C.POINTER(vp)], i),
+        "cfd_launch_count": ([vp, C.POINTER(C.c_longlong)], i),
         "cfd_time_kernels": ([vp, i, dp, i], i),
     }
     for name, (args, res) in proto.items():

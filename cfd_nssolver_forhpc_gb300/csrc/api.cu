@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -97,6 +98,8 @@ struct cfd_ctx {
     long long loop = 1;
     double time = 0.0;
     bool use_graphs = true;
+    int debug = 0;
+    long long launches = 0;  // kernels issued by the step and solver paths
 };
 
 namespace {
@@ -251,6 +254,7 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
              BicgScal *sc, int which_graph)
 {
     launch_bicg_init<Op, V>(c->lc, A, b, x, w, px1, px2, sc);
+    c->launches += 1;
     CK(cudaGetLastError());
     const int batch = c->cfg.check_every;
     cudaGraphExec_t &ge = c->graph[which_graph];
@@ -268,6 +272,7 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
     }
     const long long cap_batches = (long long)c->cfg.p_iter_max / batch + 3;
     for (long long nb = 0;; ++nb) {
+        c->launches += 5LL * batch;
         if (c->use_graphs) {
             CK(cudaGraphLaunch(ge, c->s));
         } else {
@@ -276,6 +281,11 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
         }
         CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
+        if (c->debug > 1)
+            std::fprintf(stderr, "[cfdgpu] graph %d batch %lld: done %d iter %d relres %.3e rho %.3e alpha %.3e "
+                         "omega %.3e beta %.3e restart %d\n", which_graph, nb, c->h_sc->done, c->h_sc->iter,
+                         c->h_sc->relres, c->h_sc->rho, c->h_sc->alpha, c->h_sc->omega, c->h_sc->beta,
+                         c->h_sc->restart);
         if (c->h_sc->done != BICG_RUNNING) break;
         if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "BiCGSTAB did not report completion");
     }
@@ -291,6 +301,7 @@ int solve64(cfd_ctx *c, const Op &A, int *iters, double *relres)
     int st = CFD_OK;
     if (c->h_sc->done == BICG_CAPPED) {
         launch_bicg_nan_reset<double>(c->lc, c->g.n, c->x, c->px1, c->px2, c->sc);
+        c->launches += 2;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(c->h_sc, c->sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
@@ -323,6 +334,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
     // vector in mixed-precision contexts)
     double norm0 = 0.0;
     residual64(c, A64, c->b, c->w64.r0, c->r32, c->dscal + 4);
+    c->launches += 1;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
@@ -338,6 +350,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
     int st = CFD_OK;
     for (;;) {
         residual64(c, A64, c->b, c->x, c->r32, c->dscal + 3);
+        c->launches += 1;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
@@ -347,7 +360,12 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
         CK(cudaMemsetAsync(c->e32, 0, (size_t)n * sizeof(float), c->s));
         CKS((bicg_run<Op32, float>(c, A32, c->r32, c->e32, c->w32, nullptr, nullptr, c->sc_in, 1)));
         total += c->h_sc->iter;
+        if (c->debug)
+            std::fprintf(stderr, "[cfdgpu] outer %d rel %.3e | inner done %d iter %d relres %.3e norm0 %.3e "
+                         "rho %.3e alpha %.3e omega %.3e\n", sweeps, rel, c->h_sc->done, c->h_sc->iter,
+                         c->h_sc->relres, c->h_sc->norm0, c->h_sc->rho, c->h_sc->alpha, c->h_sc->omega);
         launch_correct<float>(c->lc, n, c->x, c->e32);
+        c->launches += 1;
         CK(cudaGetLastError());
         ++sweeps;
     }
@@ -377,15 +395,18 @@ int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
     const Metrics<double> m = metrics_of<double>(c);
     launch_sor_rhs<T>(c->s, g, m, 1.0 / c->cfg.dt, dv<T>(c, si, 0), dv<T>(c, si, 1), dv<T>(c, si, 2),
                       c->cf6);
+    c->launches += 1;
     const int itmax = c->cfg.p_sor_iter_max;
     CK(cudaMemsetAsync(c->sor_res, 0, (size_t)(itmax + 1) * sizeof(unsigned long long), c->s));
     CK(cudaMemsetAsync(c->sor_state, 0, 2 * sizeof(int), c->s));
     const int batch = c->cfg.check_every;
     int sweep = 0;
     for (;;) {
-        for (int q = 0; q < batch && sweep <= itmax; ++q, ++sweep)
+        for (int q = 0; q < batch && sweep <= itmax; ++q, ++sweep) {
             launch_sor_sweep(c->s, g, m, c->cf6, c->cf7, c->p, c->cfg.p_sor_omega, c->cfg.p_criteria,
                              itmax, sweep, c->sor_res, c->sor_state);
+            c->launches += 2;
+        }
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(c->h_sor_state, c->sor_state, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
@@ -412,10 +433,12 @@ int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer)
     }
     launch_rhs<T>(c->lc, g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, si, 0),
                   dv<T>(c, si, 1), dv<T>(c, si, 2), c->b, c->cfg.compat_rhs != 0, c->dscal + 0);
+    c->launches += c->cfg.compat_rhs ? 2 : 1;
     CK(cudaGetLastError());
     int st = poisson_solve(c, iters, relres, outer);
     if (st != CFD_OK && st != CFD_ERR_NOCONV) return st;
     launch_transform(c->s, g, c->x, c->p);
+    c->launches += 1;
     CK(cudaGetLastError());
     return st;
 }
@@ -440,6 +463,7 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
         launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, u1, v1, w1,
                            (pc && aligned && pass > 0) ? src : nullptr);
         if (pc && !aligned) launch_src_add<T>(c->lc, g, 0, u1, v1, w1, src);
+        c->launches += (pc && !aligned) ? 2 : 1;
         CK(cudaGetLastError());
         if (c->loop > 1) {
             int s2 = pressure_step<T>(c, 1, &loc.iters[pass], &loc.relres[pass], &loc.outer[pass]);
@@ -449,6 +473,7 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
         launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
                             u1, v1, w1, u3, v3, w3, f);
         if (pc && pass < 3) launch_src_accumulate<T>(c->lc, 3 * g.n, dt, src, f);
+        c->launches += (pc && pass < 3) ? 2 : 1;
         CK(cudaGetLastError());
     }
     const size_t bytes = (size_t)g.ng * sizeof(T);
@@ -460,6 +485,7 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
     launch_bc_main<T>(c->s, g, bc, u0, v0, w0, c->p);
     launch_bc_copy<T>(c->s, g, u0, v0, w0, u1, v1, w1);
     launch_cdcl<T>(c->lc, g, metrics_of<double>(c), c->cfg.lz, f, c->dscal + 1);
+    c->launches += 3 + 1 + 1;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
@@ -596,6 +622,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     g.ng = (long long)g.nx * g.ny * g.nz;
     g.n = n;
     if (const char *e = std::getenv("CFDGPU_NO_GRAPH")) c->use_graphs = !(e[0] == '1');
+    if (const char *e = std::getenv("CFDGPU_DEBUG")) c->debug = std::atoi(e);
 
     int st = CFD_OK;
     auto bail = [&](int code) { free_ctx(c); return code; };
@@ -659,7 +686,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     AL(c->sc_in, sizeof(BicgScal));
     AL(c->sc_t, sizeof(BicgScal));
     AL(c->dscal, 8 * sizeof(double));
-    AL(c->dmax, sizeof(unsigned long long));
+    AL(c->dmax, 2 * sizeof(unsigned long long));
     const int red_blocks = blocks_for(n, sms * 8);
     AL(c->lc.partials, (size_t)4 * red_blocks * sizeof(double));
     AL(c->lc.counter, sizeof(unsigned int));
@@ -668,7 +695,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (cudaMallocHost(reinterpret_cast<void **>(&c->h_sc), sizeof(BicgScal)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_scal), 8 * sizeof(double)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_sor_state), 4 * sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(reinterpret_cast<void **>(&c->h_max), sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMallocHost(reinterpret_cast<void **>(&c->h_max), 2 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(CFD_ERR_NOMEM, "pinned host allocation failed"));
     }
@@ -1082,6 +1109,35 @@ int cfd_div_inf(cfd_ctx *c, int slot, double *out)
     CK(cudaMemcpyAsync(c->h_max, c->dmax, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
     std::memcpy(out, c->h_max, sizeof(double));
+    return CFD_OK;
+}
+
+int cfd_div_projected(cfd_ctx *c, int slot, double *div_inf, double *dev_inf)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot));
+    const int a = slot_index(slot);
+    CK(cudaMemsetAsync(c->dmax, 0, 2 * sizeof(unsigned long long), c->s));
+    const double *mean = c->cfg.compat_rhs ? c->dscal + 0 : nullptr;
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_div_projected<T>(c->lc, c->g, metrics_of<double>(c), c->cfg.dt, c->p, dv<T>(c, a, 0),
+                                dv<T>(c, a, 1), dv<T>(c, a, 2), mean, c->dmax);
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(c->h_max, c->dmax, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    if (div_inf) std::memcpy(div_inf, c->h_max, sizeof(double));
+    if (dev_inf) std::memcpy(dev_inf, c->h_max + 1, sizeof(double));
+    return CFD_OK;
+}
+
+int cfd_launch_count(cfd_ctx *c, long long *count)
+{
+    CKS(check_ctx(c));
+    if (!count) return fail(CFD_ERR_ARG, "null output");
+    *count = c->launches;
     return CFD_OK;
 }
 

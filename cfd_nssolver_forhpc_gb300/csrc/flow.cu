@@ -472,6 +472,45 @@ k_div_inf(Geo g, Metrics<double> m, const T *__restrict__ u, const T *__restrict
     grid_max_nonneg(mx, slot);
 }
 
+// Divergence of the projected field T2 = u* - dt grad p (updateUandF.hpp:136,
+// 158, 179) per interior cell, with the reference's face rules: faces between
+// two interior cells are projected, the domain-boundary faces and the
+// skipped last normal faces keep u*.  slot[0] <- max |div T2|, slot[1] <-
+// max |div T2 - c| with c = -dt * (removed RHS mean), the value a converged
+// solve of the compatible system leaves in every cell.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_div_projected(Geo g, Metrics<double> m, double dt, const double *__restrict__ p,
+                const T *__restrict__ u1, const T *__restrict__ v1, const T *__restrict__ w1,
+                const double *__restrict__ mean, unsigned long long *slot)
+{
+    const double c = -dt * (mean ? *mean : 0.0);
+    double mx = 0.0, md = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        const double pc = p[ic];
+        double ue = (double)u1[ic], uw = (double)u1[ic - g.sx];
+        if (i < g.nx - GC - 1) ue -= dt * (p[ic + g.sx] - pc) * m.x(AX_RDS, i);
+        if (i > GC) uw -= dt * (pc - p[ic - g.sx]) * m.x(AX_RDS, i - 1);
+        double vn = (double)v1[ic], vs = (double)v1[ic - g.sy];
+        if (j < g.ny - GC - 1) vn -= dt * (p[ic + g.sy] - pc) * m.y(AX_RDS, j);
+        if (j > GC) vs -= dt * (pc - p[ic - g.sy]) * m.y(AX_RDS, j - 1);
+        double wt = (double)w1[ic], wb = (double)w1[ic - 1];
+        if (k < g.nz - GC - 1) wt -= dt * (p[ic + 1] - pc) * m.z(AX_RDS, k);
+        if (k > GC) wb -= dt * (pc - p[ic - 1]) * m.z(AX_RDS, k - 1);
+        const double d = (ue - uw) * m.x(AX_RD, i) + (vn - vs) * m.y(AX_RD, j) + (wt - wb) * m.z(AX_RD, k);
+        const double a = fabs(d), b = fabs(d - c);
+        mx = (a > mx || a != a) ? a : mx;
+        md = (b > md || b != b) ? b : md;
+    }
+    grid_max_nonneg(mx, slot);
+    __syncthreads();
+    grid_max_nonneg(md, slot + 1);
+}
+
 template <class T>
 __global__ void k_fill(long long n, T *__restrict__ a, T val)
 {
@@ -586,6 +625,14 @@ void launch_div_inf(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, c
 }
 
 template <class T>
+void launch_div_projected(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double dt,
+                          const double *p, const T *u1, const T *v1, const T *w1, const double *mean,
+                          unsigned long long *slot2)
+{
+    k_div_projected<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, dt, p, u1, v1, w1, mean, slot2);
+}
+
+template <class T>
 void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val)
 {
     k_fill<T><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, val);
@@ -616,7 +663,10 @@ void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b)
                                     T *, T *, T *);                                              \
     template void launch_div_inf<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,      \
                                     const T *, const T *, const T *, unsigned long long *);      \
-    template void launch_fill<T>(cfd_launch_ctx &, long long, T *, T);
+    template void launch_fill<T>(cfd_launch_ctx &, long long, T *, T);                           \
+    template void launch_div_projected<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,  \
+                                          double, const double *, const T *, const T *, const T *, \
+                                          const double *, unsigned long long *);
 
 CFD_FLOW_INSTANTIATE(double)
 CFD_FLOW_INSTANTIATE(float)

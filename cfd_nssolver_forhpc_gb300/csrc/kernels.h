@@ -54,6 +54,10 @@ template <class T>
 void launch_div_inf(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const T *u,
                     const T *v, const T *w, unsigned long long *slot);
 template <class T>
+void launch_div_projected(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double dt,
+                          const double *p, const T *u1, const T *v1, const T *w1, const double *mean,
+                          unsigned long long *slot2);
+template <class T>
 void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val);
 template <class A, class B>
 void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b);

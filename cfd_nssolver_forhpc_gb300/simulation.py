@@ -194,6 +194,12 @@ class Simulation:
         check(lib().cfd_div_inf(self._h, slot, C.byref(out)))
         return out.value
 
+    def div_projected(self, slot=T1) -> tuple[float, float]:
+        """(max |div T2|, max |div T2 + dt * removed mean|) of T2 = u* - dt grad p."""
+        a, b = C.c_double(), C.c_double()
+        check(lib().cfd_div_projected(self._h, slot, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def step(self, allow_noconv=False) -> dict:
         info = capi.CfdStepInfo()
         check(lib().cfd_step(self._h, C.byref(info)), allow=(-4,) if allow_noconv else ())
@@ -205,6 +211,11 @@ class Simulation:
         out = C.c_void_p()
         check(lib().cfd_stream(self._h, C.byref(out)))
         return out.value or 0
+
+    def launch_count(self) -> int:
+        n = C.c_longlong()
+        check(lib().cfd_launch_count(self._h, C.byref(n)))
+        return n.value
 
     def time_kernels(self, reps: int = 20) -> dict:
         """Mean ms per launch of each hot kernel (CUDA events on the context

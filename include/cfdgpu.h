@@ -190,8 +190,22 @@ int cfd_eta_cylinder_z(cfd_ctx *ctx, double cx, double cy, double radius, int ns
 int cfd_step(cfd_ctx *ctx, cfd_step_info *info);
 /* max |div T[slot]| over interior cells, FP64 */
 int cfd_div_inf(cfd_ctx *ctx, int slot, double *out);
+/* Divergence of the projected field T2 = u* - dt grad p that update_UandF
+   forms (updateUandF.hpp:136, 158, 179), with u* = T[slot] and the current p,
+   using the reference's face rules (boundary faces and the skipped last
+   normal faces are not projected).  *div_inf = max |div T2|; *dev_inf =
+   max |div T2 + dt * m| where m is the RHS mean removed by the last
+   compatibility projection (0 when compat_rhs is off): the part of the
+   divergence a converged pressure solve is responsible for.  FP64. */
+int cfd_div_projected(cfd_ctx *ctx, int slot, double *div_inf, double *dev_inf);
 
 /* ---- instrumentation ---------------------------------------------------- */
+/* Number of kernels the context has issued from the time-step and solver
+   paths (cfd_step, cfd_bicgstab, cfd_sor and what they call), counting every
+   kernel node of a replayed CUDA graph, including Krylov iterations queued
+   past convergence that return at once. */
+int cfd_launch_count(cfd_ctx *ctx, long long *count);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that record events
    or order their own work on it. */
 int cfd_stream(cfd_ctx *ctx, void **stream);

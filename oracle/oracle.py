@@ -321,6 +321,9 @@ class RefHarness:
         self.ng = (self.nxc + 4) * (self.nyc + 4) * (self.nzc + 4)
         self.n = self.nxc * self.nyc * self.nzc
 
+    def set_threads(self, n: int):
+        self.L.ref_set_threads(int(n))
+
     def setup(self, dt, re, tol=1e-3, with_eta=True):
         self.L.ref_setup(dt, re, tol, int(with_eta))
 

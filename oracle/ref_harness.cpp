@@ -76,6 +76,11 @@ void compat_hook(MxClass &Mx, const std::vector<double> &jp)
 
 extern "C" {
 
+// OpenMP thread count of the reference's loops.  BC_staggered_main races
+// between its `omp for nowait` face loops (Boundary_Condition.hpp:72-142)
+// when more than one thread runs it; parity checks use 1.
+void ref_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
+
 void ref_dims(int *nxc, int *nyc, int *nzc, double *lens)
 {
     grid g;

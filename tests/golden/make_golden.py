@@ -47,6 +47,7 @@ def summary(a: np.ndarray) -> np.ndarray:
 def make_g0() -> None:
     w = WORKLOADS["g0"]
     R = RefHarness("g0")
+    R.set_threads(1)
     R.setup(w.dt, w.re, 1e-10, True)
     ng, n = R.ng, R.n
     I = kernel_inputs(ng, n)
@@ -90,6 +91,7 @@ def run_pc(name: str, steps: int, tol: float, solvers=(0,), with_fields=True) ->
     out = {}
     for solver in solvers:
         R = RefHarness(name)
+        R.set_threads(1)
         R.setup(w.dt, w.re, tol, True)
         u0, v0, w0 = initial_velocity(w.nxc, w.nyc, w.nzc)
         R.pc_start(u0, v0, w0)
