@@ -89,6 +89,11 @@ struct EllOp {
 // plus its persistent counters).
 struct BicgScal {
     double norm0, rho, alpha, omega, beta, relres, tol, restart_tol;
+    // restart_rel > 0 selects the scale-invariant restart of the FP32 inner
+    // solves: restart when |r1.r0| < restart_rel |r1| |r0| (r0n2 = |r0|^2),
+    // re-seeding the shadow residual with r1 and rho with |r1|^2.
+    // restart_rel == 0 keeps bicgstabRe2's absolute rule.
+    double restart_rel, r0n2;
     int iter, done, restart, timestep, maxit, restarts, total_iters, nonfinite;
 };
 enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
@@ -115,6 +120,12 @@ void launch_bicg_init(cfd_launch_ctx &c, const Op &A, const V *b, V *x, const Bi
                       V *px1, V *px2, BicgScal *sc);
 template <class Op, class V>
 void launch_bicg_iteration(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc);
+// fused FP32 iteration of the mixed-precision inner solves (SPE operator):
+// k_bicg_pap (p update + SpMV), k_bicg_sas (s update + SpMV), k_bicg_xr;
+// p/ap alternate between (w.p1, w.ap) and (p_alt, ap_alt)
+template <class V>
+void launch_bicg_fused_iteration(cfd_launch_ctx &c, const SpeOp<V> &A, V *x, const BicgVecs<V> &w,
+                                 V *p_alt, V *ap_alt, BicgScal *sc, int from, bool first);
 // one kernel of the iteration (0 ap, 1 s, 2 as, 3 xr, 4 p), for timing
 template <class Op, class V>
 void launch_bicg_iteration_part(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc,

@@ -50,6 +50,35 @@ __device__ __forceinline__ V apply_row(const EllOp<V> &A, const V *__restrict__ 
     return s;
 }
 
+// Same operator with the x values supplied by a functor (used by the fused
+// kernels that form their input vector on the fly) and, when A.jp is null,
+// the Jacobi scale recomputed as 1 / (sum of the present coefficients): the
+// diagonal of SPE_matrix1 (SPE_sparseMatrix1.hpp:86-96).
+template <class V, class F>
+__device__ __forceinline__ V apply_row_f(const SpeOp<V> &A, long long row, F &&xat)
+{
+    const int i = (int)(row / A.sxc);
+    const long long rem = row - (long long)i * A.sxc;
+    const int j = (int)(rem / A.nzc);
+    const int k = (int)(rem - (long long)j * A.nzc);
+    const long long xw = i > 0 ? row - A.sxc : row;
+    const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
+    const long long ys = j > 0 ? row - A.nzc : row;
+    const long long yn = j < A.nyc - 1 ? row + A.nzc : row;
+    const long long zb = k > 0 ? row - 1 : row;
+    const long long zt = k < A.nzc - 1 ? row + 1 : row;
+    const V cxm = __ldg(A.cxm + i), cxp = __ldg(A.cxp + i), cym = __ldg(A.cym + j), cyp = __ldg(A.cyp + j);
+    const V czm = __ldg(A.czm + k), czp = __ldg(A.czp + k);
+    V s = cxm * xat(xw);
+    s = fma(cym, xat(ys), s);
+    s = fma(czm, xat(zb), s);
+    s = fma(czp, xat(zt), s);
+    s = fma(cyp, xat(yn), s);
+    s = fma(cxp, xat(xe), s);
+    const V jp = A.jp ? A.jp[row] : V(1) / (((((cxm + cxp) + cym) + cyp) + czm) + czp);
+    return fma(-jp, s, xat(row));
+}
+
 template <class Op>
 __global__ void __launch_bounds__(kBlock) k_apply(Op A, const double *__restrict__ x, double *__restrict__ r)
 {
@@ -210,6 +239,7 @@ k_bicg_init(Op A, const V *__restrict__ b, V *__restrict__ x, V *__restrict__ r0
     if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
         sc->norm0 = sqrt(tot[0]);
         sc->rho = tot[1];
+        sc->r0n2 = tot[1];
         sc->iter = 0;
         sc->restart = 0;
         sc->nonfinite = 0;
@@ -279,7 +309,7 @@ k_bicg_xr(long long n, V *__restrict__ x, const V *__restrict__ p1, const V *__r
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
          row += (long long)gridDim.x * blockDim.x) {
         const V s = s1[row];
-        x[row] += fma(alpha, p1[row], omega * s);
+        x[row] = fma(omega, s, fma(alpha, p1[row], x[row]));  // x + alpha p + omega s, 2 FMA
         const V r = fma(-omega, as[row], s);
         r1[row] = r;
         const double rd = (double)r;
@@ -296,9 +326,17 @@ k_bicg_xr(long long n, V *__restrict__ x, const V *__restrict__ p1, const V *__r
             sc->done = BICG_CAPPED;
         } else {
             const double pre = sc->rho;
-            sc->rho = tot[1];
+            int restart;
+            if (sc->restart_rel > 0.0) {
+                restart = !(fabs(tot[1]) >= sc->restart_rel * sqrt(tot[0] * sc->r0n2));
+                sc->rho = restart ? tot[0] : tot[1];
+                if (restart) sc->r0n2 = tot[0];
+            } else {
+                // bicgstabRe2.hpp:166-182 (rho keeps r1.r0 of the old shadow)
+                restart = !(sc->timestep < 10 || fabs(pre) > sc->restart_tol);
+                sc->rho = tot[1];
+            }
             sc->beta = (sc->alpha / sc->omega) * (tot[1] / pre);
-            const int restart = !(sc->timestep < 10 || fabs(pre) > sc->restart_tol);
             sc->restart = restart;
             sc->restarts += restart;
             sc->iter += 1;
@@ -327,6 +365,107 @@ k_bicg_p(long long n, V *__restrict__ r0, const V *__restrict__ r1, V *__restric
          row += (long long)gridDim.x * blockDim.x)
         p1[row] = fma(beta, fma(-omega, ap[row], p1[row]), r1[row]);
 }
+
+// ---------------------------------------------------------------------------
+// Fused kernels of the FP32 inner solves (memory-bound, so forming an input
+// vector at the seven stencil points costs FP32 issue slots, not bytes).
+//
+// k_bicg_pap: the p update of iteration k-1 fused with the SpMV of iteration
+// k: pn = r1 + beta (p - omega ap) (or r1 after a restart, which also sets
+// r0 = r1), apn = A pn, alpha = rho / (apn . r0).  p/ap are read from one
+// buffer pair and written to the other.
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_pap(SpeOp<V> A, const V *__restrict__ r1, const V *__restrict__ p, const V *__restrict__ ap,
+           V *__restrict__ pn, V *__restrict__ apn, V *__restrict__ r0, BicgScal *sc, double *partials,
+           unsigned int *counter)
+{
+    if (sc->done) return;
+    const bool restart = sc->restart != 0;
+    const V beta = restart ? V(0) : (V)sc->beta, omega = restart ? V(0) : (V)sc->omega;
+    auto pat = [&](long long q) { return fma(beta, fma(-omega, ap[q], p[q]), r1[q]); };
+    double acc[1] = {0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V a = apply_row_f(A, row, pat);
+        const V pr = pat(row);
+        pn[row] = pr;
+        apn[row] = a;
+        V rr0;
+        if (restart) {
+            rr0 = r1[row];
+            r0[row] = rr0;
+        } else {
+            rr0 = r0[row];
+        }
+        acc[0] += (double)a * (double)rr0;
+    }
+    double tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+}
+
+// k_bicg_sas: s = r1 - alpha ap fused with as = A s and the two dots.
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_sas(SpeOp<V> A, const V *__restrict__ r1, const V *__restrict__ ap, V *__restrict__ s1,
+           V *__restrict__ as, BicgScal *sc, double *partials, unsigned int *counter)
+{
+    if (sc->done) return;
+    const V alpha = (V)sc->alpha;
+    auto sat = [&](long long q) { return fma(-alpha, ap[q], r1[q]); };
+    double acc[2] = {0.0, 0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V a = apply_row_f(A, row, sat);
+        const V sv = sat(row);
+        s1[row] = sv;
+        as[row] = a;
+        const double ad = (double)a;
+        acc[0] += ad * (double)sv;
+        acc[1] += ad * ad;
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) sc->omega = tot[0] / tot[1];
+}
+
+// k_bicg_ap1: the first SpMV of a solve (p1 = r0 after init), jp on the fly.
+template <class V>
+__global__ void __launch_bounds__(kBlock)
+k_bicg_ap1(SpeOp<V> A, const V *__restrict__ p1, const V *__restrict__ r0, V *__restrict__ ap, BicgScal *sc,
+           double *partials, unsigned int *counter)
+{
+    if (sc->done) return;
+    auto pat = [&](long long q) { return p1[q]; };
+    double acc[1] = {0.0};
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        const V a = apply_row_f(A, row, pat);
+        ap[row] = a;
+        acc[0] += (double)a * (double)r0[row];
+    }
+    double tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+}
+
+// One fused iteration reading p/ap from buffer pair `from` and writing the
+// other pair (first == true: the solve's first iteration, p1 = r0).
+template <class V>
+void launch_bicg_fused_iteration(cfd_launch_ctx &c, const SpeOp<V> &A, V *x, const BicgVecs<V> &w,
+                                 V *p_alt, V *ap_alt, BicgScal *sc, int from, bool first)
+{
+    const int G = c.red_blocks;
+    V *P[2] = {w.p1, p_alt}, *AP[2] = {w.ap, ap_alt};
+    const int to = first ? from : 1 - from;
+    if (first)
+        k_bicg_ap1<V><<<G, kBlock, 0, c.s>>>(A, P[from], w.r0, AP[from], sc, c.partials, c.counter);
+    else
+        k_bicg_pap<V><<<G, kBlock, 0, c.s>>>(A, w.r1, P[from], AP[from], P[to], AP[to], w.r0, sc, c.partials,
+                                             c.counter);
+    k_bicg_sas<V><<<G, kBlock, 0, c.s>>>(A, w.r1, AP[to], w.s1, w.as, sc, c.partials, c.counter);
+    k_bicg_xr<V><<<G, kBlock, 0, c.s>>>(A.n, x, P[to], w.s1, w.as, w.r0, w.r1, sc, c.partials, c.counter);
+}
+template void launch_bicg_fused_iteration<float>(cfd_launch_ctx &, const SpeOp<float> &, float *,
+                                                 const BicgVecs<float> &, float *, float *, BicgScal *, int, bool);
 
 // NaN/Inf reset at the iteration cap (bicgstabRe2.hpp:143-163): non-finite
 // entries of x take the previous initial guess px1; if more than 10% were

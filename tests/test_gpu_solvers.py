@@ -123,7 +123,7 @@ def test_mixed_precision_defect_correction(oracle, solver):
     g = Grid.of(w, oracle)
     b, op = _consistent_rhs(oracle, g, solver)
     tol = 1e-10
-    with Simulation(w, solver=solver, tol=tol, precision=capi.PREC_MIXED, inner_tol=1e-4) as S:
+    with Simulation(w, solver=solver, tol=tol, precision=capi.PREC_MIXED) as S:
         S.grid_uniform()
         S.upload("B", b)
         it, res = S.pSolver()
