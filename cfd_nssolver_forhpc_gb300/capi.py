@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
         "cfd_div_projected": ([vp, i, dp, dp], i),
         "cfd_stream": ([vp, C.POINTER(vp)], i),
         "cfd_launch_count": ([vp, C.POINTER(C.c_longlong)], i),
+        "cfd_cdcl_noalloc": ([i, i, i, d, vp, vp, vp, vp, dp, dp, vp], i),
         "cfd_time_kernels": ([vp, i, dp, i], i),
     }
     for name, (args, res) in proto.items():

@@ -47,6 +47,10 @@ struct Tag {
 
 }  // namespace
 
+namespace cfd {
+int set_last_error(int code, const std::string &msg) { return fail(code, msg); }
+}
+
 struct cfd_ctx {
     cfd_config cfg{};
     Geo g{};

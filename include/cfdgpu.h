@@ -232,6 +232,27 @@ typedef enum {
    entries are written). */
 int cfd_time_kernels(cfd_ctx *ctx, int reps, double *ms, int nms);
 
+/* ---- allocation-free drag and lift ------------------------------------- */
+/* No counterpart in the reference.  The same drag and lift as cfd_cdcl, for
+   callers that cannot allocate device memory: an application whose own pool
+   owns the GPU's memory and forbids allocations outside it, or a loop that
+   cannot afford the device-wide synchronisation a cudaMalloc may cause.
+   The caller passes device arrays: Dx, Dy, Dz (ghosted widths, nx_cal+4 ...
+   entries) and f (3 x compact forcing, DfibArray::f layout); cd and cl are
+   host outputs.  The work is ordered on `stream` (a cudaStream_t, NULL for
+   the default stream), which is synchronised before returning.
+   Nothing is allocated: the scratch is one file-scope device array of about
+   1 MiB that every GPU that loads the library keeps until the process exits.
+   At most CFD_NOALLOC_MAX_CELLS interior cells; larger grids return
+   CFD_ERR_ARG.  The first call on a device looks up that array's device
+   address with the device current; make that first call before any stream
+   capture.  Every call uses the same scratch: calls that overlap on the GPU
+   (other streams, other host threads) race and must be serialised. */
+#define CFD_NOALLOC_MAX_CELLS 268435456
+int cfd_cdcl_noalloc(int nx_cal, int ny_cal, int nz_cal, double lz, const double *Dx,
+                     const double *Dy, const double *Dz, const double *f, double *cd, double *cl,
+                     void *stream);
+
 #ifdef __cplusplus
 }
 #endif
