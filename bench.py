@@ -43,6 +43,9 @@ METRIC = "Mcell-steps/s mixed vs FP64 on GPU at ||div u||<1e-10; adjoint/forward
 UNIT = "Mcell-steps/s"
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM_GBS = 6800.0
+# FP64 FMA instructions per second of one GB300, measured with a register-
+# resident DFMA loop (2 FP64 FMA per SM per clock)
+FP64_PEAK_TOPS = 0.599
 
 # Algorithmic bytes per row (compact cell) of one launch of each kernel, FP64
 # fields (8 B); the FP32 inner kernels of the mixed path move half of the
@@ -251,22 +254,37 @@ def e2e_steps(S, K, dist):
     return max(e0.elapsed_time(e1) / 1e3, 0.0), wall, nbytes
 
 
+# FP32 kernels of the mixed-precision inner CG (bytes per row) and the FP64
+# residual of its defect correction
+KERNEL_BYTES_MIXED = {
+    "cg_pq": 16,       # read z, p; write p', q (FP32)
+    "cg_upd": 28,      # read e, p, h, q; write e, h, z (FP32)
+    "residual64": 28,  # read b, x, jp (FP64); write r (FP32)
+}
+
+
 def roofline(S, w, infos, precision):
     """Dominant kernel by share of device time, its achieved GB/s."""
     ms = S.time_kernels(reps=20)
     iters = sum(sum(i["iters"]) for i in infos) / len(infos)
+    outer = sum(sum(i["outer"]) for i in infos) / len(infos)
     npass = 4
-    counts = {k: iters for k in KERNEL_BYTES_PER_ROW}
+    if precision == "mixed":
+        counts = {"cg_pq": iters, "cg_upd": iters, "residual64": outer + npass}
+        per_row = dict(KERNEL_BYTES_MIXED)
+    else:
+        counts = {k: iters for k in KERNEL_BYTES_PER_ROW}
+        per_row = {k: v * 8 for k, v in KERNEL_BYTES_PER_ROW.items()}
     counts.update({"convdiff": npass, "update_uf": npass, "rhs": npass})
-    shares = {k: ms[k] * counts.get(k, 0) for k in ms}
+    word = 4 if precision == "mixed" else 8
+    per_row.update({k: v * word for k, v in KERNEL_BYTES_PER_CELL_FLOW.items()})
+    shares = {k: ms[k] * counts[k] for k in ms if k in counts}
     total = sum(shares.values()) or 1.0
     top = max(shares, key=shares.get)
-    word = 4 if precision == "mixed" else 8
-    per_row = KERNEL_BYTES_PER_ROW.get(top, KERNEL_BYTES_PER_CELL_FLOW.get(top, 0))
-    bytes_launch = per_row * word * w.n_cells
+    bytes_launch = per_row[top] * w.n_cells
     peak, how = peaks()
     achieved = bytes_launch / (ms[top] * 1e-3) / 1e9
-    return {
+    out = {
         "kernel": top, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
         "frac": round(achieved / peak, 4), "peak_source": f"{how} hbm_gbs",
         "traffic": ncu_traffic(w.name, top),
@@ -276,6 +294,16 @@ def roofline(S, w, infos, precision):
         "kernels_ms": {k: round(v, 5) for k, v in ms.items()},
         "shares": {k: round(v / total, 3) for k, v in shares.items()},
     }
+    if precision != "mixed":
+        # the FP64 Krylov kernels are bound by the FP64 pipe: FP64 operations
+        # per row (SpMV 7, each dot 1, updates as written) / measured DFMA rate
+        fp64_ops = {"bicg_ap": 8, "bicg_s": 1, "bicg_as": 9, "bicg_xr": 6, "bicg_p": 2}
+        if top in fp64_ops:
+            rate = fp64_ops[top] * w.n_cells / (ms[top] * 1e-3) / 1e12
+            out["fp64_pipe"] = {"achieved_tops": round(rate, 4), "peak_tops": FP64_PEAK_TOPS,
+                                "frac": round(rate / FP64_PEAK_TOPS, 3),
+                                "peak_source": "register-resident DFMA loop on GB300 (0.599 T FMA/s)"}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -399,6 +427,7 @@ def main():
     value = w.n_cells * K * dist.world / sec_max / 1e6
     mixed = args.precision == "mixed"
     rl = roofline(S, w, infos, args.precision)
+    cd64 = infos[-1]["cd"]
     div = S.div_inf(0)
     e2e = None
     if not args.no_e2e:
@@ -413,13 +442,16 @@ def main():
         M = build_sim(args, w, "mixed")
         for _ in range(W):
             M.step(allow_noconv=True)
-        msec, minfos, _ = timed_steps(M, K, dist)
+        msec, minfos, mlaunch = timed_steps(M, K, dist)
         msec = dist.max(msec)
         mval = w.n_cells * K * dist.world / msec / 1e6
         mixed_leg = {"value": round(mval, 4), "unit": UNIT, "ratio_vs_fp64": round(mval / value, 3),
+                     "dtype": "f32+f64", "ms_per_step": round(msec / K * 1e3, 3),
                      "iters_per_step": [sum(i["iters"]) for i in minfos],
                      "outer_per_step": [sum(i["outer"]) for i in minfos],
-                     "cd_last": minfos[-1]["cd"]}
+                     "max_relres": max(r for i in minfos[1:] or minfos for r in i["relres"]),
+                     "cd_last": minfos[-1]["cd"], "cd_rel_vs_fp64": abs(minfos[-1]["cd"] / cd64 - 1.0),
+                     "gpu_launches": mlaunch, "roofline": roofline(M, w, minfos, "mixed")}
         M.close()
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:

@@ -20,9 +20,10 @@ STATUS = {0: "CFD_OK", -1: "CFD_ERR_ARG", -2: "CFD_ERR_CUDA", -3: "CFD_ERR_NOMEM
 SOLVER_BICG_SPE, SOLVER_BICG_ELL, SOLVER_SOR_RB = 0, 1, 3
 METHOD_PC, METHOD_PLAIN = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+INNER_CG, INNER_BICGSTAB = 0, 1
 T0, T1, T3 = 0, 1, 3
 KERNELS = ["bicg_ap", "bicg_s", "bicg_as", "bicg_xr", "bicg_p", "convdiff", "update_uf", "rhs",
-           "sor_sweep"]
+           "sor_sweep", "cg_pq", "cg_upd", "residual64"]
 FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "P", "ETA", "F", "SRC", "X", "B", "JP"]
 FIELD = {name: i for i, name in enumerate(FIELDS)}
 
@@ -42,7 +43,8 @@ class CfdConfig(C.Structure):
                 ("p_sor_omega", C.c_double), ("p_sor_iter_max", C.c_int),
                 ("aligned_source", C.c_int), ("compat_rhs", C.c_int),
                 ("bc_dir", (C.c_double * 3) * 6), ("bc_num", (C.c_double * 3) * 6),
-                ("check_every", C.c_int), ("inner_tol", C.c_double), ("max_outer", C.c_int)]
+                ("check_every", C.c_int), ("inner_tol", C.c_double), ("max_outer", C.c_int),
+                ("inner_solver", C.c_int)]
 
 
 class CfdStepInfo(C.Structure):

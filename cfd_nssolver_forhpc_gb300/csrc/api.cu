@@ -87,9 +87,12 @@ struct cfd_ctx {
     double *px1 = nullptr, *px2 = nullptr;
     float *r32 = nullptr, *e32 = nullptr;
     float *p_alt = nullptr, *ap_alt = nullptr;  // second p/ap pair of the fused FP32 iteration
+    float *fv_sum[3] = {};                      // per-axis cm + cp (FP32) of the CG inner solve
+    float *cg_ip = nullptr;                     // 1 / diag(M) (FP32) of the CG inner solve
     BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
-    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};  // [0] FP64, [1] FP32 inner, [2] fused FP32
-    int graph_batch[3] = {0, 0, 0};
+    // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    int graph_batch[4] = {0, 0, 0, 0};
 
     // SOR
     double *cf6 = nullptr, *cf7 = nullptr;
@@ -164,13 +167,27 @@ SpeOp<double> spe64(cfd_ctx *c)
 {
     const Geo &g = c->g;
     return {c->spe_c[0], c->spe_c[0] + g.nxc, c->spe_c[1], c->spe_c[1] + g.nyc, c->spe_c[2],
-            c->spe_c[2] + g.nzc, c->jp, g.nxc, g.nyc, g.nzc, g.sxc, g.n};
+            c->spe_c[2] + g.nzc, c->jp, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc, FastDiv((unsigned int)g.nzc)};
 }
 SpeOp<float> spe32(cfd_ctx *c)
 {
     const Geo &g = c->g;
     return {c->spe_c32[0], c->spe_c32[0] + g.nxc, c->spe_c32[1], c->spe_c32[1] + g.nyc, c->spe_c32[2],
-            c->spe_c32[2] + g.nzc, c->jp32, g.nxc, g.nyc, g.nzc, g.sxc, g.n};
+            c->spe_c32[2] + g.nzc, c->jp32, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc,
+            FastDiv((unsigned int)g.nzc)};
+}
+FvOp<float> fv32(cfd_ctx *c)
+{
+    const Geo &g = c->g;
+    FvOp<float> F;
+    F.A = spe32(c);
+    F.wx = c->tab32[0] + (size_t)AX_D * g.nx + GC;
+    F.wy = c->tab32[1] + (size_t)AX_D * g.ny + GC;
+    F.wz = c->tab32[2] + (size_t)AX_D * g.nz + GC;
+    F.sx = c->fv_sum[0];
+    F.sy = c->fv_sum[1];
+    F.sz = c->fv_sum[2];
+    return F;
 }
 EllOp<double> ell64(cfd_ctx *c) { return {c->ell_cols, c->ell_vals, c->g.n}; }
 EllOp<float> ell32(cfd_ctx *c) { return {c->ell_cols, c->ell_vals32, c->g.n}; }
@@ -298,25 +315,26 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
     return CFD_OK;
 }
 
-// FP32 inner solve with the fused kernels (SPE operator, jp formed on the
-// fly): init and the first iteration run directly, then iteration pairs are
-// replayed from a graph (the pair returns p/ap to the first buffer pair).
-int bicg_run_fused(cfd_ctx *c, const SpeOp<float> &Ainit, const SpeOp<float> &A, const float *b, float *x,
-                   BicgScal *sc)
+// Runs an inner solve whose first iteration is issued directly and whose
+// later iterations come in pairs (the pair brings the alternating buffers
+// back): prologue(), then graph replays of `pairs` x pair(0), pair(1),
+// polling the scalars once per replay.
+template <class Pro, class Pair>
+int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int launches_prologue,
+              int launches_pair)
 {
-    launch_bicg_init<SpeOp<float>, float>(c->lc, Ainit, b, x, c->w32, nullptr, nullptr, sc);
-    launch_bicg_fused_iteration<float>(c->lc, A, x, c->w32, c->p_alt, c->ap_alt, sc, 0, true);
-    c->launches += 4;
+    prologue();
+    c->launches += launches_prologue;
     CK(cudaGetLastError());
     const int pairs = (c->cfg.check_every + 1) / 2;
-    cudaGraphExec_t &ge = c->graph[2];
+    cudaGraphExec_t &ge = c->graph[gi];
     auto body = [&] {
         for (int q = 0; q < pairs; ++q) {
-            launch_bicg_fused_iteration<float>(c->lc, A, x, c->w32, c->p_alt, c->ap_alt, sc, 0, false);
-            launch_bicg_fused_iteration<float>(c->lc, A, x, c->w32, c->p_alt, c->ap_alt, sc, 1, false);
+            pair(0);
+            pair(1);
         }
     };
-    if (c->use_graphs && (!ge || c->graph_batch[2] != pairs)) {
+    if (c->use_graphs && (!ge || c->graph_batch[gi] != pairs)) {
         if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
         cudaGraph_t gr = nullptr;
         CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
@@ -326,18 +344,18 @@ int bicg_run_fused(cfd_ctx *c, const SpeOp<float> &Ainit, const SpeOp<float> &A,
         e = cudaGraphInstantiate(&ge, gr, 0);
         cudaGraphDestroy(gr);
         if (e != cudaSuccess) { ge = nullptr; return fail(CFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
-        c->graph_batch[2] = pairs;
+        c->graph_batch[gi] = pairs;
     }
     const long long cap_batches = (long long)c->cfg.p_iter_max / (2 * pairs) + 3;
     for (long long nb = 0;; ++nb) {
         CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
         if (c->debug > 1)
-            std::fprintf(stderr, "[cfdgpu] fused batch %lld: done %d iter %d relres %.3e restarts %d\n", nb,
-                         c->h_sc->done, c->h_sc->iter, c->h_sc->relres, c->h_sc->restarts);
+            std::fprintf(stderr, "[cfdgpu] inner graph %d batch %lld: done %d iter %d relres %.3e restarts %d\n", gi,
+                         nb, c->h_sc->done, c->h_sc->iter, c->h_sc->relres, c->h_sc->restarts);
         if (c->h_sc->done != BICG_RUNNING) break;
-        if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "BiCGSTAB did not report completion");
-        c->launches += 6LL * pairs;
+        if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "inner solve did not report completion");
+        c->launches += (long long)launches_pair * 2 * pairs;
         if (c->use_graphs) {
             CK(cudaGraphLaunch(ge, c->s));
         } else {
@@ -346,6 +364,36 @@ int bicg_run_fused(cfd_ctx *c, const SpeOp<float> &Ainit, const SpeOp<float> &A,
         }
     }
     return CFD_OK;
+}
+
+// FP32 inner BiCGSTAB with the fused kernels (SPE operator, jp formed on the fly)
+int bicg_run_fused(cfd_ctx *c, const SpeOp<float> &Ainit, const SpeOp<float> &A, const float *b, float *x,
+                   BicgScal *sc)
+{
+    return run_pairs(
+        c, 2, sc,
+        [&] {
+            launch_bicg_init<SpeOp<float>, float>(c->lc, Ainit, b, x, c->w32, nullptr, nullptr, sc);
+            launch_bicg_fused_iteration<float>(c->lc, A, x, c->w32, c->p_alt, c->ap_alt, sc, 0, true);
+        },
+        [&](int from) { launch_bicg_fused_iteration<float>(c->lc, A, x, c->w32, c->p_alt, c->ap_alt, sc, from, false); },
+        4, 3);
+}
+
+// FP32 Jacobi-preconditioned CG on M e = P r (h = r32 in, scaled in place)
+int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
+{
+    return run_pairs(
+        c, 3, sc,
+        [&] {
+            launch_cg_init(c->lc, F, h, c->w32.p1, sc);
+            launch_cg_iteration(c->lc, F, c->cg_ip, e, h, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap, sc, 0, true);
+        },
+        [&](int from) {
+            launch_cg_iteration(c->lc, F, c->cg_ip, e, h, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap, sc, from,
+                                false);
+        },
+        3, 2);
 }
 
 // The graphs bake in the buffers and operator of the context; they are
@@ -417,7 +465,8 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
         if constexpr (std::is_same<Op32, SpeOp<float>>::value) {
             SpeOp<float> Afly = A32;
             Afly.jp = nullptr;
-            if (c->fused) CKS(bicg_run_fused(c, A32, Afly, c->r32, c->e32, c->sc_in));
+            if (c->cfg.inner_solver == CFD_INNER_CG) CKS(cg_run(c, fv32(c), c->r32, c->e32, c->sc_in));
+            else if (c->fused) CKS(bicg_run_fused(c, A32, Afly, c->r32, c->e32, c->sc_in));
             else CKS((bicg_run<Op32, float>(c, A32, c->r32, c->e32, c->w32, nullptr, nullptr, c->sc_in, 1)));
         } else {
             CKS((bicg_run<Op32, float>(c, A32, c->r32, c->e32, c->w32, nullptr, nullptr, c->sc_in, 1)));
@@ -596,8 +645,10 @@ int build_tables(cfd_ctx *c)
         for (int a = 0; a < 3; ++a) {
             const int na = a == 0 ? g.nxc : a == 1 ? g.nyc : g.nzc;
             launch_convert<double, float>(c->lc, 2LL * na, c->spe_c[a], c->spe_c32[a]);
+            if (c->fv_sum[a]) launch_fv_axes(c->s, na, c->spe_c32[a], c->fv_sum[a]);
         }
         launch_convert<double, float>(c->lc, g.n, c->jp, c->jp32);
+        if (c->cg_ip) launch_cg_ip(c->lc, fv32(c), c->cg_ip);
         if (c->cfg.solver == CFD_SOLVER_BICG_ELL)
             launch_convert<double, float>(c->lc, 7 * g.n, c->ell_vals, c->ell_vals32);
     }
@@ -677,6 +728,8 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (k.precision != CFD_PREC_FP64 && k.precision != CFD_PREC_MIXED)
         return fail(CFD_ERR_ARG, "unknown precision");
     if (k.check_every < 1 || k.check_every > 4096) return fail(CFD_ERR_ARG, "check_every out of range");
+    if (k.inner_solver != CFD_INNER_CG && k.inner_solver != CFD_INNER_BICGSTAB)
+        return fail(CFD_ERR_ARG, "unknown inner solver");
     if (k.precision == CFD_PREC_MIXED && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
         return fail(CFD_ERR_ARG, "mixed precision needs 0 < inner_tol < 1 and max_outer >= 1");
 
@@ -690,6 +743,8 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     g.sxc = (long long)g.nyc * g.nzc; g.syc = g.nzc;
     g.ng = (long long)g.nx * g.ny * g.nz;
     g.n = n;
+    g.fsxc = FastDiv((unsigned int)g.sxc);
+    g.fsyc = FastDiv((unsigned int)g.syc);
     if (const char *e = std::getenv("CFDGPU_NO_GRAPH")) c->use_graphs = !(e[0] == '1');
     if (const char *e = std::getenv("CFDGPU_DEBUG")) c->debug = std::atoi(e);
     if (const char *e = std::getenv("CFDGPU_NO_FUSED")) c->fused = !(e[0] == '1');
@@ -744,6 +799,8 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         AL(c->r32, n * 4); AL(c->e32, n * 4);
         AL(c->p_alt, n * 4); AL(c->ap_alt, n * 4);
         for (int a = 0; a < 3; ++a) AL(c->spe_c32[a], (size_t)2 * nc[a] * sizeof(float));
+        for (int a = 0; a < 3; ++a) AL(c->fv_sum[a], (size_t)nc[a] * sizeof(float));
+        AL(c->cg_ip, n * 4);
         AL(c->jp32, n * 4);
         if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
     }
@@ -773,6 +830,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     c->lc.s = c->s;
     c->lc.red_blocks = red_blocks;
     c->lc.grid_cap = sms * 16;
+    c->lc.cg_grid = cg_resident_grid(sms, red_blocks);
 
     // zero everything, then the reference's initial values
     e = cudaMemsetAsync(c->lc.counter, 0, sizeof(unsigned int), c->s);
@@ -1272,6 +1330,25 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
             CK(cudaMemcpyAsync(c->px2, c->px1, (size_t)g.n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
         }
         if (st != CFD_OK) return st;
+        if (c->fp32 && c->cfg.solver == CFD_SOLVER_BICG_SPE) {
+            const FvOp<float> F = fv32(c);
+            CK(cudaMemcpyAsync(c->sc_t, &hs, sizeof(hs), cudaMemcpyHostToDevice, c->s));
+            CK(cudaMemsetAsync(c->e32, 0, (size_t)g.n * sizeof(float), c->s));
+            if ((st = timed(CFD_KERNEL_CG_PQ, [&] {
+                     launch_cg_part(c->lc, F, c->cg_ip, c->e32, c->r32, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap,
+                                    c->sc_t, 0);
+                 })) != CFD_OK)
+                return st;
+            if ((st = timed(CFD_KERNEL_CG_UPD, [&] {
+                     launch_cg_part(c->lc, F, c->cg_ip, c->e32, c->r32, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap,
+                                    c->sc_t, 1);
+                 })) != CFD_OK)
+                return st;
+            if ((st = timed(CFD_KERNEL_RESIDUAL64, [&] {
+                     residual64(c, spe64(c), c->b, c->x, c->r32, c->dscal + 5);
+                 })) != CFD_OK)
+                return st;
+        }
     }
     st = dispatch(c, [&](auto tag) -> int {
         using T = typename decltype(tag)::type;

@@ -20,6 +20,22 @@ namespace cfd {
 constexpr int GC = 2;
 constexpr int kBlock = 256;
 
+// Division by a loop-invariant divisor d for dividends below 2^31:
+// q = (umulhi(n, m) + n) >> s with s = ceil(log2 d) and
+// m = 2^32 (2^s - d) / d + 1 (the round-up method for invariant integer
+// division).  Replaces 64-bit integer divides in the row decompositions.
+struct FastDiv {
+    unsigned int d = 1, m = 1, s = 0;
+    FastDiv() = default;
+    __host__ explicit FastDiv(unsigned int dv) : d(dv ? dv : 1)
+    {
+        s = 0;
+        while ((1ull << s) < d) ++s;
+        m = (unsigned int)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+    }
+    __device__ __forceinline__ unsigned int div(unsigned int n) const { return (__umulhi(n, m) + n) >> s; }
+};
+
 struct Geo {
     int nx, ny, nz;       // ghosted
     int nxc, nyc, nzc;    // interior
@@ -28,6 +44,7 @@ struct Geo {
     long long sxc;        // compact i stride = nyc*nzc
     int syc;              // compact j stride = nzc
     long long ng, n;      // ghosted and compact element counts
+    FastDiv fsxc, fsyc;   // division by sxc and syc (n < 2^31)
 };
 
 __host__ __device__ __forceinline__ long long icel(const Geo &g, int i, int j, int k)

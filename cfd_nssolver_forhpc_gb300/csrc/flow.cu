@@ -44,12 +44,13 @@ __device__ __forceinline__ void quick_b(T Up, T Un, T pp, T p, T c, T n, T nn, c
 
 __device__ __forceinline__ void cell_of(const Geo &g, long long t, int &i, int &j, int &k)
 {
-    const long long ii = t / g.sxc;
-    const long long rem = t - ii * g.sxc;
-    const int jj = (int)(rem / g.syc);
+    const unsigned int t32 = (unsigned int)t;
+    const unsigned int ii = g.fsxc.div(t32);
+    const unsigned int rem = t32 - ii * (unsigned int)g.sxc;
+    const unsigned int jj = g.fsyc.div(rem);
     i = (int)ii + GC;
-    j = jj + GC;
-    k = (int)(rem - (long long)jj * g.syc) + GC;
+    j = (int)jj + GC;
+    k = (int)(rem - jj * (unsigned int)g.syc) + GC;
 }
 
 // ConvectionDifussion (convection_and_difussion.hpp:168-446): explicit Euler

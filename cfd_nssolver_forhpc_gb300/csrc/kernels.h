@@ -18,6 +18,7 @@ struct cfd_launch_ctx {
     cudaStream_t s;
     int red_blocks;         // grid size of every reducing launch
     int grid_cap;           // cap for grid-stride elementwise launches
+    int cg_grid;            // resident-block grid of the CG inner kernels (<= red_blocks)
     double *partials;       // >= 4 * red_blocks doubles
     unsigned int *counter;  // last-block ticket, zero between launches
 };
@@ -75,6 +76,18 @@ struct SpeOp {
     int nxc, nyc, nzc;
     long long sxc;
     long long n;
+    FastDiv fsxc, fnzc;                           // division by sxc and nzc
+};
+
+// The finite-volume form M = D_V L of the same operator (D_V = cell
+// volumes): (M x)_r = dV_r (diag_r x_r - sum c_nb x_nb), symmetric positive
+// semi-definite, with Jacobi preconditioner P_r = dV_r diag_r.  wx/wy/wz are
+// the interior cell widths, sx/sy/sz the per-axis sums cm + cp.
+template <class V>
+struct FvOp {
+    SpeOp<V> A;
+    const V *wx, *wy, *wz;
+    const V *sx, *sy, *sz;
 };
 
 // ELL operator, slot-major: vals[s * n + row], cols[s * n + row], s < 7
@@ -126,6 +139,19 @@ void launch_bicg_iteration(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<
 template <class V>
 void launch_bicg_fused_iteration(cfd_launch_ctx &c, const SpeOp<V> &A, V *x, const BicgVecs<V> &w,
                                  V *p_alt, V *ap_alt, BicgScal *sc, int from, bool first);
+// FP32 Jacobi-preconditioned CG on M e = P r (the mixed-precision inner
+// solve): init, first M p, then (fused p update + M p, update) pairs
+void launch_cg_init(cfd_launch_ctx &c, const FvOp<float> &F, float *h, float *p, BicgScal *sc);
+void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
+                         float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first);
+// one full wave of the CG inner kernels on this device, capped at red_blocks
+int cg_resident_grid(int sms, int red_blocks);
+// iP = 1 / diag(M), once per context
+void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP);
+void launch_fv_axes(cudaStream_t s, int n, const float *c, float *sum);
+// one CG kernel (0 = fused p update + M p, 1 = update), for timing
+void launch_cg_part(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
+                    float *p, float *pn, float *q, BicgScal *sc, int part);
 // one kernel of the iteration (0 ap, 1 s, 2 as, 3 xr, 4 p), for timing
 template <class Op, class V>
 void launch_bicg_iteration_part(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc,

@@ -17,12 +17,22 @@ namespace cfd {
 // ---------------------------------------------------------------------------
 // operator application
 template <class V>
+__device__ __forceinline__ void decompose(const SpeOp<V> &A, long long row, int &i, int &j, int &k)
+{
+    const unsigned int r = (unsigned int)row;
+    const unsigned int ii = A.fsxc.div(r);
+    const unsigned int rem = r - ii * (unsigned int)A.sxc;
+    const unsigned int jj = A.fnzc.div(rem);
+    i = (int)ii;
+    j = (int)jj;
+    k = (int)(rem - jj * (unsigned int)A.nzc);
+}
+
+template <class V>
 __device__ __forceinline__ V apply_row(const SpeOp<V> &A, const V *__restrict__ x, long long row)
 {
-    const int i = (int)(row / A.sxc);
-    const long long rem = row - (long long)i * A.sxc;
-    const int j = (int)(rem / A.nzc);
-    const int k = (int)(rem - (long long)j * A.nzc);
+    int i, j, k;
+    decompose(A, row, i, j, k);
     const long long xw = i > 0 ? row - A.sxc : row;
     const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
     const long long ys = j > 0 ? row - A.nzc : row;
@@ -57,10 +67,8 @@ __device__ __forceinline__ V apply_row(const EllOp<V> &A, const V *__restrict__ 
 template <class V, class F>
 __device__ __forceinline__ V apply_row_f(const SpeOp<V> &A, long long row, F &&xat)
 {
-    const int i = (int)(row / A.sxc);
-    const long long rem = row - (long long)i * A.sxc;
-    const int j = (int)(rem / A.nzc);
-    const int k = (int)(rem - (long long)j * A.nzc);
+    int i, j, k;
+    decompose(A, row, i, j, k);
     const long long xw = i > 0 ? row - A.sxc : row;
     const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
     const long long ys = j > 0 ? row - A.nzc : row;
@@ -255,14 +263,14 @@ k_bicg_ap(Op A, const V *__restrict__ p1, const V *__restrict__ r0, V *__restric
           double *partials, unsigned int *counter)
 {
     if (sc->done) return;
-    double acc[1] = {0.0};
+    V pa = V(0);
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const V a = apply_row(A, p1, row);
         ap[row] = a;
-        acc[0] += (double)a * (double)r0[row];
+        pa = fma(a, r0[row], pa);
     }
-    double tot[1];
+    double acc[1] = {(double)pa}, tot[1];
     if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
 }
 
@@ -284,16 +292,15 @@ k_bicg_as(Op A, const V *__restrict__ s1, V *__restrict__ as, BicgScal *sc, doub
           unsigned int *counter)
 {
     if (sc->done) return;
-    double acc[2] = {0.0, 0.0};
+    V pa0 = V(0), pa1 = V(0);
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const V a = apply_row(A, s1, row);
         as[row] = a;
-        const double ad = (double)a;
-        acc[0] += ad * (double)s1[row];
-        acc[1] += ad * ad;
+        pa0 = fma(a, s1[row], pa0);
+        pa1 = fma(a, a, pa1);
     }
-    double tot[2];
+    double acc[2] = {(double)pa0, (double)pa1}, tot[2];
     if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) sc->omega = tot[0] / tot[1];
 }
 
@@ -305,18 +312,17 @@ k_bicg_xr(long long n, V *__restrict__ x, const V *__restrict__ p1, const V *__r
 {
     if (sc->done) return;
     const V alpha = (V)sc->alpha, omega = (V)sc->omega;
-    double acc[2] = {0.0, 0.0};
+    V pa0 = V(0), pa1 = V(0);
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
          row += (long long)gridDim.x * blockDim.x) {
         const V s = s1[row];
         x[row] = fma(omega, s, fma(alpha, p1[row], x[row]));  // x + alpha p + omega s, 2 FMA
         const V r = fma(-omega, as[row], s);
         r1[row] = r;
-        const double rd = (double)r;
-        acc[0] += rd * rd;
-        acc[1] += rd * (double)r0[row];
+        pa0 = fma(r, r, pa0);
+        pa1 = fma(r, r0[row], pa1);
     }
-    double tot[2];
+    double acc[2] = {(double)pa0, (double)pa1}, tot[2];
     if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
         const double rel = sqrt(tot[0]) / sc->norm0;
         sc->relres = rel;
@@ -384,7 +390,7 @@ k_bicg_pap(SpeOp<V> A, const V *__restrict__ r1, const V *__restrict__ p, const 
     const bool restart = sc->restart != 0;
     const V beta = restart ? V(0) : (V)sc->beta, omega = restart ? V(0) : (V)sc->omega;
     auto pat = [&](long long q) { return fma(beta, fma(-omega, ap[q], p[q]), r1[q]); };
-    double acc[1] = {0.0};
+    V pa = V(0);
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const V a = apply_row_f(A, row, pat);
@@ -398,9 +404,9 @@ k_bicg_pap(SpeOp<V> A, const V *__restrict__ r1, const V *__restrict__ p, const 
         } else {
             rr0 = r0[row];
         }
-        acc[0] += (double)a * (double)rr0;
+        pa = fma(a, rr0, pa);
     }
-    double tot[1];
+    double acc[1] = {(double)pa}, tot[1];
     if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
 }
 
@@ -413,18 +419,17 @@ k_bicg_sas(SpeOp<V> A, const V *__restrict__ r1, const V *__restrict__ ap, V *__
     if (sc->done) return;
     const V alpha = (V)sc->alpha;
     auto sat = [&](long long q) { return fma(-alpha, ap[q], r1[q]); };
-    double acc[2] = {0.0, 0.0};
+    V pa0 = V(0), pa1 = V(0);
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const V a = apply_row_f(A, row, sat);
         const V sv = sat(row);
         s1[row] = sv;
         as[row] = a;
-        const double ad = (double)a;
-        acc[0] += ad * (double)sv;
-        acc[1] += ad * ad;
+        pa0 = fma(a, sv, pa0);
+        pa1 = fma(a, a, pa1);
     }
-    double tot[2];
+    double acc[2] = {(double)pa0, (double)pa1}, tot[2];
     if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) sc->omega = tot[0] / tot[1];
 }
 
@@ -436,14 +441,14 @@ k_bicg_ap1(SpeOp<V> A, const V *__restrict__ p1, const V *__restrict__ r0, V *__
 {
     if (sc->done) return;
     auto pat = [&](long long q) { return p1[q]; };
-    double acc[1] = {0.0};
+    V pa = V(0);
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const V a = apply_row_f(A, row, pat);
         ap[row] = a;
-        acc[0] += (double)a * (double)r0[row];
+        pa = fma(a, r0[row], pa);
     }
-    double tot[1];
+    double acc[1] = {(double)pa}, tot[1];
     if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
 }
 
@@ -466,6 +471,332 @@ void launch_bicg_fused_iteration(cfd_launch_ctx &c, const SpeOp<V> &A, V *x, con
 }
 template void launch_bicg_fused_iteration<float>(cfd_launch_ctx &, const SpeOp<float> &, float *,
                                                  const BicgVecs<float> &, float *, float *, BicgScal *, int, bool);
+
+// ---------------------------------------------------------------------------
+// FP32 Jacobi-preconditioned CG of the mixed-precision inner solves.
+//
+// A e = r with A = J L (J = diag(jp)) is the same system as M e = P r with
+// M = D_V L symmetric positive semi-definite (D_V = cell volumes; the face
+// coefficients dV c_nb = face area / distance are symmetric) and P = D_V
+// diag(L) = diag(M).  CG needs one SpMV per iteration and, unlike BiCGSTAB,
+// no bi-orthogonality that FP32 rounding erodes.
+//
+// P at row (i,j,k): dV (sx_i + sy_j + sz_k) with sx = cxm + cxp (present
+// neighbours only), dV = wx_i wy_j wz_k.
+__device__ __forceinline__ float fv_P(const FvOp<float> &F, int i, int j, int k)
+{
+    return (__ldg(F.wx + i) * __ldg(F.wy + j) * __ldg(F.wz + k)) * (__ldg(F.sx + i) + __ldg(F.sy + j) + __ldg(F.sz + k));
+}
+
+// q = M x at `row` with x values from a functor
+template <class Fn>
+__device__ __forceinline__ float fv_apply(const FvOp<float> &F, long long row, int i, int j, int k, Fn &&xat)
+{
+    const SpeOp<float> &A = F.A;
+    const long long xw = i > 0 ? row - A.sxc : row;
+    const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
+    const long long ys = j > 0 ? row - A.nzc : row;
+    const long long yn = j < A.nyc - 1 ? row + A.nzc : row;
+    const long long zb = k > 0 ? row - 1 : row;
+    const long long zt = k < A.nzc - 1 ? row + 1 : row;
+    float s = __ldg(A.cxm + i) * xat(xw);
+    s = fmaf(__ldg(A.cym + j), xat(ys), s);
+    s = fmaf(__ldg(A.czm + k), xat(zb), s);
+    s = fmaf(__ldg(A.czp + k), xat(zt), s);
+    s = fmaf(__ldg(A.cyp + j), xat(yn), s);
+    s = fmaf(__ldg(A.cxp + i), xat(xe), s);
+    const float diag = __ldg(F.sx + i) + __ldg(F.sy + j) + __ldg(F.sz + k);
+    const float dv = __ldg(F.wx + i) * __ldg(F.wy + j) * __ldg(F.wz + k);
+    return dv * fmaf(diag, xat(row), -s);
+}
+
+// init: h = P r (in place), p = z = P^-1 h = r, rho = h.z
+__global__ void __launch_bounds__(kBlock)
+k_cg_init(FvOp<float> F, float *__restrict__ h, float *__restrict__ p, BicgScal *sc, double *partials,
+          unsigned int *counter)
+{
+    float pa = 0.f;
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < F.A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decompose(F.A, row, i, j, k);
+        const float r = h[row];
+        const float hv = fv_P(F, i, j, k) * r;
+        h[row] = hv;
+        p[row] = r;
+        pa = fmaf(hv, r, pa);
+    }
+    double acc[1] = {(double)pa}, tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        sc->rho = tot[0];
+        sc->r0n2 = tot[0];
+        sc->norm0 = sqrt(tot[0]);
+        sc->iter = 0;
+        sc->restart = 0;
+        sc->timestep += 1;
+        sc->done = tot[0] > 0.0 ? BICG_RUNNING : BICG_ZERO_RHS;
+        sc->relres = tot[0] > 0.0 ? 1.0 : 0.0;
+    }
+}
+
+// shared plane of the tiled kernel: (kBlock / TK + 2) x (TK + 2) floats,
+// largest for TK = 8
+constexpr int kCgTileSmem = (kBlock / 8 + 2) * (8 + 2);
+
+// pn = z + beta p (z = P^-1 h), q = M pn, alpha = rho / (pn . q).
+//
+// 2.5D tiling: a block owns a (TJ x TK) tile of the (j, k) plane and marches
+// along i over a chunk of planes.  Each thread keeps pn at i-1, i, i+1 in
+// registers and stages plane i in a double-buffered shared plane with a
+// one-cell halo in j and k (the 2 TK + 2 TJ halo cells are spread over the
+// first threads), so one barrier per plane suffices.  The raw z and p loads
+// run two planes ahead of their use to keep enough bytes in flight.  Values
+// outside the domain are 0; their coefficients are 0 as well.
+// first: the solve's first iteration, pn = z (beta = 0, p not read, pn not
+// written: the caller passes pn = z).
+template <bool first>
+__global__ void __launch_bounds__(kBlock, 5)
+k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p, float *__restrict__ pn,
+        float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter, int TK, int ichunk)
+{
+    if (sc->done) return;
+    const SpeOp<float> &A = F.A;
+    const int TJ = kBlock / TK, SW = TK + 2;
+    const int t = threadIdx.x, tk = t % TK, tj = t / TK;
+    const int nxc = A.nxc, nyc = A.nyc, nzc = A.nzc;
+    const long long sxc = A.sxc;
+    const int tiles_k = (nzc + TK - 1) / TK, tiles_j = (nyc + TJ - 1) / TJ;
+    const int tiles = tiles_k * tiles_j, items = tiles * ((nxc + ichunk - 1) / ichunk);
+    const float beta = first ? 0.f : (float)sc->beta;
+    // halo cell of this thread in tile coordinates (-1..TJ, -1..TK)
+    int hj = 0, hk = 0;
+    const bool hv = t < 2 * TK + 2 * TJ;
+    if (t < TK) {
+        hj = -1; hk = t;
+    } else if (t < 2 * TK) {
+        hj = TJ; hk = t - TK;
+    } else if (t < 2 * TK + TJ) {
+        hj = t - 2 * TK; hk = -1;
+    } else if (hv) {
+        hj = t - 2 * TK - TJ; hk = TK;
+    }
+    const int cslot = (tj + 1) * SW + tk + 1, hslot = (hj + 1) * SW + hk + 1;
+    // raw (z, p) at (i, jj, kk), zeros outside the domain (p not read when first)
+    auto ld = [&](int i, int jj, int kk, float &zv, float &pv) {
+        zv = 0.f;
+        pv = 0.f;
+        if (i >= 0 && i < nxc && jj >= 0 && jj < nyc && kk >= 0 && kk < nzc) {
+            const long long r = (long long)i * sxc + (jj * nzc + kk);
+            zv = z[r];
+            if (!first) pv = p[r];
+        }
+    };
+    __shared__ float sm[2][kCgTileSmem];
+    float pa = 0.f;
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int tile = item % tiles, chunk = item / tiles;
+        const int k0 = (tile % tiles_k) * TK, j0 = (tile / tiles_k) * TJ;
+        const int k = k0 + tk, j = j0 + tj, hjj = j0 + hj, hkk = k0 + hk;
+        const int ib = chunk * ichunk, ie = min(nxc, ib + ichunk);
+        const bool in = j < nyc && k < nzc;
+        const float cym = in ? __ldg(A.cym + j) : 0.f, cyp = in ? __ldg(A.cyp + j) : 0.f;
+        const float czm = in ? __ldg(A.czm + k) : 0.f, czp = in ? __ldg(A.czp + k) : 0.f;
+        const float syz = in ? __ldg(F.sy + j) + __ldg(F.sz + k) : 0.f;
+        const float wyz = in ? __ldg(F.wy + j) * __ldg(F.wz + k) : 0.f;
+        float zm, pm, z0, p0, z1, p1, z2, p2;
+        float hz0 = 0.f, hp0 = 0.f, hz1 = 0.f, hp1 = 0.f;
+        ld(ib - 1, j, k, zm, pm);
+        ld(ib, j, k, z0, p0);
+        ld(ib + 1, j, k, z1, p1);
+        ld(ib + 2, j, k, z2, p2);
+        if (hv) {
+            ld(ib, hjj, hkk, hz0, hp0);
+            ld(ib + 1, hjj, hkk, hz1, hp1);
+        }
+        float vm = fmaf(beta, pm, zm), vc = fmaf(beta, p0, z0);
+        for (int i = ib; i < ie; ++i) {
+            float z3, p3, hz2 = 0.f, hp2 = 0.f;
+            ld(i + 3, j, k, z3, p3);
+            if (hv) ld(i + 2, hjj, hkk, hz2, hp2);
+            const float vp = fmaf(beta, p1, z1);
+            float *buf = sm[i & 1];
+            buf[cslot] = vc;
+            if (hv) buf[hslot] = fmaf(beta, hp0, hz0);
+            __syncthreads();
+            if (in) {
+                const float vs = buf[cslot - SW], vn = buf[cslot + SW];
+                const float vb = buf[cslot - 1], vt = buf[cslot + 1];
+                float sum = __ldg(A.cxm + i) * vm;
+                sum = fmaf(cym, vs, sum);
+                sum = fmaf(czm, vb, sum);
+                sum = fmaf(czp, vt, sum);
+                sum = fmaf(cyp, vn, sum);
+                sum = fmaf(__ldg(A.cxp + i), vp, sum);
+                const float diag = __ldg(F.sx + i) + syz;
+                const float qv = (__ldg(F.wx + i) * wyz) * fmaf(diag, vc, -sum);
+                const long long r = (long long)i * sxc + (j * nzc + k);
+                if (!first) pn[r] = vc;
+                q[r] = qv;
+                pa = fmaf(vc, qv, pa);
+            }
+            vm = vc;
+            vc = vp;
+            z1 = z2; p1 = p2; z2 = z3; p2 = p3;
+            hz0 = hz1; hp0 = hp1; hz1 = hz2; hp1 = hp2;
+        }
+        __syncthreads();  // the next item rewrites both planes
+    }
+    double acc[1] = {(double)pa}, tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+}
+
+// e += alpha p, h -= alpha q, z = iP h, rho' = h . z (pure streaming, four
+// rows per thread step); convergence on sqrt(rho'/rho0)
+__global__ void __launch_bounds__(kBlock, 6)
+k_cg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float *__restrict__ h,
+         const float *__restrict__ q, const float *__restrict__ iP, float *__restrict__ z, BicgScal *sc,
+         double *partials, unsigned int *counter)
+{
+    if (sc->done) return;
+    const float alpha = (float)sc->alpha;
+    float pa = 0.f;
+    const long long n4 = n >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < n4; v += stride) {
+        float4 ev = reinterpret_cast<float4 *>(e)[v];
+        const float4 pv = reinterpret_cast<const float4 *>(p)[v];
+        float4 hv = reinterpret_cast<float4 *>(h)[v];
+        const float4 qv = reinterpret_cast<const float4 *>(q)[v];
+        const float4 iv = reinterpret_cast<const float4 *>(iP)[v];
+        ev.x = fmaf(alpha, pv.x, ev.x); ev.y = fmaf(alpha, pv.y, ev.y);
+        ev.z = fmaf(alpha, pv.z, ev.z); ev.w = fmaf(alpha, pv.w, ev.w);
+        hv.x = fmaf(-alpha, qv.x, hv.x); hv.y = fmaf(-alpha, qv.y, hv.y);
+        hv.z = fmaf(-alpha, qv.z, hv.z); hv.w = fmaf(-alpha, qv.w, hv.w);
+        const float4 zv = make_float4(hv.x * iv.x, hv.y * iv.y, hv.z * iv.z, hv.w * iv.w);
+        reinterpret_cast<float4 *>(e)[v] = ev;
+        reinterpret_cast<float4 *>(h)[v] = hv;
+        reinterpret_cast<float4 *>(z)[v] = zv;
+        pa = fmaf(hv.x, zv.x, pa); pa = fmaf(hv.y, zv.y, pa);
+        pa = fmaf(hv.z, zv.z, pa); pa = fmaf(hv.w, zv.w, pa);
+    }
+    for (long long r = 4 * n4 + (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        e[r] = fmaf(alpha, p[r], e[r]);
+        const float hv = fmaf(-alpha, q[r], h[r]);
+        h[r] = hv;
+        const float zv = hv * iP[r];
+        z[r] = zv;
+        pa = fmaf(hv, zv, pa);
+    }
+    double acc[1] = {(double)pa}, tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        const double rel = sqrt(fabs(tot[0]) / sc->r0n2);
+        sc->relres = rel;
+        if (rel < sc->tol) {
+            sc->done = BICG_CONVERGED;
+        } else if (sc->iter >= sc->maxit) {
+            sc->done = BICG_CAPPED;
+        } else {
+            sc->beta = tot[0] / sc->rho;
+            sc->rho = tot[0];
+            sc->iter += 1;
+            sc->total_iters += 1;
+        }
+    }
+}
+
+// iP = 1 / P (FP32), once per context
+__global__ void k_cg_ip(FvOp<float> F, float *__restrict__ iP)
+{
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < F.A.n;
+         row += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decompose(F.A, row, i, j, k);
+        iP[row] = 1.0f / fv_P(F, i, j, k);
+    }
+}
+
+// launch shape of the tiled kernel: a k tile of 32/16/8 cells, the i range
+// cut into chunks so that tiles x chunks fills the reduction grid (blocks
+// loop over tile-chunk items when there are more tiles than blocks)
+struct CgShape {
+    int TK, ichunk, grid;
+};
+static CgShape cg_shape(const cfd_launch_ctx &c, const FvOp<float> &F)
+{
+    const SpeOp<float> &A = F.A;
+    CgShape s;
+    s.TK = A.nzc >= 24 ? 32 : (A.nzc >= 12 ? 16 : 8);
+    const int TJ = kBlock / s.TK;
+    const int tiles = ((A.nzc + s.TK - 1) / s.TK) * ((A.nyc + TJ - 1) / TJ);
+    int chunks = c.cg_grid / tiles;
+    if (chunks < 1) chunks = 1;
+    if (chunks > A.nxc) chunks = A.nxc;
+    s.ichunk = (A.nxc + chunks - 1) / chunks;
+    chunks = (A.nxc + s.ichunk - 1) / s.ichunk;
+    s.grid = tiles * chunks < c.cg_grid ? tiles * chunks : c.cg_grid;
+    return s;
+}
+
+void launch_cg_init(cfd_launch_ctx &c, const FvOp<float> &F, float *h, float *p, BicgScal *sc)
+{
+    k_cg_init<<<c.red_blocks, kBlock, 0, c.s>>>(F, h, p, sc, c.partials, c.counter);
+}
+
+void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
+                         float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first)
+{
+    float *P[2] = {p, p_alt};
+    const int to = first ? from : 1 - from;
+    const CgShape cs = cg_shape(c, F);
+    // first iteration: pn = p0 (written by k_cg_init into P[from]), read as z
+    if (first)
+        k_cg_pq<true><<<cs.grid, kBlock, 0, c.s>>>(F, P[from], P[from], P[from], q, sc, c.partials, c.counter,
+                                                   cs.TK, cs.ichunk);
+    else
+        k_cg_pq<false><<<cs.grid, kBlock, 0, c.s>>>(F, z, P[from], P[to], q, sc, c.partials, c.counter, cs.TK,
+                                                    cs.ichunk);
+    k_cg_upd<<<c.cg_grid, kBlock, 0, c.s>>>(F.A.n, e, P[to], h, q, iP, z, sc, c.partials, c.counter);
+}
+
+int cg_resident_grid(int sms, int red_blocks)
+{
+    int a = 0, b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_cg_pq<false>, kBlock, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_cg_upd, kBlock, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return red_blocks;
+    }
+    const int per_sm = a < b ? a : b;
+    const int g = per_sm > 0 ? per_sm * sms : red_blocks;
+    return g < red_blocks ? g : red_blocks;
+}
+
+void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP)
+{
+    k_cg_ip<<<blocks_for(F.A.n, c.grid_cap), kBlock, 0, c.s>>>(F, iP);
+}
+
+void launch_cg_part(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
+                    float *p, float *pn, float *q, BicgScal *sc, int part)
+{
+    if (part == 0) {
+        const CgShape cs = cg_shape(c, F);
+        k_cg_pq<false><<<cs.grid, kBlock, 0, c.s>>>(F, z, p, pn, q, sc, c.partials, c.counter, cs.TK, cs.ichunk);
+    } else {
+        k_cg_upd<<<c.cg_grid, kBlock, 0, c.s>>>(F.A.n, e, pn, h, q, iP, z, sc, c.partials, c.counter);
+    }
+}
+
+__global__ void k_fv_axes(int n, const float *__restrict__ c, float *__restrict__ sum)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) sum[i] = c[i] + c[n + i];
+}
+
+void launch_fv_axes(cudaStream_t s, int n, const float *c, float *sum)
+{
+    k_fv_axes<<<(n + 127) / 128, 128, 0, s>>>(n, c, sum);
+}
 
 // NaN/Inf reset at the iteration cap (bicgstabRe2.hpp:143-163): non-finite
 // entries of x take the previous initial guess px1; if more than 10% were

@@ -37,7 +37,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
                 precision: int = capi.PREC_FP64, tol: float | None = None, maxit: int = 5000,
                 omega: float | None = None, sor_maxit: int = 5000, aligned_source: bool = False,
                 compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-2,
-                max_outer: int = 30) -> capi.CfdConfig:
+                max_outer: int = 30, inner_solver: int = capi.INNER_CG) -> capi.CfdConfig:
     cfg = capi.CfdConfig()
     check(lib().cfd_config_default(C.byref(cfg), w.nxc, w.nyc, w.nzc))
     cfg.lx, cfg.ly, cfg.lz = w.lx, w.ly, w.lz
@@ -56,6 +56,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
     cfg.check_every = check_every
     cfg.inner_tol = inner_tol
     cfg.max_outer = max_outer
+    cfg.inner_solver = inner_solver
     return cfg
 
 

@@ -64,6 +64,15 @@ typedef enum {
                            residual, FP64 dots and FP64 divergence check */
 } cfd_precision;
 
+/* Inner solver of the mixed-precision defect correction (matrix-free SPE
+   operator; the ELL operator always uses BiCGSTAB). */
+typedef enum {
+    CFD_INNER_CG = 0,       /* FP32 Jacobi-preconditioned CG on the symmetric
+                               finite-volume form M = D_V L of the operator */
+    CFD_INNER_BICGSTAB = 1  /* FP32 BiCGSTAB on the Jacobi-scaled operator, restarted
+                               when |r1.r0| < 1e-5 |r1||r0| */
+} cfd_inner_solver;
+
 /* Velocity slots: the reference's T0 (old), T1 (predicted u*), T3 (new). */
 enum { CFD_SLOT_T0 = 0, CFD_SLOT_T1 = 1, CFD_SLOT_T3 = 3 };
 
@@ -107,6 +116,7 @@ typedef struct {
     double inner_tol;           /* mixed precision: relative tolerance of each FP32
                                    inner solve inside the FP64 defect correction */
     int max_outer;              /* mixed precision: defect-correction sweeps cap */
+    int inner_solver;           /* mixed precision: cfd_inner_solver */
 } cfd_config;
 
 typedef struct {
@@ -221,6 +231,9 @@ typedef enum {
     CFD_KERNEL_UPDATE_UF,    /* update_UandF_omp */
     CFD_KERNEL_RHS,          /* createBMatrix_omp (+ compatibility mean) */
     CFD_KERNEL_SOR_SWEEP,    /* one red + one black SOR sweep */
+    CFD_KERNEL_CG_PQ,        /* mixed precision: p = z + beta p, q = M p, p.q (FP32) */
+    CFD_KERNEL_CG_UPD,       /* mixed precision: e, h, z update and h.z (FP32) */
+    CFD_KERNEL_RESIDUAL64,   /* mixed precision: FP64 residual b - A x of the defect correction */
     CFD_KERNEL_COUNT
 } cfd_kernel_id;
 

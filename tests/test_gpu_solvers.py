@@ -115,15 +115,18 @@ def test_zero_rhs_returns_immediately():
         assert it == 0 and res == 0.0
 
 
-@pytest.mark.parametrize("solver", [capi.SOLVER_BICG_SPE, capi.SOLVER_BICG_ELL])
-def test_mixed_precision_defect_correction(oracle, solver):
-    """FP32 inner BiCGSTAB + FP64 defect correction reaches the FP64
-    tolerance on the FP64 residual."""
+@pytest.mark.parametrize("solver,inner", [(capi.SOLVER_BICG_SPE, capi.INNER_CG),
+                                          (capi.SOLVER_BICG_SPE, capi.INNER_BICGSTAB),
+                                          (capi.SOLVER_BICG_ELL, capi.INNER_BICGSTAB)])
+def test_mixed_precision_defect_correction(oracle, solver, inner):
+    """FP32 inner solves (CG on the symmetric finite-volume form, or
+    restarted BiCGSTAB) + FP64 defect correction reach the FP64 tolerance on
+    the FP64 residual."""
     w = WORKLOADS["c1"]
     g = Grid.of(w, oracle)
     b, op = _consistent_rhs(oracle, g, solver)
     tol = 1e-10
-    with Simulation(w, solver=solver, tol=tol, precision=capi.PREC_MIXED) as S:
+    with Simulation(w, solver=solver, tol=tol, precision=capi.PREC_MIXED, inner_solver=inner) as S:
         S.grid_uniform()
         S.upload("B", b)
         it, res = S.pSolver()
