@@ -26,6 +26,9 @@ KERNELS = ["bicg_ap", "bicg_s", "bicg_as", "bicg_xr", "bicg_p", "convdiff", "upd
            "sor_sweep", "cg_pq", "cg_upd", "residual64"]
 FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "P", "ETA", "F", "SRC", "X", "B", "JP"]
 FIELD = {name: i for i, name in enumerate(FIELDS)}
+ADJ_FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "CDU", "CDV", "CDW", "X", "B", "F", "SRC",
+              "ETA", "INFLOW"]
+ADJ_FIELD = {name: i for i, name in enumerate(ADJ_FIELDS)}
 
 
 class CfdError(RuntimeError):
@@ -51,6 +54,19 @@ class CfdStepInfo(C.Structure):
     _fields_ = [("loop", C.c_longlong), ("time", C.c_double), ("iters", C.c_int * 4),
                 ("relres", C.c_double * 4), ("outer", C.c_int * 4), ("cd", C.c_double),
                 ("cl", C.c_double)]
+
+
+class CfdAdjStepInfo(C.Structure):
+    _fields_ = [("iters", C.c_int * 4), ("relres", C.c_double * 4)]
+
+
+class CfdAdjRunConfig(C.Structure):
+    _fields_ = [("first", C.c_int), ("last", C.c_int), ("interval", C.c_int)]
+
+
+class CfdAdjRunResult(C.Structure):
+    _fields_ = [("J", C.c_double), ("forward_seconds", C.c_double), ("adjoint_seconds", C.c_double),
+                ("forward_iters", C.c_longlong), ("adjoint_iters", C.c_longlong), ("checkpoints", C.c_int)]
 
 
 _lib = None
@@ -103,6 +119,28 @@ def lib() -> C.CDLL:
         "cfd_launch_count": ([vp, C.POINTER(C.c_longlong)], i),
         "cfd_cdcl_noalloc": ([i, i, i, d, vp, vp, vp, vp, dp, dp, vp], i),
         "cfd_time_kernels": ([vp, i, dp, i], i),
+        "cfd_set_inflow_profile": ([vp, dp, sz], i),
+        "cfd_adj_enable": ([vp, i], i),
+        "cfd_adj_zero": ([vp], i),
+        "cfd_adj_field_count": ([vp, i], sz),
+        "cfd_adj_upload": ([vp, i, dp, sz], i),
+        "cfd_adj_download": ([vp, i, dp, sz], i),
+        "cfd_adj_convection_diffusion": ([vp, i], i),
+        "cfd_adj_update_uf": ([vp, i, d, d], i),
+        "cfd_adj_create_b": ([vp], i),
+        "cfd_adj_pressure_solve": ([vp, ip, dp], i),
+        "cfd_adj_add_source": ([vp], i),
+        "cfd_adj_bc_main": ([vp], i),
+        "cfd_adj_bc_copy": ([vp], i),
+        "cfd_step_record": ([vp, i, C.POINTER(CfdStepInfo)], i),
+        "cfd_adj_step": ([vp, i, d, d, C.POINTER(CfdAdjStepInfo)], i),
+        "cfd_adj_finish": ([vp], i),
+        "cfd_checkpoint_alloc": ([vp, i], i),
+        "cfd_checkpoint_save": ([vp, i], i),
+        "cfd_checkpoint_load": ([vp, i], i),
+        "cfd_adj_forward": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
+        "cfd_adj_reverse": ([vp, C.POINTER(CfdAdjRunResult)], i),
+        "cfd_adj_mean_drag": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
     }
     for name, (args, res) in proto.items():
         fn = getattr(L, name)

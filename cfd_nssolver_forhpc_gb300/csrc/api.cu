@@ -12,8 +12,7 @@
 #include <type_traits>
 #include <vector>
 
-#include "../../include/cfdgpu.h"
-#include "kernels.h"
+#include "context.h"
 
 using namespace cfd;
 
@@ -21,226 +20,18 @@ namespace {
 
 thread_local std::string g_err;
 
+}  // namespace
+
+namespace cfd {
 int fail(int code, const std::string &msg)
 {
     g_err = msg;
     return code;
 }
-
-#define CK(...)                                                                            \
-    do {                                                                                   \
-        cudaError_t e_ = (__VA_ARGS__);                                                    \
-        if (e_ != cudaSuccess)                                                             \
-            return fail(CFD_ERR_CUDA, std::string(#__VA_ARGS__) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
-
-#define CKS(...)                        \
-    do {                                \
-        int st_ = (__VA_ARGS__);        \
-        if (st_ != CFD_OK) return st_;  \
-    } while (0)
-
-template <class T>
-struct Tag {
-    using type = T;
-};
-
-}  // namespace
-
-namespace cfd {
 int set_last_error(int code, const std::string &msg) { return fail(code, msg); }
-}
-
-struct cfd_ctx {
-    cfd_config cfg{};
-    Geo g{};
-    bool fp32 = false;
-    cudaStream_t s = nullptr;
-    cfd_launch_ctx lc{};
-    std::vector<void *> allocs;
-
-    // state (velocity type T = double or float)
-    void *vel[3][3] = {};  // [slot 0/1/2 = T0/T1/T3][component]
-    void *eta = nullptr, *f = nullptr, *src = nullptr;
-    double *p = nullptr, *x = nullptr, *b = nullptr, *jp = nullptr;
-    double *staging = nullptr;  // FP64 staging for conversions (mixed precision)
-
-    // metrics: raw arrays (X,Y,Z,Dx,Dy,Dz,Dxs,Dys,Dzs) and per-axis tables
-    double *raw = nullptr;
-    double *rawp[9] = {};
-    double *tab64[3] = {};
-    float *tab32[3] = {};
-    bool metrics = false;
-    std::vector<double> hraw[9];
-
-    // Poisson operators
-    double *spe_c[3] = {};
-    float *spe_c32[3] = {};
-    float *jp32 = nullptr;
-    int *ell_cols = nullptr;
-    double *ell_vals = nullptr;
-    float *ell_vals32 = nullptr;
-
-    // BiCGSTAB work
-    BicgVecs<double> w64{};
-    BicgVecs<float> w32{};
-    double *px1 = nullptr, *px2 = nullptr;
-    float *r32 = nullptr, *e32 = nullptr;
-    float *p_alt = nullptr, *ap_alt = nullptr;  // second p/ap pair of the fused FP32 iteration
-    float *fv_sum[3] = {};                      // per-axis cm + cp (FP32) of the CG inner solve
-    float *cg_ip = nullptr;                     // 1 / diag(M) (FP32) of the CG inner solve
-    BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
-    // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-    int graph_batch[4] = {0, 0, 0, 0};
-
-    // SOR
-    double *cf6 = nullptr, *cf7 = nullptr;
-    unsigned long long *sor_res = nullptr;
-    int *sor_state = nullptr, *h_sor_state = nullptr;
-
-    // scalars: [0] rhs mean, [1..2] cd/cl, [3] residual norm^2, [4] dot
-    double *dscal = nullptr, *h_scal = nullptr;
-    unsigned long long *dmax = nullptr, *h_max = nullptr;
-
-    long long loop = 1;
-    double time = 0.0;
-    bool use_graphs = true;
-    int debug = 0;
-    bool fused = true;  // fused FP32 inner iterations (SPE operator)
-    long long launches = 0;  // kernels issued by the step and solver paths
-};
+}  // namespace cfd
 
 namespace {
-
-template <class T>
-T *dv(cfd_ctx *c, int slot, int comp)
-{
-    return static_cast<T *>(c->vel[slot][comp]);
-}
-
-int slot_index(int slot)
-{
-    return slot == CFD_SLOT_T0 ? 0 : slot == CFD_SLOT_T1 ? 1 : slot == CFD_SLOT_T3 ? 2 : -1;
-}
-
-int dalloc(cfd_ctx *c, void **p, size_t bytes)
-{
-    if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(CFD_ERR_NOMEM, std::string("cudaMalloc(") + std::to_string(bytes) +
-                                       "): " + cudaGetErrorString(e));
-    }
-    c->allocs.push_back(*p);
-    return CFD_OK;
-}
-
-template <class P>
-int dalloc_t(cfd_ctx *c, P **p, size_t count)
-{
-    return dalloc(c, reinterpret_cast<void **>(p), count * sizeof(P));
-}
-
-template <class Fn>
-auto dispatch(cfd_ctx *c, Fn &&fn)
-{
-    if (c->fp32) return fn(Tag<float>{});
-    return fn(Tag<double>{});
-}
-
-template <class T>
-Metrics<T> metrics_of(cfd_ctx *c);
-template <>
-Metrics<double> metrics_of<double>(cfd_ctx *c)
-{
-    return {{c->tab64[0], c->g.nx}, {c->tab64[1], c->g.ny}, {c->tab64[2], c->g.nz}};
-}
-template <>
-Metrics<float> metrics_of<float>(cfd_ctx *c)
-{
-    return {{c->tab32[0], c->g.nx}, {c->tab32[1], c->g.ny}, {c->tab32[2], c->g.nz}};
-}
-
-SpeOp<double> spe64(cfd_ctx *c)
-{
-    const Geo &g = c->g;
-    return {c->spe_c[0], c->spe_c[0] + g.nxc, c->spe_c[1], c->spe_c[1] + g.nyc, c->spe_c[2],
-            c->spe_c[2] + g.nzc, c->jp, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc, FastDiv((unsigned int)g.nzc)};
-}
-SpeOp<float> spe32(cfd_ctx *c)
-{
-    const Geo &g = c->g;
-    return {c->spe_c32[0], c->spe_c32[0] + g.nxc, c->spe_c32[1], c->spe_c32[1] + g.nyc, c->spe_c32[2],
-            c->spe_c32[2] + g.nzc, c->jp32, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc,
-            FastDiv((unsigned int)g.nzc)};
-}
-FvOp<float> fv32(cfd_ctx *c)
-{
-    const Geo &g = c->g;
-    FvOp<float> F;
-    F.A = spe32(c);
-    F.wx = c->tab32[0] + (size_t)AX_D * g.nx + GC;
-    F.wy = c->tab32[1] + (size_t)AX_D * g.ny + GC;
-    F.wz = c->tab32[2] + (size_t)AX_D * g.nz + GC;
-    F.sx = c->fv_sum[0];
-    F.sy = c->fv_sum[1];
-    F.sz = c->fv_sum[2];
-    return F;
-}
-EllOp<double> ell64(cfd_ctx *c) { return {c->ell_cols, c->ell_vals, c->g.n}; }
-EllOp<float> ell32(cfd_ctx *c) { return {c->ell_cols, c->ell_vals32, c->g.n}; }
-
-// Per-axis tables (row-major [AX_ROWS][n]) from the cell and staggered
-// widths, with the reference's evaluation order for every factor.
-std::vector<double> axis_table(const std::vector<double> &D, const std::vector<double> &Ds)
-{
-    const int n = (int)D.size();
-    std::vector<double> t((size_t)AX_ROWS * n, 0.0);
-    auto T = [&](int r, int i) -> double & { return t[(size_t)r * n + i]; };
-    for (int i = 0; i < n; ++i) {
-        T(AX_D, i) = D[i];
-        T(AX_DS, i) = Ds[i];
-        T(AX_RD, i) = 1.0 / D[i];
-        T(AX_RDS, i) = 1.0 / Ds[i];
-        T(AX_IT, i) = (Ds[i] * 0.5) / D[i];
-        if (i + 1 < n) {
-            T(AX_CAPP, i) = 0.125 * D[i + 1] * D[i + 1] / Ds[i];
-            T(AX_CAPN, i) = 0.125 * D[i + 1] * D[i + 1] / Ds[i + 1];
-            T(AX_CBPN, i) = 0.125 * Ds[i] * Ds[i] / D[i + 1];
-            T(AX_PP, i) = 1.0 / D[i] / Ds[i];
-        }
-        if (i >= 1) {
-            T(AX_CANP, i) = 0.125 * D[i] * D[i] / Ds[i - 1];
-            T(AX_CBNP, i) = 0.125 * Ds[i - 1] * Ds[i - 1] / D[i - 1];
-            T(AX_CBNN, i) = 0.125 * Ds[i - 1] * Ds[i - 1] / D[i];
-            T(AX_PM, i) = 1.0 / D[i] / Ds[i - 1];
-        }
-        T(AX_CANN, i) = 0.125 * D[i] * D[i] / Ds[i];
-        T(AX_CBPP, i) = 0.125 * Ds[i] * Ds[i] / D[i];
-    }
-    return t;
-}
-
-int check_ctx(cfd_ctx *c)
-{
-    if (!c) return fail(CFD_ERR_ARG, "null context");
-    return CFD_OK;
-}
-
-int need_metrics(cfd_ctx *c)
-{
-    CKS(check_ctx(c));
-    if (!c->metrics) return fail(CFD_ERR_STATE, "grid metrics not set (cfd_grid_uniform / cfd_set_metrics)");
-    return CFD_OK;
-}
-
-int check_slot(int slot)
-{
-    if (slot_index(slot) < 0) return fail(CFD_ERR_ARG, "velocity slot must be 0 (T0), 1 (T1) or 3 (T3)");
-    return CFD_OK;
-}
 
 size_t field_count(const cfd_ctx *c, int field)
 {
@@ -429,7 +220,8 @@ void residual64(cfd_ctx *c, const EllOp<double> &A, const double *b, const doubl
 //   r = b - A x (FP64, written as FP32);  stop when |r|/|b| < tol
 //   solve A e = r in FP32 to inner_tol (e from 0);  x += e (FP64)
 template <class Op64, class Op32>
-int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double *relres, int *outer)
+int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, double *x, const double *zero,
+                bool cg, int *iters, double *relres, int *outer, bool zero_x_if_zero_rhs = false)
 {
     const long long n = c->g.n;
     // |b|^2 via the residual kernel with x = 0 would need a zero vector; the
@@ -437,7 +229,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
     // |b|^2 from the residual kernel with x = 0 (w64.r0 is an FP64 zero
     // vector in mixed-precision contexts)
     double norm0 = 0.0;
-    residual64(c, A64, c->b, c->w64.r0, c->r32, c->dscal + 4);
+    residual64(c, A64, b, zero, c->r32, c->dscal + 4);
     c->launches += 1;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
@@ -446,6 +238,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
     int total = 0, sweeps = 0;
     double rel = 0.0;
     if (norm0 == 0.0) {
+        if (zero_x_if_zero_rhs) CK(cudaMemsetAsync(x, 0, (size_t)n * sizeof(double), c->s));
         if (iters) *iters = 0;
         if (relres) *relres = 0.0;
         if (outer) *outer = 0;
@@ -453,7 +246,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
     }
     int st = CFD_OK;
     for (;;) {
-        residual64(c, A64, c->b, c->x, c->r32, c->dscal + 3);
+        residual64(c, A64, b, x, c->r32, c->dscal + 3);
         c->launches += 1;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
@@ -465,7 +258,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
         if constexpr (std::is_same<Op32, SpeOp<float>>::value) {
             SpeOp<float> Afly = A32;
             Afly.jp = nullptr;
-            if (c->cfg.inner_solver == CFD_INNER_CG) CKS(cg_run(c, fv32(c), c->r32, c->e32, c->sc_in));
+            if (cg) CKS(cg_run(c, fv32(c), c->r32, c->e32, c->sc_in));
             else if (c->fused) CKS(bicg_run_fused(c, A32, Afly, c->r32, c->e32, c->sc_in));
             else CKS((bicg_run<Op32, float>(c, A32, c->r32, c->e32, c->w32, nullptr, nullptr, c->sc_in, 1)));
         } else {
@@ -482,7 +275,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, int *iters, double
             std::fprintf(stderr, "[cfdgpu] outer %d rel %.3e | inner done %d iter %d relres %.3e norm0 %.3e "
                          "rho %.3e alpha %.3e omega %.3e\n", sweeps, rel, c->h_sc->done, c->h_sc->iter,
                          c->h_sc->relres, c->h_sc->norm0, c->h_sc->rho, c->h_sc->alpha, c->h_sc->omega);
-        launch_correct<float>(c->lc, n, c->x, c->e32);
+        launch_correct<float>(c->lc, n, x, c->e32);
         c->launches += 1;
         CK(cudaGetLastError());
         ++sweeps;
@@ -499,8 +292,9 @@ int poisson_solve(cfd_ctx *c, int *iters, double *relres, int *outer)
     if (outer) *outer = 0;
     const bool ell = c->cfg.solver == CFD_SOLVER_BICG_ELL;
     if (c->cfg.precision == CFD_PREC_MIXED) {
-        if (ell) return solve_mixed(c, ell64(c), ell32(c), iters, relres, outer);
-        return solve_mixed(c, spe64(c), spe32(c), iters, relres, outer);
+        const bool cg = c->cfg.inner_solver == CFD_INNER_CG;
+        if (ell) return solve_mixed(c, ell64(c), ell32(c), c->b, c->x, c->w64.r0, cg, iters, relres, outer);
+        return solve_mixed(c, spe64(c), spe32(c), c->b, c->x, c->w64.r0, cg, iters, relres, outer);
     }
     if (ell) return solve64(c, ell64(c), iters, relres);
     return solve64(c, spe64(c), iters, relres);
@@ -562,7 +356,7 @@ int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer)
 }
 
 template <class T>
-int step_t(cfd_ctx *c, cfd_step_info *info)
+int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
 {
     const Geo &g = c->g;
     const Metrics<T> m = metrics_of<T>(c);
@@ -576,6 +370,9 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
     const int npass = pc ? 4 : 1;
     int st = CFD_OK;
     cfd_step_info loc{};
+    if (rec)
+        for (int q = 0; q < 3; ++q)
+            CK(cudaMemcpyAsync(rec->T0[q], c->vel[0][q], (size_t)g.ng * sizeof(T), cudaMemcpyDeviceToDevice, c->s));
     if (pc) CK(cudaMemsetAsync(src, 0, (size_t)(3 * g.n) * sizeof(T), c->s));
     for (int pass = 0; pass < npass; ++pass) {
         launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, u1, v1, w1,
@@ -588,6 +385,10 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
             if (s2 != CFD_OK && s2 != CFD_ERR_NOCONV) return s2;
             if (s2 != CFD_OK) st = s2;
         }
+        if (rec) {
+            launch_gather_interior(c->s, g, c->p, rec->x[pass]);
+            c->launches += 1;
+        }
         launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
                             u1, v1, w1, u3, v3, w3, f);
         if (pc && pass < 3) launch_src_accumulate<T>(c->lc, 3 * g.n, dt, src, f);
@@ -597,9 +398,7 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
     const size_t bytes = (size_t)g.ng * sizeof(T);
     for (int q = 0; q < 3; ++q)
         CK(cudaMemcpyAsync(c->vel[0][q], c->vel[2][q], bytes, cudaMemcpyDeviceToDevice, c->s));
-    BcTab bc;
-    std::memcpy(bc.dir, c->cfg.bc_dir, sizeof(bc.dir));
-    std::memcpy(bc.num, c->cfg.bc_num, sizeof(bc.num));
+    const BcTab bc = bc_tab(c);
     launch_bc_main<T>(c->s, g, bc, u0, v0, w0, c->p);
     launch_bc_copy<T>(c->s, g, u0, v0, w0, u1, v1, w1);
     launch_cdcl<T>(c->lc, g, metrics_of<double>(c), c->cfg.lz, f, c->dscal + 1);
@@ -616,6 +415,65 @@ int step_t(cfd_ctx *c, cfd_step_info *info)
     if (info) *info = loc;
     return st;
 }
+
+}  // namespace
+
+namespace cfd {
+
+int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
+{
+    return dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        return step_t<T>(c, info, rec);
+    });
+}
+
+// FP64 defect correction around the FP32 CG inner solve for A x = b with
+// caller buffers (the adjoint Poisson solves): same tolerances as the
+// forward solve, residual with the FP64 matrix-free operator; b = 0 gives
+// x = 0 (the warm start is dropped)
+int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
+                    int *outer)
+{
+    return solve_mixed(c, spe64(c), spe32(c), b, x, zero, true, iters, relres, outer, true);
+}
+
+// FP32 operator tables and CG buffers in an FP64 context (for the adjoint
+// solves); a mixed-precision context has them already
+int ensure_fp32_solver(cfd_ctx *c)
+{
+    if (!c->metrics) return fail(CFD_ERR_STATE, "grid metrics not set (cfd_grid_uniform / cfd_set_metrics)");
+    if (c->cg_ip && c->w32.r0 && c->r32) return CFD_OK;
+    const Geo &g = c->g;
+    const long long n = g.n;
+    const int nc[3] = {g.nxc, g.nyc, g.nzc};
+    CK(cudaStreamSynchronize(c->s));
+    if (!c->w32.r0) CKS(dalloc_t(c, &c->w32.r0, n));
+    if (!c->w32.p1) CKS(dalloc_t(c, &c->w32.p1, n));
+    if (!c->w32.ap) CKS(dalloc_t(c, &c->w32.ap, n));
+    if (!c->p_alt) CKS(dalloc_t(c, &c->p_alt, n));
+    if (!c->r32) CKS(dalloc_t(c, &c->r32, n));
+    if (!c->e32) CKS(dalloc_t(c, &c->e32, n));
+    if (!c->jp32) CKS(dalloc_t(c, &c->jp32, n));
+    for (int a = 0; a < 3; ++a) {
+        if (!c->spe_c32[a]) CKS(dalloc_t(c, &c->spe_c32[a], 2 * (size_t)nc[a]));
+        if (!c->fv_sum[a]) CKS(dalloc_t(c, &c->fv_sum[a], (size_t)nc[a]));
+    }
+    if (!c->cg_ip) CKS(dalloc_t(c, &c->cg_ip, n));
+    for (int a = 0; a < 3; ++a) {
+        launch_convert<double, float>(c->lc, 2LL * nc[a], c->spe_c[a], c->spe_c32[a]);
+        launch_fv_axes(c->s, nc[a], c->spe_c32[a], c->fv_sum[a]);
+    }
+    launch_convert<double, float>(c->lc, n, c->jp, c->jp32);
+    launch_cg_ip(c->lc, fv32(c), c->cg_ip);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+}  // namespace cfd
+
+namespace {
 
 int build_tables(cfd_ctx *c)
 {
@@ -669,6 +527,7 @@ void free_ctx(cfd_ctx *c)
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_sor_state) cudaFreeHost(c->h_sor_state);
     if (c->h_max) cudaFreeHost(c->h_max);
+    adj_free(c->adj);
     if (c->s) cudaStreamDestroy(c->s);
     delete c;
 }
@@ -843,6 +702,8 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     hin.restart_tol = 1e-7 * k.inner_tol;
     hin.maxit = k.p_iter_max;
     hin.restart_rel = 1e-5;
+    c->sc_init = h;
+    c->sc_in_init = hin;
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->sc, &h, sizeof(h), cudaMemcpyHostToDevice, c->s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->sc_in, &hin, sizeof(hin), cudaMemcpyHostToDevice, c->s);
     const size_t zero_bytes[] = {(size_t)g.ng * ts, (size_t)(3 * n) * ts, (size_t)n * 8};
@@ -996,6 +857,13 @@ int cfd_start(cfd_ctx *c)
     for (int sl = 1; sl < 3; ++sl)
         for (int q = 0; q < 3; ++q)
             CK(cudaMemcpyAsync(c->vel[sl][q], c->vel[0][q], (size_t)c->g.ng * ts, cudaMemcpyDeviceToDevice, c->s));
+    // a fresh solver state: zero warm start and the initial scalars, so a
+    // context restarted with cfd_start repeats a fresh context's run
+    CK(cudaMemsetAsync(c->x, 0, (size_t)c->g.n * sizeof(double), c->s));
+    if (c->px1) CK(cudaMemsetAsync(c->px1, 0, (size_t)c->g.n * sizeof(double), c->s));
+    if (c->px2) CK(cudaMemsetAsync(c->px2, 0, (size_t)c->g.n * sizeof(double), c->s));
+    CK(cudaMemcpyAsync(c->sc, &c->sc_init, sizeof(BicgScal), cudaMemcpyHostToDevice, c->s));
+    CK(cudaMemcpyAsync(c->sc_in, &c->sc_in_init, sizeof(BicgScal), cudaMemcpyHostToDevice, c->s));
     CKS(cfd_bc_main(c, CFD_SLOT_T0));
     CKS(cfd_bc_copy(c, CFD_SLOT_T0, CFD_SLOT_T1));
     c->loop = 1;
@@ -1156,9 +1024,7 @@ int cfd_bc_main(cfd_ctx *c, int slot)
     CKS(check_ctx(c));
     CKS(check_slot(slot));
     const int a = slot_index(slot);
-    BcTab bc;
-    std::memcpy(bc.dir, c->cfg.bc_dir, sizeof(bc.dir));
-    std::memcpy(bc.num, c->cfg.bc_num, sizeof(bc.num));
+    const BcTab bc = bc_tab(c);
     dispatch(c, [&](auto tag) {
         using T = typename decltype(tag)::type;
         launch_bc_main<T>(c->s, c->g, bc, dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), c->p);
@@ -1218,7 +1084,7 @@ int cfd_step(cfd_ctx *c, cfd_step_info *info)
     CKS(need_metrics(c));
     return dispatch(c, [&](auto tag) {
         using T = typename decltype(tag)::type;
-        return step_t<T>(c, info);
+        return step_t<T>(c, info, nullptr);
     });
 }
 

@@ -334,7 +334,8 @@ __global__ void k_bc_main(Geo g, BcTab bc, int phase, T *__restrict__ u, T *__re
     if (phase == 0) {
         const int j = a, k = b, nx = g.nx;
         auto I = [&](int i) { return icel(g, i, j, k); };
-        T x = bc_norm<T>(bc, 0, 0, u[I(2)]); u[I(1)] = x; u[I(0)] = x;
+        T x = bc.inflow ? add_rn((T)bc.inflow[j - GC], mul_rn((T)bc.num[0], u[I(2)])) : bc_norm<T>(bc, 0, 0, u[I(2)]);
+        u[I(1)] = x; u[I(0)] = x;
         x = bc_tan<T>(bc, 0, 1, v[I(2)]); v[I(1)] = x; v[I(0)] = x;
         x = bc_tan<T>(bc, 0, 2, w[I(2)]); w[I(1)] = x; w[I(0)] = x;
         x = bc_norm<T>(bc, 1, 0, u[I(nx - 4)]); u[I(nx - 3)] = x; u[I(nx - 2)] = x; u[I(nx - 1)] = x;

@@ -10,6 +10,9 @@ namespace cfd {
 struct BcTab {
     double dir[18];
     double num[18];
+    // optional per-j Dirichlet value of u on the x-min face (interior j,
+    // nyc entries) replacing dir[0]
+    const double *inflow;
 };
 
 // What a launcher needs besides its arguments: the stream, the fixed shape
@@ -180,5 +183,44 @@ void launch_residual64_ell(cfd_launch_ctx &c, const EllOp<double> &A, const doub
                            const double *x, V *r32, double *norm2_out);
 template <class V>
 void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e);
+
+
+// ---- adjoint.cu (discrete adjoint; adjoint arrays are FP64) ----
+struct UfAdjArgs {
+    const double *x;      // pressure at interior cells (compact)
+    const double *a3[3];  // adjoint of T3 (ghosted), read only; may be null
+    const double *af;     // adjoint of f (compact 3N), may be null
+    const double *asrc;   // adjoint of src (3N), may be null
+    double src_dt;        // dt of src += dt f
+    double wcd, wcl, lz;  // drag/lift weights of the objective
+    double *a1[3];        // adjoint of T1 (ghosted), +=
+    double *ax;           // adjoint of x (compact), +=
+    double *aeta;         // adjoint of eta (ghosted), +=
+};
+template <class T>
+void launch_adj_convdiff(cudaStream_t s, const Geo &g, const Metrics<double> &m, double dt, double nudt,
+                         const T *u0, const T *v0, const T *w0, const double *lu, const double *lv,
+                         const double *lw, double *au, double *av, double *aw);
+template <class T>
+void launch_adj_update_uf(cudaStream_t s, const Geo &g, const Metrics<double> &m, double dt,
+                          const UfAdjArgs &A, const T *u1, const T *v1, const T *w1, const T *eta);
+void launch_adj_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double ddt, const double *jp,
+                    const double *lb, bool compat, double *red, double *au, double *av, double *aw);
+void launch_adj_solve_in(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const double *jp,
+                         const double *lx, double *red, double *bp);
+void launch_adj_solve_out(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const double *jp,
+                          const double *w, double *red, double *lb);
+void launch_adj_bc_main(cudaStream_t s, const Geo &g, const BcTab &bc, double *au, double *av, double *aw,
+                        double *ainflow);
+void launch_adj_bc_copy(cudaStream_t s, const Geo &g, double *a0u, double *a0v, double *a0w, double *a1u,
+                        double *a1v, double *a1w);
+void launch_adj_src_add_ref(cfd_launch_ctx &c, long long n, const double *a1u, const double *a1v,
+                            const double *a1w, double *asrc);
+void launch_adj_src_add_aligned(cudaStream_t s, const Geo &g, const double *a1u, const double *a1v,
+                                const double *a1w, double *asrc);
+void launch_adj_cd_gather(cudaStream_t s, const Geo &g, double *a1u, double *a1v, double *a1w, double *cu,
+                          double *cv, double *cw, double *asrc);
+void launch_gather_interior(cudaStream_t s, const Geo &g, const double *p, double *x);
+void launch_adj_add(cfd_launch_ctx &c, long long n, double *a, const double *b);
 
 }  // namespace cfd

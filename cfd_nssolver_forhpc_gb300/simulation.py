@@ -227,3 +227,101 @@ class Simulation:
 
     def sync(self):
         check(lib().cfd_sync(self._h))
+
+    # -- inflow profile and the discrete adjoint --------------------------
+    def set_inflow_profile(self, u_in):
+        """Per-j inflow u on the x-min face (None restores bc_dir[0][0])."""
+        if u_in is None:
+            check(lib().cfd_set_inflow_profile(self._h, None, 0))
+            return
+        a = np.ascontiguousarray(u_in, dtype=np.float64)
+        check(lib().cfd_set_inflow_profile(self._h, dptr(a), a.size))
+
+    def adj_enable(self, tape_len: int = 1):
+        check(lib().cfd_adj_enable(self._h, tape_len))
+
+    def adj_zero(self):
+        check(lib().cfd_adj_zero(self._h))
+
+    def adj_count(self, field: str) -> int:
+        return int(lib().cfd_adj_field_count(self._h, capi.ADJ_FIELD[field]))
+
+    def adj_upload(self, field: str, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        check(lib().cfd_adj_upload(self._h, capi.ADJ_FIELD[field], dptr(a), a.size))
+
+    def adj_download(self, field: str) -> np.ndarray:
+        out = np.empty(self.adj_count(field))
+        check(lib().cfd_adj_download(self._h, capi.ADJ_FIELD[field], dptr(out), out.size))
+        return out
+
+    def adj_ConvectionDifussion(self, src=T0):
+        check(lib().cfd_adj_convection_diffusion(self._h, src))
+
+    def adj_update_UandF(self, src=T1, wcd=0.0, wcl=0.0):
+        check(lib().cfd_adj_update_uf(self._h, src, wcd, wcl))
+
+    def adj_createBMatrix(self):
+        check(lib().cfd_adj_create_b(self._h))
+
+    def adj_pSolver(self, allow_noconv=False):
+        it, res = C.c_int(), C.c_double()
+        check(lib().cfd_adj_pressure_solve(self._h, C.byref(it), C.byref(res)),
+              allow=(-4,) if allow_noconv else ())
+        return it.value, res.value
+
+    def adj_add_source(self):
+        check(lib().cfd_adj_add_source(self._h))
+
+    def adj_BC_staggered_main(self):
+        check(lib().cfd_adj_bc_main(self._h))
+
+    def adj_BC_staggered_copy(self):
+        check(lib().cfd_adj_bc_copy(self._h))
+
+    def step_record(self, pos: int = 0, allow_noconv=False) -> dict:
+        info = capi.CfdStepInfo()
+        check(lib().cfd_step_record(self._h, pos, C.byref(info)), allow=(-4,) if allow_noconv else ())
+        return {"loop": info.loop, "iters": list(info.iters), "cd": info.cd, "cl": info.cl}
+
+    def adj_step(self, pos: int = 0, wcd: float = 0.0, wcl: float = 0.0, allow_noconv=False) -> dict:
+        info = capi.CfdAdjStepInfo()
+        check(lib().cfd_adj_step(self._h, pos, wcd, wcl, C.byref(info)), allow=(-4,) if allow_noconv else ())
+        return {"iters": list(info.iters), "relres": list(info.relres)}
+
+    def adj_finish(self):
+        check(lib().cfd_adj_finish(self._h))
+
+    def checkpoint_alloc(self, count: int):
+        check(lib().cfd_checkpoint_alloc(self._h, count))
+
+    def checkpoint_save(self, slot: int):
+        check(lib().cfd_checkpoint_save(self._h, slot))
+
+    def checkpoint_load(self, slot: int):
+        check(lib().cfd_checkpoint_load(self._h, slot))
+
+    @staticmethod
+    def _run_dict(res) -> dict:
+        return {"J": res.J, "forward_seconds": res.forward_seconds, "adjoint_seconds": res.adjoint_seconds,
+                "forward_iters": res.forward_iters, "adjoint_iters": res.adjoint_iters,
+                "checkpoints": res.checkpoints}
+
+    def adj_forward(self, first: int, last: int, interval: int, allow_noconv=False) -> dict:
+        cfg = capi.CfdAdjRunConfig(first, last, interval)
+        res = capi.CfdAdjRunResult()
+        check(lib().cfd_adj_forward(self._h, C.byref(cfg), C.byref(res)), allow=(-4,) if allow_noconv else ())
+        return self._run_dict(res)
+
+    def adj_reverse(self, allow_noconv=False) -> dict:
+        res = capi.CfdAdjRunResult()
+        check(lib().cfd_adj_reverse(self._h, C.byref(res)), allow=(-4,) if allow_noconv else ())
+        return self._run_dict(res)
+
+    def adj_mean_drag(self, first: int, last: int, interval: int, allow_noconv=False) -> dict:
+        """J = mean Cd over steps first..last and its gradient (ADJ_ETA,
+        ADJ_INFLOW) by checkpointed reverse time stepping."""
+        cfg = capi.CfdAdjRunConfig(first, last, interval)
+        res = capi.CfdAdjRunResult()
+        check(lib().cfd_adj_mean_drag(self._h, C.byref(cfg), C.byref(res)), allow=(-4,) if allow_noconv else ())
+        return self._run_dict(res)

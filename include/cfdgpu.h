@@ -266,6 +266,108 @@ int cfd_cdcl_noalloc(int nx_cal, int ny_cal, int nz_cal, double lz, const double
                      const double *Dy, const double *Dz, const double *f, double *cd, double *cl,
                      void *stream);
 
+
+/* ---- inflow profile -------------------------------------------------------
+   Per-j Dirichlet value of u on the x-min face (ny_cal values, interior j in
+   order), replacing the scalar bc_dir[0][0] in BC_staggered_main
+   (Boundary_Condition.hpp:72-76, face 0, component u).  u_in = NULL restores
+   the scalar.  The profile is a parameter of the discrete adjoint below.   */
+int cfd_set_inflow_profile(cfd_ctx *ctx, const double *u_in, size_t ny_cal);
+
+/* ---- discrete adjoint -------------------------------------------------------
+   No counterpart in the reference: the reverse-mode derivative of the time
+   step, kernel by kernel.  Adjoint arrays are FP64 in every context and use
+   the forward layouts; each cfd_adj_* kernel entry applies the transpose of
+   the linearised forward function named beside it to the adjoint fields.
+   Supported for the Krylov solvers (SPE, ELL); the adjoint Poisson solves use
+   FP64 defect correction around FP32 CG on the finite-volume operator, to the
+   forward tolerance.                                                        */
+typedef enum {
+    CFD_ADJ_U0 = 0, CFD_ADJ_V0, CFD_ADJ_W0, /* adjoint of T0 (ghosted)                  */
+    CFD_ADJ_U1, CFD_ADJ_V1, CFD_ADJ_W1,     /* adjoint of T1 (ghosted)                  */
+    CFD_ADJ_U3, CFD_ADJ_V3, CFD_ADJ_W3,     /* adjoint of T3 (ghosted)                  */
+    CFD_ADJ_CDU, CFD_ADJ_CDV, CFD_ADJ_CDW,  /* adjoint of the convection-diffusion
+                                               output (ghosted)                         */
+    CFD_ADJ_X,                              /* adjoint of x / interior p (compact)      */
+    CFD_ADJ_B,                              /* adjoint of b (compact)                   */
+    CFD_ADJ_F,                              /* adjoint of f (compact, 3 components)     */
+    CFD_ADJ_SRC,                            /* adjoint of source_termF (compact, 3)     */
+    CFD_ADJ_ETA,                            /* gradient w.r.t. eta (ghosted)            */
+    CFD_ADJ_INFLOW                          /* gradient w.r.t. the inflow profile (ny)  */
+} cfd_adj_field;
+
+/* Allocates the adjoint state and a tape of tape_len steps (needs metrics).  */
+int cfd_adj_enable(cfd_ctx *ctx, int tape_len);
+int cfd_adj_zero(cfd_ctx *ctx);                      /* every adjoint field = 0 */
+size_t cfd_adj_field_count(cfd_ctx *ctx, int field);
+int cfd_adj_upload(cfd_ctx *ctx, int field, const double *host, size_t count);
+int cfd_adj_download(cfd_ctx *ctx, int field, double *host, size_t count);
+
+/* Kernel adjoints (transposes of the forward entry points' linearisations):
+   ADJ_T0 += (d ConvectionDifussion(slot) / d slot)^T ADJ_CD       (cfd_convection_diffusion) */
+int cfd_adj_convection_diffusion(cfd_ctx *ctx, int src_slot);
+/* ADJ_T1, ADJ_X, ADJ_ETA += transpose of update_UandF(slot) applied to
+   (ADJ_T3, ADJ_F + the drag/lift weights: J += wcd Cd + wcl Cl)   (cfd_update_uf + cfd_cdcl) */
+int cfd_adj_update_uf(cfd_ctx *ctx, int src_slot, double wcd, double wcl);
+/* ADJ_T1 += createBMatrix^T ADJ_B (with the compatibility projection when
+   cfg.compat_rhs)                                                  (cfd_create_b) */
+int cfd_adj_create_b(cfd_ctx *ctx);
+/* ADJ_B = A^-T ADJ_X on the range of the singular operator         (cfd_bicgstab) */
+int cfd_adj_pressure_solve(cfd_ctx *ctx, int *iters, double *relres);
+/* ADJ_SRC += adjoint of the PC source coupling of ADJ_T1           (cfd_add_source) */
+int cfd_adj_add_source(cfd_ctx *ctx);
+/* ADJ_T0 (in place) and ADJ_INFLOW: BC_staggered_main^T            (cfd_bc_main) */
+int cfd_adj_bc_main(cfd_ctx *ctx);
+/* ADJ_T0 += ADJ_T1 on the copied faces, which are cleared          (cfd_bc_copy) */
+int cfd_adj_bc_copy(cfd_ctx *ctx);
+
+/* Tape.  cfd_step_record is cfd_step that also stores the step's input
+   velocity and the pressure of each pass at tape position pos (0 <= pos <
+   tape_len).  cfd_adj_step reverses the step recorded at pos: it replays the
+   passes from the tape (no Poisson solves) in adjoint-owned buffers, then
+   applies the adjoint of every operation of the step in reverse order; the
+   objective's weights on that step's drag and lift are wcd, wcl.  The
+   forward state of the context is not modified.  cfd_adj_finish applies the
+   adjoint of cfd_start's boundary conditions after the first step.         */
+typedef struct {
+    int iters[4];     /* adjoint Poisson solve iterations (FP32 inner) per pass */
+    double relres[4]; /* final FP64 relative residuals                         */
+} cfd_adj_step_info;
+int cfd_step_record(cfd_ctx *ctx, int pos, cfd_step_info *info);
+int cfd_adj_step(cfd_ctx *ctx, int pos, double wcd, double wcl, cfd_adj_step_info *info);
+int cfd_adj_finish(cfd_ctx *ctx);
+
+/* Checkpoints of the forward state (T0, T1, p, x, solver scalars, step
+   counter), device-resident.  cfd_checkpoint_alloc sizes the store.        */
+int cfd_checkpoint_alloc(cfd_ctx *ctx, int count);
+int cfd_checkpoint_save(cfd_ctx *ctx, int slot);
+int cfd_checkpoint_load(cfd_ctx *ctx, int slot);
+
+/* Gradient of the time-averaged drag J = mean(Cd over steps first..last)
+   (step n = the n-th step after cfd_start) with respect to eta and the
+   inflow profile, by checkpointed reverse time stepping.
+   cfd_adj_forward runs `last` steps from a context right after cfd_start,
+   saving a checkpoint every `interval` steps, and returns J.
+   cfd_adj_reverse recomputes each segment on the tape (interval <= tape_len)
+   and reverses it, last segment first; the gradients are left in ADJ_ETA and
+   ADJ_INFLOW and the context in the state after step `last`.
+   cfd_adj_mean_drag runs both.                                             */
+typedef struct {
+    int first, last;  /* averaging window (inclusive); the run has `last` steps */
+    int interval;     /* checkpoint interval = segment length (<= tape_len)     */
+} cfd_adj_run_config;
+typedef struct {
+    double J;                 /* the objective                                  */
+    double forward_seconds;   /* the forward run with checkpoints               */
+    double adjoint_seconds;   /* recompute + reverse sweep                      */
+    long long forward_iters;  /* forward Poisson iterations                     */
+    long long adjoint_iters;  /* adjoint Poisson iterations (FP32 inner)        */
+    int checkpoints;
+} cfd_adj_run_result;
+int cfd_adj_forward(cfd_ctx *ctx, const cfd_adj_run_config *cfg, cfd_adj_run_result *out);
+int cfd_adj_reverse(cfd_ctx *ctx, cfd_adj_run_result *out);
+int cfd_adj_mean_drag(cfd_ctx *ctx, const cfd_adj_run_config *cfg, cfd_adj_run_result *out);
+
 #ifdef __cplusplus
 }
 #endif
