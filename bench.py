@@ -1,6 +1,9 @@
 """Benchmark of the GB300 time step: Mcell-steps/s of the predictor-corrector
-step of the flow-past-a-cylinder workload at 512x256x32 (4.19 M cells), FP64,
-BiCGSTAB (matrix-free Jacobi-scaled operator) to relative residual 1e-10.
+step of the flow-past-a-cylinder workload at 512x256x32 (4.19 M cells),
+Poisson solves to relative residual 1e-10.  The headline is the mixed-precision
+step (FP32 fields and inner CG, FP64 defect correction); the FP64 step
+(BiCGSTAB over the matrix-free Jacobi-scaled operator) is timed beside it and
+ratio_mixed_vs_fp64 is their ratio at the same tolerance.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -16,6 +19,10 @@ loop (three predictor passes and the final pass, four Poisson solves).
 * roofline   -- the dominant kernel (largest share of the step's device time),
                 timed alone with CUDA events on the library stream; bytes are
                 the algorithmic bytes of one launch.
+* adjoint    -- gradient of the mean drag w.r.t. the inflow profile and eta on
+                the 256x128x16 workload (bounded sample of steps): forward run
+                with checkpoints, then recompute + reverse sweep; ratio =
+                adjoint seconds / forward seconds, FP64 and mixed forward.
 * cpu_baseline / --impl reference -- the reference's own CPU code for the step
                 (oracle/_ref/<workload>/libref.so, its headers compiled from a
                 patched copy), else the oracle's C restatement, on the host's
@@ -72,10 +79,14 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="precision of the headline step (the other one is timed beside it)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision comparison leg")
+    ap.add_argument("--no-compare", action="store_true", help="skip the other-precision comparison leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward ratio leg")
+    ap.add_argument("--adj-workload", default="c4")
+    ap.add_argument("--adj-steps", type=int, default=20, help="steps of the bounded adjoint sample")
     ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
     return ap.parse_args()
 
@@ -379,6 +390,47 @@ def cpu_baseline(args, w, warmup, steps, budget_s=600):
 
 
 # ---------------------------------------------------------------------------
+def adjoint_leg(args, dist):
+    """Gradient of the mean drag (steps n/2..n of an n-step cylinder run on the
+    adjoint workload) w.r.t. the inflow profile and eta, by checkpointed reverse
+    time stepping: forward run with checkpoints, then recompute + reverse
+    sweep.  ratio = (recompute + reverse) seconds / forward seconds, for the
+    FP64 forward and for the FP32 forward with FP64-refined solves."""
+    import numpy as np
+
+    from cfd_nssolver_forhpc_gb300 import capi
+    from cfd_nssolver_forhpc_gb300.adjoint import MeanDrag
+    from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+    wa = WORKLOADS[args.adj_workload]
+    n = max(4, args.adj_steps)
+    first, interval = n // 2, max(1, n // 4)
+    out = {"workload": f"{wa.name}: cylinder wake {wa.nxc}x{wa.nyc}x{wa.nzc}, Re {wa.re:g}, dt {wa.dt:g}, "
+                       f"tol {wa.tol:g}",
+           "objective": f"mean Cd over steps {first}..{n} (bounded sample of the {wa.steps}-step run)",
+           "parameters": f"inflow profile ({wa.nyc}) + eta ({wa.n_ghosted})",
+           "checkpoint_interval": interval}
+    for prec_name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+        m = MeanDrag(wa, first, n, interval, precision=prec, tol=wa.tol)
+        try:
+            eta = m.default_eta().numpy()
+            prof = np.full(wa.nyc, float(wa.bc_dir[0][0]))
+            dist.barrier()
+            J = m.objective(prof, eta)
+            g_in, g_eta = m.gradient()
+            run = m.last_run
+            out[prec_name] = {
+                "J": J, "forward_seconds": round(run["forward_seconds"], 4),
+                "adjoint_seconds": round(run["adjoint_seconds"], 4),
+                "ratio": round(run["adjoint_seconds"] / run["forward_seconds"], 3),
+                "forward_iters": run["forward_iters"], "adjoint_iters": run["adjoint_iters"],
+                "grad_inflow_norm": float(np.linalg.norm(g_in)), "grad_eta_norm": float(np.linalg.norm(g_eta)),
+            }
+        finally:
+            m.close()
+    out["ratio"] = out["mixed"]["ratio"] if args.precision == "mixed" else out["fp64"]["ratio"]
+    return out
+
+
 def main():
     args = parse()
     if args.cpu_worker:
@@ -437,22 +489,30 @@ def main():
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "seconds": round(wall_s, 4)}
     S.close()
-    mixed_leg = None
-    if not args.no_mixed and not mixed and args.solver != "sor":
-        M = build_sim(args, w, "mixed")
+    # the other precision on the same workload: the mixed / FP64 ratio at the
+    # same tolerance, and the drag difference
+    other = None
+    other_prec = "fp64" if mixed else "mixed"
+    if not args.no_compare and args.solver != "sor":
+        M = build_sim(args, w, other_prec)
         for _ in range(W):
             M.step(allow_noconv=True)
         msec, minfos, mlaunch = timed_steps(M, K, dist)
         msec = dist.max(msec)
         mval = w.n_cells * K * dist.world / msec / 1e6
-        mixed_leg = {"value": round(mval, 4), "unit": UNIT, "ratio_vs_fp64": round(mval / value, 3),
-                     "dtype": "f32+f64", "ms_per_step": round(msec / K * 1e3, 3),
-                     "iters_per_step": [sum(i["iters"]) for i in minfos],
-                     "outer_per_step": [sum(i["outer"]) for i in minfos],
-                     "max_relres": max(r for i in minfos[1:] or minfos for r in i["relres"]),
-                     "cd_last": minfos[-1]["cd"], "cd_rel_vs_fp64": abs(minfos[-1]["cd"] / cd64 - 1.0),
-                     "gpu_launches": mlaunch, "roofline": roofline(M, w, minfos, "mixed")}
+        mixed_v, fp64_v = (value, mval) if mixed else (mval, value)
+        other = {"precision": other_prec, "value": round(mval, 4), "unit": UNIT,
+                 "dtype": "f64" if mixed else "f32+f64", "ms_per_step": round(msec / K * 1e3, 3),
+                 "iters_per_step": [sum(i["iters"]) for i in minfos],
+                 "max_relres": max(r for i in minfos[1:] or minfos for r in i["relres"]),
+                 "cd_last": minfos[-1]["cd"], "cd_rel_vs_headline": abs(minfos[-1]["cd"] / cd64 - 1.0),
+                 "div_inf_T0": M.div_inf(0), "gpu_launches": mlaunch,
+                 "roofline": roofline(M, w, minfos, other_prec),
+                 "ratio_mixed_vs_fp64": round(mixed_v / fp64_v, 3)}
         M.close()
+    adjoint = None
+    if not args.no_adjoint and args.solver != "sor":
+        adjoint = adjoint_leg(args, dist)
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, w, 1, 1, budget_s=300)
@@ -468,12 +528,16 @@ def main():
                        "tol": w.tol, "precision": args.precision, "parallelism": f"replicas x{dist.world}",
                        "l2": "working set larger than L2 (no flush needed)"},
             "iters_per_step": [sum(i["iters"]) for i in infos],
+            "max_relres": max(r for i in infos[1:] or infos for r in i["relres"]),
             "cd_last": infos[-1]["cd"], "div_inf_T0": div,
             "roofline": rl, "cpu_baseline": cpu, "clocks": clocks, "e2e": e2e,
             "gpu_launches": launches,
         }
-        if mixed_leg:
-            line["mixed"] = mixed_leg
+        if other:
+            line[other_prec] = other
+            line["ratio_mixed_vs_fp64"] = other["ratio_mixed_vs_fp64"]
+        if adjoint:
+            line["adjoint"] = adjoint
         print(json.dumps(line))
     dist.close()
 
