@@ -269,7 +269,7 @@ def e2e_steps(S, K, dist):
 # residual of its defect correction
 KERNEL_BYTES_MIXED = {
     "cg_pq": 16,       # read z, p; write p', q (FP32)
-    "cg_upd": 28,      # read e, p, h, q; write e, h, z (FP32)
+    "cg_upd": 32,      # read e, p, h, q, 1/P; write e, h, z (FP32)
     "residual64": 28,  # read b, x, jp (FP64); write r (FP32)
 }
 

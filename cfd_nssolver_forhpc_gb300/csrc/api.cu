@@ -144,6 +144,7 @@ int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int
         if (c->debug > 1)
             std::fprintf(stderr, "[cfdgpu] inner graph %d batch %lld: done %d iter %d relres %.3e restarts %d\n", gi,
                          nb, c->h_sc->done, c->h_sc->iter, c->h_sc->relres, c->h_sc->restarts);
+        if (c->h_sc->wait_timeout) return fail(CFD_ERR_TIMEOUT, "a bounded wait of the TMA pipeline gave up");
         if (c->h_sc->done != BICG_RUNNING) break;
         if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "inner solve did not report completion");
         c->launches += (long long)launches_pair * 2 * pairs;
@@ -178,11 +179,12 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
         c, 3, sc,
         [&] {
             launch_cg_init(c->lc, F, h, c->w32.p1, sc);
-            launch_cg_iteration(c->lc, F, c->cg_ip, e, h, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap, sc, 0, true);
+            launch_cg_iteration(c->lc, F, c->cg_ip, e, h, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap, sc, 0, true,
+                                &c->cgtma);
         },
         [&](int from) {
             launch_cg_iteration(c->lc, F, c->cg_ip, e, h, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap, sc, from,
-                                false);
+                                false, &c->cgtma);
         },
         3, 2);
 }
@@ -468,6 +470,10 @@ int ensure_fp32_solver(cfd_ctx *c)
     launch_cg_ip(c->lc, fv32(c), c->cg_ip);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->s));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cg_tma_setup(c->cgtma, fv32(c), c->w32.r0, c->w32.p1, c->p_alt, sms > 0 ? sms : 148, c->lc.red_blocks);
     return CFD_OK;
 }
 
@@ -690,6 +696,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     c->lc.red_blocks = red_blocks;
     c->lc.grid_cap = sms * 16;
     c->lc.cg_grid = cg_resident_grid(sms, red_blocks);
+    if (c->cg_ip) cg_tma_setup(c->cgtma, fv32(c), c->w32.r0, c->w32.p1, c->p_alt, sms, red_blocks);
 
     // zero everything, then the reference's initial values
     e = cudaMemsetAsync(c->lc.counter, 0, sizeof(unsigned int), c->s);
@@ -1202,7 +1209,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
             CK(cudaMemsetAsync(c->e32, 0, (size_t)g.n * sizeof(float), c->s));
             if ((st = timed(CFD_KERNEL_CG_PQ, [&] {
                      launch_cg_part(c->lc, F, c->cg_ip, c->e32, c->r32, c->w32.r0, c->w32.p1, c->p_alt, c->w32.ap,
-                                    c->sc_t, 0);
+                                    c->sc_t, 0, &c->cgtma);
                  })) != CFD_OK)
                 return st;
             if ((st = timed(CFD_KERNEL_CG_UPD, [&] {

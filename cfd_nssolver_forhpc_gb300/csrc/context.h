@@ -97,6 +97,7 @@ struct cfd_ctx {
     float *p_alt = nullptr, *ap_alt = nullptr;  // second p/ap pair of the fused FP32 iteration
     float *fv_sum[3] = {};                      // per-axis cm + cp (FP32) of the CG inner solve
     float *cg_ip = nullptr;                     // 1 / diag(M) (FP32) of the CG inner solve
+    cfd::CgTma cgtma{};                         // tensor maps of the TMA-fed CG stencil
     cfd::BicgScal sc_init{}, sc_in_init{};  // scalars of a fresh solver (cfd_start restores them)
     cfd::BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
     // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cuda.h>
+
 #include "cfd_internal.cuh"
 
 namespace cfd {
@@ -111,6 +113,7 @@ struct BicgScal {
     // restart_rel == 0 keeps bicgstabRe2's absolute rule.
     double restart_rel, r0n2;
     int iter, done, restart, timestep, maxit, restarts, total_iters, nonfinite;
+    int wait_timeout;  // a bounded device wait (TMA pipeline) gave up
 };
 enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
 
@@ -145,8 +148,21 @@ void launch_bicg_fused_iteration(cfd_launch_ctx &c, const SpeOp<V> &A, V *x, con
 // FP32 Jacobi-preconditioned CG on M e = P r (the mixed-precision inner
 // solve): init, first M p, then (fused p update + M p, update) pairs
 void launch_cg_init(cfd_launch_ctx &c, const FvOp<float> &F, float *h, float *p, BicgScal *sc);
+// TMA-fed variant of the CG stencil kernel: tensor maps of the z, p and p_alt
+// vectors ([nxc][nyc][nzc] FP32, boxes of one (j, k) tile plane with halo),
+// built when nzc is a multiple of 4 (16-byte row strides)
+struct CgTma {
+    bool ok = false;
+    int TK = 0, TJ = 0, grid = 0;
+    size_t smem = 0;
+    CUtensorMap z, p, palt;
+};
+// builds the maps for the given buffers; false when TMA cannot be used
+bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *p, const float *p_alt, int sms,
+                  int red_blocks);
 void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
-                         float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first);
+                         float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first,
+                         const CgTma *tma = nullptr);
 // one full wave of the CG inner kernels on this device, capped at red_blocks
 int cg_resident_grid(int sms, int red_blocks);
 // iP = 1 / diag(M), once per context
@@ -154,7 +170,7 @@ void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP);
 void launch_fv_axes(cudaStream_t s, int n, const float *c, float *sum);
 // one CG kernel (0 = fused p update + M p, 1 = update), for timing
 void launch_cg_part(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
-                    float *p, float *pn, float *q, BicgScal *sc, int part);
+                    float *p, float *pn, float *q, BicgScal *sc, int part, const CgTma *tma = nullptr);
 // one kernel of the iteration (0 ap, 1 s, 2 as, 3 xr, 4 p), for timing
 template <class Op, class V>
 void launch_bicg_iteration_part(cfd_launch_ctx &c, const Op &A, V *x, const BicgVecs<V> &w, BicgScal *sc,

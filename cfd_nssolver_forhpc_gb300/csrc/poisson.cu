@@ -9,6 +9,8 @@
 // reproducible run to run.  Kernels of an iteration return at once when the
 // solve has finished (BicgScal::done), so the host may queue iterations
 // ahead of the convergence test.
+#include <cstdlib>
+
 #include "cfd_internal.cuh"
 #include "kernels.h"
 
@@ -536,6 +538,7 @@ k_cg_init(FvOp<float> F, float *__restrict__ h, float *__restrict__ p, BicgScal 
         sc->timestep += 1;
         sc->done = tot[0] > 0.0 ? BICG_RUNNING : BICG_ZERO_RHS;
         sc->relres = tot[0] > 0.0 ? 1.0 : 0.0;
+        sc->wait_timeout = 0;
     }
 }
 
@@ -650,6 +653,221 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
     if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
 }
 
+// ---- TMA-fed CG stencil ------------------------------------------------------
+// The same operation as k_cg_pq, with the z and p planes streamed into
+// shared memory by the tensor-memory accelerator.  A block owns a TK x TJ
+// tile of the (k, j) plane; each of its 256 threads handles one float4 of k.
+// One elected thread keeps kCgStages planes of z (and p) in flight: each TMA
+// box is one plane of the tile plus a halo of one row in j and four cells in
+// k (so the box starts on a 16-byte boundary), and the TMA fills the parts
+// outside the domain with zeros, which is the value the stencil needs there.
+// Per plane the block forms pn = z + beta p over the tile and its halo in a
+// shared plane (three rotating buffers), then applies M at the previous plane
+// with its x neighbours held in registers.  The mbarrier waits are bounded:
+// on timeout the block records sc->wait_timeout and carries on, so a lost
+// copy cannot hang the GPU; the host turns the flag into an error.
+constexpr int kCgStages = 4;
+constexpr long long kCgWaitLimit = 1LL << 24;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait: false if the phase did not complete within the limit
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    for (long long it = 0; it < kCgWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+template <int TK>
+struct CgTile {
+    static constexpr int TKQ = TK / 4;           // threads along k
+    static constexpr int TJ = kBlock / TKQ;      // rows along j
+    static constexpr int BX = TK + 8;            // box width (floats): 4-cell halo each side
+    static constexpr int BY = TJ + 2;            // box height: 1-row halo each side
+    static constexpr int BOXB = BX * BY * 4;     // bytes of one box
+    static constexpr int STRIDE = (BOXB + 127) / 128 * 128;
+    static constexpr int NHALO = 2 * TKQ + 2 * TJ;  // halo float4 items per plane
+    static constexpr size_t smem(int nv) { return 128 + (size_t)(kCgStages * nv + 3) * STRIDE + 128; }
+};
+
+template <bool first, int TK>
+__global__ void __launch_bounds__(kBlock)
+k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mz, const __grid_constant__ CUtensorMap mp,
+            float *__restrict__ pn_out, float *__restrict__ q, BicgScal *sc, double *partials,
+            unsigned int *counter, int ichunk)
+{
+    using G = CgTile<TK>;
+    constexpr int NV = first ? 1 : 2;
+    if (sc->done) return;
+    extern __shared__ unsigned char dsm[];
+    const unsigned base = (smem_u32(dsm) + 127u) & ~127u;
+    unsigned char *gbase = dsm + (base - smem_u32(dsm));
+    const unsigned bars = base;                       // kCgStages mbarriers (8 B each)
+    const unsigned stage0 = base + 128;               // stages: [stage][vector] boxes
+    float *stg = reinterpret_cast<float *>(gbase + 128);
+    float *pnb = reinterpret_cast<float *>(gbase + 128 + (size_t)kCgStages * NV * G::STRIDE);
+    constexpr int SF = G::STRIDE / 4;                 // floats per box slot
+    __shared__ int bad;
+
+    const SpeOp<float> &A = F.A;
+    const int nxc = A.nxc, nyc = A.nyc, nzc = A.nzc;
+    const long long sxc = A.sxc;
+    const int t = threadIdx.x, tk4 = t % G::TKQ, tj = t / G::TKQ;
+    const int tiles_k = (nzc + TK - 1) / TK, tiles_j = (nyc + G::TJ - 1) / G::TJ;
+    const int tiles = tiles_k * tiles_j, items = tiles * ((nxc + ichunk - 1) / ichunk);
+    const float beta = first ? 0.f : (float)sc->beta;
+    if (t == 0) {
+        bad = 0;
+        for (int s = 0; s < kCgStages; ++s) mbar_init(bars + 8 * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // one plane's TMA boxes into the stage of global plane counter g
+    auto issue = [&](long long g, int k0, int j0, int ip) {
+        const int st = (int)(g % kCgStages);
+        const unsigned bar = bars + 8 * st;
+        mbar_expect_tx(bar, NV * G::BOXB);
+        tma_load_3d(stage0 + (unsigned)(st * NV) * G::STRIDE, &mz, k0 - 4, j0 - 1, ip, bar);
+        if (!first) tma_load_3d(stage0 + (unsigned)(st * NV + 1) * G::STRIDE, &mp, k0 - 4, j0 - 1, ip, bar);
+    };
+    const int cslot = (tj + 1) * G::BX + 4 + 4 * tk4;  // this thread's float4 in a box / pn plane
+    float pa = 0.f;
+    long long g0 = 0;  // planes consumed by this block so far (mbarrier phases)
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int tile = item % tiles, chunk = item / tiles;
+        const int k0 = (tile % tiles_k) * TK, j0 = (tile / tiles_k) * G::TJ;
+        const int ib = chunk * ichunk, ie = min(nxc, ib + ichunk);
+        const int np = ie - ib + 2;  // planes ib-1 .. ie
+        const int j = j0 + tj, k = k0 + 4 * tk4;
+        const bool in = j < nyc && k < nzc;
+        if (t == 0)
+            for (int s = 0; s < kCgStages && s < np; ++s) issue(g0 + s, k0, j0, ib - 1 + s);
+        float4 czm = make_float4(0.f, 0.f, 0.f, 0.f), czp = czm, syz = czm, wyz = czm;
+        float cym = 0.f, cyp = 0.f;
+        if (in) {
+            cym = __ldg(A.cym + j);
+            cyp = __ldg(A.cyp + j);
+            czm = __ldg(reinterpret_cast<const float4 *>(A.czm + k));
+            czp = __ldg(reinterpret_cast<const float4 *>(A.czp + k));
+            const float4 sz = __ldg(reinterpret_cast<const float4 *>(F.sz + k));
+            const float sy = __ldg(F.sy + j), wy = __ldg(F.wy + j);
+            syz = make_float4(sy + sz.x, sy + sz.y, sy + sz.z, sy + sz.w);
+            wyz = make_float4(wy * __ldg(F.wz + k), wy * __ldg(F.wz + k + 1), wy * __ldg(F.wz + k + 2),
+                              wy * __ldg(F.wz + k + 3));
+        }
+        float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = p1;
+        for (int tt = 0; tt < np; ++tt) {
+            const long long g = g0 + tt;
+            const int st = (int)(g % kCgStages);
+            if (!mbar_wait(bars + 8 * st, (unsigned)((g / kCgStages) & 1))) bad = 1;
+            const float *zs = stg + (size_t)(st * NV) * SF;
+            const float *ps = stg + (size_t)(st * NV + 1) * SF;
+            float *pb = pnb + (size_t)(tt % 3) * SF;
+            auto form = [&](int off) {
+                float4 zv = *reinterpret_cast<const float4 *>(zs + off);
+                if (!first) {
+                    const float4 pv = *reinterpret_cast<const float4 *>(ps + off);
+                    zv.x = fmaf(beta, pv.x, zv.x);
+                    zv.y = fmaf(beta, pv.y, zv.y);
+                    zv.z = fmaf(beta, pv.z, zv.z);
+                    zv.w = fmaf(beta, pv.w, zv.w);
+                }
+                *reinterpret_cast<float4 *>(pb + off) = zv;
+                return zv;
+            };
+            const float4 nxt = form(cslot);
+            for (int h = t; h < G::NHALO; h += kBlock) {
+                int row, col;  // col in float4 units of the box row
+                if (h < G::TKQ) { row = 0; col = 1 + h; }
+                else if (h < 2 * G::TKQ) { row = G::TJ + 1; col = 1 + h - G::TKQ; }
+                else if (h < 2 * G::TKQ + G::TJ) { row = 1 + h - 2 * G::TKQ; col = 0; }
+                else { row = 1 + h - 2 * G::TKQ - G::TJ; col = G::TKQ + 1; }
+                form(row * G::BX + 4 * col);
+            }
+            __syncthreads();
+            // the stage of plane tt is consumed: refill it with plane tt + kCgStages
+            if (t == 0 && tt + kCgStages < np) issue(g + kCgStages, k0, j0, ib - 1 + tt + kCgStages);
+            if (tt >= 2 && in) {
+                const int c = ib + tt - 2;  // plane of the stencil (pn at c-1, c, c+1 = p2, p1, nxt)
+                const float *pc = pnb + (size_t)((tt - 1) % 3) * SF;
+                const float4 vs = *reinterpret_cast<const float4 *>(pc + cslot - G::BX);
+                const float4 vn = *reinterpret_cast<const float4 *>(pc + cslot + G::BX);
+                const float kb = pc[cslot - 1], kt = pc[cslot + 4];
+                const float cxm = __ldg(A.cxm + c), cxp = __ldg(A.cxp + c);
+                const float sxv = __ldg(F.sx + c), wxv = __ldg(F.wx + c);
+                const float4 vc = p1;
+                auto cell = [&](float vm_, float vs_, float vb_, float vt_, float vn_, float vp_, float vc_,
+                                float czm_, float czp_, float syz_, float wyz_) {
+                    float sum = cxm * vm_;
+                    sum = fmaf(cym, vs_, sum);
+                    sum = fmaf(czm_, vb_, sum);
+                    sum = fmaf(czp_, vt_, sum);
+                    sum = fmaf(cyp, vn_, sum);
+                    sum = fmaf(cxp, vp_, sum);
+                    return (wxv * wyz_) * fmaf(sxv + syz_, vc_, -sum);
+                };
+                float4 qv;
+                qv.x = cell(p2.x, vs.x, kb, vc.y, vn.x, nxt.x, vc.x, czm.x, czp.x, syz.x, wyz.x);
+                qv.y = cell(p2.y, vs.y, vc.x, vc.z, vn.y, nxt.y, vc.y, czm.y, czp.y, syz.y, wyz.y);
+                qv.z = cell(p2.z, vs.z, vc.y, vc.w, vn.z, nxt.z, vc.z, czm.z, czp.z, syz.z, wyz.z);
+                qv.w = cell(p2.w, vs.w, vc.z, kt, vn.w, nxt.w, vc.w, czm.w, czp.w, syz.w, wyz.w);
+                const long long r = (long long)c * sxc + (long long)j * nzc + k;
+                if (!first) *reinterpret_cast<float4 *>(pn_out + r) = vc;
+                *reinterpret_cast<float4 *>(q + r) = qv;
+                pa = fmaf(vc.x, qv.x, pa);
+                pa = fmaf(vc.y, qv.y, pa);
+                pa = fmaf(vc.z, qv.z, pa);
+                pa = fmaf(vc.w, qv.w, pa);
+            }
+            p2 = p1;
+            p1 = nxt;
+        }
+        g0 += np;
+        __syncthreads();  // the next item rewrites the pn planes
+    }
+    if (t == 0 && bad) sc->wait_timeout = 1;
+    double acc[1] = {(double)pa}, tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+}
+
 // e += alpha p, h -= alpha q, z = iP h, rho' = h . z (pure streaming, four
 // rows per thread step); convergence on sqrt(rho'/rho0)
 __global__ void __launch_bounds__(kBlock, 6)
@@ -742,11 +960,58 @@ void launch_cg_init(cfd_launch_ctx &c, const FvOp<float> &F, float *h, float *p,
     k_cg_init<<<c.red_blocks, kBlock, 0, c.s>>>(F, h, p, sc, c.partials, c.counter);
 }
 
+// grid shape of the TMA kernel for one launch
+static void cg_tma_launch_shape(const CgTma &t, const FvOp<float> &F, int &ichunk, int &grid)
+{
+    const SpeOp<float> &A = F.A;
+    const int TJ = t.TJ;
+    const int tiles = ((A.nzc + t.TK - 1) / t.TK) * ((A.nyc + TJ - 1) / TJ);
+    int chunks = t.grid / tiles;
+    if (chunks < 1) chunks = 1;
+    if (chunks > A.nxc) chunks = A.nxc;
+    ichunk = (A.nxc + chunks - 1) / chunks;
+    chunks = (A.nxc + ichunk - 1) / ichunk;
+    grid = tiles * chunks < t.grid ? tiles * chunks : t.grid;
+}
+
+template <bool first, int TK>
+static void launch_tma_t(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t, const CUtensorMap *mz,
+                         const CUtensorMap *mp, float *pn, float *q, BicgScal *sc)
+{
+    int ichunk, grid;
+    cg_tma_launch_shape(t, F, ichunk, grid);
+    k_cg_pq_tma<first, TK><<<grid, kBlock, CgTile<TK>::smem(first ? 1 : 2), c.s>>>(F, *mz, *mp, pn, q, sc,
+                                                                                   c.partials, c.counter, ichunk);
+}
+
+// z_map: the z vector (or p itself on the first iteration), p_map: p
+static void launch_cg_pq_tma(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t, bool first,
+                             const CUtensorMap *z_map, const CUtensorMap *p_map, float *pn, float *q, BicgScal *sc)
+{
+    if (t.TK == 32) {
+        if (first) launch_tma_t<true, 32>(c, F, t, z_map, p_map, pn, q, sc);
+        else launch_tma_t<false, 32>(c, F, t, z_map, p_map, pn, q, sc);
+    } else if (t.TK == 16) {
+        if (first) launch_tma_t<true, 16>(c, F, t, z_map, p_map, pn, q, sc);
+        else launch_tma_t<false, 16>(c, F, t, z_map, p_map, pn, q, sc);
+    } else {
+        if (first) launch_tma_t<true, 8>(c, F, t, z_map, p_map, pn, q, sc);
+        else launch_tma_t<false, 8>(c, F, t, z_map, p_map, pn, q, sc);
+    }
+}
+
 void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
-                         float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first)
+                         float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first, const CgTma *tma)
 {
     float *P[2] = {p, p_alt};
     const int to = first ? from : 1 - from;
+    if (tma && tma->ok) {
+        const CUtensorMap *pmap = from == 0 ? &tma->p : &tma->palt;
+        // first iteration: pn = p0, which k_cg_init wrote into P[from]
+        launch_cg_pq_tma(c, F, *tma, first, first ? pmap : &tma->z, pmap, P[to], q, sc);
+        k_cg_upd<<<c.cg_grid, kBlock, 0, c.s>>>(F.A.n, e, P[to], h, q, iP, z, sc, c.partials, c.counter);
+        return;
+    }
     const CgShape cs = cg_shape(c, F);
     // first iteration: pn = p0 (written by k_cg_init into P[from]), read as z
     if (first)
@@ -756,6 +1021,80 @@ void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *i
         k_cg_pq<false><<<cs.grid, kBlock, 0, c.s>>>(F, z, P[from], P[to], q, sc, c.partials, c.counter, cs.TK,
                                                     cs.ichunk);
     k_cg_upd<<<c.cg_grid, kBlock, 0, c.s>>>(F.A.n, e, P[to], h, q, iP, z, sc, c.partials, c.counter);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(ptr);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// [nxc][nyc][nzc] FP32 vector, box {TK + 8, TJ + 2, 1} (k, j, i)
+static bool make_map(CUtensorMap &m, const float *base, const SpeOp<float> &A, int TK, int TJ)
+{
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn || !base || (reinterpret_cast<unsigned long long>(base) & 15ull)) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)A.nzc, (cuuint64_t)A.nyc, (cuuint64_t)A.nxc};
+    const cuuint64_t strides[2] = {(cuuint64_t)A.nzc * 4, (cuuint64_t)A.nyc * A.nzc * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)(TK + 8), (cuuint32_t)(TJ + 2), 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, es,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int TK>
+static bool tma_attrs(size_t &smem, int &per_sm)
+{
+    smem = CgTile<TK>::smem(2);
+    if (cudaFuncSetAttribute(k_cg_pq_tma<false, TK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_cg_pq_tma<true, TK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)CgTile<TK>::smem(1)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_pq_tma<false, TK>, kBlock, smem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return per_sm > 0;
+}
+
+bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *p, const float *p_alt, int sms,
+                  int red_blocks)
+{
+    t.ok = false;
+    const SpeOp<float> &A = F.A;
+    if (A.nzc % 4 != 0) return false;
+    if (const char *e = std::getenv("CFDGPU_NO_TMA"))
+        if (e[0] == '1') return false;
+    t.TK = A.nzc >= 24 ? 32 : (A.nzc >= 12 ? 16 : 8);
+    t.TJ = kBlock / (t.TK / 4);
+    int per_sm = 0;
+    bool ok = t.TK == 32 ? tma_attrs<32>(t.smem, per_sm) : t.TK == 16 ? tma_attrs<16>(t.smem, per_sm)
+                                                                      : tma_attrs<8>(t.smem, per_sm);
+    if (!ok) return false;
+    t.grid = per_sm * sms < red_blocks ? per_sm * sms : red_blocks;
+    if (!make_map(t.z, z, A, t.TK, t.TJ) || !make_map(t.p, p, A, t.TK, t.TJ) ||
+        !make_map(t.palt, p_alt, A, t.TK, t.TJ))
+        return false;
+    t.ok = true;
+    return true;
 }
 
 int cg_resident_grid(int sms, int red_blocks)
@@ -777,8 +1116,12 @@ void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP)
 }
 
 void launch_cg_part(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
-                    float *p, float *pn, float *q, BicgScal *sc, int part)
+                    float *p, float *pn, float *q, BicgScal *sc, int part, const CgTma *tma)
 {
+    if (part == 0 && tma && tma->ok) {  // z, p = the z and p1 buffers of the maps
+        launch_cg_pq_tma(c, F, *tma, false, &tma->z, &tma->p, pn, q, sc);
+        return;
+    }
     if (part == 0) {
         const CgShape cs = cg_shape(c, F);
         k_cg_pq<false><<<cs.grid, kBlock, 0, c.s>>>(F, z, p, pn, q, sc, c.partials, c.counter, cs.TK, cs.ichunk);
