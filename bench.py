@@ -268,8 +268,8 @@ def e2e_steps(S, K, dist):
 # FP32 kernels of the mixed-precision inner CG (bytes per row) and the FP64
 # residual of its defect correction
 KERNEL_BYTES_MIXED = {
-    "cg_pq": 16,       # read z, p; write p', q (FP32)
-    "cg_upd": 32,      # read e, p, h, q, 1/P; write e, h, z (FP32)
+    "cg_pq": 16,       # read h (z = h/P formed in the kernel), p; write p', q (FP32)
+    "cg_upd": 24,      # read e, p, h, q; write e, h (FP32; 1/P from the axis tables)
     "residual64": 28,  # read b, x, jp (FP64); write r (FP32)
 }
 

@@ -459,12 +459,12 @@ int ensure_fp32_solver(cfd_ctx *c)
     if (!c->jp32) CKS(dalloc_t(c, &c->jp32, n));
     for (int a = 0; a < 3; ++a) {
         if (!c->spe_c32[a]) CKS(dalloc_t(c, &c->spe_c32[a], 2 * (size_t)nc[a]));
-        if (!c->fv_sum[a]) CKS(dalloc_t(c, &c->fv_sum[a], (size_t)nc[a]));
+        if (!c->fv_sum[a]) CKS(dalloc_t(c, &c->fv_sum[a], 2 * (size_t)nc[a]));
     }
     if (!c->cg_ip) CKS(dalloc_t(c, &c->cg_ip, n));
     for (int a = 0; a < 3; ++a) {
         launch_convert<double, float>(c->lc, 2LL * nc[a], c->spe_c[a], c->spe_c32[a]);
-        launch_fv_axes(c->s, nc[a], c->spe_c32[a], c->fv_sum[a]);
+        launch_fv_axes(c->s, nc[a], c->spe_c32[a], fv_width_src(c, a), c->fv_sum[a]);
     }
     launch_convert<double, float>(c->lc, n, c->jp, c->jp32);
     launch_cg_ip(c->lc, fv32(c), c->cg_ip);
@@ -473,7 +473,8 @@ int ensure_fp32_solver(cfd_ctx *c)
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cg_tma_setup(c->cgtma, fv32(c), c->w32.r0, c->w32.p1, c->p_alt, sms > 0 ? sms : 148, c->lc.red_blocks);
+    cg_tma_setup(c->cgtma, fv32(c), c->w32.r0, c->r32, c->w32.p1, c->p_alt, sms > 0 ? sms : 148,
+                 c->lc.red_blocks);
     return CFD_OK;
 }
 
@@ -509,7 +510,7 @@ int build_tables(cfd_ctx *c)
         for (int a = 0; a < 3; ++a) {
             const int na = a == 0 ? g.nxc : a == 1 ? g.nyc : g.nzc;
             launch_convert<double, float>(c->lc, 2LL * na, c->spe_c[a], c->spe_c32[a]);
-            if (c->fv_sum[a]) launch_fv_axes(c->s, na, c->spe_c32[a], c->fv_sum[a]);
+            if (c->fv_sum[a]) launch_fv_axes(c->s, na, c->spe_c32[a], fv_width_src(c, a), c->fv_sum[a]);
         }
         launch_convert<double, float>(c->lc, g.n, c->jp, c->jp32);
         if (c->cg_ip) launch_cg_ip(c->lc, fv32(c), c->cg_ip);
@@ -664,7 +665,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         AL(c->r32, n * 4); AL(c->e32, n * 4);
         AL(c->p_alt, n * 4); AL(c->ap_alt, n * 4);
         for (int a = 0; a < 3; ++a) AL(c->spe_c32[a], (size_t)2 * nc[a] * sizeof(float));
-        for (int a = 0; a < 3; ++a) AL(c->fv_sum[a], (size_t)nc[a] * sizeof(float));
+        for (int a = 0; a < 3; ++a) AL(c->fv_sum[a], 2 * (size_t)nc[a] * sizeof(float));
         AL(c->cg_ip, n * 4);
         AL(c->jp32, n * 4);
         if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
@@ -696,7 +697,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     c->lc.red_blocks = red_blocks;
     c->lc.grid_cap = sms * 16;
     c->lc.cg_grid = cg_resident_grid(sms, red_blocks);
-    if (c->cg_ip) cg_tma_setup(c->cgtma, fv32(c), c->w32.r0, c->w32.p1, c->p_alt, sms, red_blocks);
+    if (c->cg_ip) cg_tma_setup(c->cgtma, fv32(c), c->w32.r0, c->r32, c->w32.p1, c->p_alt, sms, red_blocks);
 
     // zero everything, then the reference's initial values
     e = cudaMemsetAsync(c->lc.counter, 0, sizeof(unsigned int), c->s);

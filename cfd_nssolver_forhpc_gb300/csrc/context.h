@@ -95,7 +95,7 @@ struct cfd_ctx {
     double *px1 = nullptr, *px2 = nullptr;
     float *r32 = nullptr, *e32 = nullptr;
     float *p_alt = nullptr, *ap_alt = nullptr;  // second p/ap pair of the fused FP32 iteration
-    float *fv_sum[3] = {};                      // per-axis cm + cp (FP32) of the CG inner solve
+    float *fv_sum[3] = {};                      // per-axis [cm + cp | interior width] (FP32), CG inner solve
     float *cg_ip = nullptr;                     // 1 / diag(M) (FP32) of the CG inner solve
     cfd::CgTma cgtma{};                         // tensor maps of the TMA-fed CG stencil
     cfd::BicgScal sc_init{}, sc_in_init{};  // scalars of a fresh solver (cfd_start restores them)
@@ -192,14 +192,22 @@ inline SpeOp<float> spe32(cfd_ctx *c)
             c->spe_c32[2] + g.nzc, c->jp32, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc,
             FastDiv((unsigned int)g.nzc)};
 }
+// interior cell widths of axis a (FP32 metric table row AX_D from the first
+// interior cell)
+inline const float *fv_width_src(cfd_ctx *c, int a)
+{
+    const int n[3] = {c->g.nx, c->g.ny, c->g.nz};
+    return c->tab32[a] + (size_t)AX_D * n[a] + GC;
+}
+
 inline FvOp<float> fv32(cfd_ctx *c)
 {
     const Geo &g = c->g;
     FvOp<float> F;
     F.A = spe32(c);
-    F.wx = c->tab32[0] + (size_t)AX_D * g.nx + GC;
-    F.wy = c->tab32[1] + (size_t)AX_D * g.ny + GC;
-    F.wz = c->tab32[2] + (size_t)AX_D * g.nz + GC;
+    F.wx = c->fv_sum[0] + g.nxc;
+    F.wy = c->fv_sum[1] + g.nyc;
+    F.wz = c->fv_sum[2] + g.nzc;
     F.sx = c->fv_sum[0];
     F.sy = c->fv_sum[1];
     F.sz = c->fv_sum[2];

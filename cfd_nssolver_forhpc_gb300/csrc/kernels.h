@@ -155,11 +155,12 @@ struct CgTma {
     bool ok = false;
     int TK = 0, TJ = 0, grid = 0;
     size_t smem = 0;
-    CUtensorMap z, p, palt;
+    bool form_z = false;     // z = h / P formed in the stencil kernel (no z vector)
+    CUtensorMap zh, p, palt;  // z (or the residual h when form_z), p, p_alt
 };
 // builds the maps for the given buffers; false when TMA cannot be used
-bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *p, const float *p_alt, int sms,
-                  int red_blocks);
+bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *h, const float *p,
+                  const float *p_alt, int sms, int red_blocks);
 void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
                          float *p, float *p_alt, float *q, BicgScal *sc, int from, bool first,
                          const CgTma *tma = nullptr);
@@ -167,7 +168,7 @@ void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *i
 int cg_resident_grid(int sms, int red_blocks);
 // iP = 1 / diag(M), once per context
 void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP);
-void launch_fv_axes(cudaStream_t s, int n, const float *c, float *sum);
+void launch_fv_axes(cudaStream_t s, int n, const float *c, const float *width, float *out);
 // one CG kernel (0 = fused p update + M p, 1 = update), for timing
 void launch_cg_part(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
                     float *p, float *pn, float *q, BicgScal *sc, int part, const CgTma *tma = nullptr);
