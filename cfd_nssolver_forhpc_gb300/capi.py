@@ -141,6 +141,12 @@ def lib() -> C.CDLL:
         "cfd_adj_forward": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
         "cfd_adj_reverse": ([vp, C.POINTER(CfdAdjRunResult)], i),
         "cfd_adj_mean_drag": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
+        "cfd_write_plot3d_x": ([vp, C.c_char_p], i),
+        "cfd_write_plot3d_q": ([vp, i, C.c_char_p], i),
+        "cfd_plot3d_q_host": ([C.c_char_p, i, i, i, d, d, dp, dp, dp, dp, dp], i),
+        "cfd_read_plot3d_q": ([C.c_char_p, i, i, i, dp, dp, dp, dp, dp, dp], i),
+        "cfd_save_state": ([vp, C.c_char_p], i),
+        "cfd_load_state": ([vp, C.c_char_p], i),
     }
     for name, (args, res) in proto.items():
         fn = getattr(L, name)

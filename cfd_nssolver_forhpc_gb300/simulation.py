@@ -228,6 +228,22 @@ class Simulation:
     def sync(self):
         check(lib().cfd_sync(self._h))
 
+    # -- files: Plot3D (the reference's format) and the FP64 state ---------
+    def OutputPlot3D_Xfile(self, path):
+        """Cell-centre grid file (io/Plot3D/xfileWrite.hpp:6)."""
+        check(lib().cfd_write_plot3d_x(self._h, str(path).encode()))
+
+    def OutputPLOT3D_Qfile(self, path, slot=T3):
+        """p, cell-centred u, v, w and eta of `slot` (io/Plot3D/qfile.hpp:7)."""
+        check(lib().cfd_write_plot3d_q(self._h, slot, str(path).encode()))
+
+    def save_state(self, path):
+        """Bitwise restart file (T0, T1, eta, p, x, solver scalars, counters)."""
+        check(lib().cfd_save_state(self._h, str(path).encode()))
+
+    def load_state(self, path):
+        check(lib().cfd_load_state(self._h, str(path).encode()))
+
     # -- inflow profile and the discrete adjoint --------------------------
     def set_inflow_profile(self, u_in):
         """Per-j inflow u on the x-min face (None restores bc_dir[0][0])."""
@@ -325,3 +341,19 @@ class Simulation:
         res = capi.CfdAdjRunResult()
         check(lib().cfd_adj_mean_drag(self._h, C.byref(cfg), C.byref(res)), allow=(-4,) if allow_noconv else ())
         return self._run_dict(res)
+
+
+def plot3d_q_host(path, w: Workload, re: float, time: float, p, u, v, w_, eta):
+    """Plot3D q file from ghosted FP64 host arrays (the same bytes as
+    Simulation.OutputPLOT3D_Qfile)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (p, u, v, w_, eta)]
+    check(lib().cfd_plot3d_q_host(str(path).encode(), w.nxc, w.nyc, w.nzc, re, time, *[dptr(a) for a in arrs]))
+
+
+def QfileRead(path, w: Workload):
+    """io/Plot3D/qfileRead.hpp:6: ((mach, alpha, Re, time), p, u, v, w, eta)
+    as ghosted FP64 arrays with the staggered faces rebuilt from the centres."""
+    cond = np.zeros(4)
+    out = [np.empty(w.n_ghosted) for _ in range(5)]
+    check(lib().cfd_read_plot3d_q(str(path).encode(), w.nxc, w.nyc, w.nzc, dptr(cond), *[dptr(a) for a in out]))
+    return (tuple(cond), *out)

@@ -368,6 +368,34 @@ int cfd_adj_forward(cfd_ctx *ctx, const cfd_adj_run_config *cfg, cfd_adj_run_res
 int cfd_adj_reverse(cfd_ctx *ctx, cfd_adj_run_result *out);
 int cfd_adj_mean_drag(cfd_ctx *ctx, const cfd_adj_run_config *cfg, cfd_adj_run_result *out);
 
+
+/* ---- Plot3D files and the FP64 state file ----------------------------------
+   Plot3D as the reference writes it: single block, whole grid, native-endian
+   int32/float32, no record markers, i fastest.
+     cfd_write_plot3d_x  OutputPlot3D_Xfile (io/Plot3D/xfileWrite.hpp:6): cell
+                         centres Xc = (X[i+2] + X[i+3]) / 2 etc.
+     cfd_write_plot3d_q  OutputPLOT3D_Qfile (io/Plot3D/qfile.hpp:7): header
+                         (0, 0, Re, time), then p, the cell-centred u, v, w
+                         (face pairs averaged) and eta of velocity slot `slot`;
+                         formed on the GPU, one copy to the host.
+     cfd_plot3d_q_host   the same file from ghosted FP64 host arrays.
+     cfd_read_plot3d_q   QfileRead (io/Plot3D/qfileRead.hpp:6): cond[4] = (mach,
+                         alpha, Re, time); ghosted FP64 p, u, v, w, eta with the
+                         staggered faces rebuilt as the average of the two
+                         adjacent centres (the last face of a line takes the
+                         last centre), ghosts zero.
+   cfd_save_state / cfd_load_state: no counterpart in the reference; a bitwise
+   restart file of T0, T1, eta, p, x, the solver scalars, the step counter,
+   the time and the inflow profile.                                          */
+int cfd_write_plot3d_x(cfd_ctx *ctx, const char *path);
+int cfd_write_plot3d_q(cfd_ctx *ctx, int slot, const char *path);
+int cfd_plot3d_q_host(const char *path, int nx_cal, int ny_cal, int nz_cal, double re, double time,
+                      const double *p, const double *u, const double *v, const double *w, const double *eta);
+int cfd_read_plot3d_q(const char *path, int nx_cal, int ny_cal, int nz_cal, double *cond, double *p,
+                      double *u, double *v, double *w, double *eta);
+int cfd_save_state(cfd_ctx *ctx, const char *path);
+int cfd_load_state(cfd_ctx *ctx, const char *path);
+
 #ifdef __cplusplus
 }
 #endif

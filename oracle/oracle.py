@@ -324,6 +324,31 @@ class RefHarness:
     def set_threads(self, n: int):
         self.L.ref_set_threads(int(n))
 
+    def plot3d_x(self, directory):
+        """OutputPlot3D_Xfile into directory/mx_out/P3D.x (the directory must exist)."""
+        (Path(directory) / "mx_out").mkdir(exist_ok=True)
+        assert self.L.ref_plot3d_x(str(directory).encode()) == 0
+        return Path(directory) / "mx_out" / "P3D.x"
+
+    def plot3d_q(self, directory, io, time, pr, u, v, w, eta):
+        """OutputPLOT3D_Qfile of the given ghosted fields into
+        directory/mx_out/P3D<io>.q."""
+        (Path(directory) / "mx_out").mkdir(exist_ok=True)
+        L = self.L
+        L.ref_plot3d_q.argtypes = [C.c_char_p, C.c_int, C.c_double] + [_dp] * 5
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (pr, u, v, w, eta)]
+        assert L.ref_plot3d_q(str(directory).encode(), int(io), float(time), *[p(a) for a in arrs]) == 0
+        return Path(directory) / "mx_out" / f"P3D{io:02d}.q"
+
+    def plot3d_read(self, path):
+        """QfileRead: ((mach, alpha, Re, time), p, u, v, w, eta) ghosted."""
+        L = self.L
+        L.ref_plot3d_read.argtypes = [C.c_char_p] + [_dp] * 6
+        cond = np.zeros(4)
+        out = [np.zeros(self.ng) for _ in range(5)]
+        L.ref_plot3d_read(str(path).encode(), p(cond), *[p(a) for a in out])
+        return (tuple(cond), *out)
+
     def setup(self, dt, re, tol=1e-3, with_eta=True):
         self.L.ref_setup(dt, re, tol, int(with_eta))
 

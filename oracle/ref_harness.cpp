@@ -15,6 +15,7 @@
 #include <chrono>
 #include <cstring>
 #include <memory>
+#include <unistd.h>
 
 namespace {
 
@@ -359,6 +360,50 @@ void ref_state(double *u, double *v, double *w, double *p, double *f, double *x)
     get(p, H->t1.p, ng());
     get(f, H->Dfib.f, 3 * nc());
     get(x, H->Mx.X_result, nc());
+}
+
+
+// The reference's Plot3D writers and reader (io/Plot3D/*.hpp).  They write to
+// mx_out/ under the current directory, so the harness changes into `dir`
+// (which must hold an mx_out/ directory) around the call.
+int ref_plot3d_x(const char *dir)
+{
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof(cwd)) || chdir(dir) != 0) return -1;
+    OutputPlot3D_Xfile(H->simu, H->gA);
+    return chdir(cwd);
+}
+
+int ref_plot3d_q(const char *dir, int io, double time, const double *p, const double *u, const double *v,
+                 const double *w, const double *eta)
+{
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof(cwd)) || chdir(dir) != 0) return -1;
+    put(H->t1.p, p, ng());
+    put(H->T3.u, u, ng());
+    put(H->T3.v, v, ng());
+    put(H->T3.w, w, ng());
+    put(H->Dfib.eta, eta, ng());
+    H->simu.currentFile = (size_t)io;
+    H->simu.set_time(time);
+    OutputPLOT3D_Qfile(H->Dfib, H->simu, H->t1, H->T3, H->gA);
+    return chdir(cwd);
+}
+
+// QfileRead: cond = (mach, alpha, Re, time), ghosted p, u, v, w, eta
+void ref_plot3d_read(const char *path, double *cond, double *p, double *u, double *v, double *w, double *eta)
+{
+    auto [nb, mach, alpha, reyn, time, dp, du, dv, dw, deta] = QfileRead(H->gA, std::string(path));
+    (void)nb;
+    cond[0] = mach;
+    cond[1] = alpha;
+    cond[2] = reyn;
+    cond[3] = time;
+    get(p, dp, ng());
+    get(u, du, ng());
+    get(v, dv, ng());
+    get(w, dw, ng());
+    get(eta, deta, ng());
 }
 
 }  // extern "C"
