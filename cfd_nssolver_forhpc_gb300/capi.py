@@ -56,6 +56,11 @@ class CfdStepInfo(C.Structure):
                 ("cl", C.c_double)]
 
 
+class CfdCflInfo(C.Structure):
+    _fields_ = [("cfl", C.c_double), ("cfl_max", C.c_double), ("u_max", C.c_double * 3),
+                ("u_min", C.c_double * 3), ("dt_next", C.c_double)]
+
+
 class CfdAdjStepInfo(C.Structure):
     _fields_ = [("iters", C.c_int * 4), ("relres", C.c_double * 4)]
 
@@ -141,6 +146,8 @@ def lib() -> C.CDLL:
         "cfd_adj_forward": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
         "cfd_adj_reverse": ([vp, C.POINTER(CfdAdjRunResult)], i),
         "cfd_adj_mean_drag": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
+        "cfd_cfl": ([vp, i, C.POINTER(CfdCflInfo)], i),
+        "cfd_steady_max": ([vp, i, i, dp], i),
         "cfd_write_plot3d_x": ([vp, C.c_char_p], i),
         "cfd_write_plot3d_q": ([vp, i, C.c_char_p], i),
         "cfd_plot3d_q_host": ([C.c_char_p, i, i, i, d, d, dp, dp, dp, dp, dp], i),

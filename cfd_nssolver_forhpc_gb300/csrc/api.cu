@@ -4,6 +4,7 @@
 // red-black SOR, mixed-precision defect correction).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -680,6 +681,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     AL(c->sc_in, sizeof(BicgScal));
     AL(c->sc_t, sizeof(BicgScal));
     AL(c->dscal, 8 * sizeof(double));
+    AL(c->mon, 8 * sizeof(double));
     AL(c->dmax, 2 * sizeof(unsigned long long));
     const int red_blocks = blocks_for(n, sms * 8);
     AL(c->lc.partials, (size_t)4 * red_blocks * sizeof(double));
@@ -876,6 +878,11 @@ int cfd_start(cfd_ctx *c)
     CKS(cfd_bc_copy(c, CFD_SLOT_T0, CFD_SLOT_T1));
     c->loop = 1;
     c->time = 0.0;
+    for (int q = 0; q < 3; ++q) {
+        c->run_umax[q] = -1e10;
+        c->run_umin[q] = 1e10;
+    }
+    c->cfl_max = 0.0;
     return CFD_OK;
 }
 
@@ -1134,6 +1141,60 @@ int cfd_div_projected(cfd_ctx *c, int slot, double *div_inf, double *dev_inf)
     CK(cudaStreamSynchronize(c->s));
     if (div_inf) std::memcpy(div_inf, c->h_max, sizeof(double));
     if (dev_inf) std::memcpy(dev_inf, c->h_max + 1, sizeof(double));
+    return CFD_OK;
+}
+
+int cfd_cfl(cfd_ctx *c, int slot, cfd_cfl_info *out)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot));
+    if (!out) return fail(CFD_ERR_ARG, "null output");
+    const int a = slot_index(slot);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_cfl<T>(c->lc, c->g, metrics_of<double>(c), dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), c->mon);
+        return 0;
+    });
+    c->launches += 1;
+    CK(cudaGetLastError());
+    double h[7];
+    CK(cudaMemcpyAsync(h, c->mon, sizeof(h), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    out->cfl = h[0] * c->cfg.dt;
+    c->cfl_max = std::max(c->cfl_max, out->cfl);
+    out->cfl_max = c->cfl_max;
+    for (int q = 0; q < 3; ++q) {
+        c->run_umax[q] = std::max(c->run_umax[q], h[1 + 2 * q]);
+        c->run_umin[q] = std::min(c->run_umin[q], -h[2 + 2 * q]);
+        out->u_max[q] = c->run_umax[q];
+        out->u_min[q] = c->run_umin[q];
+    }
+    // simuClass::timestepper (simuClass.hpp:185-199) with its default factors
+    const double re = c->cfg.re, cfl_factor = 0.05, grid_fo_factor = 0.15, dt_min = 1e-12;
+    double dt = 1e10;
+    for (int q = 0; q < 3; ++q) dt = std::min(dt, cfl_factor / (re * out->u_max[q] * out->u_max[q]));
+    for (int q = 0; q < 3; ++q) dt = std::min(dt, grid_fo_factor * 0.5 * re * out->u_min[q] * out->u_min[q]);
+    out->dt_next = dt < dt_min ? dt_min : dt;
+    return CFD_OK;
+}
+
+int cfd_steady_max(cfd_ctx *c, int slot_new, int slot_old, double *out)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot_new));
+    CKS(check_slot(slot_old));
+    if (!out) return fail(CFD_ERR_ARG, "null output");
+    const int a = slot_index(slot_new), b = slot_index(slot_old);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_steady_max<T>(c->lc, c->g, dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), dv<T>(c, b, 0),
+                             dv<T>(c, b, 1), dv<T>(c, b, 2), c->mon);
+        return 0;
+    });
+    c->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, c->mon, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
     return CFD_OK;
 }
 

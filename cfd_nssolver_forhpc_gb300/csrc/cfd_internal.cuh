@@ -163,6 +163,76 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials,
     return true;
 }
 
+// The same last-block scheme for maxima (order-independent, so any launch
+// shape gives the same result): the last block returns true with tot[].
+template <int NV>
+__device__ __forceinline__ void warp_max(double (&v)[NV])
+{
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v[q] = fmax(v[q], __shfl_down_sync(0xffffffffu, v[q], off));
+}
+
+template <int NV>
+__device__ __forceinline__ bool grid_reduce_max(double (&v)[NV], double *partials, unsigned int *counter,
+                                                double (&tot)[NV])
+{
+    __shared__ double sm[32][NV];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    warp_max<NV>(v);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sm[warp][q] = v[q];
+    __syncthreads();
+    if (warp == 0) {
+        double w[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? sm[lane][q] : -INFINITY;
+        warp_max<NV>(w);
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) partials[q * gridDim.x + blockIdx.x] = w[q];
+            __threadfence();
+            unsigned int t = atomicAdd(counter, 1u);
+            last = (t == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double s[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        s[q] = -INFINITY;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            s[q] = fmax(s[q], __ldcg(partials + q * gridDim.x + b));
+    }
+    warp_max<NV>(s);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sm[warp][q] = s[q];
+    __syncthreads();
+    if (warp == 0) {
+        double w[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? sm[lane][q] : -INFINITY;
+        warp_max<NV>(w);
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) sm[0][q] = w[q];
+            *counter = 0u;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) tot[q] = sm[0][q];
+    return true;
+}
+
 // Block-level max of a non-negative double folded into a global slot with an
 // order-independent atomicMax on the bit pattern (non-negative IEEE doubles
 // order like their unsigned bit patterns).  NaN propagates as the largest.

@@ -124,6 +124,12 @@ struct cfd_ctx {
     // the scalar bc_dir[0][0]); a parameter of the adjoint
     double *inflow = nullptr;
     double *inflow_buf = nullptr;
+
+    // monitors: reduction outputs (8 doubles) and the running extremes of
+    // get_Cfl (the reference's simuClass::U_max / U_min / cfl_max persist
+    // across calls), reset by cfd_start
+    double *mon = nullptr;
+    double run_umax[3] = {-1e10, -1e10, -1e10}, run_umin[3] = {1e10, 1e10, 1e10}, cfl_max = 0.0;
     AdjState *adj = nullptr;  // discrete-adjoint state (cfd_adj_enable)
 };
 

@@ -530,6 +530,71 @@ __global__ void k_convert(long long n, const A *__restrict__ a, B *__restrict__ 
 }
 
 // ---------------------------------------------------------------------------
+// Monitors.  get_Cfl (analyses/cfl.hpp:3-80): per cell the signed sum
+// u/Dxs + v/Dys + w/Dzs over the faces the convection-diffusion writes (the
+// last normal face skipped), true FP64 divisions in the reference's order;
+// out = {max c, max u, -min u, max v, -min v, max w, -min w}.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_cfl(Geo g, Metrics<double> m, const T *__restrict__ u, const T *__restrict__ v, const T *__restrict__ w,
+      double *partials, unsigned int *counter, double *out)
+{
+    double acc[7] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        double c = 0.0;
+        if (i < g.nx - GC - 1) {
+            const double a = (double)u[ic];
+            c += a / m.x(AX_DS, i);
+            acc[1] = fmax(acc[1], a);
+            acc[2] = fmax(acc[2], -a);
+        }
+        if (j < g.ny - GC - 1) {
+            const double a = (double)v[ic];
+            c += a / m.y(AX_DS, j);
+            acc[3] = fmax(acc[3], a);
+            acc[4] = fmax(acc[4], -a);
+        }
+        if (k < g.nz - GC - 1) {
+            const double a = (double)w[ic];
+            c += a / m.z(AX_DS, k);
+            acc[5] = fmax(acc[5], a);
+            acc[6] = fmax(acc[6], -a);
+        }
+        acc[0] = fmax(acc[0], c);
+    }
+    double tot[7];
+    if (grid_reduce_max<7>(acc, partials, counter, tot) && threadIdx.x == 0)
+        for (int q = 0; q < 7; ++q) out[q] = tot[q];
+}
+
+// CheckSteadyStatebyMaxVal_omp (analyses/CheckSteadystate.hpp:166-215):
+// max(0, max over interior cells of (a - b)) per component
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_steady_max(Geo g, const T *__restrict__ ua, const T *__restrict__ va, const T *__restrict__ wa,
+             const T *__restrict__ ub, const T *__restrict__ vb, const T *__restrict__ wb, double *partials,
+             unsigned int *counter, double *out)
+{
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        acc[0] = fmax(acc[0], (double)ua[ic] - (double)ub[ic]);
+        acc[1] = fmax(acc[1], (double)va[ic] - (double)vb[ic]);
+        acc[2] = fmax(acc[2], (double)wa[ic] - (double)wb[ic]);
+    }
+    double tot[3];
+    if (grid_reduce_max<3>(acc, partials, counter, tot) && threadIdx.x == 0)
+        for (int q = 0; q < 3; ++q) out[q] = tot[q];
+}
+
+// ---------------------------------------------------------------------------
 // host launchers
 static inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
@@ -635,6 +700,20 @@ void launch_div_projected(cfd_launch_ctx &c, const Geo &g, const Metrics<double>
 }
 
 template <class T>
+void launch_cfl(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const T *u, const T *v, const T *w,
+                double *out)
+{
+    k_cfl<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, u, v, w, c.partials, c.counter, out);
+}
+
+template <class T>
+void launch_steady_max(cfd_launch_ctx &c, const Geo &g, const T *ua, const T *va, const T *wa, const T *ub,
+                       const T *vb, const T *wb, double *out)
+{
+    k_steady_max<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, ua, va, wa, ub, vb, wb, c.partials, c.counter, out);
+}
+
+template <class T>
 void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val)
 {
     k_fill<T><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, val);
@@ -666,6 +745,10 @@ void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b)
     template void launch_div_inf<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,      \
                                     const T *, const T *, const T *, unsigned long long *);      \
     template void launch_fill<T>(cfd_launch_ctx &, long long, T *, T);                           \
+    template void launch_cfl<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, const T *,   \
+                                const T *, const T *, double *);                                   \
+    template void launch_steady_max<T>(cfd_launch_ctx &, const Geo &, const T *, const T *, const T *, \
+                                       const T *, const T *, const T *, double *);                \
     template void launch_div_projected<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,  \
                                           double, const double *, const T *, const T *, const T *, \
                                           const double *, unsigned long long *);

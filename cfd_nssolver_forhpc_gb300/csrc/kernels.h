@@ -202,6 +202,14 @@ template <class V>
 void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e);
 
 
+// monitors (flow.cu): out[7] = {max c, max u, -min u, max v, -min v, max w, -min w}
+template <class T>
+void launch_cfl(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const T *u, const T *v, const T *w,
+                double *out);
+template <class T>
+void launch_steady_max(cfd_launch_ctx &c, const Geo &g, const T *ua, const T *va, const T *wa, const T *ub,
+                       const T *vb, const T *wb, double *out);
+
 // ---- adjoint.cu (discrete adjoint; adjoint arrays are FP64) ----
 struct UfAdjArgs {
     const double *x;      // pressure at interior cells (compact)

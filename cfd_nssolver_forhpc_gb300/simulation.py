@@ -228,6 +228,21 @@ class Simulation:
     def sync(self):
         check(lib().cfd_sync(self._h))
 
+    # -- monitors -----------------------------------------------------------
+    def get_Cfl(self, slot=T0) -> dict:
+        """analyses/cfl.hpp:3 + simuClass::timestepper: cfl of `slot`, running
+        cfl_max / U_max / U_min since start(), and the next dt."""
+        info = capi.CfdCflInfo()
+        check(lib().cfd_cfl(self._h, slot, C.byref(info)))
+        return {"cfl": info.cfl, "cfl_max": info.cfl_max, "u_max": list(info.u_max), "u_min": list(info.u_min),
+                "dt_next": info.dt_next}
+
+    def CheckSteadyStatebyMaxVal(self, new=T0, old=T3) -> tuple:
+        """analyses/CheckSteadystate.hpp:166: max(0, max(new - old)) per component."""
+        out = np.zeros(3)
+        check(lib().cfd_steady_max(self._h, new, old, dptr(out)))
+        return tuple(out)
+
     # -- files: Plot3D (the reference's format) and the FP64 state ---------
     def OutputPlot3D_Xfile(self, path):
         """Cell-centre grid file (io/Plot3D/xfileWrite.hpp:6)."""

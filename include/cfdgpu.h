@@ -369,6 +369,23 @@ int cfd_adj_reverse(cfd_ctx *ctx, cfd_adj_run_result *out);
 int cfd_adj_mean_drag(cfd_ctx *ctx, const cfd_adj_run_config *cfg, cfd_adj_run_result *out);
 
 
+/* ---- monitors ----------------------------------------------------------------
+   cfd_cfl: get_Cfl (analyses/cfl.hpp:3) of velocity slot `slot`: cfl = dt *
+   max over cells of the signed sum u/Dxs + v/Dys + w/Dzs (last normal face
+   skipped, as the reference does).  u_max/u_min and cfl_max are running
+   values since cfd_start, as the reference's simuClass keeps them; dt_next is
+   simuClass::timestepper (simuClass.hpp:185) with its default factors
+   (cflFactor 0.05, gridFoFactor 0.15, dtMin 1e-12) on those extremes.
+   cfd_steady_max: CheckSteadyStatebyMaxVal_omp (analyses/CheckSteadystate.hpp:
+   166): out[c] = max(0, max over interior cells of (new - old)).           */
+typedef struct {
+    double cfl, cfl_max;
+    double u_max[3], u_min[3];
+    double dt_next;
+} cfd_cfl_info;
+int cfd_cfl(cfd_ctx *ctx, int slot, cfd_cfl_info *out);
+int cfd_steady_max(cfd_ctx *ctx, int slot_new, int slot_old, double *out3);
+
 /* ---- Plot3D files and the FP64 state file ----------------------------------
    Plot3D as the reference writes it: single block, whole grid, native-endian
    int32/float32, no record markers, i fastest.

@@ -953,6 +953,81 @@ double og_div_inf(const og_grid *g, const double *u, const double *v, const doub
     return m;
 }
 
+/* get_Cfl (analyses/cfl.hpp:3-80).  The per-cell sum starts at 0 and takes
+   u/Dxs (i < nx-gC-1), v/Dys (j < ny-gC-1), w/Dzs (k < nz-gC-1) in that order. */
+double og_cfl(const og_grid *g, double dt, const double *u, const double *v, const double *w,
+              double *umax, double *umin, double *cfl_max)
+{
+    const long long n = (long long)g->nxc * g->nyc * g->nzc;
+    double *c = (double *)calloc((size_t)n, sizeof(double));
+    for (int i = GC; i < g->nx - GC - 1; ++i)
+        for (int j = GC; j < g->ny - GC; ++j)
+            for (int k = GC; k < g->nz - GC; ++k) {
+                const long long ic = icel(g, i, j, k);
+                c[icelcal(g, i, j, k)] += u[ic] / g->Dxs[i];
+                if (u[ic] > umax[0]) umax[0] = u[ic];
+                if (u[ic] < umin[0]) umin[0] = u[ic];
+            }
+    for (int i = GC; i < g->nx - GC; ++i)
+        for (int j = GC; j < g->ny - GC - 1; ++j)
+            for (int k = GC; k < g->nz - GC; ++k) {
+                const long long ic = icel(g, i, j, k);
+                c[icelcal(g, i, j, k)] += v[ic] / g->Dys[j];
+                if (v[ic] > umax[1]) umax[1] = v[ic];
+                if (v[ic] < umin[1]) umin[1] = v[ic];
+            }
+    for (int i = GC; i < g->nx - GC; ++i)
+        for (int j = GC; j < g->ny - GC; ++j)
+            for (int k = GC; k < g->nz - GC - 1; ++k) {
+                const long long ic = icel(g, i, j, k);
+                c[icelcal(g, i, j, k)] += w[ic] / g->Dzs[k];
+                if (w[ic] > umax[2]) umax[2] = w[ic];
+                if (w[ic] < umin[2]) umin[2] = w[ic];
+            }
+    double m = c[0];
+    for (long long t = 1; t < n; ++t)
+        if (c[t] > m) m = c[t];
+    free(c);
+    const double cfl = m * dt;
+    if (cfl > *cfl_max) *cfl_max = cfl;
+    return cfl;
+}
+
+/* simuClass::timestepper (simuClass.hpp:185-199) */
+double og_timestepper(double re, const double *umax, const double *umin, double cfl_factor,
+                      double grid_fo_factor, double dt_min)
+{
+    double dt = 1e10;
+    for (int q = 0; q < 3; ++q) {
+        const double a = cfl_factor / (re * umax[q] * umax[q]);
+        if (a < dt) dt = a;
+    }
+    for (int q = 0; q < 3; ++q) {
+        const double b = grid_fo_factor * 0.5 * re * umin[q] * umin[q];
+        if (b < dt) dt = b;
+    }
+    if (dt < dt_min) dt = dt_min;
+    return dt;
+}
+
+/* CheckSteadyStatebyMaxVal_omp (analyses/CheckSteadystate.hpp:166-215) */
+void og_steady_max(const og_grid *g, const double *u0, const double *v0, const double *w0,
+                   const double *u3, const double *v3, const double *w3, double *out3)
+{
+    const double *a[3] = {u0, v0, w0}, *b[3] = {u3, v3, w3};
+    for (int q = 0; q < 3; ++q) {
+        double m = 0.0;
+        for (int i = GC; i < g->nx - GC; ++i)
+            for (int j = GC; j < g->ny - GC; ++j)
+                for (int k = GC; k < g->nz - GC; ++k) {
+                    const long long ic = icel(g, i, j, k);
+                    const double d = a[q][ic] - b[q][ic];
+                    if (d > m) m = d;
+                }
+        out3[q] = m;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Whole time step. */
 struct og_sim {

@@ -106,6 +106,21 @@ void og_eta_cylinder_z(const og_grid *g, double cx, double cy, double radius, in
 
 /* ---- diagnostics ---- */
 double og_div_inf(const og_grid *g, const double *u, const double *v, const double *w);
+
+/* ---- monitors (analyses/cfl.hpp:3-80, simuClass.hpp:185-199,
+        analyses/CheckSteadystate.hpp:166-215) ---- */
+/* cfl = dt * max over cells of (u/Dxs + v/Dys + w/Dzs) (signed, last normal
+   face skipped); umax/umin[3] are updated in place (running extremes, the
+   reference never resets them), *cfl_max likewise. */
+double og_cfl(const og_grid *g, double dt, const double *u, const double *v, const double *w,
+              double *umax, double *umin, double *cfl_max);
+/* timestepper: min(cflFactor/(Re U^2) over umax, gridFoFactor 0.5 Re U^2
+   over umin), at least dt_min */
+double og_timestepper(double re, const double *umax, const double *umin, double cfl_factor,
+                      double grid_fo_factor, double dt_min);
+/* max(0, max over interior of (new - old)) per component */
+void og_steady_max(const og_grid *g, const double *u0, const double *v0, const double *w0,
+                   const double *u3, const double *v3, const double *w3, double *out3);
 double og_dot(const double *a, const double *b, long long n);
 
 /* ---- whole time step (RUN_CPU_PC_METHOD.hpp:287-627, RUN_CPU.hpp:290-462) ---- */

@@ -214,6 +214,30 @@ class Oracle:
     def dot(self, a, b):
         return self.lib.og_dot(p(a), p(b), C.c_longlong(a.size))
 
+    # -- monitors ---------------------------------------------------------
+    def cfl(self, g, dt, u, v, w, umax=None, umin=None, cfl_max=-1e300):
+        """(cfl, umax, umin, cfl_max); umax/umin/cfl_max are running values."""
+        umax = np.full(3, -1e10) if umax is None else np.array(umax, dtype=np.float64)
+        umin = np.full(3, 1e10) if umin is None else np.array(umin, dtype=np.float64)
+        cm = C.c_double(cfl_max)
+        L = self.lib
+        L.og_cfl.restype = C.c_double
+        L.og_cfl.argtypes = [C.c_void_p, C.c_double] + [_dp] * 5 + [_dp]
+        c = L.og_cfl(g.ref(), dt, p(u), p(v), p(w), p(umax), p(umin), C.byref(cm))
+        return c, umax, umin, cm.value
+
+    def timestepper(self, re, umax, umin, cfl_factor=0.05, grid_fo_factor=0.15, dt_min=1e-12):
+        L = self.lib
+        L.og_timestepper.restype = C.c_double
+        L.og_timestepper.argtypes = [C.c_double, _dp, _dp, C.c_double, C.c_double, C.c_double]
+        return L.og_timestepper(re, p(np.asarray(umax, dtype=np.float64)), p(np.asarray(umin, dtype=np.float64)),
+                                cfl_factor, grid_fo_factor, dt_min)
+
+    def steady_max(self, g, u0, v0, w0, u3, v3, w3):
+        out = np.zeros(3)
+        self.lib.og_steady_max(g.ref(), p(u0), p(v0), p(w0), p(u3), p(v3), p(w3), p(out))
+        return out
+
     # -- BiCGSTAB ---------------------------------------------------------
     class Bicg:
         def __init__(self, orc, g, tol, maxit=5000, spe=None, ell=None):
@@ -339,6 +363,28 @@ class RefHarness:
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (pr, u, v, w, eta)]
         assert L.ref_plot3d_q(str(directory).encode(), int(io), float(time), *[p(a) for a in arrs]) == 0
         return Path(directory) / "mx_out" / f"P3D{io:02d}.q"
+
+    def cfl(self, u, v, w):
+        """get_Cfl of one field: (cfl, U_max[3], U_min[3]) of this call."""
+        L = self.L
+        L.ref_cfl.argtypes = [_dp] * 6
+        c = np.zeros(1)
+        umax, umin = np.zeros(3), np.zeros(3)
+        L.ref_cfl(p(u), p(v), p(w), p(c), p(umax), p(umin))
+        return c[0], umax, umin
+
+    def timestepper(self, umax, umin):
+        L = self.L
+        L.ref_timestepper.restype = C.c_double
+        L.ref_timestepper.argtypes = [_dp, _dp]
+        return L.ref_timestepper(p(np.asarray(umax, dtype=np.float64)), p(np.asarray(umin, dtype=np.float64)))
+
+    def steady_max(self, u0, v0, w0, u3, v3, w3):
+        L = self.L
+        L.ref_steady.argtypes = [_dp] * 7
+        out = np.zeros(3)
+        L.ref_steady(p(u0), p(v0), p(w0), p(u3), p(v3), p(w3), p(out))
+        return out
 
     def plot3d_read(self, path):
         """QfileRead: ((mach, alpha, Re, time), p, u, v, w, eta) ghosted."""

@@ -406,4 +406,47 @@ void ref_plot3d_read(const char *path, double *cond, double *p, double *u, doubl
     get(eta, deta, ng());
 }
 
+// get_Cfl (analyses/cfl.hpp:3) for one field: the running extremes are reset
+// first, so the returned cfl, U_max and U_min are this call's
+void ref_cfl(const double *u, const double *v, const double *w, double *cfl, double *umax, double *umin)
+{
+    put(H->T0.u, u, ng());
+    put(H->T0.v, v, ng());
+    put(H->T0.w, w, ng());
+    H->simu.U_max.clear();
+    H->simu.U_min.clear();
+    H->simu.cfl_max = -1e300;
+    get_Cfl(H->T0, H->Lo, H->gA, H->simu);
+    *cfl = H->simu.cfl_max;
+    for (int q = 0; q < 3; ++q) {
+        umax[q] = H->simu.U_max[q];
+        umin[q] = H->simu.U_min[q];
+    }
+}
+
+// simuClass::timestepper (simuClass.hpp:185) with the given extremes
+double ref_timestepper(const double *umax, const double *umin)
+{
+    H->simu.U_max.assign(umax, umax + 3);
+    H->simu.U_min.assign(umin, umin + 3);
+    H->simu.timestepper();
+    return H->simu.dt_next;
+}
+
+// CheckSteadyStatebyMaxVal_omp (analyses/CheckSteadystate.hpp:166)
+void ref_steady(const double *u0, const double *v0, const double *w0, const double *u3, const double *v3,
+                const double *w3, double *out)
+{
+    put(H->T0.u, u0, ng());
+    put(H->T0.v, v0, ng());
+    put(H->T0.w, w0, ng());
+    put(H->T3.u, u3, ng());
+    put(H->T3.v, v3, ng());
+    put(H->T3.w, w3, ng());
+    auto [a, b, c] = CheckSteadyStatebyMaxVal_omp(H->simu, H->ShareM, H->T0, H->T3, H->Lo, H->gA);
+    out[0] = a;
+    out[1] = b;
+    out[2] = c;
+}
+
 }  // extern "C"

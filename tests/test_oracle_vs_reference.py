@@ -104,3 +104,26 @@ def test_pc_run_matches_reference(pair, oracle):
     np.testing.assert_allclose([r[0] for r in res], cd_r, rtol=1e-8)
     st = R.state()
     assert np.max(np.abs(st["u"] - S.field("u0"))) < 1e-9
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_monitors_bitwise(pair, oracle, seed):
+    """get_Cfl, timestepper and CheckSteadyStatebyMaxVal_omp of the oracle
+    equal the reference's on seeded fields (signed velocities, so the
+    signed-sum and signed-difference conventions are exercised)."""
+    w, R, g = pair
+    I = inputs(g, seed)
+    c_r, umax_r, umin_r = R.cfl(I["u0"], I["v0"], I["w0"])
+    c_o, umax_o, umin_o, cm = oracle.cfl(g, R_dt(R, w), I["u0"], I["v0"], I["w0"])
+    assert c_o == c_r and cm == c_r
+    np.testing.assert_array_equal(umax_o, umax_r)
+    np.testing.assert_array_equal(umin_o, umin_r)
+    assert oracle.timestepper(w.re, umax_o, umin_o) == R.timestepper(umax_r, umin_r)
+    u3 = I["u0"] + seeded_field(g.ng, 900 + seed, -0.2, 0.2)
+    np.testing.assert_array_equal(oracle.steady_max(g, I["u0"], I["v0"], I["w0"], u3, I["v0"], I["w0"] * 0.5),
+                                  R.steady_max(I["u0"], I["v0"], I["w0"], u3, I["v0"], I["w0"] * 0.5))
+
+
+def R_dt(R, w):
+    """the dt the harness was set up with (the pair fixture uses w.dt)"""
+    return w.dt
