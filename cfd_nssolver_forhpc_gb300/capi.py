@@ -56,6 +56,10 @@ class CfdStepInfo(C.Structure):
                 ("cl", C.c_double)]
 
 
+class CfdSmlConfig(C.Structure):
+    _fields_ = [("fine_fraction", C.c_double * 3), ("fine_cells", C.c_int * 3), ("offset", C.c_int * 3)]
+
+
 class CfdCflInfo(C.Structure):
     _fields_ = [("cfl", C.c_double), ("cfl_max", C.c_double), ("u_max", C.c_double * 3),
                 ("u_min", C.c_double * 3), ("dt_next", C.c_double)]
@@ -147,6 +151,9 @@ def lib() -> C.CDLL:
         "cfd_adj_reverse": ([vp, C.POINTER(CfdAdjRunResult)], i),
         "cfd_adj_mean_drag": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
         "cfd_cfl": ([vp, i, C.POINTER(CfdCflInfo)], i),
+        "cfd_sml_default": ([C.POINTER(CfdSmlConfig)], i),
+        "cfd_sml_metrics": ([i, i, i, d, d, d, C.POINTER(CfdSmlConfig)] + [dp] * 9, i),
+        "cfd_grid_sml": ([vp, C.POINTER(CfdSmlConfig)], i),
         "cfd_steady_max": ([vp, i, i, dp], i),
         "cfd_write_plot3d_x": ([vp, C.c_char_p], i),
         "cfd_write_plot3d_q": ([vp, i, C.c_char_p], i),

@@ -80,6 +80,9 @@ WORKLOADS = {
     "g0": Workload("g0", 10, 8, 6, 2.5, 2.0, 0.75, re=100.0, dt=2e-3, steps=5, cx=1.0),
     "g1": Workload("g1", 16, 12, 6, 4.0, 3.0, 0.75, re=100.0, dt=2e-3, steps=10, cx=1.5),
     "g2": Workload("g2", 24, 20, 8, 6.0, 5.0, 1.0, re=100.0, dt=2e-3, steps=10, cx=2.0),
+    # stretched-grid case: the reference's SML settings (fine region of 100
+    # cells in x and y, offset -4 in x) need more than 100 interior cells
+    "s1": Workload("s1", 120, 108, 8, 20.0, 10.0, 1.25, re=100.0, dt=1e-3, steps=10, cx=5.0),
     # profiling case: Krylov vectors (65 MB each) and per-kernel traffic above
     # the 129 MB L2, device footprint about 2 GB
     "p1": Workload("p1", 640, 320, 40, 20.0, 10.0, 1.25, re=100.0, dt=5e-4, steps=2, tol=1e-10),

@@ -97,6 +97,12 @@ class Simulation:
     def grid_uniform(self):
         check(lib().cfd_grid_uniform(self._h))
 
+    def grid_sml(self, cfg=None):
+        """The reference's stretched SML grid (structureGrid.hpp:326-405);
+        cfg = capi.CfdSmlConfig or None for the reference's settings."""
+        cfg = sml_default() if cfg is None else cfg
+        check(lib().cfd_grid_sml(self._h, C.byref(cfg)))
+
     def set_metrics(self, m: dict):
         arrs = [np.ascontiguousarray(m[k], dtype=np.float64) for k in
                 ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")]
@@ -372,3 +378,24 @@ def QfileRead(path, w: Workload):
     out = [np.empty(w.n_ghosted) for _ in range(5)]
     check(lib().cfd_read_plot3d_q(str(path).encode(), w.nxc, w.nyc, w.nzc, dptr(cond), *[dptr(a) for a in out]))
     return (tuple(cond), *out)
+
+
+def sml_default() -> capi.CfdSmlConfig:
+    cfg = capi.CfdSmlConfig()
+    check(lib().cfd_sml_default(C.byref(cfg)))
+    return cfg
+
+
+def sml_metrics(w: Workload, cfg=None) -> dict:
+    """Host-side SML metrics of workload w: X, Y, Z (n+1 nodes) and the
+    ghosted widths Dx..Dzs, as cfd_set_metrics takes them."""
+    cfg = sml_default() if cfg is None else cfg
+    n = (w.nxc + 4, w.nyc + 4, w.nzc + 4)
+    out = {k: np.zeros(n[a] + 1) for a, k in enumerate(("X", "Y", "Z"))}
+    for pre in ("D", "Ds"):
+        for a, ax in enumerate("xyz"):
+            out[pre[0] + ax + pre[1:]] = np.zeros(n[a])
+    names = ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")
+    check(lib().cfd_sml_metrics(w.nxc, w.nyc, w.nzc, w.lx, w.ly, w.lz, C.byref(cfg),
+                                *[dptr(out[k]) for k in names]))
+    return out

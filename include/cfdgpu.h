@@ -369,6 +369,26 @@ int cfd_adj_reverse(cfd_ctx *ctx, cfd_adj_run_result *out);
 int cfd_adj_mean_drag(cfd_ctx *ctx, const cfd_adj_run_config *cfg, cfd_adj_run_result *out);
 
 
+/* ---- stretched grid ------------------------------------------------------------
+   The reference's default "non_uniform-SML" grid (grid::unit_SML,
+   grid::init_nonuniform_SML, structureGrid.hpp:326-405; ghosts as
+   init_gC_dx, :506-559): per axis a fine region of fine_cells cells over
+   fine_fraction of the length, centred and shifted by offset cells, coarse
+   cells either side; fine_cells = 0 gives a uniform axis.  cfd_sml_default
+   fills the reference's settings (0.3, 0.3, 0.5; 100, 100, 0; -4, 0, 0).
+   cfd_sml_metrics computes the arrays on the host (X..Z: n+1 nodes, widths:
+   n, ghosted); cfd_grid_sml applies them to a context (cfd_set_metrics).   */
+typedef struct {
+    double fine_fraction[3];
+    int fine_cells[3];
+    int offset[3];
+} cfd_sml_config;
+int cfd_sml_default(cfd_sml_config *cfg);
+int cfd_sml_metrics(int nx_cal, int ny_cal, int nz_cal, double lx, double ly, double lz,
+                    const cfd_sml_config *cfg, double *X, double *Y, double *Z, double *Dx, double *Dy,
+                    double *Dz, double *Dxs, double *Dys, double *Dzs);
+int cfd_grid_sml(cfd_ctx *ctx, const cfd_sml_config *cfg);
+
 /* ---- monitors ----------------------------------------------------------------
    cfd_cfl: get_Cfl (analyses/cfl.hpp:3) of velocity slot `slot`: cfl = dt *
    max over cells of the signed sum u/Dxs + v/Dys + w/Dzs (last normal face

@@ -153,3 +153,34 @@ def test_divergence_of_projected_field():
         div, dev = S.div_projected(S.T1)
     assert abs(div - abs(w.dt * mean)) <= 1e-8 * max(1.0, div)
     assert dev < 1e-8 * max(1.0, div)
+
+
+def test_pc_steps_on_sml_grid_match_oracle(oracle):
+    """The reference's default stretched SML grid (fine cells around the
+    cylinder in x and y): GPU steps against the oracle on the same metrics
+    (the SML generator is pinned bitwise to the reference on the CPU)."""
+    from cfd_nssolver_forhpc_gb300.simulation import sml_metrics
+    w = WORKLOADS["s1"]
+    m = sml_metrics(w)
+    g = Grid(w.nxc, w.nyc, w.nzc, w.lx, w.ly, w.lz, oracle=oracle, metrics=m)
+    eta = oracle.eta_cylinder_z(g, w.cx, w.center_y)
+    O = oracle.sim(g, method=0, solver=0, aligned_src=False, compat=True, dt=w.dt, nu=1.0 / w.re, tol=1e-10,
+                   omega=w.omega, bc_dir=w.bc_dir, bc_num=w.bc_num, eta=eta)
+    O.init()
+    u0, v0, w0 = initial_velocity(w.nxc, w.nyc, w.nzc)
+    for f, a in (("u0", u0), ("v0", v0), ("w0", w0)):
+        O.field(f)[:] = a
+    O.start()
+    ohist = [O.step() for _ in range(3)]
+    with Simulation(w, tol=1e-10) as S:
+        S.grid_sml()
+        S.init_uniform(1.0, 0.0, 0.0)
+        S.DFIB_CylinderZ(w.cx, w.center_y, w.radius, w.nsub)
+        np.testing.assert_array_equal(S.download("ETA"), eta)
+        for nm, a in (("U0", u0), ("V0", v0), ("W0", w0)):
+            S.upload(nm, a)
+        S.start()
+        hist = [S.step() for _ in range(3)]
+        np.testing.assert_allclose([h["cd"] for h in hist], [h[0] for h in ohist], rtol=1e-7)
+        for k, f in (("U0", "u0"), ("V0", "v0"), ("W0", "w0")):
+            assert rel_err(S.download(k), O.field(f)) < 1e-7, k
