@@ -24,7 +24,7 @@ INNER_CG, INNER_BICGSTAB = 0, 1
 T0, T1, T3 = 0, 1, 3
 KERNELS = ["bicg_ap", "bicg_s", "bicg_as", "bicg_xr", "bicg_p", "convdiff", "update_uf", "rhs",
            "sor_sweep", "cg_pq", "cg_upd", "residual64"]
-FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "P", "ETA", "F", "SRC", "X", "B", "JP"]
+FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "P", "ETA", "F", "SRC", "X", "B", "JP", "VIS"]
 FIELD = {name: i for i, name in enumerate(FIELDS)}
 ADJ_FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "CDU", "CDV", "CDW", "X", "B", "F", "SRC",
               "ETA", "INFLOW"]
@@ -47,7 +47,7 @@ class CfdConfig(C.Structure):
                 ("aligned_source", C.c_int), ("compat_rhs", C.c_int),
                 ("bc_dir", (C.c_double * 3) * 6), ("bc_num", (C.c_double * 3) * 6),
                 ("check_every", C.c_int), ("inner_tol", C.c_double), ("max_outer", C.c_int),
-                ("inner_solver", C.c_int)]
+                ("inner_solver", C.c_int), ("les_smagorinsky", C.c_int)]
 
 
 class CfdStepInfo(C.Structure):
@@ -151,6 +151,7 @@ def lib() -> C.CDLL:
         "cfd_adj_reverse": ([vp, C.POINTER(CfdAdjRunResult)], i),
         "cfd_adj_mean_drag": ([vp, C.POINTER(CfdAdjRunConfig), C.POINTER(CfdAdjRunResult)], i),
         "cfd_cfl": ([vp, i, C.POINTER(CfdCflInfo)], i),
+        "cfd_smagorinsky": ([vp, i], i),
         "cfd_sml_default": ([C.POINTER(CfdSmlConfig)], i),
         "cfd_sml_metrics": ([i, i, i, d, d, d, C.POINTER(CfdSmlConfig)] + [dp] * 9, i),
         "cfd_grid_sml": ([vp, C.POINTER(CfdSmlConfig)], i),

@@ -341,6 +341,7 @@ int cfd_adj_enable(cfd_ctx *c, int tape_len)
     CKS(need_metrics(c));
     if (c->cfg.solver == CFD_SOLVER_SOR_RB)
         return fail(CFD_ERR_ARG, "the adjoint needs a Krylov pressure solver (SPE or ELL)");
+    if (c->cfg.les_smagorinsky) return fail(CFD_ERR_ARG, "the adjoint does not cover the Smagorinsky model");
     if (tape_len < 1) return fail(CFD_ERR_ARG, "tape_len must be at least 1");
     if (c->adj) {
         if (tape_len > c->adj->tape_len) CKS(alloc_tape(c, tape_len));

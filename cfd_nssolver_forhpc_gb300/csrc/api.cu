@@ -39,6 +39,7 @@ size_t field_count(const cfd_ctx *c, int field)
     if (field >= CFD_FIELD_U0 && field <= CFD_FIELD_ETA) return (size_t)c->g.ng;
     if (field == CFD_FIELD_F || field == CFD_FIELD_SRC) return (size_t)(3 * c->g.n);
     if (field >= CFD_FIELD_X && field <= CFD_FIELD_JP) return (size_t)c->g.n;
+    if (field == CFD_FIELD_VIS) return c->vis ? (size_t)c->g.n : 0;
     return 0;
 }
 
@@ -58,6 +59,7 @@ void *field_ptr(cfd_ctx *c, int field, bool &is_t)
     case CFD_FIELD_X: return c->x;
     case CFD_FIELD_B: return c->b;
     case CFD_FIELD_JP: return c->jp;
+    case CFD_FIELD_VIS: is_t = true; return c->vis;
     default: return nullptr;
     }
 }
@@ -377,9 +379,14 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
         for (int q = 0; q < 3; ++q)
             CK(cudaMemcpyAsync(rec->T0[q], c->vel[0][q], (size_t)g.ng * sizeof(T), cudaMemcpyDeviceToDevice, c->s));
     if (pc) CK(cudaMemsetAsync(src, 0, (size_t)(3 * g.n) * sizeof(T), c->s));
+    T *vis = static_cast<T *>(c->vis);
+    if (vis) {  // SmagorinskyModel of T0 (the same in every pass of the step)
+        launch_smagorinsky<T>(c->s, g, metrics_of<double>(c), u0, v0, w0, vis);
+        c->launches += 1;
+    }
     for (int pass = 0; pass < npass; ++pass) {
         launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, u1, v1, w1,
-                           (pc && aligned && pass > 0) ? src : nullptr);
+                           (pc && aligned && pass > 0) ? src : nullptr, vis, (T)(1.0 / c->cfg.re));
         if (pc && !aligned) launch_src_add<T>(c->lc, g, 0, u1, v1, w1, src);
         c->launches += (pc && !aligned) ? 2 : 1;
         CK(cudaGetLastError());
@@ -573,6 +580,7 @@ int cfd_config_default(cfd_config *cfg, int nx, int ny, int nz)
     cfg->check_every = 16;
     cfg->inner_tol = 1e-2;
     cfg->max_outer = 30;
+    cfg->les_smagorinsky = 0;
     return CFD_OK;
 }
 
@@ -595,6 +603,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (k.precision != CFD_PREC_FP64 && k.precision != CFD_PREC_MIXED)
         return fail(CFD_ERR_ARG, "unknown precision");
     if (k.check_every < 1 || k.check_every > 4096) return fail(CFD_ERR_ARG, "check_every out of range");
+    if (k.les_smagorinsky != 0 && k.les_smagorinsky != 1) return fail(CFD_ERR_ARG, "les_smagorinsky must be 0 or 1");
     if (k.inner_solver != CFD_INNER_CG && k.inner_solver != CFD_INNER_BICGSTAB)
         return fail(CFD_ERR_ARG, "unknown inner solver");
     if (k.precision == CFD_PREC_MIXED && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
@@ -682,6 +691,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     AL(c->sc_t, sizeof(BicgScal));
     AL(c->dscal, 8 * sizeof(double));
     AL(c->mon, 8 * sizeof(double));
+    if (k.les_smagorinsky) AL(c->vis, (size_t)n * ts);
     AL(c->dmax, 2 * sizeof(unsigned long long));
     const int red_blocks = blocks_for(n, sms * 8);
     AL(c->lc.partials, (size_t)4 * red_blocks * sizeof(double));
@@ -895,9 +905,11 @@ int cfd_convection_diffusion(cfd_ctx *c, int src_slot, int dst_slot)
     const int a = slot_index(src_slot), b = slot_index(dst_slot);
     dispatch(c, [&](auto tag) {
         using T = typename decltype(tag)::type;
+        if (c->vis) launch_smagorinsky<T>(c->s, c->g, metrics_of<double>(c), dv<T>(c, a, 0), dv<T>(c, a, 1),
+                                          dv<T>(c, a, 2), static_cast<T *>(c->vis));
         launch_convdiff<T>(c->s, c->g, metrics_of<T>(c), (T)c->cfg.dt, (T)((1.0 / c->cfg.re) * c->cfg.dt),
                            dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2), dv<T>(c, b, 0), dv<T>(c, b, 1),
-                           dv<T>(c, b, 2), nullptr);
+                           dv<T>(c, b, 2), nullptr, static_cast<T *>(c->vis), (T)(1.0 / c->cfg.re));
         return 0;
     });
     CK(cudaGetLastError());
@@ -1175,6 +1187,23 @@ int cfd_cfl(cfd_ctx *c, int slot, cfd_cfl_info *out)
     for (int q = 0; q < 3; ++q) dt = std::min(dt, cfl_factor / (re * out->u_max[q] * out->u_max[q]));
     for (int q = 0; q < 3; ++q) dt = std::min(dt, grid_fo_factor * 0.5 * re * out->u_min[q] * out->u_min[q]);
     out->dt_next = dt < dt_min ? dt_min : dt;
+    return CFD_OK;
+}
+
+int cfd_smagorinsky(cfd_ctx *c, int slot)
+{
+    CKS(need_metrics(c));
+    CKS(check_slot(slot));
+    if (!c->vis) return fail(CFD_ERR_STATE, "the context was created without les_smagorinsky");
+    const int a = slot_index(slot);
+    dispatch(c, [&](auto tag) {
+        using T = typename decltype(tag)::type;
+        launch_smagorinsky<T>(c->s, c->g, metrics_of<double>(c), dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2),
+                              static_cast<T *>(c->vis));
+        return 0;
+    });
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
     return CFD_OK;
 }
 

@@ -129,6 +129,7 @@ struct cfd_ctx {
     // get_Cfl (the reference's simuClass::U_max / U_min / cfl_max persist
     // across calls), reset by cfd_start
     double *mon = nullptr;
+    void *vis = nullptr;  // Smagorinsky eddy viscosity (compact, T), LES contexts only
     double run_umax[3] = {-1e10, -1e10, -1e10}, run_umin[3] = {1e10, 1e10, 1e10}, cfl_max = 0.0;
     AdjState *adj = nullptr;  // discrete-adjoint state (cfd_adj_enable)
 };

@@ -53,6 +53,40 @@ __device__ __forceinline__ void cell_of(const Geo &g, long long t, int &i, int &
     k = (int)(rem - jj * (unsigned int)g.syc) + GC;
 }
 
+// SmagorinskyModel (source/smagorinskyModel.hpp:31-78) with GradientGauss
+// (:6-27): central differences 0.5/D (phi[-] - phi[+]) with the staggered
+// width along the component's own axis; temp = |2 ux^2 + vy^2 + wz^2 +
+// (uy + vx)^2 + (uz + wx)^2 + (vz + wy)^2| (the factor 2 on the first term
+// only, as the reference writes it); nu_t = (0.18 delta)^2 sqrt(temp) with
+// delta = (Dx Dy Dz)^(1/3).  One cell per thread, FP64.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_smagorinsky(Geo g, Metrics<double> m, const T *__restrict__ u, const T *__restrict__ v, const T *__restrict__ w,
+              T *__restrict__ vis)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.n) return;
+    int i, j, k;
+    cell_of(g, t, i, j, k);
+    const long long ic = icel(g, i, j, k), sx = g.sx, sy = g.sy;
+    auto D = [&](const T *f, long long s) { return (double)f[ic - s] - (double)f[ic + s]; };
+    const double ux = 0.5 / m.x(AX_DS, i) * D(u, sx), uy = 0.5 / m.y(AX_D, j) * D(u, sy);
+    const double uz = 0.5 / m.z(AX_D, k) * D(u, 1);
+    const double vx = 0.5 / m.x(AX_D, i) * D(v, sx), vy = 0.5 / m.y(AX_DS, j) * D(v, sy);
+    const double vz = 0.5 / m.z(AX_D, k) * D(v, 1);
+    const double wx = 0.5 / m.x(AX_D, i) * D(w, sx), wy = 0.5 / m.y(AX_D, j) * D(w, sy);
+    const double wz = 0.5 / m.z(AX_DS, k) * D(w, 1);
+    const double temp = fabs(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(2.0, __dmul_rn(ux, ux)),
+                                                                              __dmul_rn(vy, vy)),
+                                                                    __dmul_rn(wz, wz)),
+                                                          __dmul_rn(uy + vx, uy + vx)),
+                                                __dmul_rn(uz + wx, uz + wx)),
+                                      __dmul_rn(vz + wy, vz + wy)));
+    const double delta = pow(m.x(AX_D, i) * m.y(AX_D, j) * m.z(AX_D, k), 1.0 / 3.0);
+    const double cd = 0.18 * delta;
+    vis[t] = (T)(__dmul_rn(cd, cd) * sqrt(temp));
+}
+
 // ConvectionDifussion (convection_and_difussion.hpp:168-446): explicit Euler
 // u* = u + dt(-div(u u) + nu lap u) for the three staggered components of
 // one cell per thread.  The normal component skips the domain's last face
@@ -62,7 +96,7 @@ template <class T>
 __global__ void __launch_bounds__(kBlock)
 k_convdiff(Geo g, Metrics<T> m, T dt, T nudt, const T *__restrict__ u0, const T *__restrict__ v0,
            const T *__restrict__ w0, T *__restrict__ u1, T *__restrict__ v1, T *__restrict__ w1,
-           const T *__restrict__ src)
+           const T *__restrict__ src, const T *__restrict__ vis, T nu)
 {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= g.n) return;
@@ -72,6 +106,9 @@ k_convdiff(Geo g, Metrics<T> m, T dt, T nudt, const T *__restrict__ u0, const T 
     const long long ic = icel(g, i, j, k);
     const Axis<T> &X = m.x, &Y = m.y, &Z = m.z;
     const T uc = __ldg(u0 + ic), vc = __ldg(v0 + ic), wc = __ldg(w0 + ic);
+    // LES (TERBULENCE_SMAGORINSKY, convection_and_difussion.hpp:246-250):
+    // the diffusion of this cell's faces uses nu + nu_t
+    if (vis) nudt = (nu + vis[t]) * dt;
     const T u_xp = __ldg(u0 + ic + sx), u_xm = __ldg(u0 + ic - sx);
     const T v_yp = __ldg(v0 + ic + sy), v_ym = __ldg(v0 + ic - sy);
     const T w_zp = __ldg(w0 + ic + 1), w_zm = __ldg(w0 + ic - 1);
@@ -600,9 +637,16 @@ static inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 template <class T>
 void launch_convdiff(cudaStream_t s, const Geo &g, const Metrics<T> &m, T dt, T nudt, const T *u0,
-                     const T *v0, const T *w0, T *u1, T *v1, T *w1, const T *src_aligned)
+                     const T *v0, const T *w0, T *u1, T *v1, T *w1, const T *src_aligned, const T *vis, T nu)
 {
-    k_convdiff<T><<<nblk(g.n), kBlock, 0, s>>>(g, m, dt, nudt, u0, v0, w0, u1, v1, w1, src_aligned);
+    k_convdiff<T><<<nblk(g.n), kBlock, 0, s>>>(g, m, dt, nudt, u0, v0, w0, u1, v1, w1, src_aligned, vis, nu);
+}
+
+template <class T>
+void launch_smagorinsky(cudaStream_t s, const Geo &g, const Metrics<double> &m, const T *u, const T *v,
+                        const T *w, T *vis)
+{
+    k_smagorinsky<T><<<nblk(g.n), kBlock, 0, s>>>(g, m, u, v, w, vis);
 }
 
 template <class T>
@@ -727,7 +771,10 @@ void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b)
 
 #define CFD_FLOW_INSTANTIATE(T)                                                                   \
     template void launch_convdiff<T>(cudaStream_t, const Geo &, const Metrics<T> &, T, T,        \
-                                     const T *, const T *, const T *, T *, T *, T *, const T *); \
+                                     const T *, const T *, const T *, T *, T *, T *, const T *,  \
+                                     const T *, T);                                              \
+    template void launch_smagorinsky<T>(cudaStream_t, const Geo &, const Metrics<double> &,      \
+                                        const T *, const T *, const T *, T *); \
     template void launch_src_add<T>(cfd_launch_ctx &, const Geo &, int, T *, T *, T *, const T *); \
     template void launch_src_accumulate<T>(cfd_launch_ctx &, long long, T, T *, const T *);      \
     template void launch_rhs<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double,  \

@@ -31,7 +31,12 @@ struct cfd_launch_ctx {
 // ---- flow.cu ----
 template <class T>
 void launch_convdiff(cudaStream_t s, const Geo &g, const Metrics<T> &m, T dt, T nudt, const T *u0,
-                     const T *v0, const T *w0, T *u1, T *v1, T *w1, const T *src_aligned);
+                     const T *v0, const T *w0, T *u1, T *v1, T *w1, const T *src_aligned,
+                     const T *vis = nullptr, T nu = T(0));
+// Smagorinsky eddy viscosity (compact) of (u, v, w)
+template <class T>
+void launch_smagorinsky(cudaStream_t s, const Geo &g, const Metrics<double> &m, const T *u, const T *v,
+                        const T *w, T *vis);
 template <class T>
 void launch_src_add(cfd_launch_ctx &c, const Geo &g, int aligned, T *u1, T *v1, T *w1, const T *src);
 template <class T>

@@ -37,7 +37,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
                 precision: int = capi.PREC_FP64, tol: float | None = None, maxit: int = 5000,
                 omega: float | None = None, sor_maxit: int = 5000, aligned_source: bool = False,
                 compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-2,
-                max_outer: int = 30, inner_solver: int = capi.INNER_CG) -> capi.CfdConfig:
+                max_outer: int = 30, inner_solver: int = capi.INNER_CG, les: bool = False) -> capi.CfdConfig:
     cfg = capi.CfdConfig()
     check(lib().cfd_config_default(C.byref(cfg), w.nxc, w.nyc, w.nzc))
     cfg.lx, cfg.ly, cfg.lz = w.lx, w.ly, w.lz
@@ -57,6 +57,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
     cfg.inner_tol = inner_tol
     cfg.max_outer = max_outer
     cfg.inner_solver = inner_solver
+    cfg.les_smagorinsky = int(les)
     return cfg
 
 
@@ -242,6 +243,10 @@ class Simulation:
         check(lib().cfd_cfl(self._h, slot, C.byref(info)))
         return {"cfl": info.cfl, "cfl_max": info.cfl_max, "u_max": list(info.u_max), "u_min": list(info.u_min),
                 "dt_next": info.dt_next}
+
+    def SmagorinskyModel(self, slot=T0):
+        """source/smagorinskyModel.hpp:31: eddy viscosity of `slot` into VIS."""
+        check(lib().cfd_smagorinsky(self._h, slot))
 
     def CheckSteadyStatebyMaxVal(self, new=T0, old=T3) -> tuple:
         """analyses/CheckSteadystate.hpp:166: max(0, max(new - old)) per component."""

@@ -88,6 +88,7 @@ typedef enum {
     CFD_FIELD_X,                                  /* MxClass::X_result (compact) */
     CFD_FIELD_B,                                  /* MxClass::matB (compact) */
     CFD_FIELD_JP,                                 /* grid::jp Jacobi scaling (compact) */
+    CFD_FIELD_VIS,                                /* velocity::Viseff eddy viscosity (compact, LES) */
     CFD_FIELD_COUNT
 } cfd_field;
 
@@ -117,6 +118,8 @@ typedef struct {
                                    inner solve inside the FP64 defect correction */
     int max_outer;              /* mixed precision: defect-correction sweeps cap */
     int inner_solver;           /* mixed precision: cfd_inner_solver */
+    int les_smagorinsky;        /* 1: Smagorinsky eddy viscosity added to nu in the diffusion
+                                   (source/smagorinskyModel.hpp:31, TERBULENCE_SMAGORINSKY) */
 } cfd_config;
 
 typedef struct {
@@ -388,6 +391,11 @@ int cfd_sml_metrics(int nx_cal, int ny_cal, int nz_cal, double lx, double ly, do
                     const cfd_sml_config *cfg, double *X, double *Y, double *Z, double *Dx, double *Dy,
                     double *Dz, double *Dxs, double *Dys, double *Dzs);
 int cfd_grid_sml(cfd_ctx *ctx, const cfd_sml_config *cfg);
+
+/* SmagorinskyModel (source/smagorinskyModel.hpp:31): eddy viscosity of
+   velocity slot `slot` into CFD_FIELD_VIS (contexts created with
+   les_smagorinsky = 1; the step and cfd_convection_diffusion call it on T0). */
+int cfd_smagorinsky(cfd_ctx *ctx, int slot);
 
 /* ---- monitors ----------------------------------------------------------------
    cfd_cfl: get_Cfl (analyses/cfl.hpp:3) of velocity slot `slot`: cfl = dt *

@@ -47,8 +47,8 @@ def _bc_table(w: Workload) -> str:
     return "\n".join(lines) + "\n"
 
 
-def patch_tree(w: Workload, gridder: str = "uniform") -> Path:
-    dst = OUT / w.name / "inc"
+def patch_tree(w: Workload, gridder: str = "uniform", out_name: str | None = None) -> Path:
+    dst = OUT / (out_name or w.name) / "inc"
     if dst.exists():
         shutil.rmtree(dst)
     shutil.copytree(REFERENCE / "inc", dst, ignore=shutil.ignore_patterns("amgcl", "yakutat"))
@@ -64,6 +64,10 @@ def patch_tree(w: Workload, gridder: str = "uniform") -> Path:
     bc = dst / "BoundaryCondition" / "Boundary_Condition.hpp"
     _replace_once(bc, '#include "BC_Cavity_A.hpp"', '#include "BC_HARNESS_TABLE.hpp"')
     (dst / "BoundaryCondition" / "BC_HARNESS_TABLE.hpp").write_text(_bc_table(w))
+    # the LES model does not compile as shipped (a misspelt `auto`,
+    # source/smagorinskyModel.hpp:63); fixed here so the TERBULENCE_SMAGORINSKY
+    # build used by the LES parity tests can be made
+    _replace_once(dst / "source" / "smagorinskyModel.hpp", "const auot icelCal", "const auto icelCal")
     eta = dst / "dfib" / "setEta.hpp"
     _replace_once(eta, "double  center_x    = 6.5,", f"double  center_x    = {w.cx!r},")
     if abs(w.center_y - w.ly / 2.0) > 0.0:
@@ -71,12 +75,15 @@ def patch_tree(w: Workload, gridder: str = "uniform") -> Path:
     return dst
 
 
-def build(name: str, gridder: str = "uniform", force: bool = False) -> Path:
+def build(name: str, gridder: str = "uniform", force: bool = False, les: bool = False) -> Path:
+    """les: the reference's Smagorinsky model compiled in
+    (TERBULENCE_SMAGORINSKY), output under oracle/_ref/<name>_les/."""
     w = WORKLOADS[name]
-    lib = OUT / name / "libref.so"
-    inc = OUT / name / "inc"
+    out_name = name + ("_les" if les else "")
+    lib = OUT / out_name / "libref.so"
+    inc = OUT / out_name / "inc"
     if REFERENCE.exists() and (force or not inc.exists()):
-        patch_tree(w, gridder)
+        patch_tree(w, gridder, out_name)
     if not inc.exists():
         raise FileNotFoundError(f"no reference sources for {name}: {REFERENCE} absent")
     src = HERE / "ref_harness.cpp"
@@ -84,6 +91,8 @@ def build(name: str, gridder: str = "uniform", force: bool = False) -> Path:
         return lib
     cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
            "-I", str(inc), str(src), "-o", str(lib)]
+    if les:
+        cmd[1:1] = ["-DTERBULENCE_SMAGORINSKY"]
     subprocess.run(cmd, check=True)
     return lib
 

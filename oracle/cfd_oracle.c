@@ -139,6 +139,16 @@ void og_convdiff(const og_grid *g, double dt, double nu,
                  const double *u0, const double *v0, const double *w0,
                  double *u1, double *v1, double *w1)
 {
+    og_convdiff_les(g, dt, nu, NULL, u0, v0, w0, u1, v1, w1);
+}
+
+/* With vis != NULL the diffusion of every face of cell (i,j,k) uses
+   nu + vis[icelCal(i,j,k)] (the TERBULENCE_SMAGORINSKY branches of
+   convection_and_difussion.hpp:246-250, 330-334, 413-417). */
+void og_convdiff_les(const og_grid *g, double dt, double nu_mol, const double *vis,
+                     const double *u0, const double *v0, const double *w0,
+                     double *u1, double *v1, double *w1)
+{
     const int nx = g->nx, ny = g->ny, nz = g->nz;
     const long long sx = (long long)ny * nz, sy = nz, sz = 1;
     const double *Dx = g->Dx, *Dy = g->Dy, *Dz = g->Dz;
@@ -166,6 +176,7 @@ void og_convdiff(const og_grid *g, double dt, double nu,
                 double convection = -dt * ((uPx * uPx - uNx * uNx) / Dxs[i]
                                            + (uPy * Vp - uNy * Vn) / Dy[j]
                                            + (uPz * Wp - uNz * Wn) / Dz[k]);
+                const double nu = vis ? nu_mol + vis[icelcal(g, i, j, k)] : nu_mol;
                 double difussion = nu * dt
                     * (((u0[xp] - u0[ic]) / Dx[i + 1] - (u0[ic] - u0[xm]) / Dx[i]) / Dxs[i]
                        + ((u0[yp] - u0[ic]) / Dys[j] - (u0[ic] - u0[ym]) / Dys[j - 1]) / Dy[j]
@@ -195,6 +206,7 @@ void og_convdiff(const og_grid *g, double dt, double nu,
                 double convection = -dt * ((Up * vPx - Un * vNx) / Dx[i]
                                            + (vPy * vPy - vNy * vNy) / Dys[j]
                                            + (Wp * vPz - Wn * vNz) / Dz[k]);
+                const double nu = vis ? nu_mol + vis[icelcal(g, i, j, k)] : nu_mol;
                 double difussion = nu * dt
                     * (((v0[xp] - v0[ic]) / Dxs[i] - (v0[ic] - v0[xm]) / Dxs[i - 1]) / Dx[i]
                        + ((v0[yp] - v0[ic]) / Dy[j + 1] - (v0[ic] - v0[ym]) / Dy[j]) / Dys[j]
@@ -224,6 +236,7 @@ void og_convdiff(const og_grid *g, double dt, double nu,
                 double convection = -dt * ((Up * wPx - Un * wNx) / Dx[i]
                                            + (Vp * wPy - Vn * wNy) / Dy[j]
                                            + (wPz * wPz - wNz * wNz) / Dzs[k]);
+                const double nu = vis ? nu_mol + vis[icelcal(g, i, j, k)] : nu_mol;
                 double difussion = nu * dt
                     * (((w0[xp] - w0[ic]) / Dxs[i] - (w0[ic] - w0[xm]) / Dxs[i - 1]) / Dx[i]
                        + ((w0[yp] - w0[ic]) / Dys[j] - (w0[ic] - w0[ym]) / Dys[j - 1]) / Dy[j]
@@ -1026,6 +1039,37 @@ void og_steady_max(const og_grid *g, const double *u0, const double *v0, const d
                 }
         out3[q] = m;
     }
+}
+
+/* SmagorinskyModel (source/smagorinskyModel.hpp:31-78) with GradientGauss
+   (:6-27): central differences 0.5/D (phi[-] - phi[+]) with the staggered
+   width along the component's own axis; temp = |2 ux^2 + vy^2 + wz^2 +
+   (uy + vx)^2 + (uz + wx)^2 + (vz + wy)^2| (the factor 2 on the first term
+   only, as written); vis = (Cs delta)^2 sqrt(temp), delta = (Dx Dy Dz)^(1/3),
+   Cs = 0.18; vis compact (icelCal). */
+void og_smagorinsky(const og_grid *g, const double *u, const double *v, const double *w, double *vis)
+{
+    const long long sx = (long long)g->ny * g->nz, sy = g->nz;
+    const double CS = 0.18;
+    for (int i = GC; i < g->nx - GC; ++i)
+        for (int j = GC; j < g->ny - GC; ++j)
+            for (int k = GC; k < g->nz - GC; ++k) {
+                const long long ic = icel(g, i, j, k);
+                const double ux = 0.5 / g->Dxs[i] * (u[ic - sx] - u[ic + sx]);
+                const double uy = 0.5 / g->Dy[j] * (u[ic - sy] - u[ic + sy]);
+                const double uz = 0.5 / g->Dz[k] * (u[ic - 1] - u[ic + 1]);
+                const double vx = 0.5 / g->Dx[i] * (v[ic - sx] - v[ic + sx]);
+                const double vy = 0.5 / g->Dys[j] * (v[ic - sy] - v[ic + sy]);
+                const double vz = 0.5 / g->Dz[k] * (v[ic - 1] - v[ic + 1]);
+                const double wx = 0.5 / g->Dx[i] * (w[ic - sx] - w[ic + sx]);
+                const double wy = 0.5 / g->Dy[j] * (w[ic - sy] - w[ic + sy]);
+                const double wz = 0.5 / g->Dzs[k] * (w[ic - 1] - w[ic + 1]);
+                const double temp = fabs(2.0 * (ux * ux) + vy * vy + wz * wz + (uy + vx) * (uy + vx)
+                                         + (uz + wx) * (uz + wx) + (vz + wy) * (vz + wy));
+                const double delta = pow(g->Dx[i] * g->Dy[j] * g->Dz[k], 1.0 / 3.0);
+                const double cd = CS * delta;
+                vis[icelcal(g, i, j, k)] = cd * cd * sqrt(temp);
+            }
 }
 
 /* ------------------------------------------------------------------------ */

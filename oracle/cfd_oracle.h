@@ -107,6 +107,13 @@ void og_eta_cylinder_z(const og_grid *g, double cx, double cy, double radius, in
 /* ---- diagnostics ---- */
 double og_div_inf(const og_grid *g, const double *u, const double *v, const double *w);
 
+/* ---- LES (source/smagorinskyModel.hpp:31-78): eddy viscosity per cell,
+   compact; og_convdiff_les uses nu + vis[cell] in the diffusion ---- */
+void og_smagorinsky(const og_grid *g, const double *u, const double *v, const double *w, double *vis);
+void og_convdiff_les(const og_grid *g, double dt, double nu, const double *vis,
+                     const double *u0, const double *v0, const double *w0,
+                     double *u1, double *v1, double *w1);
+
 /* ---- monitors (analyses/cfl.hpp:3-80, simuClass.hpp:185-199,
         analyses/CheckSteadystate.hpp:166-215) ---- */
 /* cfl = dt * max over cells of (u/Dxs + v/Dys + w/Dzs) (signed, last normal

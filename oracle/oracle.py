@@ -134,6 +134,15 @@ class Oracle:
         self.lib.og_convdiff(g.ref(), C.c_double(dt), C.c_double(nu), p(u0), p(v0), p(w0),
                              p(u1), p(v1), p(w1))
 
+    def convdiff_les(self, g, dt, nu, vis, u0, v0, w0, u1, v1, w1):
+        self.lib.og_convdiff_les(g.ref(), C.c_double(dt), C.c_double(nu), p(vis), p(u0), p(v0), p(w0),
+                                 p(u1), p(v1), p(w1))
+
+    def smagorinsky(self, g, u, v, w):
+        vis = np.zeros(g.n)
+        self.lib.og_smagorinsky(g.ref(), p(u), p(v), p(w), p(vis))
+        return vis
+
     def src_add(self, g, aligned, u1, v1, w1, src):
         self.lib.og_src_add(g.ref(), int(aligned), p(u1), p(v1), p(w1), p(src))
 
@@ -421,6 +430,14 @@ class RefHarness:
 
     def convdiff(self, u0, v0, w0, u1, v1, w1):
         self.L.ref_convdiff(p(u0), p(v0), p(w0), p(u1), p(v1), p(w1))
+
+    def smagorinsky(self, u, v, w):
+        """SmagorinskyModel of (u, v, w) (LES builds only); afterwards
+        convdiff of the same T0 uses this eddy viscosity."""
+        vis = np.zeros(self.n)
+        self.L.ref_smagorinsky.argtypes = [_dp] * 4
+        self.L.ref_smagorinsky(p(u), p(v), p(w), p(vis))
+        return vis
 
     def rhs(self, kind, u1, v1, w1):
         b = np.zeros(self.n)

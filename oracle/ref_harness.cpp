@@ -449,4 +449,17 @@ void ref_steady(const double *u0, const double *v0, const double *w0, const doub
     out[2] = c;
 }
 
+#ifdef TERBULENCE_SMAGORINSKY
+// SmagorinskyModel (source/smagorinskyModel.hpp:31) of (u, v, w): the eddy
+// viscosity per cell (compact); ref_convdiff then uses it for T0
+void ref_smagorinsky(const double *u, const double *v, const double *w, double *vis)
+{
+    put(H->T0.u, u, ng());
+    put(H->T0.v, v, ng());
+    put(H->T0.w, w, ng());
+    SmagorinskyModel(H->ShareM, H->simu, H->T0, H->t1, H->Lo, H->gA);
+    get(vis, H->T0.Viseff, nc());
+}
+#endif
+
 }  // extern "C"

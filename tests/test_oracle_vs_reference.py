@@ -127,3 +127,32 @@ def test_monitors_bitwise(pair, oracle, seed):
 def R_dt(R, w):
     """the dt the harness was set up with (the pair fixture uses w.dt)"""
     return w.dt
+
+
+def test_smagorinsky_les_bitwise(oracle):
+    """The LES option: the reference compiled with TERBULENCE_SMAGORINSKY (its
+    one misspelt `auto` corrected in the scratch copy).  The oracle's eddy
+    viscosity and its convection-diffusion with nu + nu_t equal the
+    reference's bitwise."""
+    from oracle import build_ref
+    from oracle.oracle import RefHarness
+    w = WORKLOADS["g1"]
+    try:
+        build_ref.build(w.name, les=True)
+    except (FileNotFoundError, OSError) as e:
+        pytest.skip(f"reference sources unavailable: {e}")
+    R = RefHarness(w.name + "_les", build=False)
+    R.set_threads(1)
+    R.setup(w.dt, w.re, 1e-8, True)
+    g = Grid.of(w, oracle)
+    I = inputs(g, 7)
+    vis_r = R.smagorinsky(I["u0"], I["v0"], I["w0"])
+    vis_o = oracle.smagorinsky(g, I["u0"], I["v0"], I["w0"])
+    assert vis_o.max() > 0
+    np.testing.assert_array_equal(vis_o, vis_r)
+    out_r = [g.zeros() for _ in range(3)]
+    out_o = [g.zeros() for _ in range(3)]
+    R.convdiff(I["u0"], I["v0"], I["w0"], *out_r)
+    oracle.convdiff_les(g, w.dt, 1.0 / w.re, vis_o, I["u0"], I["v0"], I["w0"], *out_o)
+    for a, b in zip(out_o, out_r):
+        np.testing.assert_array_equal(a, b)
