@@ -694,7 +694,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (k.les_smagorinsky) AL(c->vis, (size_t)n * ts);
     AL(c->dmax, 2 * sizeof(unsigned long long));
     const int red_blocks = blocks_for(n, sms * 8);
-    AL(c->lc.partials, (size_t)4 * red_blocks * sizeof(double));
+    AL(c->lc.partials, (size_t)kMaxReduce * red_blocks * sizeof(double));
     AL(c->lc.counter, sizeof(unsigned int));
     if (c->fp32) AL(c->staging, (size_t)g.ng * sizeof(double));
 #undef AL

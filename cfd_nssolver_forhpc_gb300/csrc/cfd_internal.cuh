@@ -19,6 +19,9 @@ namespace cfd {
 
 constexpr int GC = 2;
 constexpr int kBlock = 256;
+// values per block of the widest grid reduction; the partials buffer of a
+// context holds kMaxReduce * red_blocks doubles
+constexpr int kMaxReduce = 8;
 
 // Division by a loop-invariant divisor d for dividends below 2^31:
 // q = (umulhi(n, m) + n) >> s with s = ceil(log2 d) and
@@ -108,6 +111,7 @@ template <int NV>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials,
                                             unsigned int *counter, double (&tot)[NV])
 {
+    static_assert(NV <= kMaxReduce, "wider than the partials buffer");
     __shared__ double sm[32][NV];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -178,6 +182,7 @@ template <int NV>
 __device__ __forceinline__ bool grid_reduce_max(double (&v)[NV], double *partials, unsigned int *counter,
                                                 double (&tot)[NV])
 {
+    static_assert(NV <= kMaxReduce, "wider than the partials buffer");
     __shared__ double sm[32][NV];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

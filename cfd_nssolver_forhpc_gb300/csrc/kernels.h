@@ -24,7 +24,7 @@ struct cfd_launch_ctx {
     int red_blocks;         // grid size of every reducing launch
     int grid_cap;           // cap for grid-stride elementwise launches
     int cg_grid;            // resident-block grid of the CG inner kernels (<= red_blocks)
-    double *partials;       // >= 4 * red_blocks doubles
+    double *partials;       // kMaxReduce * red_blocks doubles
     unsigned int *counter;  // last-block ticket, zero between launches
 };
 

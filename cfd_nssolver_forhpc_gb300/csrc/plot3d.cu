@@ -79,7 +79,7 @@ int write_q(const char *path, int nx, int ny, int nz, double re, double time, co
 }
 
 // state file: magic, version, dims, precision, loop, time, then the arrays
-constexpr char kStateMagic[8] = {'C', 'F', 'D', 'G', 'P', 'U', 'S', '1'};
+constexpr char kStateMagic[8] = {'C', 'F', 'D', 'G', 'P', 'U', 'S', '2'};
 
 struct StateHeader {
     char magic[8];
@@ -222,7 +222,8 @@ int cfd_save_state(cfd_ctx *c, const char *path)
     std::memcpy(h.magic, kStateMagic, 8);
     h.nxc = g.nxc; h.nyc = g.nyc; h.nzc = g.nzc; h.fp32 = c->fp32 ? 1 : 0;
     h.loop = c->loop; h.time = c->time; h.has_inflow = c->inflow ? 1 : 0;
-    // device arrays in file order: T0, T1 (3 each), eta, p, x, solver scalars, inflow
+    // device arrays in file order: T0, T1, T3 (3 each), eta, p, x, solver
+    // scalars, inflow (T3's ghost corners reach T0 through the T0 = T3 copy)
     std::vector<unsigned char> buf;
     auto add = [&](const void *dptr, size_t bytes) -> int {
         const size_t off = buf.size();
@@ -231,7 +232,7 @@ int cfd_save_state(cfd_ctx *c, const char *path)
         return CFD_OK;
     };
     CK(cudaStreamSynchronize(c->s));
-    for (int sl = 0; sl < 2; ++sl)
+    for (int sl = 0; sl < 3; ++sl)
         for (int q = 0; q < 3; ++q) CKS(add(c->vel[sl][q], (size_t)g.ng * ts));
     CKS(add(c->eta, (size_t)g.ng * ts));
     CKS(add(c->p, (size_t)g.ng * sizeof(double)));
@@ -259,7 +260,7 @@ int cfd_load_state(cfd_ctx *c, const char *path)
     if (std::memcmp(h.magic, kStateMagic, 8) != 0) return fail(CFD_ERR_ARG, std::string("not a state file: ") + path);
     if (h.nxc != g.nxc || h.nyc != g.nyc || h.nzc != g.nzc || h.fp32 != (c->fp32 ? 1 : 0))
         return fail(CFD_ERR_ARG, "state file grid or precision does not match the context");
-    size_t bytes = (size_t)7 * g.ng * ts + (size_t)g.ng * sizeof(double) + (size_t)g.n * sizeof(double) +
+    size_t bytes = (size_t)10 * g.ng * ts + (size_t)g.ng * sizeof(double) + (size_t)g.n * sizeof(double) +
                    2 * sizeof(BicgScal) + (h.has_inflow ? (size_t)g.nyc * sizeof(double) : 0);
     std::vector<unsigned char> buf(bytes);
     CKS(read_all(F.f, buf.data(), bytes, path));
@@ -273,7 +274,7 @@ int cfd_load_state(cfd_ctx *c, const char *path)
         off += n;
         return CFD_OK;
     };
-    for (int sl = 0; sl < 2; ++sl)
+    for (int sl = 0; sl < 3; ++sl)
         for (int q = 0; q < 3; ++q) CKS(take(c->vel[sl][q], (size_t)g.ng * ts));
     CKS(take(c->eta, (size_t)g.ng * ts));
     CKS(take(c->p, (size_t)g.ng * sizeof(double)));

@@ -430,7 +430,7 @@ int cfd_steady_max(cfd_ctx *ctx, int slot_new, int slot_old, double *out3);
                          adjacent centres (the last face of a line takes the
                          last centre), ghosts zero.
    cfd_save_state / cfd_load_state: no counterpart in the reference; a bitwise
-   restart file of T0, T1, eta, p, x, the solver scalars, the step counter,
+   restart file of T0, T1, T3, eta, p, x, the solver scalars, the step counter,
    the time and the inflow profile.                                          */
 int cfd_write_plot3d_x(cfd_ctx *ctx, const char *path);
 int cfd_write_plot3d_q(cfd_ctx *ctx, int slot, const char *path);
