@@ -18,7 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_lib"
 LIB = OUT / "libcfdgpu.so"
-SOURCES = ["flow.cu", "poisson.cu", "adjoint.cu", "api.cu", "adjoint_api.cu", "plot3d.cu", "grid.cu", "noalloc.cu"]
+SOURCES = ["flow.cu", "poisson.cu", "adjoint.cu", "api.cu", "adjoint_api.cu", "plot3d.cu", "grid.cu", "multigrid.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

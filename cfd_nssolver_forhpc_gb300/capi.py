@@ -20,7 +20,7 @@ STATUS = {0: "CFD_OK", -1: "CFD_ERR_ARG", -2: "CFD_ERR_CUDA", -3: "CFD_ERR_NOMEM
 SOLVER_BICG_SPE, SOLVER_BICG_ELL, SOLVER_SOR_RB = 0, 1, 3
 METHOD_PC, METHOD_PLAIN = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
-INNER_CG, INNER_BICGSTAB = 0, 1
+INNER_CG, INNER_BICGSTAB, INNER_MG = 0, 1, 2
 T0, T1, T3 = 0, 1, 3
 KERNELS = ["bicg_ap", "bicg_s", "bicg_as", "bicg_xr", "bicg_p", "convdiff", "update_uf", "rhs",
            "sor_sweep", "cg_pq", "cg_upd", "residual64"]

@@ -115,12 +115,12 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
 // polling the scalars once per replay.
 template <class Pro, class Pair>
 int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int launches_prologue,
-              int launches_pair)
+              int launches_pair, int pairs_req = 0)
 {
     prologue();
     c->launches += launches_prologue;
     CK(cudaGetLastError());
-    const int pairs = (c->cfg.check_every + 1) / 2;
+    const int pairs = pairs_req > 0 ? pairs_req : (c->cfg.check_every + 1) / 2;
     cudaGraphExec_t &ge = c->graph[gi];
     auto body = [&] {
         for (int q = 0; q < pairs; ++q) {
@@ -192,6 +192,35 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
         3, 2);
 }
 
+// FP32 CG on M e = P r preconditioned by one multigrid V-cycle per iteration
+// (multigrid.cu): z = V(h), rho = h.z, p0 = z, then per iteration the
+// stencil launch (pn, q, alpha), the update (e, h), a V-cycle and rho'.  Few
+// iterations per solve, so a graph replay holds two pairs.
+int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
+{
+    const int v = 10 * c->mg.first_small + 1;
+    float *z = c->w32.r0, *q = c->w32.ap;
+    return run_pairs(
+        c, 4, sc,
+        [&] {
+            mg_h(c, h);
+            mg_vcycle(c, c->mg.never);
+            mg_rho(c, h, z, c->w32.p1, sc);
+            launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
+            mg_upd(c, e, c->w32.p1, h, q, sc);
+            mg_vcycle(c, &sc->done);
+            mg_rho(c, h, z, nullptr, sc);
+        },
+        [&](int from) {
+            float *P[2] = {c->w32.p1, c->p_alt};
+            launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, from, false);
+            mg_upd(c, e, P[1 - from], h, q, sc);
+            mg_vcycle(c, &sc->done);
+            mg_rho(c, h, z, nullptr, sc);
+        },
+        2 * v + 5, v + 3, 2);
+}
+
 // The graphs bake in the buffers and operator of the context; they are
 // captured for the configured operator only.
 template <class Op>
@@ -226,7 +255,7 @@ void residual64(cfd_ctx *c, const EllOp<double> &A, const double *b, const doubl
 //   solve A e = r in FP32 to inner_tol (e from 0);  x += e (FP64)
 template <class Op64, class Op32>
 int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, double *x, const double *zero,
-                bool cg, int *iters, double *relres, int *outer, bool zero_x_if_zero_rhs = false)
+                int inner, int *iters, double *relres, int *outer, bool zero_x_if_zero_rhs = false)
 {
     const long long n = c->g.n;
     // |b|^2 via the residual kernel with x = 0 would need a zero vector; the
@@ -263,7 +292,8 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
         if constexpr (std::is_same<Op32, SpeOp<float>>::value) {
             SpeOp<float> Afly = A32;
             Afly.jp = nullptr;
-            if (cg) CKS(cg_run(c, fv32(c), c->r32, c->e32, c->sc_in));
+            if (inner == CFD_INNER_MG && c->mg.usable) CKS(cg_run_mg(c, fv32(c), c->r32, c->e32, c->sc_in));
+            else if (inner == CFD_INNER_CG || inner == CFD_INNER_MG) CKS(cg_run(c, fv32(c), c->r32, c->e32, c->sc_in));
             else if (c->fused) CKS(bicg_run_fused(c, A32, Afly, c->r32, c->e32, c->sc_in));
             else CKS((bicg_run<Op32, float>(c, A32, c->r32, c->e32, c->w32, nullptr, nullptr, c->sc_in, 1)));
         } else {
@@ -297,9 +327,10 @@ int poisson_solve(cfd_ctx *c, int *iters, double *relres, int *outer)
     if (outer) *outer = 0;
     const bool ell = c->cfg.solver == CFD_SOLVER_BICG_ELL;
     if (c->cfg.precision == CFD_PREC_MIXED) {
-        const bool cg = c->cfg.inner_solver == CFD_INNER_CG;
-        if (ell) return solve_mixed(c, ell64(c), ell32(c), c->b, c->x, c->w64.r0, cg, iters, relres, outer);
-        return solve_mixed(c, spe64(c), spe32(c), c->b, c->x, c->w64.r0, cg, iters, relres, outer);
+        const int inner = c->cfg.inner_solver;
+        if (inner == CFD_INNER_MG) CKS(mg_setup(c));
+        if (ell) return solve_mixed(c, ell64(c), ell32(c), c->b, c->x, c->w64.r0, inner, iters, relres, outer);
+        return solve_mixed(c, spe64(c), spe32(c), c->b, c->x, c->w64.r0, inner, iters, relres, outer);
     }
     if (ell) return solve64(c, ell64(c), iters, relres);
     return solve64(c, spe64(c), iters, relres);
@@ -445,7 +476,12 @@ int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
 int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
                     int *outer)
 {
-    return solve_mixed(c, spe64(c), spe32(c), b, x, zero, true, iters, relres, outer, true);
+    int inner = CFD_INNER_CG;
+    if (c->cfg.inner_solver == CFD_INNER_MG) {
+        CKS(mg_setup(c));
+        inner = CFD_INNER_MG;
+    }
+    return solve_mixed(c, spe64(c), spe32(c), b, x, zero, inner, iters, relres, outer, true);
 }
 
 // FP32 operator tables and CG buffers in an FP64 context (for the adjoint
@@ -492,6 +528,13 @@ namespace {
 
 int build_tables(cfd_ctx *c)
 {
+    // new metrics: the multigrid levels and their graph are rebuilt on demand
+    if (c->graph[4]) {
+        cudaGraphExecDestroy(c->graph[4]);
+        c->graph[4] = nullptr;
+    }
+    c->mg.nlev = 0;
+    c->mg.usable = false;
     const Geo &g = c->g;
     const int n[3] = {g.nx, g.ny, g.nz};
     for (int a = 0; a < 3; ++a) {
@@ -578,7 +621,8 @@ int cfd_config_default(cfd_config *cfg, int nx, int ny, int nz)
     cfg->aligned_source = 0;
     cfg->compat_rhs = 0;
     cfg->check_every = 16;
-    cfg->inner_tol = 1e-2;
+    cfg->inner_tol = 1e-3;
+    cfg->inner_solver = CFD_INNER_MG;
     cfg->max_outer = 30;
     cfg->les_smagorinsky = 0;
     return CFD_OK;
@@ -604,7 +648,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         return fail(CFD_ERR_ARG, "unknown precision");
     if (k.check_every < 1 || k.check_every > 4096) return fail(CFD_ERR_ARG, "check_every out of range");
     if (k.les_smagorinsky != 0 && k.les_smagorinsky != 1) return fail(CFD_ERR_ARG, "les_smagorinsky must be 0 or 1");
-    if (k.inner_solver != CFD_INNER_CG && k.inner_solver != CFD_INNER_BICGSTAB)
+    if (k.inner_solver != CFD_INNER_CG && k.inner_solver != CFD_INNER_BICGSTAB && k.inner_solver != CFD_INNER_MG)
         return fail(CFD_ERR_ARG, "unknown inner solver");
     if (k.precision == CFD_PREC_MIXED && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
         return fail(CFD_ERR_ARG, "mixed precision needs 0 < inner_tol < 1 and max_outer >= 1");

@@ -54,6 +54,12 @@ int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec);
 int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
                     int *outer);
 int ensure_fp32_solver(cfd_ctx *c);
+// multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
+int mg_setup(cfd_ctx *c);
+void mg_vcycle(cfd_ctx *c, const int *done);
+void mg_h(cfd_ctx *c, float *h);
+void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state
 void adj_free(AdjState *a);
 
@@ -98,11 +104,13 @@ struct cfd_ctx {
     float *fv_sum[3] = {};                      // per-axis [cm + cp | interior width] (FP32), CG inner solve
     float *cg_ip = nullptr;                     // 1 / diag(M) (FP32) of the CG inner solve
     cfd::CgTma cgtma{};                         // tensor maps of the TMA-fed CG stencil
+    cfd::Mg mg{};                               // multigrid levels of the MG-preconditioned CG
     cfd::BicgScal sc_init{}, sc_in_init{};  // scalars of a fresh solver (cfd_start restores them)
     cfd::BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
     // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
-    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
-    int graph_batch[4] = {0, 0, 0, 0};
+    // [4] multigrid-preconditioned CG
+    cudaGraphExec_t graph[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int graph_batch[5] = {0, 0, 0, 0, 0};
 
     // SOR
     double *cf6 = nullptr, *cf7 = nullptr;
@@ -291,6 +299,12 @@ int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec);
 int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
                     int *outer);
 int ensure_fp32_solver(cfd_ctx *c);
+// multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
+int mg_setup(cfd_ctx *c);
+void mg_vcycle(cfd_ctx *c, const int *done);
+void mg_h(cfd_ctx *c, float *h);
+void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state
 void adj_free(AdjState *a);
 
@@ -300,6 +314,12 @@ int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec);
 int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
                     int *outer);
 int ensure_fp32_solver(cfd_ctx *c);
+// multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
+int mg_setup(cfd_ctx *c);
+void mg_vcycle(cfd_ctx *c, const int *done);
+void mg_h(cfd_ctx *c, float *h);
+void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state
 void adj_free(AdjState *a);
 

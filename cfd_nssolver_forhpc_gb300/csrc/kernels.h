@@ -162,6 +162,7 @@ struct CgTma {
     size_t smem = 0;
     bool form_z = false;     // z = h / P formed in the stencil kernel (no z vector)
     CUtensorMap zh, p, palt;  // z (or the residual h when form_z), p, p_alt
+    CUtensorMap zv;           // the z vector (read by the multigrid-preconditioned CG)
 };
 // builds the maps for the given buffers; false when TMA cannot be used
 bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *h, const float *p,
@@ -171,6 +172,10 @@ void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *i
                          const CgTma *tma = nullptr);
 // one full wave of the CG inner kernels on this device, capped at red_blocks
 int cg_resident_grid(int sms, int red_blocks);
+// one stencil launch of the multigrid-preconditioned CG: pn = z + beta p
+// (first: pn = p0), q = M pn, alpha; z is a vector (the V-cycle's output)
+void launch_cg_pq_mg(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma *tma, float *z, float *p, float *p_alt,
+                     float *q, BicgScal *sc, int from, bool first);
 // iP = 1 / diag(M), once per context
 void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP);
 void launch_fv_axes(cudaStream_t s, int n, const float *c, const float *width, float *out);
@@ -252,5 +257,28 @@ void launch_adj_cd_gather(cudaStream_t s, const Geo &g, double *a1u, double *a1v
                           double *cv, double *cw, double *asrc);
 void launch_gather_interior(cudaStream_t s, const Geo &g, const double *p, double *x);
 void launch_adj_add(cfd_launch_ctx &c, long long n, double *a, const double *b);
+
+
+// ---- multigrid.cu: V-cycle preconditioner of the FP32 inner CG ----
+constexpr int kMgMaxLevels = 10;
+constexpr long long kMgSmall = 16384;  // levels at or below this size run in one block
+struct MgLevel {
+    int nx, ny, nz;
+    long long n;
+    FastDiv fyz, fz;  // division by ny*nz and nz
+    const float *cm[3], *cp[3], *sum[3], *w[3];  // per axis: -face, +face, cm + cp, width
+    float *x, *b;
+};
+struct MgSmall {
+    int first, nlev, pre, post, coarse;
+    const int *done;
+    MgLevel lev[kMgMaxLevels];
+};
+struct Mg {
+    int nlev = 0, first_small = 0;
+    bool usable = false;
+    int *never = nullptr;  // a device flag that stays 0 (the ungated V-cycle)
+    MgLevel lev[kMgMaxLevels];
+};
 
 }  // namespace cfd

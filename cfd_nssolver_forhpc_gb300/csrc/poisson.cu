@@ -1083,12 +1083,12 @@ static void cg_tma_launch_shape(const CgTma &t, const FvOp<float> &F, int &ichun
 
 template <bool first, int TK>
 static void launch_tma_t(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t, const CUtensorMap *mz,
-                         const CUtensorMap *mp, float *pn, float *q, BicgScal *sc)
+                         const CUtensorMap *mp, float *pn, float *q, BicgScal *sc, bool form_z)
 {
     int ichunk, grid;
     cg_tma_launch_shape(t, F, ichunk, grid);
     const size_t sm = CgTile<TK>::smem(first ? 1 : 2);
-    if (t.form_z)
+    if (form_z)
         k_cg_pq_tma<first, TK, true><<<grid, kBlock, sm, c.s>>>(F, *mz, *mp, pn, q, sc, c.partials, c.counter, ichunk);
     else
         k_cg_pq_tma<first, TK, false><<<grid, kBlock, sm, c.s>>>(F, *mz, *mp, pn, q, sc, c.partials, c.counter,
@@ -1097,18 +1097,38 @@ static void launch_tma_t(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t
 
 // z_map: the z vector (or p itself on the first iteration), p_map: p
 static void launch_cg_pq_tma(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t, bool first,
-                             const CUtensorMap *z_map, const CUtensorMap *p_map, float *pn, float *q, BicgScal *sc)
+                             const CUtensorMap *z_map, const CUtensorMap *p_map, float *pn, float *q, BicgScal *sc,
+                             bool form_z)
 {
     if (t.TK == 32) {
-        if (first) launch_tma_t<true, 32>(c, F, t, z_map, p_map, pn, q, sc);
-        else launch_tma_t<false, 32>(c, F, t, z_map, p_map, pn, q, sc);
+        if (first) launch_tma_t<true, 32>(c, F, t, z_map, p_map, pn, q, sc, form_z);
+        else launch_tma_t<false, 32>(c, F, t, z_map, p_map, pn, q, sc, form_z);
     } else if (t.TK == 16) {
-        if (first) launch_tma_t<true, 16>(c, F, t, z_map, p_map, pn, q, sc);
-        else launch_tma_t<false, 16>(c, F, t, z_map, p_map, pn, q, sc);
+        if (first) launch_tma_t<true, 16>(c, F, t, z_map, p_map, pn, q, sc, form_z);
+        else launch_tma_t<false, 16>(c, F, t, z_map, p_map, pn, q, sc, form_z);
     } else {
-        if (first) launch_tma_t<true, 8>(c, F, t, z_map, p_map, pn, q, sc);
-        else launch_tma_t<false, 8>(c, F, t, z_map, p_map, pn, q, sc);
+        if (first) launch_tma_t<true, 8>(c, F, t, z_map, p_map, pn, q, sc, form_z);
+        else launch_tma_t<false, 8>(c, F, t, z_map, p_map, pn, q, sc, form_z);
     }
+}
+
+void launch_cg_pq_mg(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma *tma, float *z, float *p, float *p_alt,
+                     float *q, BicgScal *sc, int from, bool first)
+{
+    float *P[2] = {p, p_alt};
+    const int to = first ? from : 1 - from;
+    if (tma && tma->ok) {
+        const CUtensorMap *pmap = from == 0 ? &tma->p : &tma->palt;
+        launch_cg_pq_tma(c, F, *tma, first, first ? pmap : &tma->zv, pmap, P[to], q, sc, false);
+        return;
+    }
+    const CgShape cs = cg_shape(c, F);
+    if (first)
+        k_cg_pq<true><<<cs.grid, kBlock, 0, c.s>>>(F, P[from], P[from], P[from], q, sc, c.partials, c.counter, cs.TK,
+                                                   cs.ichunk);
+    else
+        k_cg_pq<false><<<cs.grid, kBlock, 0, c.s>>>(F, z, P[from], P[to], q, sc, c.partials, c.counter, cs.TK,
+                                                    cs.ichunk);
 }
 
 void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
@@ -1119,7 +1139,7 @@ void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *i
     if (tma && tma->ok) {
         const CUtensorMap *pmap = from == 0 ? &tma->p : &tma->palt;
         // first iteration: pn = p0, which k_cg_init wrote into P[from]
-        launch_cg_pq_tma(c, F, *tma, first, first ? pmap : &tma->zh, pmap, P[to], q, sc);
+        launch_cg_pq_tma(c, F, *tma, first, first ? pmap : &tma->zh, pmap, P[to], q, sc, tma->form_z);
         if (tma->form_z)
             k_cg_upd_fv<<<c.cg_grid, kBlock, 0, c.s>>>(F, e, P[to], h, q, sc, c.partials, c.counter);
         else
@@ -1218,7 +1238,8 @@ bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *h
     // 12% (33.5 M cells) faster per step than reading a z vector
     t.form_z = true;
     if (const char *e = std::getenv("CFDGPU_CG_FORM_Z")) t.form_z = e[0] != '0';
-    if (!make_map(t.zh, t.form_z ? h : z, A, t.TK, t.TJ) || !make_map(t.p, p, A, t.TK, t.TJ) ||
+    if (!make_map(t.zh, t.form_z ? h : z, A, t.TK, t.TJ) || !make_map(t.zv, z, A, t.TK, t.TJ) ||
+        !make_map(t.p, p, A, t.TK, t.TJ) ||
         !make_map(t.palt, p_alt, A, t.TK, t.TJ))
         return false;
     t.ok = true;
@@ -1249,7 +1270,7 @@ void launch_cg_part(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, fl
                     float *p, float *pn, float *q, BicgScal *sc, int part, const CgTma *tma)
 {
     if (tma && tma->ok) {  // z (or h), p = the buffers of the maps
-        if (part == 0) launch_cg_pq_tma(c, F, *tma, false, &tma->zh, &tma->p, pn, q, sc);
+        if (part == 0) launch_cg_pq_tma(c, F, *tma, false, &tma->zh, &tma->p, pn, q, sc, tma->form_z);
         else if (tma->form_z) k_cg_upd_fv<<<c.cg_grid, kBlock, 0, c.s>>>(F, e, pn, h, q, sc, c.partials, c.counter);
         else k_cg_upd<<<c.cg_grid, kBlock, 0, c.s>>>(F.A.n, e, pn, h, q, iP, z, sc, c.partials, c.counter);
         return;

@@ -36,8 +36,8 @@ from .configs import Workload
 def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi.SOLVER_BICG_SPE,
                 precision: int = capi.PREC_FP64, tol: float | None = None, maxit: int = 5000,
                 omega: float | None = None, sor_maxit: int = 5000, aligned_source: bool = False,
-                compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-2,
-                max_outer: int = 30, inner_solver: int = capi.INNER_CG, les: bool = False) -> capi.CfdConfig:
+                compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-3,
+                max_outer: int = 30, inner_solver: int = capi.INNER_MG, les: bool = False) -> capi.CfdConfig:
     cfg = capi.CfdConfig()
     check(lib().cfd_config_default(C.byref(cfg), w.nxc, w.nyc, w.nzc))
     cfg.lx, cfg.ly, cfg.lz = w.lx, w.ly, w.lz

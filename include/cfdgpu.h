@@ -69,8 +69,11 @@ typedef enum {
 typedef enum {
     CFD_INNER_CG = 0,       /* FP32 Jacobi-preconditioned CG on the symmetric
                                finite-volume form M = D_V L of the operator */
-    CFD_INNER_BICGSTAB = 1  /* FP32 BiCGSTAB on the Jacobi-scaled operator, restarted
+    CFD_INNER_BICGSTAB = 1, /* FP32 BiCGSTAB on the Jacobi-scaled operator, restarted
                                when |r1.r0| < 1e-5 |r1||r0| */
+    CFD_INNER_MG = 2        /* FP32 CG on the finite-volume form preconditioned by a
+                               geometric multigrid V-cycle (SPE operator; falls back to
+                               Jacobi-PCG where the grid does not coarsen) */
 } cfd_inner_solver;
 
 /* Velocity slots: the reference's T0 (old), T1 (predicted u*), T3 (new). */

@@ -116,6 +116,7 @@ def test_zero_rhs_returns_immediately():
 
 
 @pytest.mark.parametrize("solver,inner", [(capi.SOLVER_BICG_SPE, capi.INNER_CG),
+                                          (capi.SOLVER_BICG_SPE, capi.INNER_MG),
                                           (capi.SOLVER_BICG_SPE, capi.INNER_BICGSTAB),
                                           (capi.SOLVER_BICG_ELL, capi.INNER_BICGSTAB)])
 def test_mixed_precision_defect_correction(oracle, solver, inner):
@@ -176,7 +177,7 @@ def test_cg_stencil_tma_matches_plain_kernel(monkeypatch, dims):
     out = []
     for flag in ("0", "1"):
         monkeypatch.setenv("CFDGPU_NO_TMA", flag)
-        with Simulation(w, tol=1e-10, precision=capi.PREC_MIXED) as S:
+        with Simulation(w, tol=1e-10, precision=capi.PREC_MIXED, inner_solver=capi.INNER_CG, inner_tol=1e-2) as S:
             S.grid_uniform()
             jp = S.download("JP")
             r = rng.standard_normal(w.n_cells) if flag == "0" else out[0][2]
@@ -189,3 +190,26 @@ def test_cg_stencil_tma_matches_plain_kernel(monkeypatch, dims):
     assert abs(it_t - it_p) <= 0.05 * it_p + 4
     d_t, d_p = x_t - x_t.mean(), x_p - x_p.mean()
     assert np.linalg.norm(d_t - d_p) <= 1e-8 * np.linalg.norm(d_p)
+
+
+@pytest.mark.parametrize("dims", [(64, 48, 32), (32, 20, 8), (30, 18, 6)])
+def test_multigrid_inner_solve_reaches_tolerance_in_few_iterations(dims):
+    """Multigrid-preconditioned FP32 CG inside the FP64 defect correction:
+    the FP64 tolerance is reached, with far fewer inner iterations than
+    Jacobi-PCG (the 30x18x6 grid does not coarsen to a small level, so it
+    falls back to Jacobi-PCG and must still converge)."""
+    nx, ny, nz = dims
+    w = WORKLOADS["c1"].with_(nxc=nx, nyc=ny, nzc=nz, lx=nx * 0.25, ly=ny * 0.25, lz=nz * 0.25, cx=nx * 0.1)
+    rng = np.random.default_rng(5)
+    its = {}
+    for inner in (capi.INNER_CG, capi.INNER_MG):
+        with Simulation(w, tol=1e-10, precision=capi.PREC_MIXED, inner_solver=inner) as S:
+            S.grid_uniform()
+            jp = S.download("JP")
+            r = rng.standard_normal(w.n_cells) if inner == capi.INNER_CG else r
+            S.upload("B", r - jp * np.mean(r / jp))
+            it, res = S.pSolver()
+            assert res < 1e-10
+            its[inner] = it
+    if dims != (30, 18, 6):
+        assert its[capi.INNER_MG] * 5 < its[capi.INNER_CG], its

@@ -124,10 +124,11 @@ def test_steps_are_bitwise_reproducible():
     b.close()
 
 
-def test_mixed_precision_step_close_to_fp64():
+@pytest.mark.parametrize("inner", [capi.INNER_CG, capi.INNER_MG])
+def test_mixed_precision_step_close_to_fp64(inner):
     w = WORKLOADS["c1"]
     S64, h64 = gpu_run(w, 4, tol=1e-10)
-    S32, h32 = gpu_run(w, 4, tol=1e-10, precision=capi.PREC_MIXED)
+    S32, h32 = gpu_run(w, 4, tol=1e-10, precision=capi.PREC_MIXED, inner_solver=inner)
     cd64 = np.array([h["cd"] for h in h64])
     cd32 = np.array([h["cd"] for h in h32])
     np.testing.assert_allclose(cd32, cd64, rtol=1e-4)
