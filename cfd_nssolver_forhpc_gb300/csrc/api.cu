@@ -198,7 +198,7 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 // iterations per solve, so a graph replay holds two pairs.
 int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 {
-    const int v = 10 * c->mg.first_small + 1;
+    const int v = (4 * c->mg.sweeps + 2) * c->mg.first_small + 1;
     float *z = c->w32.r0, *q = c->w32.ap;
     return run_pairs(
         c, 4, sc,
@@ -1356,6 +1356,23 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                      residual64(c, spe64(c), c->b, c->x, c->r32, c->dscal + 5);
                  })) != CFD_OK)
                 return st;
+            if (c->cfg.inner_solver == CFD_INNER_MG) {
+                CKS(mg_setup(c));
+                if (c->mg.usable) {
+                    const int ids[5] = {CFD_KERNEL_MG_SMOOTH, CFD_KERNEL_MG_RESTRICT, CFD_KERNEL_MG_PROLONG,
+                                        CFD_KERNEL_MG_SMALL, CFD_KERNEL_MG_VCYCLE};
+                    for (int part = 0; part < 5; ++part)
+                        if (!(part < 3 && c->mg.first_small == 0))
+                            if ((st = timed(ids[part], [&] { mg_time_part(c, part); })) != CFD_OK) return st;
+                    if ((st = timed(CFD_KERNEL_MG_UPD, [&] {
+                             mg_upd(c, c->e32, c->w32.p1, c->r32, c->w32.ap, c->sc_t);
+                         })) != CFD_OK)
+                        return st;
+                    if ((st = timed(CFD_KERNEL_MG_RHO, [&] { mg_rho(c, c->r32, c->w32.r0, nullptr, c->sc_t); })) !=
+                        CFD_OK)
+                        return st;
+                }
+            }
         }
     }
     st = dispatch(c, [&](auto tag) -> int {

@@ -58,6 +58,7 @@ int ensure_fp32_solver(cfd_ctx *c);
 int mg_setup(cfd_ctx *c);
 void mg_vcycle(cfd_ctx *c, const int *done);
 void mg_h(cfd_ctx *c, float *h);
+void mg_time_part(cfd_ctx *c, int part);
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
 void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state
@@ -303,6 +304,7 @@ int ensure_fp32_solver(cfd_ctx *c);
 int mg_setup(cfd_ctx *c);
 void mg_vcycle(cfd_ctx *c, const int *done);
 void mg_h(cfd_ctx *c, float *h);
+void mg_time_part(cfd_ctx *c, int part);
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
 void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state
@@ -318,6 +320,7 @@ int ensure_fp32_solver(cfd_ctx *c);
 int mg_setup(cfd_ctx *c);
 void mg_vcycle(cfd_ctx *c, const int *done);
 void mg_h(cfd_ctx *c, float *h);
+void mg_time_part(cfd_ctx *c, int part);
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
 void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state

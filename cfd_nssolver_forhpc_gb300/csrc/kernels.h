@@ -265,17 +265,22 @@ constexpr long long kMgSmall = 16384;  // levels at or below this size run in on
 struct MgLevel {
     int nx, ny, nz;
     long long n;
-    FastDiv fyz, fz;  // division by ny*nz and nz
+    FastDiv fyz, fz;      // division by ny*nz and nz
+    FastDiv fyh, fh;      // division by ny*(nz/2) and nz/2 (cell pairs along k, nz even)
     const float *cm[3], *cp[3], *sum[3], *w[3];  // per axis: -face, +face, cm + cp, width
+    const float *rw[3];   // per axis: 1 / width
     float *x, *b;
 };
 struct MgSmall {
-    int first, nlev, pre, post, coarse;
+    int first, nlev, pre, post;
     const int *done;
+    const float *cinv;  // dense inverse of the coarsest operator (regularised), n x n
     MgLevel lev[kMgMaxLevels];
 };
 struct Mg {
     int nlev = 0, first_small = 0;
+    int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
+    float *cinv = nullptr;
     bool usable = false;
     int *never = nullptr;  // a device flag that stays 0 (the ungated V-cycle)
     MgLevel lev[kMgMaxLevels];

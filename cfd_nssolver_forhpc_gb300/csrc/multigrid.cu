@@ -13,16 +13,20 @@
 // (restriction); the coarse correction is added to every child (prolongation,
 // the transpose of the restriction).  Smoother: red-black Gauss-Seidel
 // x_c = (b_c / dV_c + sum cm x_- + cp x_+) / (sum cm + cp), red then black
-// before the coarse correction and black then red after it, so the V-cycle is
-// a symmetric operator and CG keeps its short recurrences.  The coarsest
-// level (a few dozen cells) has its mean removed (M is singular, constants
-// are its null space) and is relaxed with symmetric sweeps.
+// before the coarse correction and black then red after it.  The coarsest
+// level (at most kMgCoarsest cells) is solved exactly in the range of M: its
+// right-hand side loses its mean (constants are M's null space) and is
+// multiplied by the dense inverse of M + a 1 1^T, a > 0, built on the host.
+// Every piece is a fixed symmetric linear map, so the V-cycle is a symmetric
+// operator and CG keeps its short recurrences.
 //
-// Levels above kMgSmall cells run as grid-wide kernels; the remaining small
-// levels run inside one single-block kernel that performs their whole sub-
-// cycle with block barriers, so a V-cycle is about 10 launches per large
-// level plus one.
+// Levels above kMgSmall cells run as grid-wide kernels (the smoother works
+// on cell pairs along k, one thread per pair updating the cell of the
+// requested colour); the small levels run inside one single-block kernel
+// that performs their whole sub-cycle with block barriers.
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -32,24 +36,10 @@ using namespace cfd;
 
 namespace {
 
-inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
+constexpr int kSmallThreads = 1024;
+constexpr int kMgCoarsest = 256;  // cells of the coarsest level at most (dense inverse)
 
-// one cell of the level operator: the neighbour sum and the diagonal of L
-__device__ __forceinline__ void mg_cell(const MgLevel &L, const float *__restrict__ x, int i, int j, int k,
-                                         long long t, float &nb, float &diag, float &dv)
-{
-    const long long sx = (long long)L.ny * L.nz, sy = L.nz;
-    float s = 0.f;
-    if (i > 0) s = fmaf(__ldg(L.cm[0] + i), x[t - sx], s);
-    if (i < L.nx - 1) s = fmaf(__ldg(L.cp[0] + i), x[t + sx], s);
-    if (j > 0) s = fmaf(__ldg(L.cm[1] + j), x[t - sy], s);
-    if (j < L.ny - 1) s = fmaf(__ldg(L.cp[1] + j), x[t + sy], s);
-    if (k > 0) s = fmaf(__ldg(L.cm[2] + k), x[t - 1], s);
-    if (k < L.nz - 1) s = fmaf(__ldg(L.cp[2] + k), x[t + 1], s);
-    nb = s;
-    diag = __ldg(L.sum[0] + i) + __ldg(L.sum[1] + j) + __ldg(L.sum[2] + k);
-    dv = __ldg(L.w[0] + i) * __ldg(L.w[1] + j) * __ldg(L.w[2] + k);
-}
+inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 __device__ __forceinline__ void decomp(const MgLevel &L, long long t, int &i, int &j, int &k)
 {
@@ -60,12 +50,58 @@ __device__ __forceinline__ void decomp(const MgLevel &L, long long t, int &i, in
     k = (int)(r - jj * (unsigned)L.nz);
 }
 
-// one colour of a Gauss-Seidel sweep over cells [t0, n) with stride; with
-// zero_init the level starts from x = 0 (neighbours read as 0, the other
-// colour written as 0)
-__device__ __forceinline__ void smooth_cells(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
+// the neighbour sum of L at (i, j, k), cell t
+__device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict__ x, int i, int j, int k, long long t)
+{
+    const long long sx = (long long)L.ny * L.nz, sy = L.nz;
+    float s = 0.f;
+    if (i > 0) s = fmaf(__ldg(L.cm[0] + i), x[t - sx], s);
+    if (i < L.nx - 1) s = fmaf(__ldg(L.cp[0] + i), x[t + sx], s);
+    if (j > 0) s = fmaf(__ldg(L.cm[1] + j), x[t - sy], s);
+    if (j < L.ny - 1) s = fmaf(__ldg(L.cp[1] + j), x[t + sy], s);
+    if (k > 0) s = fmaf(__ldg(L.cm[2] + k), x[t - 1], s);
+    if (k < L.nz - 1) s = fmaf(__ldg(L.cp[2] + k), x[t + 1], s);
+    return s;
+}
+
+__device__ __forceinline__ float mg_diag(const MgLevel &L, int i, int j, int k)
+{
+    return __ldg(L.sum[0] + i) + __ldg(L.sum[1] + j) + __ldg(L.sum[2] + k);
+}
+
+__device__ __forceinline__ float mg_rdv(const MgLevel &L, int i, int j, int k)
+{
+    return __ldg(L.rw[0] + i) * __ldg(L.rw[1] + j) * __ldg(L.rw[2] + k);
+}
+
+// Gauss-Seidel update of one cell: x = (b / dV + neighbours) / diag
+__device__ __forceinline__ void gs_cell(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x, int i,
+                                        int j, int k, long long t, bool zero_init)
+{
+    const float nb = zero_init ? 0.f : mg_nb(L, x, i, j, k, t);
+    x[t] = fmaf(b[t], mg_rdv(L, i, j, k), nb) * __frcp_rn(mg_diag(L, i, j, k));
+}
+
+// one colour over the level: pairs (k = 2m, 2m + 1) when nz is even (one
+// thread per pair updates the cell of that colour), single cells otherwise;
+// zero_init starts from x = 0 (the other colour written as 0)
+__device__ __forceinline__ void smooth_level(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
                                              int color, bool zero_init, long long t0, long long stride)
 {
+    if ((L.nz & 1) == 0) {
+        const long long np = L.n >> 1;
+        const int nh = L.nz >> 1;
+        for (long long q = t0; q < np; q += stride) {
+            const unsigned u = (unsigned)q;
+            const unsigned i = L.fyh.div(u), r = u - i * (unsigned)(L.ny * nh), j = L.fh.div(r);
+            const int m = (int)(r - j * (unsigned)nh);
+            const int k = 2 * m + (int)((color + i + j) & 1u);
+            const long long t = ((long long)i * L.ny + j) * L.nz + k;
+            gs_cell(L, b, x, (int)i, (int)j, k, t, zero_init);
+            if (zero_init) x[t + ((k & 1) ? -1 : 1)] = 0.f;
+        }
+        return;
+    }
     for (long long t = t0; t < L.n; t += stride) {
         int i, j, k;
         decomp(L, t, i, j, k);
@@ -73,20 +109,12 @@ __device__ __forceinline__ void smooth_cells(const MgLevel &L, const float *__re
             if (zero_init) x[t] = 0.f;
             continue;
         }
-        float nb, diag, dv;
-        if (zero_init) {
-            nb = 0.f;
-            diag = __ldg(L.sum[0] + i) + __ldg(L.sum[1] + j) + __ldg(L.sum[2] + k);
-            dv = __ldg(L.w[0] + i) * __ldg(L.w[1] + j) * __ldg(L.w[2] + k);
-        } else {
-            mg_cell(L, x, i, j, k, t, nb, diag, dv);
-        }
-        x[t] = (b[t] / dv + nb) / diag;
+        gs_cell(L, b, x, i, j, k, t, zero_init);
     }
 }
 
 // coarse b = sum over the children of (b - M x) on the fine level
-__device__ __forceinline__ void restrict_cells(const MgLevel &F, const MgLevel &C, const float *__restrict__ bf,
+__device__ __forceinline__ void restrict_level(const MgLevel &F, const MgLevel &C, const float *__restrict__ bf,
                                                const float *__restrict__ xf, float *__restrict__ bc, long long t0,
                                                long long stride)
 {
@@ -100,23 +128,27 @@ __device__ __forceinline__ void restrict_cells(const MgLevel &F, const MgLevel &
                 for (int c = 0; c < fz; ++c) {
                     const int i = fx * I + a, j = fy * J + b2, k = fz * K + c;
                     const long long t = ((long long)i * F.ny + j) * F.nz + k;
-                    float nb, diag, dv;
-                    mg_cell(F, xf, i, j, k, t, nb, diag, dv);
-                    s += bf[t] - dv * (diag * xf[t] - nb);
+                    const float dv = __ldg(F.w[0] + i) * __ldg(F.w[1] + j) * __ldg(F.w[2] + k);
+                    s += bf[t] - dv * (mg_diag(F, i, j, k) * xf[t] - mg_nb(F, xf, i, j, k, t));
                 }
         bc[T] = s;
     }
 }
 
-// fine x += coarse x of the parent cell
-__device__ __forceinline__ void prolong_cells(const MgLevel &F, const MgLevel &C, const float *__restrict__ xc,
+// fine x += coarse x: one thread per coarse cell writes its children
+__device__ __forceinline__ void prolong_level(const MgLevel &F, const MgLevel &C, const float *__restrict__ xc,
                                               float *__restrict__ xf, long long t0, long long stride)
 {
     const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
-    for (long long t = t0; t < F.n; t += stride) {
-        int i, j, k;
-        decomp(F, t, i, j, k);
-        xf[t] += xc[((long long)(i / fx) * C.ny + j / fy) * C.nz + k / fz];
+    for (long long T = t0; T < C.n; T += stride) {
+        int I, J, K;
+        decomp(C, T, I, J, K);
+        const float v = xc[T];
+        for (int a = 0; a < fx; ++a)
+            for (int b2 = 0; b2 < fy; ++b2) {
+                const long long base = ((long long)(fx * I + a) * F.ny + fy * J + b2) * F.nz + fz * K;
+                for (int c = 0; c < fz; ++c) xf[base + c] += v;
+            }
     }
 }
 
@@ -124,7 +156,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b,
                                                       const int *done)
 {
     if (*done) return;
-    smooth_cells(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+    smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                  (long long)gridDim.x * blockDim.x);
 }
 
@@ -132,7 +164,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, co
                                                         float *bc, const int *done)
 {
     if (*done) return;
-    restrict_cells(F, C, bf, xf, bc, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+    restrict_level(F, C, bf, xf, bc, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                    (long long)gridDim.x * blockDim.x);
 }
 
@@ -140,13 +172,11 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevel F, MgLevel C, con
                                                        const int *done)
 {
     if (*done) return;
-    prolong_cells(F, C, xc, xf, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+    prolong_level(F, C, xc, xf, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
-constexpr int kSmallThreads = 1024;
-
-// the whole sub-cycle of levels first..last-1 (the coarsest is last-1) in one
-// block: pre-smooth and restrict down, relax the coarsest, prolong and
+// the whole sub-cycle of levels first..nlev-1 (nlev-1 the coarsest) in one
+// block: pre-smooth and restrict down, solve the coarsest, prolong and
 // post-smooth up; block barriers between the phases
 __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 {
@@ -156,19 +186,19 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
     for (int l = first; l < last - 1; ++l) {
         const MgLevel &L = S.lev[l];
         for (int s = 0; s < S.pre; ++s) {
-            smooth_cells(L, L.b, L.x, 0, s == 0, t0, st);
+            smooth_level(L, L.b, L.x, 0, s == 0, t0, st);
             __syncthreads();
-            smooth_cells(L, L.b, L.x, 1, false, t0, st);
+            smooth_level(L, L.b, L.x, 1, false, t0, st);
             __syncthreads();
         }
-        restrict_cells(L, S.lev[l + 1], L.b, L.x, S.lev[l + 1].b, t0, st);
+        restrict_level(L, S.lev[l + 1], L.b, L.x, S.lev[l + 1].b, t0, st);
         __syncthreads();
     }
-    // coarsest: remove the mean of b (the null space of M), then symmetric
-    // sweeps from zero
     {
+        // coarsest: x = (M + a 1 1^T)^-1 (b - mean b)
         const MgLevel &L = S.lev[last - 1];
         __shared__ float red[kSmallThreads / 32];
+        __shared__ float bs[kMgCoarsest];
         float s = 0.f;
         for (long long t = t0; t < L.n; t += st) s += L.b[t];
         for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
@@ -177,29 +207,24 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
         float tot = 0.f;
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += red[q];
         const float mean = tot / (float)L.n;
-        for (long long t = t0; t < L.n; t += st) L.b[t] -= mean;
+        for (long long t = t0; t < L.n; t += st) bs[t] = L.b[t] - mean;
         __syncthreads();
-        for (int s2 = 0; s2 < S.coarse; ++s2) {
-            smooth_cells(L, L.b, L.x, 0, s2 == 0, t0, st);
-            __syncthreads();
-            smooth_cells(L, L.b, L.x, 1, false, t0, st);
-            __syncthreads();
+        for (long long r = t0; r < L.n; r += st) {
+            const float *row = S.cinv + r * L.n;
+            float a = 0.f;
+            for (long long cidx = 0; cidx < L.n; ++cidx) a = fmaf(__ldg(row + cidx), bs[cidx], a);
+            L.x[r] = a;
         }
-        for (int s2 = 0; s2 < S.coarse; ++s2) {
-            smooth_cells(L, L.b, L.x, 1, false, t0, st);
-            __syncthreads();
-            smooth_cells(L, L.b, L.x, 0, false, t0, st);
-            __syncthreads();
-        }
+        __syncthreads();
     }
     for (int l = last - 2; l >= first; --l) {
         const MgLevel &L = S.lev[l];
-        prolong_cells(L, S.lev[l + 1], S.lev[l + 1].x, L.x, t0, st);
+        prolong_level(L, S.lev[l + 1], S.lev[l + 1].x, L.x, t0, st);
         __syncthreads();
         for (int s = 0; s < S.post; ++s) {
-            smooth_cells(L, L.b, L.x, 1, false, t0, st);
+            smooth_level(L, L.b, L.x, 1, false, t0, st);
             __syncthreads();
-            smooth_cells(L, L.b, L.x, 0, false, t0, st);
+            smooth_level(L, L.b, L.x, 0, false, t0, st);
             __syncthreads();
         }
     }
@@ -270,40 +295,143 @@ __global__ void __launch_bounds__(kBlock) k_mg_upd(long long n, float *__restric
     }
 }
 
+// per-axis device arrays {cm, cp, cm + cp, w, 1/w} of m entries
+int upload_axis(cfd_ctx *c, const std::vector<double> &W, MgLevel &L, int a)
+{
+    const int m = (int)W.size();
+    std::vector<float> all((size_t)5 * m, 0.f);
+    for (int i = 0; i < m; ++i) {
+        float cm = 0.f, cp = 0.f;
+        if (i > 0) cm = (float)(1.0 / (W[i] * 0.5 * (W[i - 1] + W[i])));
+        if (i < m - 1) cp = (float)(1.0 / (W[i] * 0.5 * (W[i] + W[i + 1])));
+        all[i] = cm;
+        all[m + i] = cp;
+        all[2 * m + i] = cm + cp;
+        all[3 * m + i] = (float)W[i];
+        all[4 * m + i] = (float)(1.0 / W[i]);
+    }
+    float *d = nullptr;
+    CKS(dalloc_t(c, &d, all.size()));
+    CK(cudaMemcpy(d, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice));
+    L.cm[a] = d;
+    L.cp[a] = d + m;
+    L.sum[a] = d + 2 * m;
+    L.w[a] = d + 3 * m;
+    L.rw[a] = d + 4 * m;
+    return CFD_OK;
+}
+
+void set_divs(MgLevel &L)
+{
+    L.fyz = FastDiv((unsigned)(L.ny * L.nz));
+    L.fz = FastDiv((unsigned)L.nz);
+    const int nh = L.nz / 2 > 0 ? L.nz / 2 : 1;
+    L.fyh = FastDiv((unsigned)(L.ny * nh));
+    L.fh = FastDiv((unsigned)nh);
+}
+
+// dense (M + a 1 1^T)^-1 of a level given its per-axis widths (Gauss-Jordan
+// in FP64; M symmetric positive semi-definite with constants as null space)
+int coarse_inverse(cfd_ctx *c, const std::vector<double> (&W)[3], float **out)
+{
+    const int nx = (int)W[0].size(), ny = (int)W[1].size(), nz = (int)W[2].size(), n = nx * ny * nz;
+    std::vector<double> A((size_t)n * n, 0.0), I((size_t)n * n, 0.0);
+    auto id = [&](int i, int j, int k) { return (i * ny + j) * nz + k; };
+    double dmax = 0.0;
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const int r = id(i, j, k);
+                const double dv = W[0][i] * W[1][j] * W[2][k];
+                const int ax[3] = {i, j, k}, lim[3] = {nx, ny, nz};
+                double diag = 0.0;
+                for (int a = 0; a < 3; ++a)
+                    for (int side = -1; side <= 1; side += 2) {
+                        const int o = ax[a] + side;
+                        if (o < 0 || o >= lim[a]) continue;
+                        const double cf = dv / (W[a][ax[a]] * 0.5 * (W[a][ax[a]] + W[a][o]));
+                        int ii = i, jj = j, kk = k;
+                        (a == 0 ? ii : a == 1 ? jj : kk) = o;
+                        A[(size_t)r * n + id(ii, jj, kk)] -= cf;
+                        diag += cf;
+                    }
+                A[(size_t)r * n + r] += diag;
+                dmax = std::max(dmax, diag);
+            }
+    const double alpha = dmax / n;
+    for (size_t q = 0; q < A.size(); ++q) A[q] += alpha;
+    for (int r = 0; r < n; ++r) I[(size_t)r * n + r] = 1.0;
+    for (int col = 0; col < n; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < n; ++r)
+            if (std::fabs(A[(size_t)r * n + col]) > std::fabs(A[(size_t)piv * n + col])) piv = r;
+        if (std::fabs(A[(size_t)piv * n + col]) == 0.0) return fail(CFD_ERR_STATE, "singular coarsest operator");
+        if (piv != col)
+            for (int q = 0; q < n; ++q) {
+                std::swap(A[(size_t)piv * n + q], A[(size_t)col * n + q]);
+                std::swap(I[(size_t)piv * n + q], I[(size_t)col * n + q]);
+            }
+        const double inv = 1.0 / A[(size_t)col * n + col];
+        for (int q = 0; q < n; ++q) {
+            A[(size_t)col * n + q] *= inv;
+            I[(size_t)col * n + q] *= inv;
+        }
+        for (int r = 0; r < n; ++r) {
+            if (r == col) continue;
+            const double f = A[(size_t)r * n + col];
+            if (f == 0.0) continue;
+            for (int q = 0; q < n; ++q) {
+                A[(size_t)r * n + q] -= f * A[(size_t)col * n + q];
+                I[(size_t)r * n + q] -= f * I[(size_t)col * n + q];
+            }
+        }
+    }
+    std::vector<float> f(I.begin(), I.end());
+    CKS(dalloc_t(c, out, f.size()));
+    CK(cudaMemcpy(*out, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return CFD_OK;
+}
+
 }  // namespace
 
 namespace cfd {
 
-// host set-up of the level hierarchy below level 0 (the CG's own operator)
+// host set-up of the level hierarchy (level 0 is the CG's own operator)
 int mg_setup(cfd_ctx *c)
 {
     Mg &G = c->mg;
     if (G.nlev > 0) return CFD_OK;
     const Geo &g = c->g;
-    // level 0: the FP32 finite-volume operator of the CG
+    if (const char *e = std::getenv("CFDGPU_MG_SWEEPS")) G.sweeps = std::atoi(e) > 0 ? std::atoi(e) : 2;
+    long long small = kMgSmall;
+    if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
     const FvOp<float> F = fv32(c);
-    MgLevel L0{};
-    L0.nx = g.nxc; L0.ny = g.nyc; L0.nz = g.nzc; L0.n = g.n;
-    L0.cm[0] = F.A.cxm; L0.cp[0] = F.A.cxp; L0.sum[0] = F.sx; L0.w[0] = F.wx;
-    L0.cm[1] = F.A.cym; L0.cp[1] = F.A.cyp; L0.sum[1] = F.sy; L0.w[1] = F.wy;
-    L0.cm[2] = F.A.czm; L0.cp[2] = F.A.czp; L0.sum[2] = F.sz; L0.w[2] = F.wz;
-    L0.x = c->w32.r0;  // z
-    L0.b = c->r32;     // h
-    L0.fyz = FastDiv((unsigned)(g.nyc * g.nzc));
-    L0.fz = FastDiv((unsigned)g.nzc);
-    G.lev[0] = L0;
-    // interior widths (FP64) of level 0, then halve while possible
     std::vector<double> W[3];
     const int n0[3] = {g.nxc, g.nyc, g.nzc};
     for (int a = 0; a < 3; ++a) {
         W[a].resize(n0[a]);
         for (int i = 0; i < n0[a]; ++i) W[a][i] = c->hraw[3 + a][i + GC];
     }
+    MgLevel L0{};
+    L0.nx = g.nxc; L0.ny = g.nyc; L0.nz = g.nzc; L0.n = g.n;
+    L0.cm[0] = F.A.cxm; L0.cp[0] = F.A.cxp; L0.sum[0] = F.sx; L0.w[0] = F.wx;
+    L0.cm[1] = F.A.cym; L0.cp[1] = F.A.cyp; L0.sum[1] = F.sy; L0.w[1] = F.wy;
+    L0.cm[2] = F.A.czm; L0.cp[2] = F.A.czp; L0.sum[2] = F.sz; L0.w[2] = F.wz;
+    for (int a = 0; a < 3; ++a) {  // 1 / width of level 0
+        std::vector<float> rw(n0[a]);
+        for (int i = 0; i < n0[a]; ++i) rw[i] = (float)(1.0 / W[a][i]);
+        float *d = nullptr;
+        CKS(dalloc_t(c, &d, rw.size()));
+        CK(cudaMemcpy(d, rw.data(), rw.size() * sizeof(float), cudaMemcpyHostToDevice));
+        L0.rw[a] = d;
+    }
+    L0.x = c->w32.r0;  // z
+    L0.b = c->r32;     // h
+    set_divs(L0);
+    G.lev[0] = L0;
     int nl = 1;
     int n[3] = {g.nxc, g.nyc, g.nzc};
-    while (nl < kMgMaxLevels) {
-        long long cells = (long long)n[0] * n[1] * n[2];
-        if (cells <= 32) break;
+    while (nl < kMgMaxLevels && (long long)n[0] * n[1] * n[2] > kMgCoarsest) {
         int f[3];
         bool any = false;
         for (int a = 0; a < 3; ++a) {
@@ -312,56 +440,50 @@ int mg_setup(cfd_ctx *c)
         }
         if (!any) break;
         MgLevel L{};
-        std::vector<float> host;
         for (int a = 0; a < 3; ++a) {
             std::vector<double> Wc(n[a] / f[a]);
             for (size_t I = 0; I < Wc.size(); ++I) Wc[I] = f[a] == 2 ? W[a][2 * I] + W[a][2 * I + 1] : W[a][I];
             W[a] = Wc;
             n[a] = (int)Wc.size();
+            CKS(upload_axis(c, W[a], L, a));
         }
         L.nx = n[0]; L.ny = n[1]; L.nz = n[2];
         L.n = (long long)n[0] * n[1] * n[2];
-        L.fyz = FastDiv((unsigned)(n[1] * n[2]));
-        L.fz = FastDiv((unsigned)n[2]);
-        for (int a = 0; a < 3; ++a) {
-            const int m = n[a];
-            std::vector<float> cm(m, 0.f), cp(m, 0.f), sm(m, 0.f), w(m, 0.f);
-            for (int i = 0; i < m; ++i) {
-                w[i] = (float)W[a][i];
-                if (i > 0) cm[i] = (float)(1.0 / (W[a][i] * 0.5 * (W[a][i - 1] + W[a][i])));
-                if (i < m - 1) cp[i] = (float)(1.0 / (W[a][i] * 0.5 * (W[a][i] + W[a][i + 1])));
-                sm[i] = cm[i] + cp[i];
-            }
-            float *d = nullptr;
-            CKS(dalloc_t(c, &d, (size_t)4 * m));
-            std::vector<float> all;
-            all.insert(all.end(), cm.begin(), cm.end());
-            all.insert(all.end(), cp.begin(), cp.end());
-            all.insert(all.end(), sm.begin(), sm.end());
-            all.insert(all.end(), w.begin(), w.end());
-            CK(cudaMemcpy(d, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice));
-            L.cm[a] = d; L.cp[a] = d + m; L.sum[a] = d + 2 * m; L.w[a] = d + 3 * m;
-        }
+        set_divs(L);
         CKS(dalloc_t(c, &L.x, (size_t)L.n));
         CKS(dalloc_t(c, &L.b, (size_t)L.n));
         G.lev[nl++] = L;
     }
     G.nlev = nl;
-    G.first_small = nl;
+    const long long ncoarse = G.lev[nl - 1].n;
+    G.usable = nl > 1 && ncoarse <= kMgCoarsest;
+    if (!G.usable) return CFD_OK;
+    CKS(coarse_inverse(c, W, &G.cinv));
+    G.first_small = nl - 1;
     for (int l = 0; l < nl; ++l)
-        if (G.lev[l].n <= kMgSmall) {
+        if (G.lev[l].n <= small) {
             G.first_small = l;
             break;
         }
-    // usable when there is a coarse level and the coarsest fits the one-block kernel
-    G.usable = nl > 1 && G.first_small < nl;
     CKS(dalloc_t(c, &G.never, 1));
     CK(cudaMemset(G.never, 0, sizeof(int)));
     return CFD_OK;
 }
 
-// z = V(h): one V-cycle (pre = post = 2 sweeps on the large levels); every
-// kernel returns at once when the solve is done
+static MgSmall small_desc(const Mg &G, const int *done)
+{
+    MgSmall S{};
+    S.done = done;
+    S.first = G.first_small;
+    S.nlev = G.nlev;
+    S.pre = G.sweeps;
+    S.post = G.sweeps;
+    S.cinv = G.cinv;
+    for (int l = 0; l < G.nlev; ++l) S.lev[l] = G.lev[l];
+    return S;
+}
+
+// z = V(h): one V-cycle; every kernel returns at once when *done
 void mg_vcycle(cfd_ctx *c, const int *done)
 {
     Mg &G = c->mg;
@@ -369,32 +491,40 @@ void mg_vcycle(cfd_ctx *c, const int *done)
     const int fs = G.first_small;
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
-        for (int q = 0; q < 2; ++q) {
-            k_mg_smooth<<<nblk(L.n), kBlock, 0, s>>>(L, L.b, L.x, 0, q == 0, done);
-            k_mg_smooth<<<nblk(L.n), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
+        const long long work = (L.nz % 2 == 0) ? L.n / 2 : L.n;
+        for (int q = 0; q < G.sweeps; ++q) {
+            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, q == 0, done);
+            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
         }
         k_mg_restrict<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], L.b, L.x, G.lev[l + 1].b, done);
     }
-    {
-        MgSmall S{};
-        S.done = done;
-        S.first = fs;
-        S.nlev = G.nlev;
-        S.pre = 2;
-        S.post = 2;
-        S.coarse = 24;
-        for (int l = 0; l < G.nlev; ++l) S.lev[l] = G.lev[l];
-        k_mg_small<<<1, kSmallThreads, 0, s>>>(S);
-    }
+    k_mg_small<<<1, kSmallThreads, 0, s>>>(small_desc(G, done));
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
-        k_mg_prolong<<<nblk(L.n), kBlock, 0, s>>>(L, G.lev[l + 1], G.lev[l + 1].x, L.x, done);
-        for (int q = 0; q < 2; ++q) {
-            k_mg_smooth<<<nblk(L.n), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
-            k_mg_smooth<<<nblk(L.n), kBlock, 0, s>>>(L, L.b, L.x, 0, 0, done);
+        const long long work = (L.nz % 2 == 0) ? L.n / 2 : L.n;
+        k_mg_prolong<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], G.lev[l + 1].x, L.x, done);
+        for (int q = 0; q < G.sweeps; ++q) {
+            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
+            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, 0, done);
         }
     }
-    c->launches += 10LL * fs + 1;
+    c->launches += (4LL * G.sweeps + 2) * fs + 1;
+}
+
+// one piece of the V-cycle for timing: 0 finest smoothing colour, 1 finest
+// restriction, 2 finest prolongation, 3 small-level kernel, 4 whole V-cycle
+void mg_time_part(cfd_ctx *c, int part)
+{
+    Mg &G = c->mg;
+    const cudaStream_t s = c->s;
+    const MgLevel &L = G.lev[0];
+    const int *done = G.never;
+    const long long work = (L.nz % 2 == 0) ? L.n / 2 : L.n;
+    if (part == 0) k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, 0, done);
+    else if (part == 1) k_mg_restrict<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], L.b, L.x, G.lev[1].b, done);
+    else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
+    else if (part == 3) k_mg_small<<<1, kSmallThreads, 0, s>>>(small_desc(G, done));
+    else mg_vcycle(c, done);
 }
 
 void mg_h(cfd_ctx *c, float *h)

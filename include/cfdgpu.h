@@ -240,6 +240,13 @@ typedef enum {
     CFD_KERNEL_CG_PQ,        /* mixed precision: p = z + beta p, q = M p, p.q (FP32) */
     CFD_KERNEL_CG_UPD,       /* mixed precision: e, h, z update and h.z (FP32) */
     CFD_KERNEL_RESIDUAL64,   /* mixed precision: FP64 residual b - A x of the defect correction */
+    CFD_KERNEL_MG_SMOOTH,    /* multigrid: one colour of a Gauss-Seidel sweep on the finest level */
+    CFD_KERNEL_MG_RESTRICT,  /* multigrid: residual of the finest level summed to the next */
+    CFD_KERNEL_MG_PROLONG,   /* multigrid: coarse correction added to the finest level */
+    CFD_KERNEL_MG_SMALL,     /* multigrid: the single-block sub-cycle of the small levels */
+    CFD_KERNEL_MG_VCYCLE,    /* multigrid: one whole V-cycle (all its launches) */
+    CFD_KERNEL_MG_UPD,       /* multigrid CG: e, h update */
+    CFD_KERNEL_MG_RHO,       /* multigrid CG: h.z and the scalar update */
     CFD_KERNEL_COUNT
 } cfd_kernel_id;
 
