@@ -265,13 +265,19 @@ def e2e_steps(S, K, dist):
     return max(e0.elapsed_time(e1) / 1e3, 0.0), wall, nbytes
 
 
-# FP32 kernels of the mixed-precision inner CG (bytes per row) and the FP64
-# residual of its defect correction
+# FP32 kernels of the mixed-precision inner solve (bytes per row) and the
+# FP64 residual of its defect correction
 KERNEL_BYTES_MIXED = {
-    "cg_pq": 16,       # read h (z = h/P formed in the kernel), p; write p', q (FP32)
+    "cg_pq": 16,       # read z (or h), p; write p', q (FP32)
     "cg_upd": 24,      # read e, p, h, q; write e, h (FP32; 1/P from the axis tables)
     "residual64": 28,  # read b, x, jp (FP64); write r (FP32)
+    "mg_smooth": 8,    # one colour on the finest level: read x (all), b (half); write x (half)
+    "mg_restrict": 8,  # read b, x of the finest level (coarse writes 1/8)
+    "mg_prolong": 8,   # read and write x of the finest level
+    "mg_upd": 24,      # read e, p, h, q; write e, h
+    "mg_rho": 8,       # read h, z
 }
+MG_SWEEPS = 2  # smoothing sweeps per level before and after the coarse correction
 
 
 def roofline(S, w, infos, precision):
@@ -280,7 +286,16 @@ def roofline(S, w, infos, precision):
     iters = sum(sum(i["iters"]) for i in infos) / len(infos)
     outer = sum(sum(i["outer"]) for i in infos) / len(infos)
     npass = 4
-    if precision == "mixed":
+    if precision == "mixed" and "mg_smooth" in ms:
+        # multigrid-preconditioned CG: one V-cycle per inner iteration and one
+        # per inner solve (its start); per V-cycle 4 * sweeps colour passes,
+        # one restriction and one prolongation on the finest level and the
+        # single-block kernel of the small levels
+        v = iters + outer
+        counts = {"mg_smooth": 4 * MG_SWEEPS * v, "mg_restrict": v, "mg_prolong": v, "mg_small": v,
+                  "cg_pq": iters, "mg_upd": iters, "mg_rho": v, "residual64": outer + npass}
+        per_row = dict(KERNEL_BYTES_MIXED)
+    elif precision == "mixed":
         counts = {"cg_pq": iters, "cg_upd": iters, "residual64": outer + npass}
         per_row = dict(KERNEL_BYTES_MIXED)
     else:
@@ -291,7 +306,7 @@ def roofline(S, w, infos, precision):
     per_row.update({k: v * word for k, v in KERNEL_BYTES_PER_CELL_FLOW.items()})
     shares = {k: ms[k] * counts[k] for k in ms if k in counts}
     total = sum(shares.values()) or 1.0
-    top = max(shares, key=shares.get)
+    top = max((k for k in shares if k in per_row), key=shares.get)
     bytes_launch = per_row[top] * w.n_cells
     peak, how = peaks()
     achieved = bytes_launch / (ms[top] * 1e-3) / 1e9
@@ -305,6 +320,8 @@ def roofline(S, w, infos, precision):
         "kernels_ms": {k: round(v, 5) for k, v in ms.items()},
         "shares": {k: round(v / total, 3) for k, v in shares.items()},
     }
+    if "mg_vcycle" in ms:
+        out["mg_vcycle_ms"] = round(ms["mg_vcycle"], 5)
     if precision != "mixed":
         # the FP64 Krylov kernels are bound by the FP64 pipe: FP64 operations
         # per row (SpMV 7, each dot 1, updates as written) / measured DFMA rate

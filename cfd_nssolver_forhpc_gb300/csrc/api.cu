@@ -66,97 +66,161 @@ void *field_ptr(cfd_ctx *c, int field, bool &is_t)
 
 // ---- solvers ----------------------------------------------------------------
 
+// One CUDA graph per solve: head() (the solve's set-up and first steps),
+// then a WHILE node whose body is body() followed by the loop condition
+// (k_loop_cond), so the whole solve runs on the device and the host waits
+// once.  The graph is rebuilt when `key` (its shape) changes.
+template <class Head, class Body>
+int while_graph(cfd_ctx *c, int gi, long long key, BicgScal *sc, int cap, Head &&head, Body &&body)
+{
+    cudaGraphExec_t &ge = c->graph[gi];
+    if (ge && c->graph_batch[gi] == key) return CFD_OK;
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    std::string what;
+    cudaError_t e = cudaSuccess;
+    do {
+        cudaGraphConditionalHandle h;
+        if ((e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) { what = "handle"; break; }
+        if ((e = cudaStreamBeginCaptureToGraph(c->s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { what = "capture"; break; }
+        head();
+        launch_loop_cond(c->s, h, sc, cap, 1);
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(c->s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        std::vector<cudaGraphNode_t> last(deps, deps + (e == cudaSuccess ? nd : 0));
+        cudaGraph_t cap_g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(c->s, &cap_g);
+        if (e != cudaSuccess || e2 != cudaSuccess) { e = e != cudaSuccess ? e : e2; what = "capture"; break; }
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t wn;
+        if ((e = cudaGraphAddNode(&wn, g, last.data(), nullptr, last.size(), &p)) != cudaSuccess) { what = "while node"; break; }
+        if ((e = cudaStreamBeginCaptureToGraph(c->s, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { what = "body capture"; break; }
+        body();
+        launch_loop_cond(c->s, h, sc, cap, 0);
+        if ((e = cudaStreamEndCapture(c->s, &cap_g)) != cudaSuccess) { what = "body capture"; break; }
+        if ((e = cudaGraphInstantiate(&ge, g, 0)) != cudaSuccess) { ge = nullptr; what = "instantiate"; break; }
+    } while (false);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(CFD_ERR_CUDA, "solve graph (" + what + "): " + cudaGetErrorString(e));
+    c->graph_batch[gi] = key;
+    return CFD_OK;
+}
+
+// launch a solve graph and wait for it; `what` names the solve in errors
+int run_while_graph(cfd_ctx *c, int gi, BicgScal *sc, long long launches_head, long long launches_body,
+                    const char *what)
+{
+    CK(cudaGraphLaunch(c->graph[gi], c->s));
+    CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    c->launches += launches_head + 1 + (long long)c->h_sc->loop_trips * (launches_body + 1);
+    if (c->debug > 1)
+        std::fprintf(stderr, "[cfdgpu] %s graph %d: trips %d done %d iter %d relres %.3e restarts %d\n", what, gi,
+                     c->h_sc->loop_trips, c->h_sc->done, c->h_sc->iter, c->h_sc->relres, c->h_sc->restarts);
+    if (c->h_sc->wait_timeout) return fail(CFD_ERR_TIMEOUT, "a bounded wait of the TMA pipeline gave up");
+    if (c->h_sc->done == BICG_RUNNING) return fail(CFD_ERR_TIMEOUT, std::string(what) + " did not report completion");
+    return CFD_OK;
+}
+
+// A graph of body() alone (no condition), replayed by the host until the
+// solve reports completion: the form used when device loops are off.
+template <class Body>
+int batch_graph(cfd_ctx *c, int gi, long long key, Body &&body)
+{
+    cudaGraphExec_t &ge = c->graph[gi];
+    if (ge && c->graph_batch[gi] == key) return CFD_OK;
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+    body();
+    cudaError_t e = cudaStreamEndCapture(c->s, &gr);
+    if (e != cudaSuccess) return fail(CFD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&ge, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) { ge = nullptr; return fail(CFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
+    c->graph_batch[gi] = key;
+    return CFD_OK;
+}
+
 template <class Op, class V>
 int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V *px1, V *px2,
              BicgScal *sc, int which_graph)
 {
+    const int batch = c->cfg.check_every;
+    const int cap = (int)std::min<long long>((long long)c->cfg.p_iter_max / batch + 3, 1 << 30);
+    auto iterations = [&] { for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc); };
+    if (c->use_graphs && c->device_loops) {
+        CKS(while_graph(
+            c, which_graph, ((long long)cap << 20) | batch, sc, cap,
+            [&] { launch_bicg_init<Op, V>(c->lc, A, b, x, w, px1, px2, sc); },
+            [&] { for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc); }));
+        return run_while_graph(c, which_graph, sc, 1, 5LL * batch, "BiCGSTAB");
+    }
+    if (c->use_graphs) CKS(batch_graph(c, which_graph, -batch, iterations));
     launch_bicg_init<Op, V>(c->lc, A, b, x, w, px1, px2, sc);
     c->launches += 1;
     CK(cudaGetLastError());
-    const int batch = c->cfg.check_every;
-    cudaGraphExec_t &ge = c->graph[which_graph];
-    if (c->use_graphs && (!ge || c->graph_batch[which_graph] != batch)) {
-        if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
-        cudaGraph_t gr = nullptr;
-        CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
-        for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc);
-        cudaError_t e = cudaStreamEndCapture(c->s, &gr);
-        if (e != cudaSuccess) return fail(CFD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&ge, gr, 0);
-        cudaGraphDestroy(gr);
-        if (e != cudaSuccess) { ge = nullptr; return fail(CFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
-        c->graph_batch[which_graph] = batch;
-    }
-    const long long cap_batches = (long long)c->cfg.p_iter_max / batch + 3;
     for (long long nb = 0;; ++nb) {
         c->launches += 5LL * batch;
-        if (c->use_graphs) {
-            CK(cudaGraphLaunch(ge, c->s));
-        } else {
-            for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc);
-            CK(cudaGetLastError());
-        }
+        if (c->use_graphs) CK(cudaGraphLaunch(c->graph[which_graph], c->s));
+        else iterations();
+        CK(cudaGetLastError());
         CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
         if (c->debug > 1)
-            std::fprintf(stderr, "[cfdgpu] graph %d batch %lld: done %d iter %d relres %.3e rho %.3e alpha %.3e "
-                         "omega %.3e beta %.3e restart %d\n", which_graph, nb, c->h_sc->done, c->h_sc->iter,
+            std::fprintf(stderr, "[cfdgpu] batch %lld: done %d iter %d relres %.3e rho %.3e alpha %.3e "
+                         "omega %.3e beta %.3e restart %d\n", nb, c->h_sc->done, c->h_sc->iter,
                          c->h_sc->relres, c->h_sc->rho, c->h_sc->alpha, c->h_sc->omega, c->h_sc->beta,
                          c->h_sc->restart);
         if (c->h_sc->done != BICG_RUNNING) break;
-        if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "BiCGSTAB did not report completion");
+        if (nb >= cap) return fail(CFD_ERR_TIMEOUT, "BiCGSTAB did not report completion");
     }
     return CFD_OK;
 }
 
 // Runs an inner solve whose first iteration is issued directly and whose
 // later iterations come in pairs (the pair brings the alternating buffers
-// back): prologue(), then graph replays of `pairs` x pair(0), pair(1),
-// polling the scalars once per replay.
+// back): prologue(), then pair(0), pair(1) while the solve runs -- inside
+// one graph (a WHILE node over `pairs` pairs) or, without graphs, polled
+// from the host after every `pairs` pairs.
 template <class Pro, class Pair>
 int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int launches_prologue,
               int launches_pair, int pairs_req = 0)
 {
-    prologue();
-    c->launches += launches_prologue;
-    CK(cudaGetLastError());
     const int pairs = pairs_req > 0 ? pairs_req : (c->cfg.check_every + 1) / 2;
-    cudaGraphExec_t &ge = c->graph[gi];
+    const int cap = (int)std::min<long long>((long long)c->cfg.p_iter_max / (2 * pairs) + 3, 1 << 30);
     auto body = [&] {
         for (int q = 0; q < pairs; ++q) {
             pair(0);
             pair(1);
         }
     };
-    if (c->use_graphs && (!ge || c->graph_batch[gi] != pairs)) {
-        if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
-        cudaGraph_t gr = nullptr;
-        CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
-        body();
-        cudaError_t e = cudaStreamEndCapture(c->s, &gr);
-        if (e != cudaSuccess) return fail(CFD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-        e = cudaGraphInstantiate(&ge, gr, 0);
-        cudaGraphDestroy(gr);
-        if (e != cudaSuccess) { ge = nullptr; return fail(CFD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e)); }
-        c->graph_batch[gi] = pairs;
+    if (c->use_graphs && c->device_loops) {
+        CKS(while_graph(c, gi, ((long long)cap << 20) | pairs, sc, cap, prologue, body));
+        return run_while_graph(c, gi, sc, launches_prologue, (long long)launches_pair * 2 * pairs, "inner solve");
     }
-    const long long cap_batches = (long long)c->cfg.p_iter_max / (2 * pairs) + 3;
+    if (c->use_graphs) CKS(batch_graph(c, gi, -pairs, body));
+    prologue();
+    c->launches += launches_prologue;
+    CK(cudaGetLastError());
     for (long long nb = 0;; ++nb) {
         CK(cudaMemcpyAsync(c->h_sc, sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
         CK(cudaStreamSynchronize(c->s));
-        if (c->debug > 1)
-            std::fprintf(stderr, "[cfdgpu] inner graph %d batch %lld: done %d iter %d relres %.3e restarts %d\n", gi,
-                         nb, c->h_sc->done, c->h_sc->iter, c->h_sc->relres, c->h_sc->restarts);
         if (c->h_sc->wait_timeout) return fail(CFD_ERR_TIMEOUT, "a bounded wait of the TMA pipeline gave up");
         if (c->h_sc->done != BICG_RUNNING) break;
-        if (nb > cap_batches) return fail(CFD_ERR_TIMEOUT, "inner solve did not report completion");
+        if (nb >= cap) return fail(CFD_ERR_TIMEOUT, "inner solve did not report completion");
         c->launches += (long long)launches_pair * 2 * pairs;
-        if (c->use_graphs) {
-            CK(cudaGraphLaunch(ge, c->s));
-        } else {
-            body();
-            CK(cudaGetLastError());
-        }
+        if (c->use_graphs) CK(cudaGraphLaunch(c->graph[gi], c->s));
+        else body();
+        CK(cudaGetLastError());
     }
     return CFD_OK;
 }
@@ -195,7 +259,7 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 // FP32 CG on M e = P r preconditioned by one multigrid V-cycle per iteration
 // (multigrid.cu): z = V(h), rho = h.z, p0 = z, then per iteration the
 // stencil launch (pn, q, alpha), the update (e, h), a V-cycle and rho'.  Few
-// iterations per solve, so a graph replay holds two pairs.
+// iterations per solve, so the loop body holds one pair.
 int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 {
     const int v = (4 * c->mg.sweeps + 2) * c->mg.first_small + 1;
@@ -218,7 +282,7 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
             mg_vcycle(c, &sc->done);
             mg_rho(c, h, z, nullptr, sc);
         },
-        2 * v + 5, v + 3, 2);
+        2 * v + 5, v + 3, c->mg.pairs);
 }
 
 // The graphs bake in the buffers and operator of the context; they are
@@ -666,6 +730,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     g.fsxc = FastDiv((unsigned int)g.sxc);
     g.fsyc = FastDiv((unsigned int)g.syc);
     if (const char *e = std::getenv("CFDGPU_NO_GRAPH")) c->use_graphs = !(e[0] == '1');
+    if (const char *e = std::getenv("CFDGPU_SOLVE_LOOP")) c->device_loops = std::strcmp(e, "host") != 0;
     if (const char *e = std::getenv("CFDGPU_DEBUG")) c->debug = std::atoi(e);
     if (const char *e = std::getenv("CFDGPU_NO_FUSED")) c->fused = !(e[0] == '1');
 

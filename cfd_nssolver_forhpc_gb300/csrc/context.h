@@ -111,7 +111,7 @@ struct cfd_ctx {
     // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
     // [4] multigrid-preconditioned CG
     cudaGraphExec_t graph[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    int graph_batch[5] = {0, 0, 0, 0, 0};
+    long long graph_batch[5] = {0, 0, 0, 0, 0};  // shape key of each cached graph
 
     // SOR
     double *cf6 = nullptr, *cf7 = nullptr;
@@ -125,6 +125,7 @@ struct cfd_ctx {
     long long loop = 1;
     double time = 0.0;
     bool use_graphs = true;
+    bool device_loops = true;  // solve loops as graph WHILE nodes (else host-polled graph batches)
     int debug = 0;
     bool fused = true;  // fused FP32 inner iterations (SPE operator)
     long long launches = 0;  // kernels issued by the step and solver paths

@@ -119,6 +119,7 @@ struct BicgScal {
     double restart_rel, r0n2;
     int iter, done, restart, timestep, maxit, restarts, total_iters, nonfinite;
     int wait_timeout;  // a bounded device wait (TMA pipeline) gave up
+    int loop_trips;    // body runs of the solve's device-side loop (graph WHILE node)
 };
 enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
 
@@ -127,6 +128,12 @@ template <class V>
 struct BicgVecs {
     V *r0, *r1, *p1, *s1, *ap, *as;
 };
+
+// the WHILE condition of a solve loop inside one CUDA graph: continue while
+// sc->done is BICG_RUNNING, no bounded wait gave up and the body has run
+// fewer than cap times; first != 0 is the check after the head (resets the
+// trip count)
+void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc, int cap, int first);
 
 void launch_spe_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
                       const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
@@ -267,22 +274,37 @@ struct MgLevel {
     long long n;
     FastDiv fyz, fz;      // division by ny*nz and nz
     FastDiv fyh, fh;      // division by ny*(nz/2) and nz/2 (cell pairs along k, nz even)
+    FastDiv fyq, fq;      // division by ny*(nz/4) and nz/4 (cell quads along k, nz % 4 == 0)
     const float *cm[3], *cp[3], *sum[3], *w[3];  // per axis: -face, +face, cm + cp, width
     const float *rw[3];   // per axis: 1 / width
     float *x, *b;
+    const float *rv, *rg;  // per cell 1 / dV and 1 / diag (small-level kernel only)
+    bool quads;           // the float4 smoother applies (nz % 4 == 0, aligned arrays)
 };
+constexpr int kMgSmallSmem = 200 * 1024;  // shared-memory bytes for the small levels' x and b
 struct MgSmall {
     int first, nlev, pre, post;
     const int *done;
-    const float *cinv;  // dense inverse of the coarsest operator (regularised), n x n
+    const float *cinv;   // dense inverse of the coarsest operator (regularised, symmetric), n x n
+    const float *image;  // the static part of the shared-memory layout, copied in at the start
+    int image_floats;    // its size (a multiple of 4)
+    int cinv_off;        // shared-memory float offset of the dense inverse, -1: read it from global
+    int rv_off[kMgMaxLevels];   // per small level: per-cell 1 / dV, then 1 / diag
+    int tab_off[kMgMaxLevels];  // ... its axis tables (per axis cm, cp, sum, w, 1 / w)
+    int off[kMgMaxLevels];      // ... its x, then b (not part of the image)
     MgLevel lev[kMgMaxLevels];
 };
 struct Mg {
     int nlev = 0, first_small = 0;
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
+    int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve
     float *cinv = nullptr;
     bool usable = false;
     int *never = nullptr;  // a device flag that stays 0 (the ungated V-cycle)
+    int small_smem = 0;    // dynamic shared memory of the small-level kernel (bytes)
+    bool cinv_smem = false;  // the dense inverse is staged in that shared memory
+    float *image = nullptr;  // static part of that shared memory (inverse, per-cell and axis tables)
+    int image_floats = 0;
     MgLevel lev[kMgMaxLevels];
 };
 

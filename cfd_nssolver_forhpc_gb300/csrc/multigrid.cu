@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "context.h"
@@ -37,7 +38,8 @@ using namespace cfd;
 namespace {
 
 constexpr int kSmallThreads = 1024;
-constexpr int kMgCoarsest = 256;  // cells of the coarsest level at most (dense inverse)
+constexpr int kMgCoarsest = 256;     // cells of the coarsest level at most (dense inverse)
+constexpr int kMgCoarseTarget = 64;  // coarsening goes on while a level has more cells and an axis halves
 
 inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
@@ -50,76 +52,185 @@ __device__ __forceinline__ void decomp(const MgLevel &L, long long t, int &i, in
     k = (int)(r - jj * (unsigned)L.nz);
 }
 
-// the neighbour sum of L at (i, j, k), cell t
-__device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict__ x, int i, int j, int k, long long t)
+// table loads: read-only global loads for the grid-wide kernels, plain
+// loads where the small-level kernel has staged the tables in shared memory
+template <bool SM>
+__device__ __forceinline__ float tl(const float *p)
 {
-    const long long sx = (long long)L.ny * L.nz, sy = L.nz;
+    if constexpr (SM) return *p;
+    else return __ldg(p);
+}
+template <bool SM>
+__device__ __forceinline__ float4 tl4(const float *p)
+{
+    if constexpr (SM) return *reinterpret_cast<const float4 *>(p);
+    else return __ldg(reinterpret_cast<const float4 *>(p));
+}
+
+// index type: 32-bit inside the small-level kernel's shared memory
+template <bool SM>
+using Ix = std::conditional_t<SM, int, long long>;
+
+// the neighbour sum of L at (i, j, k), cell t
+template <bool SM = false>
+__device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict__ x, int i, int j, int k, Ix<SM> t)
+{
+    const Ix<SM> sx = (Ix<SM>)L.ny * L.nz, sy = L.nz;
     float s = 0.f;
-    if (i > 0) s = fmaf(__ldg(L.cm[0] + i), x[t - sx], s);
-    if (i < L.nx - 1) s = fmaf(__ldg(L.cp[0] + i), x[t + sx], s);
-    if (j > 0) s = fmaf(__ldg(L.cm[1] + j), x[t - sy], s);
-    if (j < L.ny - 1) s = fmaf(__ldg(L.cp[1] + j), x[t + sy], s);
-    if (k > 0) s = fmaf(__ldg(L.cm[2] + k), x[t - 1], s);
-    if (k < L.nz - 1) s = fmaf(__ldg(L.cp[2] + k), x[t + 1], s);
+    if (i > 0) s = fmaf(tl<SM>(L.cm[0] + i), x[t - sx], s);
+    if (i < L.nx - 1) s = fmaf(tl<SM>(L.cp[0] + i), x[t + sx], s);
+    if (j > 0) s = fmaf(tl<SM>(L.cm[1] + j), x[t - sy], s);
+    if (j < L.ny - 1) s = fmaf(tl<SM>(L.cp[1] + j), x[t + sy], s);
+    if (k > 0) s = fmaf(tl<SM>(L.cm[2] + k), x[t - 1], s);
+    if (k < L.nz - 1) s = fmaf(tl<SM>(L.cp[2] + k), x[t + 1], s);
     return s;
 }
 
+template <bool SM = false>
 __device__ __forceinline__ float mg_diag(const MgLevel &L, int i, int j, int k)
 {
-    return __ldg(L.sum[0] + i) + __ldg(L.sum[1] + j) + __ldg(L.sum[2] + k);
+    return tl<SM>(L.sum[0] + i) + tl<SM>(L.sum[1] + j) + tl<SM>(L.sum[2] + k);
 }
 
+template <bool SM = false>
 __device__ __forceinline__ float mg_rdv(const MgLevel &L, int i, int j, int k)
 {
-    return __ldg(L.rw[0] + i) * __ldg(L.rw[1] + j) * __ldg(L.rw[2] + k);
+    return tl<SM>(L.rw[0] + i) * tl<SM>(L.rw[1] + j) * tl<SM>(L.rw[2] + k);
 }
 
-// Gauss-Seidel update of one cell: x = (b / dV + neighbours) / diag
+// Gauss-Seidel update of one cell: x = (b / dV + neighbours) / diag; the
+// small-level kernel reads 1 / dV and 1 / diag from its per-cell tables
+// (the same values, computed once by k_mg_cell_tables)
+template <bool SM = false>
 __device__ __forceinline__ void gs_cell(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x, int i,
-                                        int j, int k, long long t, bool zero_init)
+                                        int j, int k, Ix<SM> t, bool zero_init)
 {
-    const float nb = zero_init ? 0.f : mg_nb(L, x, i, j, k, t);
-    x[t] = fmaf(b[t], mg_rdv(L, i, j, k), nb) * __frcp_rn(mg_diag(L, i, j, k));
+    const float nb = zero_init ? 0.f : mg_nb<SM>(L, x, i, j, k, t);
+    if constexpr (SM) x[t] = fmaf(b[t], L.rv[t], nb) * L.rg[t];
+    else x[t] = fmaf(b[t], mg_rdv<SM>(L, i, j, k), nb) * __frcp_rn(mg_diag<SM>(L, i, j, k));
+}
+
+// one colour over a level with nz % 4 == 0: one thread per quad of cells
+// k = 4m..4m+3 (float4 rows), updating the two cells of that colour
+template <bool SM = false>
+__device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
+                                             int color, bool zero_init, Ix<SM> t0, Ix<SM> stride)
+{
+    const Ix<SM> nq = L.n >> 2;
+    const int n4 = L.nz >> 2;
+    const Ix<SM> sx = (Ix<SM>)L.ny * L.nz, sy = L.nz;
+    for (Ix<SM> q = t0; q < nq; q += stride) {
+        const unsigned u = (unsigned)q;
+        const unsigned i = L.fyq.div(u), r = u - i * (unsigned)(L.ny * n4), j = L.fq.div(r);
+        const int k0 = 4 * (int)(r - j * (unsigned)n4);
+        const Ix<SM> t = ((Ix<SM>)i * L.ny + j) * L.nz + k0;
+        const int e0 = (int)((color + i + j) & 1u);  // first updated cell of the quad: e0, then e0 + 2
+        const bool odd = e0 != 0;
+        // the two cells of the colour sit at quad offsets e0 and e0 + 2:
+        // pick their per-cell values with selects (no local arrays)
+        auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+        const float4 bv = *reinterpret_cast<const float4 *>(b + t);
+        const float bA = pick(bv.x, bv.y), bB = pick(bv.z, bv.w);
+        float rA, rB, dA, dB;
+        if constexpr (SM) {
+            const float4 rv = *reinterpret_cast<const float4 *>(L.rv + t);
+            const float4 rg = *reinterpret_cast<const float4 *>(L.rg + t);
+            rA = pick(rv.x, rv.y);
+            rB = pick(rv.z, rv.w);
+            dA = pick(rg.x, rg.y);
+            dB = pick(rg.z, rg.w);
+        } else {
+            const float rxy = tl<SM>(L.rw[0] + i) * tl<SM>(L.rw[1] + j);
+            const float sxy = tl<SM>(L.sum[0] + i) + tl<SM>(L.sum[1] + j);
+            const float4 rz = tl4<SM>(L.rw[2] + k0);
+            const float4 sz = tl4<SM>(L.sum[2] + k0);
+            rA = rxy * pick(rz.x, rz.y);
+            rB = rxy * pick(rz.z, rz.w);
+            dA = __frcp_rn(sxy + pick(sz.x, sz.y));
+            dB = __frcp_rn(sxy + pick(sz.z, sz.w));
+        }
+        float4 xc = make_float4(0.f, 0.f, 0.f, 0.f);
+        float nA = 0.f, nB = 0.f;
+        if (!zero_init) {
+            xc = *reinterpret_cast<const float4 *>(x + t);
+            float4 xm = make_float4(0.f, 0.f, 0.f, 0.f), xp = xm, ym = xm, yp = xm;
+            if (i > 0) xm = *reinterpret_cast<const float4 *>(x + t - sx);
+            if ((int)i < L.nx - 1) xp = *reinterpret_cast<const float4 *>(x + t + sx);
+            if (j > 0) ym = *reinterpret_cast<const float4 *>(x + t - sy);
+            if ((int)j < L.ny - 1) yp = *reinterpret_cast<const float4 *>(x + t + sy);
+            const float zlo = k0 > 0 ? x[t - 1] : 0.f, zhi = k0 + 4 < L.nz ? x[t + 4] : 0.f;
+            const float cxm = tl<SM>(L.cm[0] + i), cxp = tl<SM>(L.cp[0] + i);
+            const float cym = tl<SM>(L.cm[1] + j), cyp = tl<SM>(L.cp[1] + j);
+            const float4 czm = tl4<SM>(L.cm[2] + k0);
+            const float4 czp = tl4<SM>(L.cp[2] + k0);
+            // cell A = e0: k-neighbours (zlo | x0, x1 | x2); cell B = e0 + 2: (x1 | x2, x3 | zhi)
+            nA = cxm * pick(xm.x, xm.y);
+            nA = fmaf(cxp, pick(xp.x, xp.y), nA);
+            nA = fmaf(cym, pick(ym.x, ym.y), nA);
+            nA = fmaf(cyp, pick(yp.x, yp.y), nA);
+            nA = fmaf(pick(czm.x, czm.y), pick(zlo, xc.x), nA);
+            nA = fmaf(pick(czp.x, czp.y), pick(xc.y, xc.z), nA);
+            nB = cxm * pick(xm.z, xm.w);
+            nB = fmaf(cxp, pick(xp.z, xp.w), nB);
+            nB = fmaf(cym, pick(ym.z, ym.w), nB);
+            nB = fmaf(cyp, pick(yp.z, yp.w), nB);
+            nB = fmaf(pick(czm.z, czm.w), pick(xc.y, xc.z), nB);
+            nB = fmaf(pick(czp.z, czp.w), pick(xc.w, zhi), nB);
+        }
+        const float vA = fmaf(bA, rA, nA) * dA, vB = fmaf(bB, rB, nB) * dB;
+        float xo[4];
+        xo[0] = odd ? xc.x : vA;
+        xo[1] = odd ? vA : xc.y;
+        xo[2] = odd ? xc.z : vB;
+        xo[3] = odd ? vB : xc.w;
+        *reinterpret_cast<float4 *>(x + t) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+    }
 }
 
 // one colour over the level: pairs (k = 2m, 2m + 1) when nz is even (one
 // thread per pair updates the cell of that colour), single cells otherwise;
 // zero_init starts from x = 0 (the other colour written as 0)
+template <bool SM = false>
 __device__ __forceinline__ void smooth_level(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
-                                             int color, bool zero_init, long long t0, long long stride)
+                                             int color, bool zero_init, Ix<SM> t0, Ix<SM> stride)
 {
     if ((L.nz & 1) == 0) {
-        const long long np = L.n >> 1;
+        const Ix<SM> np = L.n >> 1;
         const int nh = L.nz >> 1;
-        for (long long q = t0; q < np; q += stride) {
+        for (Ix<SM> q = t0; q < np; q += stride) {
             const unsigned u = (unsigned)q;
             const unsigned i = L.fyh.div(u), r = u - i * (unsigned)(L.ny * nh), j = L.fh.div(r);
             const int m = (int)(r - j * (unsigned)nh);
             const int k = 2 * m + (int)((color + i + j) & 1u);
-            const long long t = ((long long)i * L.ny + j) * L.nz + k;
-            gs_cell(L, b, x, (int)i, (int)j, k, t, zero_init);
+            const Ix<SM> t = ((Ix<SM>)i * L.ny + j) * L.nz + k;
+            gs_cell<SM>(L, b, x, (int)i, (int)j, k, t, zero_init);
             if (zero_init) x[t + ((k & 1) ? -1 : 1)] = 0.f;
         }
         return;
     }
-    for (long long t = t0; t < L.n; t += stride) {
+    for (Ix<SM> t = t0; t < L.n; t += stride) {
         int i, j, k;
         decomp(L, t, i, j, k);
         if (((i + j + k) & 1) != color) {
             if (zero_init) x[t] = 0.f;
             continue;
         }
-        gs_cell(L, b, x, i, j, k, t, zero_init);
+        gs_cell<SM>(L, b, x, i, j, k, t, zero_init);
     }
 }
 
-// coarse b = sum over the children of (b - M x) on the fine level
+// coarse b = sum over the children of (b - M x) on the fine level.  The
+// restriction follows a pre-smoothing that ends with colour 1, after which
+// the residual of every colour-1 cell is zero (its Gauss-Seidel equation
+// holds exactly for the colour-0 values around it, none of which changed
+// since), so only the colour-0 children are summed.
+template <bool SM = false>
 __device__ __forceinline__ void restrict_level(const MgLevel &F, const MgLevel &C, const float *__restrict__ bf,
-                                               const float *__restrict__ xf, float *__restrict__ bc, long long t0,
-                                               long long stride)
+                                               const float *__restrict__ xf, float *__restrict__ bc, Ix<SM> t0,
+                                               Ix<SM> stride)
 {
     const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
-    for (long long T = t0; T < C.n; T += stride) {
+    for (Ix<SM> T = t0; T < C.n; T += stride) {
         int I, J, K;
         decomp(C, T, I, J, K);
         float s = 0.f;
@@ -127,28 +238,41 @@ __device__ __forceinline__ void restrict_level(const MgLevel &F, const MgLevel &
             for (int b2 = 0; b2 < fy; ++b2)
                 for (int c = 0; c < fz; ++c) {
                     const int i = fx * I + a, j = fy * J + b2, k = fz * K + c;
-                    const long long t = ((long long)i * F.ny + j) * F.nz + k;
-                    const float dv = __ldg(F.w[0] + i) * __ldg(F.w[1] + j) * __ldg(F.w[2] + k);
-                    s += bf[t] - dv * (mg_diag(F, i, j, k) * xf[t] - mg_nb(F, xf, i, j, k, t));
+                    if ((i + j + k) & 1) continue;
+                    const Ix<SM> t = ((Ix<SM>)i * F.ny + j) * F.nz + k;
+                    const float dv = tl<SM>(F.w[0] + i) * tl<SM>(F.w[1] + j) * tl<SM>(F.w[2] + k);
+                    s += bf[t] - dv * (mg_diag<SM>(F, i, j, k) * xf[t] - mg_nb<SM>(F, xf, i, j, k, t));
                 }
         bc[T] = s;
     }
 }
 
 // fine x += coarse x: one thread per coarse cell writes its children
+template <bool SM = false>
 __device__ __forceinline__ void prolong_level(const MgLevel &F, const MgLevel &C, const float *__restrict__ xc,
-                                              float *__restrict__ xf, long long t0, long long stride)
+                                              float *__restrict__ xf, Ix<SM> t0, Ix<SM> stride)
 {
     const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
-    for (long long T = t0; T < C.n; T += stride) {
+    for (Ix<SM> T = t0; T < C.n; T += stride) {
         int I, J, K;
         decomp(C, T, I, J, K);
         const float v = xc[T];
         for (int a = 0; a < fx; ++a)
             for (int b2 = 0; b2 < fy; ++b2) {
-                const long long base = ((long long)(fx * I + a) * F.ny + fy * J + b2) * F.nz + fz * K;
+                const Ix<SM> base = ((Ix<SM>)(fx * I + a) * F.ny + fy * J + b2) * F.nz + fz * K;
                 for (int c = 0; c < fz; ++c) xf[base + c] += v;
             }
+    }
+}
+
+// per-cell 1 / dV and 1 / diag of a level (for the small-level kernel)
+__global__ void k_mg_cell_tables(MgLevel L, float *__restrict__ rv, float *__restrict__ rg)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < L.n; t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        decomp(L, t, i, j, k);
+        rv[t] = mg_rdv(L, i, j, k);
+        rg[t] = __frcp_rn(mg_diag(L, i, j, k));
     }
 }
 
@@ -156,8 +280,12 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b,
                                                       const int *done)
 {
     if (*done) return;
-    smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
-                 (long long)gridDim.x * blockDim.x);
+    if (L.quads)
+        smooth_quads(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                     (long long)gridDim.x * blockDim.x);
+    else
+        smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                     (long long)gridDim.x * blockDim.x);
 }
 
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, const float *bf, const float *xf,
@@ -175,58 +303,124 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevel F, MgLevel C, con
     prolong_level(F, C, xc, xf, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
+// a small level's x and b in shared memory, each rounded up to 4 floats so
+// the float4 smoother's rows stay 16-byte aligned
+__host__ __device__ inline long long small_pad(long long n) { return (n + 3) & ~3LL; }
+
+static_assert(kSmallThreads == 4 * kMgCoarsest, "coarsest product: 4 threads per row");
+
+// level l of the small sub-cycle as seen in shared memory: x, b, the
+// per-cell and the axis tables redirected to their staged copies
+__device__ __forceinline__ MgLevel small_view(const MgSmall &S, float *sm, int l)
+{
+    MgLevel L = S.lev[l];
+    float *p = sm + S.tab_off[l];
+    const int dims[3] = {L.nx, L.ny, L.nz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int m = (int)small_pad(dims[a]);
+        L.cm[a] = p;
+        L.cp[a] = p + m;
+        L.sum[a] = p + 2 * m;
+        L.w[a] = p + 3 * m;
+        L.rw[a] = p + 4 * m;
+        p += 5 * m;
+    }
+    L.rv = sm + S.rv_off[l];
+    L.rg = L.rv + small_pad(L.n);
+    L.x = sm + S.off[l];
+    L.b = L.x + small_pad(L.n);
+    return L;
+}
+
 // the whole sub-cycle of levels first..nlev-1 (nlev-1 the coarsest) in one
-// block: pre-smooth and restrict down, solve the coarsest, prolong and
-// post-smooth up; block barriers between the phases
+// block, in shared memory: copy in the static image (dense inverse, per-cell
+// and axis tables; asynchronous 16-byte copies) and the first small level's
+// b; pre-smooth and restrict down, solve the coarsest, prolong and
+// post-smooth up; store the first small level's x.  Block barriers separate
+// the phases.
 __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 {
     if (*S.done) return;
-    const long long t0 = threadIdx.x, st = blockDim.x;
+    extern __shared__ float4 small_sm4[];
+    float *sm = reinterpret_cast<float *>(small_sm4);
+    __shared__ float red[kSmallThreads / 32];
+    __shared__ float part[4][kMgCoarsest];
+    const int t0 = threadIdx.x, st = blockDim.x;
     const int first = S.first, last = S.nlev;
+    const int nc = (int)S.lev[last - 1].n;
+    {
+        const unsigned base = (unsigned)__cvta_generic_to_shared(sm);
+        for (int q = t0; q < (S.image_floats >> 2); q += st)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(base + 16u * q), "l"(S.image + 4 * q)
+                         : "memory");
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        const MgLevel &G = S.lev[first];
+        float *b = sm + S.off[first] + small_pad(G.n);
+        for (int t = t0; t < (int)G.n; t += st) b[t] = G.b[t];
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+    }
     for (int l = first; l < last - 1; ++l) {
-        const MgLevel &L = S.lev[l];
+        const MgLevel L = small_view(S, sm, l);
         for (int s = 0; s < S.pre; ++s) {
-            smooth_level(L, L.b, L.x, 0, s == 0, t0, st);
+            if (L.quads) smooth_quads<true>(L, L.b, L.x, 0, s == 0, t0, st);
+            else smooth_level<true>(L, L.b, L.x, 0, s == 0, t0, st);
             __syncthreads();
-            smooth_level(L, L.b, L.x, 1, false, t0, st);
+            if (L.quads) smooth_quads<true>(L, L.b, L.x, 1, false, t0, st);
+            else smooth_level<true>(L, L.b, L.x, 1, false, t0, st);
             __syncthreads();
         }
-        restrict_level(L, S.lev[l + 1], L.b, L.x, S.lev[l + 1].b, t0, st);
+        const MgLevel C = small_view(S, sm, l + 1);
+        restrict_level<true>(L, C, L.b, L.x, C.b, t0, st);
         __syncthreads();
     }
     {
-        // coarsest: x = (M + a 1 1^T)^-1 (b - mean b)
-        const MgLevel &L = S.lev[last - 1];
-        __shared__ float red[kSmallThreads / 32];
-        __shared__ float bs[kMgCoarsest];
+        // coarsest: x = C (b - mean b), C = (M + a 1 1^T)^-1 symmetric, so
+        // thread r sums column r over a quarter of the rows
+        const MgLevel L = small_view(S, sm, last - 1);
         float s = 0.f;
-        for (long long t = t0; t < L.n; t += st) s += L.b[t];
+        for (int t = t0; t < nc; t += st) s += L.b[t];
         for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
         __syncthreads();
         float tot = 0.f;
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += red[q];
-        const float mean = tot / (float)L.n;
-        for (long long t = t0; t < L.n; t += st) bs[t] = L.b[t] - mean;
-        __syncthreads();
-        for (long long r = t0; r < L.n; r += st) {
-            const float *row = S.cinv + r * L.n;
-            float a = 0.f;
-            for (long long cidx = 0; cidx < L.n; ++cidx) a = fmaf(__ldg(row + cidx), bs[cidx], a);
-            L.x[r] = a;
+        const float mean = tot / (float)nc;
+        const int r = threadIdx.x % kMgCoarsest, q4 = threadIdx.x / kMgCoarsest;
+        float acc = 0.f;
+        if (r < nc) {
+            if (S.cinv_off >= 0) {
+                const float *cs = sm + S.cinv_off;
+                for (int cidx = q4; cidx < nc; cidx += 4) acc = fmaf(cs[cidx * nc + r], L.b[cidx] - mean, acc);
+            } else {
+                for (int cidx = q4; cidx < nc; cidx += 4)
+                    acc = fmaf(__ldg(S.cinv + (long long)cidx * nc + r), L.b[cidx] - mean, acc);
+            }
         }
+        part[q4][r] = acc;
+        __syncthreads();
+        if (threadIdx.x < nc)
+            L.x[threadIdx.x] = (part[0][threadIdx.x] + part[1][threadIdx.x]) + (part[2][threadIdx.x] + part[3][threadIdx.x]);
         __syncthreads();
     }
     for (int l = last - 2; l >= first; --l) {
-        const MgLevel &L = S.lev[l];
-        prolong_level(L, S.lev[l + 1], S.lev[l + 1].x, L.x, t0, st);
+        const MgLevel L = small_view(S, sm, l);
+        prolong_level<true>(L, S.lev[l + 1], small_view(S, sm, l + 1).x, L.x, t0, st);
         __syncthreads();
         for (int s = 0; s < S.post; ++s) {
-            smooth_level(L, L.b, L.x, 1, false, t0, st);
+            if (L.quads) smooth_quads<true>(L, L.b, L.x, 1, false, t0, st);
+            else smooth_level<true>(L, L.b, L.x, 1, false, t0, st);
             __syncthreads();
-            smooth_level(L, L.b, L.x, 0, false, t0, st);
+            if (L.quads) smooth_quads<true>(L, L.b, L.x, 0, false, t0, st);
+            else smooth_level<true>(L, L.b, L.x, 0, false, t0, st);
             __syncthreads();
         }
+    }
+    {
+        const MgLevel &G = S.lev[first];
+        const float *x = sm + S.off[first];
+        for (int t = t0; t < (int)G.n; t += st) G.x[t] = x[t];
     }
 }
 
@@ -328,6 +522,12 @@ void set_divs(MgLevel &L)
     const int nh = L.nz / 2 > 0 ? L.nz / 2 : 1;
     L.fyh = FastDiv((unsigned)(L.ny * nh));
     L.fh = FastDiv((unsigned)nh);
+    const int nq = L.nz / 4 > 0 ? L.nz / 4 : 1;
+    L.fyq = FastDiv((unsigned)(L.ny * nq));
+    L.fq = FastDiv((unsigned)nq);
+    // float4 rows need nz % 4 == 0 and 16-byte aligned z-axis tables
+    auto al = [](const void *p) { return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0; };
+    L.quads = L.nz % 4 == 0 && al(L.x) && al(L.b) && al(L.rw[2]) && al(L.sum[2]) && al(L.cm[2]) && al(L.cp[2]);
 }
 
 // dense (M + a 1 1^T)^-1 of a level given its per-axis widths (Gauss-Jordan
@@ -386,9 +586,67 @@ int coarse_inverse(cfd_ctx *c, const std::vector<double> (&W)[3], float **out)
             }
         }
     }
-    std::vector<float> f(I.begin(), I.end());
+    // exact symmetry in float (the device product reads columns for rows)
+    std::vector<float> f((size_t)small_pad((long long)n * n), 0.f);  // padded to whole 16-byte chunks
+    for (int r = 0; r < n; ++r)
+        for (int q = 0; q < n; ++q) f[(size_t)r * n + q] = (float)(0.5 * (I[(size_t)r * n + q] + I[(size_t)q * n + r]));
     CKS(dalloc_t(c, out, f.size()));
     CK(cudaMemcpy(*out, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return CFD_OK;
+}
+
+// shared-memory layout of the small kernel from level `first` on.  The
+// static image first: the dense inverse (when staged), then per level the
+// per-cell 1 / dV and 1 / diag and the axis tables; after it per level x and
+// b.  Every piece is a multiple of 4 floats.  Returns the size in bytes.
+long long small_layout(const Mg &G, int first, bool cinv, MgSmall *S)
+{
+    long long off = 0;
+    const long long nc = G.lev[G.nlev - 1].n;
+    if (S) S->cinv_off = cinv ? 0 : -1;
+    if (cinv) off += small_pad(nc * nc);
+    for (int l = first; l < G.nlev; ++l) {
+        const MgLevel &L = G.lev[l];
+        if (S) S->rv_off[l] = (int)off;
+        off += 2 * small_pad(L.n);
+        if (S) S->tab_off[l] = (int)off;
+        off += 5 * (small_pad(L.nx) + small_pad(L.ny) + small_pad(L.nz));
+    }
+    if (S) S->image_floats = (int)off;
+    for (int l = first; l < G.nlev; ++l) {
+        if (S) S->off[l] = (int)off;
+        off += 2 * small_pad(G.lev[l].n);
+    }
+    return off * (long long)sizeof(float);
+}
+
+// the static image of the small kernel's shared memory, in device memory
+int small_image(cfd_ctx *c, Mg &G)
+{
+    MgSmall S{};
+    small_layout(G, G.first_small, G.cinv_smem, &S);
+    G.image_floats = S.image_floats;
+    CKS(dalloc_t(c, &G.image, (size_t)S.image_floats));
+    CK(cudaMemset(G.image, 0, (size_t)S.image_floats * sizeof(float)));
+    const long long nc = G.lev[G.nlev - 1].n;
+    if (G.cinv_smem)
+        CK(cudaMemcpy(G.image + S.cinv_off, G.cinv, (size_t)(nc * nc) * sizeof(float), cudaMemcpyDeviceToDevice));
+    for (int l = G.first_small; l < G.nlev; ++l) {
+        const MgLevel &L = G.lev[l];
+        float *rv = G.image + S.rv_off[l];
+        k_mg_cell_tables<<<nblk(L.n), kBlock, 0, c->s>>>(L, rv, rv + small_pad(L.n));
+        CK(cudaGetLastError());
+        float *p = G.image + S.tab_off[l];
+        const int dims[3] = {L.nx, L.ny, L.nz};
+        for (int a = 0; a < 3; ++a) {
+            const int m = (int)small_pad(dims[a]);
+            const float *src[5] = {L.cm[a], L.cp[a], L.sum[a], L.w[a], L.rw[a]};
+            for (int q = 0; q < 5; ++q)
+                CK(cudaMemcpy(p + q * m, src[q], (size_t)dims[a] * sizeof(float), cudaMemcpyDeviceToDevice));
+            p += 5 * m;
+        }
+    }
+    CK(cudaStreamSynchronize(c->s));
     return CFD_OK;
 }
 
@@ -403,6 +661,7 @@ int mg_setup(cfd_ctx *c)
     if (G.nlev > 0) return CFD_OK;
     const Geo &g = c->g;
     if (const char *e = std::getenv("CFDGPU_MG_SWEEPS")) G.sweeps = std::atoi(e) > 0 ? std::atoi(e) : 2;
+    if (const char *e = std::getenv("CFDGPU_MG_PAIRS")) G.pairs = std::atoi(e) > 0 ? std::atoi(e) : 1;
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
     const FvOp<float> F = fv32(c);
@@ -431,7 +690,7 @@ int mg_setup(cfd_ctx *c)
     G.lev[0] = L0;
     int nl = 1;
     int n[3] = {g.nxc, g.nyc, g.nzc};
-    while (nl < kMgMaxLevels && (long long)n[0] * n[1] * n[2] > kMgCoarsest) {
+    while (nl < kMgMaxLevels && (long long)n[0] * n[1] * n[2] > kMgCoarseTarget) {
         int f[3];
         bool any = false;
         for (int a = 0; a < 3; ++a) {
@@ -449,9 +708,9 @@ int mg_setup(cfd_ctx *c)
         }
         L.nx = n[0]; L.ny = n[1]; L.nz = n[2];
         L.n = (long long)n[0] * n[1] * n[2];
-        set_divs(L);
         CKS(dalloc_t(c, &L.x, (size_t)L.n));
         CKS(dalloc_t(c, &L.b, (size_t)L.n));
+        set_divs(L);
         G.lev[nl++] = L;
     }
     G.nlev = nl;
@@ -459,12 +718,20 @@ int mg_setup(cfd_ctx *c)
     G.usable = nl > 1 && ncoarse <= kMgCoarsest;
     if (!G.usable) return CFD_OK;
     CKS(coarse_inverse(c, W, &G.cinv));
+    // the first small level: at most `small` cells, and all levels from it
+    // on fit the small kernel's shared memory; the dense inverse is staged
+    // there too when it fits
     G.first_small = nl - 1;
     for (int l = 0; l < nl; ++l)
-        if (G.lev[l].n <= small) {
+        if (G.lev[l].n <= small && small_layout(G, l, false, nullptr) <= kMgSmallSmem) {
             G.first_small = l;
             break;
         }
+    G.cinv_smem = small_layout(G, G.first_small, true, nullptr) <= kMgSmallSmem;
+    G.small_smem = (int)small_layout(G, G.first_small, G.cinv_smem, nullptr);
+    if (G.small_smem > kMgSmallSmem) return fail(CFD_ERR_STATE, "multigrid: coarsest level too large for shared memory");
+    CK(cudaFuncSetAttribute(k_mg_small, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
+    CKS(small_image(c, G));
     CKS(dalloc_t(c, &G.never, 1));
     CK(cudaMemset(G.never, 0, sizeof(int)));
     return CFD_OK;
@@ -479,7 +746,9 @@ static MgSmall small_desc(const Mg &G, const int *done)
     S.pre = G.sweeps;
     S.post = G.sweeps;
     S.cinv = G.cinv;
+    S.image = G.image;
     for (int l = 0; l < G.nlev; ++l) S.lev[l] = G.lev[l];
+    small_layout(G, G.first_small, G.cinv_smem, &S);
     return S;
 }
 
@@ -491,17 +760,17 @@ void mg_vcycle(cfd_ctx *c, const int *done)
     const int fs = G.first_small;
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
-        const long long work = (L.nz % 2 == 0) ? L.n / 2 : L.n;
+        const long long work = L.quads ? L.n / 4 : (L.nz % 2 == 0) ? L.n / 2 : L.n;
         for (int q = 0; q < G.sweeps; ++q) {
             k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, q == 0, done);
             k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
         }
         k_mg_restrict<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], L.b, L.x, G.lev[l + 1].b, done);
     }
-    k_mg_small<<<1, kSmallThreads, 0, s>>>(small_desc(G, done));
+    k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
-        const long long work = (L.nz % 2 == 0) ? L.n / 2 : L.n;
+        const long long work = L.quads ? L.n / 4 : (L.nz % 2 == 0) ? L.n / 2 : L.n;
         k_mg_prolong<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], G.lev[l + 1].x, L.x, done);
         for (int q = 0; q < G.sweeps; ++q) {
             k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
@@ -519,11 +788,11 @@ void mg_time_part(cfd_ctx *c, int part)
     const cudaStream_t s = c->s;
     const MgLevel &L = G.lev[0];
     const int *done = G.never;
-    const long long work = (L.nz % 2 == 0) ? L.n / 2 : L.n;
+    const long long work = L.quads ? L.n / 4 : (L.nz % 2 == 0) ? L.n / 2 : L.n;
     if (part == 0) k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, 0, done);
     else if (part == 1) k_mg_restrict<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], L.b, L.x, G.lev[1].b, done);
     else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
-    else if (part == 3) k_mg_small<<<1, kSmallThreads, 0, s>>>(small_desc(G, done));
+    else if (part == 3) k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
     else mg_vcycle(c, done);
 }
 

@@ -1521,6 +1521,21 @@ void launch_sor_sweep(cudaStream_t s, const Geo &g, const Metrics<double> &m, co
 }
 
 // ---------------------------------------------------------------------------
+// Device-side solve loops: the condition of the graph's WHILE node
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, BicgScal *sc, int cap, int first)
+{
+    if (threadIdx.x != 0) return;
+    const int trips = first ? 0 : sc->loop_trips + 1;
+    sc->loop_trips = trips;
+    cudaGraphSetConditional(h, (sc->done == BICG_RUNNING && !sc->wait_timeout && trips < cap) ? 1u : 0u);
+}
+
+void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc, int cap, int first)
+{
+    k_loop_cond<<<1, 32, 0, s>>>(h, sc, cap, first);
+}
+
+// ---------------------------------------------------------------------------
 // Mixed precision: FP64 residual of the scaled system, written as the
 // FP32 right-hand side of the next inner solve, and the FP64 correction.
 template <class Op, class V>
