@@ -267,7 +267,7 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
     return run_pairs(
         c, 4, sc,
         [&] {
-            mg_h(c, h);
+            mg_h(c, h, c->dscal + 3, sc);
             mg_vcycle(c, c->mg.never);
             mg_rho(c, h, z, c->w32.p1, sc);
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
@@ -374,7 +374,9 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
             std::fprintf(stderr, "[cfdgpu] outer %d rel %.3e | inner done %d iter %d relres %.3e norm0 %.3e "
                          "rho %.3e alpha %.3e omega %.3e\n", sweeps, rel, c->h_sc->done, c->h_sc->iter,
                          c->h_sc->relres, c->h_sc->norm0, c->h_sc->rho, c->h_sc->alpha, c->h_sc->omega);
-        launch_correct<float>(c->lc, n, x, c->e32);
+        // the multigrid-CG solved for r / |r|
+        const bool scaled = inner == CFD_INNER_MG && c->mg.usable && std::is_same<Op32, SpeOp<float>>::value;
+        launch_correct<float>(c->lc, n, x, c->e32, scaled ? &c->sc_in->rhs_scale : nullptr);
         c->launches += 1;
         CK(cudaGetLastError());
         ++sweeps;

@@ -57,10 +57,10 @@ int ensure_fp32_solver(cfd_ctx *c);
 // multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
 int mg_setup(cfd_ctx *c);
 void mg_vcycle(cfd_ctx *c, const int *done);
-void mg_h(cfd_ctx *c, float *h);
+void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc);
 void mg_time_part(cfd_ctx *c, int part);
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc);
 // adjoint_api.cu: releases the host side of the adjoint state
 void adj_free(AdjState *a);
 
@@ -293,38 +293,5 @@ inline int check_slot(int slot)
     if (slot_index(slot) < 0) return fail(CFD_ERR_ARG, "velocity slot must be 0 (T0), 1 (T1) or 3 (T3)");
     return CFD_OK;
 }
-
-
-// api.cu: the forward step with an optional tape, the CG-based linear solve
-// with caller buffers, FP32 solver tables on demand
-int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec);
-int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
-                    int *outer);
-int ensure_fp32_solver(cfd_ctx *c);
-// multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
-int mg_setup(cfd_ctx *c);
-void mg_vcycle(cfd_ctx *c, const int *done);
-void mg_h(cfd_ctx *c, float *h);
-void mg_time_part(cfd_ctx *c, int part);
-void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
-// adjoint_api.cu: releases the host side of the adjoint state
-void adj_free(AdjState *a);
-
-// api.cu: the forward step with an optional tape, the CG-based linear solve
-// with caller buffers, FP32 solver tables on demand
-int step_recorded(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec);
-int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, int *iters, double *relres,
-                    int *outer);
-int ensure_fp32_solver(cfd_ctx *c);
-// multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
-int mg_setup(cfd_ctx *c);
-void mg_vcycle(cfd_ctx *c, const int *done);
-void mg_h(cfd_ctx *c, float *h);
-void mg_time_part(cfd_ctx *c, int part);
-void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc);
-// adjoint_api.cu: releases the host side of the adjoint state
-void adj_free(AdjState *a);
 
 }  // namespace cfd

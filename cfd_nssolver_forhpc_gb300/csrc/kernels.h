@@ -120,6 +120,7 @@ struct BicgScal {
     int iter, done, restart, timestep, maxit, restarts, total_iters, nonfinite;
     int wait_timeout;  // a bounded device wait (TMA pipeline) gave up
     int loop_trips;    // body runs of the solve's device-side loop (graph WHILE node)
+    double rhs_scale;  // the multigrid-CG solves for rhs / rhs_scale; the correction multiplies back
 };
 enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
 
@@ -216,7 +217,7 @@ template <class V>
 void launch_residual64_ell(cfd_launch_ctx &c, const EllOp<double> &A, const double *b,
                            const double *x, V *r32, double *norm2_out);
 template <class V>
-void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e);
+void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e, const double *scale = nullptr);
 
 
 // monitors (flow.cu): out[7] = {max c, max u, -min u, max v, -min v, max w, -min w}

@@ -280,12 +280,17 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b,
                                                       const int *done)
 {
     if (*done) return;
-    if (L.quads)
-        smooth_quads(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
-                     (long long)gridDim.x * blockDim.x);
-    else
-        smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
-                     (long long)gridDim.x * blockDim.x);
+    smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                 (long long)gridDim.x * blockDim.x);
+}
+
+// the float4 form (nz % 4 == 0) as its own kernel
+__global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, const float *b, float *x, int color,
+                                                          int zero_init, const int *done)
+{
+    if (*done) return;
+    smooth_quads(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                 (long long)gridDim.x * blockDim.x);
 }
 
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, const float *bf, const float *xf,
@@ -425,19 +430,33 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 }
 
 // ---- CG with the V-cycle preconditioner -------------------------------------
-// h = P r (in place): the Jacobi-scaled residual in the finite-volume form
-__global__ void k_mg_h(FvOp<float> F, float *__restrict__ h)
+// h = P r / |r| (in place): the Jacobi-scaled residual in the finite-volume
+// form, normalised by the FP64 residual norm (rn2 = |r|^2) so the FP32 solve
+// works at unit scale whatever the outer tolerance; sc->rhs_scale = |r| for
+// the correction, sc->r0n2 = |h|^2 for the stopping test
+__global__ void __launch_bounds__(kBlock)
+k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, double *partials, unsigned int *counter)
 {
+    const double nr = (rn2 && *rn2 > 0.0) ? sqrt(*rn2) : 1.0;
+    const float s = (float)(1.0 / nr);
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->rhs_scale = nr;
+    float pa = 0.f;
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < F.A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const int nz = F.A.nzc, nyz = F.A.nyc * F.A.nzc;
         const int i = (int)(row / nyz), r2 = (int)(row - (long long)i * nyz), j = r2 / nz, k = r2 - j * nz;
         const float dv = __ldg(F.wx + i) * (__ldg(F.wy + j) * __ldg(F.wz + k));
-        h[row] = dv * (__ldg(F.sx + i) + (__ldg(F.sy + j) + __ldg(F.sz + k))) * h[row];
+        const float v = dv * (__ldg(F.sx + i) + (__ldg(F.sy + j) + __ldg(F.sz + k))) * (h[row] * s);
+        h[row] = v;
+        pa = fmaf(v, v, pa);
     }
+    double acc[1] = {(double)pa}, tot[1];
+    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->r0n2 = tot[0];
 }
 
 // rho = h . z; with p0 != null also p0 = z and the solve's initial scalars
+// (sc->r0n2 was set by k_mg_h), else beta and the iteration count (the
+// stopping test is in k_mg_upd, before the V-cycle)
 __global__ void __launch_bounds__(kBlock)
 k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, float *__restrict__ p0, BicgScal *sc,
          double *partials, unsigned int *counter)
@@ -453,21 +472,16 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
     if (!grid_reduce<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
     if (p0) {
         sc->rho = tot[0];
-        sc->r0n2 = fabs(tot[0]);
-        sc->norm0 = sqrt(fabs(tot[0]));
+        sc->norm0 = sqrt(sc->r0n2);
         sc->iter = 0;
         sc->restart = 0;
         sc->timestep += 1;
-        sc->done = tot[0] != 0.0 ? BICG_RUNNING : BICG_ZERO_RHS;
-        sc->relres = tot[0] != 0.0 ? 1.0 : 0.0;
+        sc->done = (tot[0] != 0.0 && sc->r0n2 != 0.0) ? BICG_RUNNING : BICG_ZERO_RHS;
+        sc->relres = sc->done == BICG_RUNNING ? 1.0 : 0.0;
         sc->wait_timeout = 0;
         return;
     }
-    const double rel = sqrt(fabs(tot[0]) / sc->r0n2);
-    sc->relres = rel;
-    if (rel < sc->tol) {
-        sc->done = BICG_CONVERGED;
-    } else if (sc->iter >= sc->maxit) {
+    if (sc->iter + 1 >= sc->maxit) {
         sc->done = BICG_CAPPED;
     } else {
         sc->beta = tot[0] / sc->rho;
@@ -477,16 +491,27 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
     }
 }
 
-// e += alpha p, h -= alpha q (no reduction: rho comes after the V-cycle)
-__global__ void __launch_bounds__(kBlock) k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p,
-                                                   float *__restrict__ h, const float *__restrict__ q, const BicgScal *sc)
+// e += alpha p, h -= alpha q and the stopping test on |h| / |h0| (the
+// unpreconditioned residual): a converged solve skips the V-cycle after it
+__global__ void __launch_bounds__(kBlock)
+k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float *__restrict__ h,
+         const float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter)
 {
     if (sc->done) return;
     const float alpha = (float)sc->alpha;
+    float pa = 0.f;
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
         e[r] = fmaf(alpha, p[r], e[r]);
-        h[r] = fmaf(-alpha, q[r], h[r]);
+        const float hv = fmaf(-alpha, q[r], h[r]);
+        h[r] = hv;
+        pa = fmaf(hv, hv, pa);
     }
+    double acc[1] = {(double)pa}, tot[1];
+    if (!grid_reduce<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    const double rel = sqrt(tot[0] / sc->r0n2);
+    sc->relres = rel;
+    if (rel < sc->tol) sc->done = BICG_CONVERGED;
+    else if (!(rel == rel)) sc->done = BICG_CAPPED;
 }
 
 // per-axis device arrays {cm, cp, cm + cp, w, 1/w} of m entries
@@ -752,6 +777,13 @@ static MgSmall small_desc(const Mg &G, const int *done)
     return S;
 }
 
+// one colour of the smoother over a grid-wide level
+static void smooth_launch(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
+{
+    if (L.quads) k_mg_smooth4<<<nblk(L.n / 4), kBlock, 0, s>>>(L, L.b, L.x, color, zero_init, done);
+    else k_mg_smooth<<<nblk((L.nz % 2 == 0) ? L.n / 2 : L.n), kBlock, 0, s>>>(L, L.b, L.x, color, zero_init, done);
+}
+
 // z = V(h): one V-cycle; every kernel returns at once when *done
 void mg_vcycle(cfd_ctx *c, const int *done)
 {
@@ -760,21 +792,19 @@ void mg_vcycle(cfd_ctx *c, const int *done)
     const int fs = G.first_small;
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
-        const long long work = L.quads ? L.n / 4 : (L.nz % 2 == 0) ? L.n / 2 : L.n;
         for (int q = 0; q < G.sweeps; ++q) {
-            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, q == 0, done);
-            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
+            smooth_launch(L, 0, q == 0, done, s);
+            smooth_launch(L, 1, 0, done, s);
         }
         k_mg_restrict<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], L.b, L.x, G.lev[l + 1].b, done);
     }
     k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
-        const long long work = L.quads ? L.n / 4 : (L.nz % 2 == 0) ? L.n / 2 : L.n;
         k_mg_prolong<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], G.lev[l + 1].x, L.x, done);
         for (int q = 0; q < G.sweeps; ++q) {
-            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 1, 0, done);
-            k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, 0, done);
+            smooth_launch(L, 1, 0, done, s);
+            smooth_launch(L, 0, 0, done, s);
         }
     }
     c->launches += (4LL * G.sweeps + 2) * fs + 1;
@@ -788,18 +818,17 @@ void mg_time_part(cfd_ctx *c, int part)
     const cudaStream_t s = c->s;
     const MgLevel &L = G.lev[0];
     const int *done = G.never;
-    const long long work = L.quads ? L.n / 4 : (L.nz % 2 == 0) ? L.n / 2 : L.n;
-    if (part == 0) k_mg_smooth<<<nblk(work), kBlock, 0, s>>>(L, L.b, L.x, 0, 0, done);
+    if (part == 0) smooth_launch(L, 0, 0, done, s);
     else if (part == 1) k_mg_restrict<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], L.b, L.x, G.lev[1].b, done);
     else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
     else if (part == 3) k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
     else mg_vcycle(c, done);
 }
 
-void mg_h(cfd_ctx *c, float *h)
+void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc)
 {
     const FvOp<float> F = fv32(c);
-    k_mg_h<<<blocks_for(F.A.n, c->lc.grid_cap), kBlock, 0, c->s>>>(F, h);
+    k_mg_h<<<c->lc.red_blocks, kBlock, 0, c->s>>>(F, h, rn2, sc, c->lc.partials, c->lc.counter);
 }
 
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc)
@@ -807,9 +836,9 @@ void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc)
     k_mg_rho<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, h, z, p0, sc, c->lc.partials, c->lc.counter);
 }
 
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const BicgScal *sc)
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc)
 {
-    k_mg_upd<<<blocks_for(c->g.n, c->lc.grid_cap), kBlock, 0, c->s>>>(c->g.n, e, p, h, q, sc);
+    k_mg_upd<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, e, p, h, q, sc, c->lc.partials, c->lc.counter);
 }
 
 }  // namespace cfd

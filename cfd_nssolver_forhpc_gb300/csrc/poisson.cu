@@ -1575,18 +1575,20 @@ template void launch_residual64_ell<float>(cfd_launch_ctx &, const EllOp<double>
 
 // x += e (FP64 accumulation of an FP32 correction)
 template <class V>
-__global__ void k_correct(long long n, double *__restrict__ x, const V *__restrict__ e)
+__global__ void k_correct(long long n, double *__restrict__ x, const V *__restrict__ e, const double *scale)
 {
+    const double sc = scale ? *scale : 1.0;
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
          row += (long long)gridDim.x * blockDim.x)
-        x[row] += (double)e[row];
+        x[row] += sc * (double)e[row];
 }
 
+// x += scale e (scale: a device scalar, 1 when null)
 template <class V>
-void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e)
+void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e, const double *scale)
 {
-    k_correct<V><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, e);
+    k_correct<V><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, e, scale);
 }
-template void launch_correct<float>(cfd_launch_ctx &, long long, double *, const float *);
+template void launch_correct<float>(cfd_launch_ctx &, long long, double *, const float *, const double *);
 
 }  // namespace cfd

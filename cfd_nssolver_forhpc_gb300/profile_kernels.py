@@ -8,6 +8,15 @@ step), the Poisson right-hand side of the first predictor pass is formed, and
 then `cfd_time_kernels` launches every hot kernel `reps` times back to back.
 The program is short and its launches are few, which makes it the target of
 the ncu captures summarised under profiles/.
+
+    python -m cfd_nssolver_forhpc_gb300.profile_kernels --workload c2 --precision mixed \
+        --tol 1e-10 --profile-step 3
+
+instead runs 3 untimed steps and then one step between cudaProfilerStart and
+cudaProfilerStop, the window of `ncu --profile-from-start off` (the launch
+list of one whole step).  ncu cannot profile the kernels of graphs with
+conditional nodes, so such a capture sets CFDGPU_SOLVE_LOOP=host: the same
+kernels, with the solve loops polled from the host.
 """
 from __future__ import annotations
 
@@ -26,11 +35,29 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--tol", type=float, default=None, help="Poisson tolerance (default: the workload's)")
+    ap.add_argument("--profile-step", type=int, default=None, metavar="K",
+                    help="run K steps, then one step inside the profiler window")
     a = ap.parse_args(argv)
     w = WORKLOADS[a.workload]
     solver = {"spe": capi.SOLVER_BICG_SPE, "ell": capi.SOLVER_BICG_ELL, "sor": capi.SOLVER_SOR_RB}[a.solver]
     prec = capi.PREC_MIXED if a.precision == "mixed" else capi.PREC_FP64
-    with Simulation(w, solver=solver, precision=prec, tol=w.tol) as S:
+    tol = a.tol if a.tol is not None else w.tol
+    if a.profile_step is not None:
+        import torch  # the profiler window API of the CUDA runtime
+        with Simulation(w, solver=solver, precision=prec, tol=tol) as S:
+            S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+            for _ in range(a.profile_step):
+                S.step()
+            S.sync()
+            torch.cuda.cudart().cudaProfilerStart()
+            info = S.step()
+            S.sync()
+            torch.cuda.cudart().cudaProfilerStop()
+        print(json.dumps({"workload": a.workload, "cells": w.n_cells, "solver": a.solver, "precision": a.precision,
+                          "tol": tol, "warm_steps": a.profile_step, "step": info}))
+        return
+    with Simulation(w, solver=solver, precision=prec, tol=tol) as S:
         S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
         S.step()
         S.ConvectionDifussion(S.T0, S.T1)
