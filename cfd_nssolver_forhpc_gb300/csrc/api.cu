@@ -271,14 +271,14 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
             mg_vcycle(c, c->mg.never);
             mg_rho(c, h, z, c->w32.p1, sc);
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
-            mg_upd(c, e, c->w32.p1, h, q, sc);
+            mg_upd(c, e, c->w32.p1, h, q, z, sc);
             mg_vcycle(c, &sc->done);
             mg_rho(c, h, z, nullptr, sc);
         },
         [&](int from) {
             float *P[2] = {c->w32.p1, c->p_alt};
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, from, false);
-            mg_upd(c, e, P[1 - from], h, q, sc);
+            mg_upd(c, e, P[1 - from], h, q, z, sc);
             mg_vcycle(c, &sc->done);
             mg_rho(c, h, z, nullptr, sc);
         },
@@ -1432,7 +1432,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                         if (!(part < 3 && c->mg.first_small == 0))
                             if ((st = timed(ids[part], [&] { mg_time_part(c, part); })) != CFD_OK) return st;
                     if ((st = timed(CFD_KERNEL_MG_UPD, [&] {
-                             mg_upd(c, c->e32, c->w32.p1, c->r32, c->w32.ap, c->sc_t);
+                             mg_upd(c, c->e32, c->w32.p1, c->r32, c->w32.ap, c->w32.r0, c->sc_t);
                          })) != CFD_OK)
                         return st;
                     if ((st = timed(CFD_KERNEL_MG_RHO, [&] { mg_rho(c, c->r32, c->w32.r0, nullptr, c->sc_t); })) !=

@@ -433,14 +433,17 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 // h = P r / |r| (in place): the Jacobi-scaled residual in the finite-volume
 // form, normalised by the FP64 residual norm (rn2 = |r|^2) so the FP32 solve
 // works at unit scale whatever the outer tolerance; sc->rhs_scale = |r| for
-// the correction, sc->r0n2 = |h|^2 for the stopping test
+// the correction, sc->r0n2 = |h - mean h|^2 for the stopping test.  M's null
+// space is the constants, so the mean of h (FP32 rounding leaves one of about
+// eps sqrt(n) |h|) is a part no iteration can reduce; the test measures the
+// rest.
 __global__ void __launch_bounds__(kBlock)
 k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, double *partials, unsigned int *counter)
 {
     const double nr = (rn2 && *rn2 > 0.0) ? sqrt(*rn2) : 1.0;
     const float s = (float)(1.0 / nr);
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->rhs_scale = nr;
-    float pa = 0.f;
+    float pa = 0.f, ps = 0.f;
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < F.A.n;
          row += (long long)gridDim.x * blockDim.x) {
         const int nz = F.A.nzc, nyz = F.A.nyc * F.A.nzc;
@@ -449,9 +452,11 @@ k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, do
         const float v = dv * (__ldg(F.sx + i) + (__ldg(F.sy + j) + __ldg(F.sz + k))) * (h[row] * s);
         h[row] = v;
         pa = fmaf(v, v, pa);
+        ps += v;
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->r0n2 = tot[0];
+    double acc[2] = {(double)pa, (double)ps}, tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0)
+        sc->r0n2 = fmax(tot[0] - tot[1] * tot[1] / (double)F.A.n, 0.0);
 }
 
 // rho = h . z; with p0 != null also p0 = z and the solve's initial scalars
@@ -484,31 +489,39 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
     if (sc->iter + 1 >= sc->maxit) {
         sc->done = BICG_CAPPED;
     } else {
-        sc->beta = tot[0] / sc->rho;
+        // flexible (Polak-Ribiere) beta = h.(z - z_old) / rho_old: keeps the
+        // recurrences sound with an FP32 V-cycle, symmetric only to rounding
+        sc->beta = (tot[0] - sc->hz_old) / sc->rho;
         sc->rho = tot[0];
         sc->iter += 1;
         sc->total_iters += 1;
     }
 }
 
-// e += alpha p, h -= alpha q and the stopping test on |h| / |h0| (the
-// unpreconditioned residual): a converged solve skips the V-cycle after it
+// e += alpha p, h -= alpha q, h . z_old for the flexible beta, and the
+// stopping test on |h - mean h| / |h0 - mean h0| (the unpreconditioned
+// residual without its null-space part): a converged solve skips the V-cycle
+// after it
 __global__ void __launch_bounds__(kBlock)
 k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float *__restrict__ h,
-         const float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter)
+         const float *__restrict__ q, const float *__restrict__ z, BicgScal *sc, double *partials,
+         unsigned int *counter)
 {
     if (sc->done) return;
     const float alpha = (float)sc->alpha;
-    float pa = 0.f;
+    float pa = 0.f, ps = 0.f, pz = 0.f;
     for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
         e[r] = fmaf(alpha, p[r], e[r]);
         const float hv = fmaf(-alpha, q[r], h[r]);
         h[r] = hv;
         pa = fmaf(hv, hv, pa);
+        ps += hv;
+        pz = fmaf(hv, z[r], pz);
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (!grid_reduce<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
-    const double rel = sqrt(tot[0] / sc->r0n2);
+    double acc[3] = {(double)pa, (double)ps, (double)pz}, tot[3];
+    if (!grid_reduce<3>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    sc->hz_old = tot[2];
+    const double rel = sqrt(fmax(tot[0] - tot[1] * tot[1] / (double)n, 0.0) / sc->r0n2);
     sc->relres = rel;
     if (rel < sc->tol) sc->done = BICG_CONVERGED;
     else if (!(rel == rel)) sc->done = BICG_CAPPED;
@@ -836,9 +849,9 @@ void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc)
     k_mg_rho<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, h, z, p0, sc, c->lc.partials, c->lc.counter);
 }
 
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc)
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const float *z, BicgScal *sc)
 {
-    k_mg_upd<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, e, p, h, q, sc, c->lc.partials, c->lc.counter);
+    k_mg_upd<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, e, p, h, q, z, sc, c->lc.partials, c->lc.counter);
 }
 
 }  // namespace cfd
