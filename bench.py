@@ -145,7 +145,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "20"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
@@ -274,7 +274,7 @@ KERNEL_BYTES_MIXED = {
     "mg_smooth": 8,    # one colour on the finest level: read x (all), b (half); write x (half)
     "mg_restrict": 8,  # read b, x of the finest level (coarse writes 1/8)
     "mg_prolong": 8,   # read and write x of the finest level
-    "mg_upd": 28,      # read e, p, h, q, z; write e, h
+    "mg_upd": 24,      # read e, p, h, q; write e, h
     "mg_rho": 8,       # read h, z
 }
 MG_SWEEPS = 2  # smoothing sweeps per level before and after the coarse correction

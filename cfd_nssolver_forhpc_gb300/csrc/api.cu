@@ -271,14 +271,14 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
             mg_vcycle(c, c->mg.never);
             mg_rho(c, h, z, c->w32.p1, sc);
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
-            mg_upd(c, e, c->w32.p1, h, q, z, sc);
+            mg_upd(c, e, c->w32.p1, h, q, sc);
             mg_vcycle(c, &sc->done);
             mg_rho(c, h, z, nullptr, sc);
         },
         [&](int from) {
             float *P[2] = {c->w32.p1, c->p_alt};
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, from, false);
-            mg_upd(c, e, P[1 - from], h, q, z, sc);
+            mg_upd(c, e, P[1 - from], h, q, sc);
             mg_vcycle(c, &sc->done);
             mg_rho(c, h, z, nullptr, sc);
         },
@@ -1378,6 +1378,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
     BicgScal hs{};
     hs.norm0 = 1.0; hs.rho = 1.0; hs.alpha = 0.5; hs.omega = 0.5; hs.beta = 0.5;
     hs.tol = 0.0; hs.restart_tol = 0.0; hs.maxit = 0x7fffffff; hs.timestep = 1;
+    hs.r0n2 = 1.0; hs.rhs_scale = 1.0;
     CK(cudaMemcpyAsync(c->sc_t, &hs, sizeof(hs), cudaMemcpyHostToDevice, c->s));
     int st = CFD_OK;
     const Geo &g = c->g;
@@ -1432,7 +1433,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                         if (!(part < 3 && c->mg.first_small == 0))
                             if ((st = timed(ids[part], [&] { mg_time_part(c, part); })) != CFD_OK) return st;
                     if ((st = timed(CFD_KERNEL_MG_UPD, [&] {
-                             mg_upd(c, c->e32, c->w32.p1, c->r32, c->w32.ap, c->w32.r0, c->sc_t);
+                             mg_upd(c, c->e32, c->w32.p1, c->r32, c->w32.ap, c->sc_t);
                          })) != CFD_OK)
                         return st;
                     if ((st = timed(CFD_KERNEL_MG_RHO, [&] { mg_rho(c, c->r32, c->w32.r0, nullptr, c->sc_t); })) !=

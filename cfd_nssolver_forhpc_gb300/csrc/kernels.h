@@ -121,7 +121,7 @@ struct BicgScal {
     int wait_timeout;  // a bounded device wait (TMA pipeline) gave up
     int loop_trips;    // body runs of the solve's device-side loop (graph WHILE node)
     double rhs_scale;  // the multigrid-CG solves for rhs / rhs_scale; the correction multiplies back
-    double hz_old;     // h_new . z_old of the flexible (Polak-Ribiere) beta of the multigrid-CG
+    double qz;         // q . z of the CG stencil launch (flexible beta: h_new . z_old = rho - alpha q . z)
 };
 enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
 

@@ -444,15 +444,38 @@ k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, do
     const float s = (float)(1.0 / nr);
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->rhs_scale = nr;
     float pa = 0.f, ps = 0.f;
-    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < F.A.n;
-         row += (long long)gridDim.x * blockDim.x) {
-        const int nz = F.A.nzc, nyz = F.A.nyc * F.A.nzc;
-        const int i = (int)(row / nyz), r2 = (int)(row - (long long)i * nyz), j = r2 / nz, k = r2 - j * nz;
-        const float dv = __ldg(F.wx + i) * (__ldg(F.wy + j) * __ldg(F.wz + k));
-        const float v = dv * (__ldg(F.sx + i) + (__ldg(F.sy + j) + __ldg(F.sz + k))) * (h[row] * s);
-        h[row] = v;
-        pa = fmaf(v, v, pa);
-        ps += v;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    const int nz = F.A.nzc, ny = F.A.nyc;
+    if ((nz & 3) == 0) {
+        // float4 rows along k (nz % 4 == 0 keeps a quad inside one (i, j) line)
+        const int n4 = nz >> 2;
+        const long long nq = F.A.n >> 2;
+        for (long long q = t0; q < nq; q += st) {
+            const long long line = q / n4;
+            const int k0 = 4 * (int)(q - line * n4), i = (int)(line / ny), j = (int)(line - (long long)i * ny);
+            const float wxy = __ldg(F.wx + i), wy = __ldg(F.wy + j), sxy = __ldg(F.sx + i);
+            const float sy = __ldg(F.sy + j);
+            const float4 wz = __ldg(reinterpret_cast<const float4 *>(F.wz + k0));
+            const float4 sz = __ldg(reinterpret_cast<const float4 *>(F.sz + k0));
+            float4 hv = reinterpret_cast<float4 *>(h)[q];
+            hv.x = wxy * (wy * wz.x) * (sxy + (sy + sz.x)) * (hv.x * s);
+            hv.y = wxy * (wy * wz.y) * (sxy + (sy + sz.y)) * (hv.y * s);
+            hv.z = wxy * (wy * wz.z) * (sxy + (sy + sz.z)) * (hv.z * s);
+            hv.w = wxy * (wy * wz.w) * (sxy + (sy + sz.w)) * (hv.w * s);
+            reinterpret_cast<float4 *>(h)[q] = hv;
+            pa = fmaf(hv.x, hv.x, fmaf(hv.y, hv.y, fmaf(hv.z, hv.z, fmaf(hv.w, hv.w, pa))));
+            ps += (hv.x + hv.y) + (hv.z + hv.w);
+        }
+    } else {
+        for (long long row = t0; row < F.A.n; row += st) {
+            const int nyz = ny * nz;
+            const int i = (int)(row / nyz), r2 = (int)(row - (long long)i * nyz), j = r2 / nz, k = r2 - j * nz;
+            const float dv = __ldg(F.wx + i) * (__ldg(F.wy + j) * __ldg(F.wz + k));
+            const float v = dv * (__ldg(F.sx + i) + (__ldg(F.sy + j) + __ldg(F.sz + k))) * (h[row] * s);
+            h[row] = v;
+            pa = fmaf(v, v, pa);
+            ps += v;
+        }
     }
     double acc[2] = {(double)pa, (double)ps}, tot[2];
     if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0)
@@ -468,7 +491,16 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
 {
     if (!p0 && sc->done) return;
     float pa = 0.f;
-    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    // float4 body (the vectors are cudaMalloc allocations: 16-byte aligned), scalar tail
+    const long long nq = n >> 2;
+    for (long long q = t0; q < nq; q += st) {
+        const float4 zv = reinterpret_cast<const float4 *>(z)[q];
+        const float4 hv = reinterpret_cast<const float4 *>(h)[q];
+        if (p0) reinterpret_cast<float4 *>(p0)[q] = zv;
+        pa = fmaf(hv.x, zv.x, fmaf(hv.y, zv.y, fmaf(hv.z, zv.z, fmaf(hv.w, zv.w, pa))));
+    }
+    for (long long r = 4 * nq + t0; r < n; r += st) {
         const float zv = z[r];
         if (p0) p0[r] = zv;
         pa = fmaf(h[r], zv, pa);
@@ -489,38 +521,53 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
     if (sc->iter + 1 >= sc->maxit) {
         sc->done = BICG_CAPPED;
     } else {
-        // flexible (Polak-Ribiere) beta = h.(z - z_old) / rho_old: keeps the
-        // recurrences sound with an FP32 V-cycle, symmetric only to rounding
-        sc->beta = (tot[0] - sc->hz_old) / sc->rho;
+        // flexible (Polak-Ribiere) beta = h.(z - z_old) / rho_old, with
+        // h.z_old = rho_old - alpha q.z_old (q.z from the stencil launch):
+        // keeps the recurrences sound with an FP32 V-cycle, symmetric only
+        // to rounding
+        sc->beta = (tot[0] - (sc->rho - sc->alpha * sc->qz)) / sc->rho;
         sc->rho = tot[0];
         sc->iter += 1;
         sc->total_iters += 1;
     }
 }
 
-// e += alpha p, h -= alpha q, h . z_old for the flexible beta, and the
-// stopping test on |h - mean h| / |h0 - mean h0| (the unpreconditioned
-// residual without its null-space part): a converged solve skips the V-cycle
-// after it
+// e += alpha p, h -= alpha q and the stopping test on |h - mean h| /
+// |h0 - mean h0| (the unpreconditioned residual without its null-space part):
+// a converged solve skips the V-cycle after it
 __global__ void __launch_bounds__(kBlock)
 k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float *__restrict__ h,
-         const float *__restrict__ q, const float *__restrict__ z, BicgScal *sc, double *partials,
-         unsigned int *counter)
+         const float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter)
 {
     if (sc->done) return;
     const float alpha = (float)sc->alpha;
-    float pa = 0.f, ps = 0.f, pz = 0.f;
-    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    float pa = 0.f, ps = 0.f;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    // float4 body (the vectors are cudaMalloc allocations: 16-byte aligned), scalar tail
+    const long long nq = n >> 2;
+    for (long long q4 = t0; q4 < nq; q4 += st) {
+        float4 ev = reinterpret_cast<float4 *>(e)[q4];
+        float4 hv = reinterpret_cast<float4 *>(h)[q4];
+        const float4 pv = reinterpret_cast<const float4 *>(p)[q4];
+        const float4 qv = reinterpret_cast<const float4 *>(q)[q4];
+        ev.x = fmaf(alpha, pv.x, ev.x); ev.y = fmaf(alpha, pv.y, ev.y);
+        ev.z = fmaf(alpha, pv.z, ev.z); ev.w = fmaf(alpha, pv.w, ev.w);
+        hv.x = fmaf(-alpha, qv.x, hv.x); hv.y = fmaf(-alpha, qv.y, hv.y);
+        hv.z = fmaf(-alpha, qv.z, hv.z); hv.w = fmaf(-alpha, qv.w, hv.w);
+        reinterpret_cast<float4 *>(e)[q4] = ev;
+        reinterpret_cast<float4 *>(h)[q4] = hv;
+        pa = fmaf(hv.x, hv.x, fmaf(hv.y, hv.y, fmaf(hv.z, hv.z, fmaf(hv.w, hv.w, pa))));
+        ps += (hv.x + hv.y) + (hv.z + hv.w);
+    }
+    for (long long r = 4 * nq + t0; r < n; r += st) {
         e[r] = fmaf(alpha, p[r], e[r]);
         const float hv = fmaf(-alpha, q[r], h[r]);
         h[r] = hv;
         pa = fmaf(hv, hv, pa);
         ps += hv;
-        pz = fmaf(hv, z[r], pz);
     }
-    double acc[3] = {(double)pa, (double)ps, (double)pz}, tot[3];
-    if (!grid_reduce<3>(acc, partials, counter, tot) || threadIdx.x != 0) return;
-    sc->hz_old = tot[2];
+    double acc[2] = {(double)pa, (double)ps}, tot[2];
+    if (!grid_reduce<2>(acc, partials, counter, tot) || threadIdx.x != 0) return;
     const double rel = sqrt(fmax(tot[0] - tot[1] * tot[1] / (double)n, 0.0) / sc->r0n2);
     sc->relres = rel;
     if (rel < sc->tol) sc->done = BICG_CONVERGED;
@@ -849,9 +896,9 @@ void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc)
     k_mg_rho<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, h, z, p0, sc, c->lc.partials, c->lc.counter);
 }
 
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, const float *z, BicgScal *sc)
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc)
 {
-    k_mg_upd<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, e, p, h, q, z, sc, c->lc.partials, c->lc.counter);
+    k_mg_upd<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, e, p, h, q, sc, c->lc.partials, c->lc.counter);
 }
 
 }  // namespace cfd

@@ -600,7 +600,7 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
         }
     };
     __shared__ float sm[2][kCgTileSmem];
-    float pa = 0.f;
+    float pa = 0.f, pz = 0.f;
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int tile = item % tiles, chunk = item / tiles;
         const int k0 = (tile % tiles_k) * TK, j0 = (tile / tiles_k) * TJ;
@@ -621,7 +621,7 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
             ld(ib, hjj, hkk, hz0, hp0);
             ld(ib + 1, hjj, hkk, hz1, hp1);
         }
-        float vm = fmaf(beta, pm, zm), vc = fmaf(beta, p0, z0);
+        float vm = fmaf(beta, pm, zm), vc = fmaf(beta, p0, z0), zc = z0;
         for (int i = ib; i < ie; ++i) {
             float z3, p3, hz2 = 0.f, hp2 = 0.f;
             ld(i + 3, j, k, z3, p3);
@@ -646,16 +646,21 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
                 if (!first) pn[r] = vc;
                 q[r] = qv;
                 pa = fmaf(vc, qv, pa);
+                pz = fmaf(zc, qv, pz);
             }
             vm = vc;
             vc = vp;
+            zc = z1;
             z1 = z2; p1 = p2; z2 = z3; p2 = p3;
             hz0 = hz1; hp0 = hp1; hz1 = hz2; hp1 = hp2;
         }
         __syncthreads();  // the next item rewrites both planes
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+    double acc[2] = {(double)pa, (double)pz}, tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        sc->alpha = sc->rho / tot[0];
+        sc->qz = tot[1];
+    }
 }
 
 // ---- TMA-fed CG stencil ------------------------------------------------------
@@ -782,7 +787,7 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
         else { row = 1 + h - 2 * G::TKQ - G::TJ; col = G::TKQ + 1; }
     };
     const int cslot = (tj + 1) * G::BX + 4 + 4 * tk4;  // this thread's float4 in a box / pn plane
-    float pa = 0.f;
+    float pa = 0.f, pz = 0.f;
     long long g0 = 0;  // planes consumed by this block so far (mbarrier phases)
     for (int item = blockIdx.x; item < items; item += gridDim.x) {
         const int tile = item % tiles, chunk = item / tiles;
@@ -833,6 +838,7 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
             }
         }
         float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = p1;
+        float4 z1 = p1;  // the loaded vector (z, or h when FZ) at this thread's cells of plane tt - 1
         for (int tt = 0; tt < np; ++tt) {
             const long long g = g0 + tt;
             const int st = (int)(g % kCgStages);
@@ -865,6 +871,7 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
                 *reinterpret_cast<float4 *>(pb + off) = zv;
                 return zv;
             };
+            const float4 zraw = *reinterpret_cast<const float4 *>(hs_ + cslot);
             const float4 nxt = form(cslot, wyz, syz);
 #pragma unroll
             for (int m = 0; m < MAXH; ++m) {
@@ -910,16 +917,23 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
                 pa = fmaf(vc.y, qv.y, pa);
                 pa = fmaf(vc.z, qv.z, pa);
                 pa = fmaf(vc.w, qv.w, pa);
+                pz = fmaf(z1.x, qv.x, fmaf(z1.y, qv.y, fmaf(z1.z, qv.z, fmaf(z1.w, qv.w, pz))));
             }
             p2 = p1;
             p1 = nxt;
+            z1 = zraw;
         }
         g0 += np;
         __syncthreads();  // the next item rewrites the pn planes
     }
     if (t == 0 && bad) sc->wait_timeout = 1;
-    double acc[1] = {(double)pa}, tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) sc->alpha = sc->rho / tot[0];
+    // pn . q gives alpha; q . z (z as loaded) serves the flexible beta of
+    // the multigrid-CG
+    double acc[2] = {(double)pa, (double)pz}, tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        sc->alpha = sc->rho / tot[0];
+        sc->qz = tot[1];
+    }
 }
 
 // Update of the TMA path: e += alpha p, h -= alpha q, rho' = h . (h / P) with
