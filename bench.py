@@ -280,8 +280,11 @@ KERNEL_BYTES_MIXED = {
 MG_SWEEPS = 2  # smoothing sweeps per level before and after the coarse correction
 
 
-def roofline(S, w, infos, precision):
-    """Dominant kernel by share of device time, its achieved GB/s."""
+def roofline(S, w, infos, precision, ms_step):
+    """Dominant kernel by share of the step's device time (count per step x
+    its CUDA-event time per launch / the measured ms per step), its achieved
+    GB/s.  "other" is the rest of the step: the coarser multigrid levels,
+    small kernels and launch gaps."""
     ms = S.time_kernels(reps=20)
     iters = sum(sum(i["iters"]) for i in infos) / len(infos)
     outer = sum(sum(i["outer"]) for i in infos) / len(infos)
@@ -305,7 +308,7 @@ def roofline(S, w, infos, precision):
     word = 4 if precision == "mixed" else 8
     per_row.update({k: v * word for k, v in KERNEL_BYTES_PER_CELL_FLOW.items()})
     shares = {k: ms[k] * counts[k] for k in ms if k in counts}
-    total = sum(shares.values()) or 1.0
+    total = ms_step if ms_step > 0 else (sum(shares.values()) or 1.0)
     top = max((k for k in shares if k in per_row), key=shares.get)
     bytes_launch = per_row[top] * w.n_cells
     peak, how = peaks()
@@ -320,6 +323,7 @@ def roofline(S, w, infos, precision):
         "kernels_ms": {k: round(v, 5) for k, v in ms.items()},
         "shares": {k: round(v / total, 3) for k, v in shares.items()},
     }
+    out["shares"]["other"] = round(max(0.0, 1.0 - sum(shares.values()) / total), 3)
     if "mg_vcycle" in ms:
         out["mg_vcycle_ms"] = round(ms["mg_vcycle"], 5)
     if precision != "mixed":
@@ -495,7 +499,7 @@ def main():
     sec_max = dist.max(sec)
     value = w.n_cells * K * dist.world / sec_max / 1e6
     mixed = args.precision == "mixed"
-    rl = roofline(S, w, infos, args.precision)
+    rl = roofline(S, w, infos, args.precision, sec_max / K * 1e3)
     cd64 = infos[-1]["cd"]
     div = S.div_inf(0)
     e2e = None
@@ -524,7 +528,7 @@ def main():
                  "max_relres": max(r for i in minfos[1:] or minfos for r in i["relres"]),
                  "cd_last": minfos[-1]["cd"], "cd_rel_vs_headline": abs(minfos[-1]["cd"] / cd64 - 1.0),
                  "div_inf_T0": M.div_inf(0), "gpu_launches": mlaunch,
-                 "roofline": roofline(M, w, minfos, other_prec),
+                 "roofline": roofline(M, w, minfos, other_prec, msec / K * 1e3),
                  "ratio_mixed_vs_fp64": round(mixed_v / fp64_v, 3)}
         M.close()
     adjoint = None

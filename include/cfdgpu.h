@@ -71,9 +71,10 @@ typedef enum {
                                finite-volume form M = D_V L of the operator */
     CFD_INNER_BICGSTAB = 1, /* FP32 BiCGSTAB on the Jacobi-scaled operator, restarted
                                when |r1.r0| < 1e-5 |r1||r0| */
-    CFD_INNER_MG = 2        /* FP32 CG on the finite-volume form preconditioned by a
-                               geometric multigrid V-cycle (SPE operator; falls back to
-                               Jacobi-PCG where the grid does not coarsen) */
+    CFD_INNER_MG = 2        /* default: FP32 flexible CG on the finite-volume form
+                               preconditioned by a geometric multigrid V-cycle (SPE
+                               operator; falls back to Jacobi-PCG where the grid does not
+                               coarsen to at most 256 cells) */
 } cfd_inner_solver;
 
 /* Velocity slots: the reference's T0 (old), T1 (predicted u*), T3 (new). */
@@ -116,7 +117,8 @@ typedef struct {
     double bc_dir[6][3];        /* Dirichlet table Dir[face][component] */
     double bc_num[6][3];        /* Neumann table Num[face][component]
                                    (Boundary_Condition.hpp:4-31) */
-    int check_every;            /* iterations between host convergence polls (>= 1) */
+    int check_every;            /* BiCGSTAB iterations per loop body of the device-side
+                                   solve loop (per host poll without graphs) (>= 1) */
     double inner_tol;           /* mixed precision: relative tolerance of each FP32
                                    inner solve inside the FP64 defect correction */
     int max_outer;              /* mixed precision: defect-correction sweeps cap */
