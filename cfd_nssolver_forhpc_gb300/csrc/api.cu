@@ -262,7 +262,7 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 // iterations per solve, so the loop body holds one pair.
 int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 {
-    const int v = (4 * c->mg.sweeps + 2) * c->mg.first_small + 1;
+    const int v = (int)mg_vcycle_launches(c->mg);
     float *z = c->w32.r0, *q = c->w32.ap;
     return run_pairs(
         c, 4, sc,
@@ -305,13 +305,15 @@ int solve64(cfd_ctx *c, const Op &A, int *iters, double *relres)
     return st;
 }
 
-void residual64(cfd_ctx *c, const SpeOp<double> &A, const double *b, const double *x, float *r32, double *out)
+void residual64(cfd_ctx *c, const SpeOp<double> &A, const double *b, const double *x, float *r32, double *out,
+                double *bout = nullptr)
 {
-    launch_residual64<float>(c->lc, A, b, x, r32, out);
+    launch_residual64<float>(c->lc, A, b, x, r32, out, bout);
 }
-void residual64(cfd_ctx *c, const EllOp<double> &A, const double *b, const double *x, float *r32, double *out)
+void residual64(cfd_ctx *c, const EllOp<double> &A, const double *b, const double *x, float *r32, double *out,
+                double *bout = nullptr)
 {
-    launch_residual64_ell<float>(c->lc, A, b, x, r32, out);
+    launch_residual64_ell<float>(c->lc, A, b, x, r32, out, bout);
 }
 
 // Mixed precision: FP64 defect correction around FP32 BiCGSTAB solves.
@@ -322,17 +324,15 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
                 int inner, int *iters, double *relres, int *outer, bool zero_x_if_zero_rhs = false)
 {
     const long long n = c->g.n;
-    // |b|^2 via the residual kernel with x = 0 would need a zero vector; the
-    // dot of b with itself is taken by the same FP64 reduction instead.
-    // |b|^2 from the residual kernel with x = 0 (w64.r0 is an FP64 zero
-    // vector in mixed-precision contexts)
-    double norm0 = 0.0;
-    residual64(c, A64, b, zero, c->r32, c->dscal + 4);
+    // the first residual (from the warm start) also gives |b|^2, the
+    // reference norm of the stopping test
+    (void)zero;
+    residual64(c, A64, b, x, c->r32, c->dscal + 3, c->dscal + 4);
     c->launches += 1;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
-    norm0 = std::sqrt(c->h_scal[4]);
+    const double norm0 = std::sqrt(c->h_scal[4]);
     int total = 0, sweeps = 0;
     double rel = 0.0;
     if (norm0 == 0.0) {
@@ -343,12 +343,14 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
         return CFD_OK;
     }
     int st = CFD_OK;
-    for (;;) {
-        residual64(c, A64, b, x, c->r32, c->dscal + 3);
-        c->launches += 1;
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
-        CK(cudaStreamSynchronize(c->s));
+    for (bool first = true;; first = false) {
+        if (!first) {
+            residual64(c, A64, b, x, c->r32, c->dscal + 3);
+            c->launches += 1;
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
+            CK(cudaStreamSynchronize(c->s));
+        }
         rel = std::sqrt(c->h_scal[3]) / norm0;
         if (rel < c->cfg.p_criteria || !std::isfinite(rel)) break;
         if (sweeps >= c->cfg.max_outer) { st = fail(CFD_ERR_NOCONV, "defect correction reached its sweep cap"); break; }
@@ -1427,10 +1429,11 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
             if (c->cfg.inner_solver == CFD_INNER_MG) {
                 CKS(mg_setup(c));
                 if (c->mg.usable) {
-                    const int ids[5] = {CFD_KERNEL_MG_SMOOTH, CFD_KERNEL_MG_RESTRICT, CFD_KERNEL_MG_PROLONG,
-                                        CFD_KERNEL_MG_SMALL, CFD_KERNEL_MG_VCYCLE};
-                    for (int part = 0; part < 5; ++part)
-                        if (!(part < 3 && c->mg.first_small == 0))
+                    const int ids[6] = {CFD_KERNEL_MG_SMOOTH, CFD_KERNEL_MG_RESTRICT, CFD_KERNEL_MG_PROLONG,
+                                        CFD_KERNEL_MG_SMALL, CFD_KERNEL_MG_VCYCLE, CFD_KERNEL_MG_SWEEP};
+                    for (int part = 0; part < 6; ++part)
+                        if (!((part < 3 || part == 5) && c->mg.first_small == 0) &&
+                            !(part == 5 && c->mg.lev[0].sweep_tj == 0))
                             if ((st = timed(ids[part], [&] { mg_time_part(c, part); })) != CFD_OK) return st;
                     if ((st = timed(CFD_KERNEL_MG_UPD, [&] {
                              mg_upd(c, c->e32, c->w32.p1, c->r32, c->w32.ap, c->sc_t);

@@ -14,8 +14,44 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <cstdlib>
 
 namespace cfd {
+
+// ---- programmatic dependent launch ------------------------------------------
+// A kernel launched with launch_pdl may start while its predecessor in the
+// stream is still running; it calls pdl_wait() before its first global
+// memory access (which returns once the predecessor grid has completed and
+// its writes are visible), then pdl_allow() so that its own successor may
+// begin launching.  A kernel launched normally passes pdl_wait() at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_allow() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+// CFDGPU_NO_PDL=1 launches these kernels without the attribute (plain stream order)
+inline bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char *e = std::getenv("CFDGPU_NO_PDL");
+        return !(e && e[0] == '1');
+    }();
+    return on;
+}
+
+template <class... KArgs, class... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 constexpr int GC = 2;
 constexpr int kBlock = 256;

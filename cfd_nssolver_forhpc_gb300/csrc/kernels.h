@@ -213,10 +213,10 @@ void launch_sor_sweep(cudaStream_t s, const Geo &g, const Metrics<double> &m, co
 // mixed precision pieces
 template <class V>
 void launch_residual64(cfd_launch_ctx &c, const SpeOp<double> &A, const double *b, const double *x,
-                       V *r32, double *norm2_out);
+                       V *r32, double *norm2_out, double *bnorm2_out = nullptr);
 template <class V>
 void launch_residual64_ell(cfd_launch_ctx &c, const EllOp<double> &A, const double *b,
-                           const double *x, V *r32, double *norm2_out);
+                           const double *x, V *r32, double *norm2_out, double *bnorm2_out = nullptr);
 template <class V>
 void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e, const double *scale = nullptr);
 
@@ -281,6 +281,8 @@ struct MgLevel {
     const float *rw[3];   // per axis: 1 / width
     float *x, *b;
     const float *rv, *rg;  // per cell 1 / dV and 1 / diag (small-level kernel only)
+    float *xalt;           // second x buffer of a grid-wide level (fused sweeps ping-pong)
+    int sweep_tj, sweep_ci;  // fused sweep tiling: j rows and i planes per block (0: not fused)
     bool quads;           // the float4 smoother applies (nz % 4 == 0, aligned arrays)
 };
 constexpr int kMgSmallSmem = 200 * 1024;  // shared-memory bytes for the small levels' x and b
@@ -299,6 +301,7 @@ struct MgSmall {
 struct Mg {
     int nlev = 0, first_small = 0;
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
+    int sweeps0 = 2; // ... on the finest level
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve
     float *cinv = nullptr;
     bool usable = false;

@@ -40,8 +40,16 @@ namespace {
 constexpr int kSmallThreads = 1024;
 constexpr int kMgCoarsest = 256;     // cells of the coarsest level at most (dense inverse)
 constexpr int kMgCoarseTarget = 64;  // coarsening goes on while a level has more cells and an axis halves
+constexpr int kSweepSmemMax = 96 * 1024;  // shared memory of a fused-sweep block at most
+
+// shared memory of a fused-sweep block: rings of 4 x planes (TJ + 4 rows),
+// 4 b planes and 3 colour planes (TJ + 2 rows each), nz floats a row
+inline size_t sweep_smem(int tj, int nz) { return (size_t)(4 * (tj + 4) + 7 * (tj + 2)) * nz * sizeof(float); }
 
 inline int nblk(long long n) { return (int)((n + kBlock - 1) / kBlock); }
+
+// smoothing sweeps of level l before and after the coarse correction
+inline int level_sweeps(const Mg &G, int l) { return l == 0 ? G.sweeps0 : G.sweeps; }
 
 __device__ __forceinline__ void decomp(const MgLevel &L, long long t, int &i, int &j, int &k)
 {
@@ -279,6 +287,8 @@ __global__ void k_mg_cell_tables(MgLevel L, float *__restrict__ rv, float *__res
 __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b, float *x, int color, int zero_init,
                                                       const int *done)
 {
+    pdl_wait();
+    pdl_allow();
     if (*done) return;
     smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                  (long long)gridDim.x * blockDim.x);
@@ -288,6 +298,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b,
 __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, const float *b, float *x, int color,
                                                           int zero_init, const int *done)
 {
+    pdl_wait();
+    pdl_allow();
     if (*done) return;
     smooth_quads(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                  (long long)gridDim.x * blockDim.x);
@@ -296,6 +308,8 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, const float *b
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, const float *bf, const float *xf,
                                                         float *bc, const int *done)
 {
+    pdl_wait();
+    pdl_allow();
     if (*done) return;
     restrict_level(F, C, bf, xf, bc, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                    (long long)gridDim.x * blockDim.x);
@@ -304,8 +318,197 @@ __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, co
 __global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevel F, MgLevel C, const float *xc, float *xf,
                                                        const int *done)
 {
+    pdl_wait();
+    pdl_allow();
     if (*done) return;
     prolong_level(F, C, xc, xf, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// ---- fused red-black sweep (grid-wide levels, nz % 4 == 0) ------------------
+// One symmetric-order sweep in one pass: xn = colour c1 applied after colour
+// c0 to xo (c1 = 1 - c0), written to a second buffer so that no block reads a
+// value another block has already replaced.  A block owns TJ rows of j (all
+// of k) over a chunk of CI planes of i and marches along i: colour c0 at
+// plane q over its rows and one halo row each side (from xo), then colour c1
+// at plane q - 1 over its own rows (from the c0 values of planes q - 2 .. q).
+// xo planes arrive two planes ahead and b planes one plane ahead through
+// cp.async rings; c0 values live in a ring of three planes.  The arithmetic
+// is that of smooth_quads term for term, so the result equals the two
+// colour launches bit for bit.  zero_init: xo is 0 (not read).
+constexpr int kSweepRing = 4;
+
+__device__ __forceinline__ int mod_ring(int p, int m) { return ((p % m) + m) % m; }
+
+__device__ __forceinline__ void cp16(unsigned dst, const void *src, bool valid)
+{
+    // 16-byte asynchronous copy; an invalid source fills zeros and reads nothing
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ float comp4(const float4 &v, int e)
+{
+    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+
+__global__ void __launch_bounds__(1024)
+k_mg_sweep(MgLevel L, const float *__restrict__ b, const float *__restrict__ xo, float *__restrict__ xn, int c0,
+           int zero_init, const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    extern __shared__ float4 sweep_sm4[];
+    float *sm = reinterpret_cast<float *>(sweep_sm4);
+    const int nx = L.nx, ny = L.ny, nz = L.nz, n4 = nz >> 2, TJ = L.sweep_tj, CI = L.sweep_ci;
+    const int XR = TJ + 4, RR = TJ + 2;  // rows of an x plane (j0-2 .. j0+TJ+1) and of a b / c0 plane (j0-1 .. j0+TJ)
+    float *xs = sm;                                  // [kSweepRing][XR * nz]
+    float *bs = xs + kSweepRing * XR * nz;           // [kSweepRing][RR * nz]
+    float *rs = bs + kSweepRing * RR * nz;           // [3][RR * nz]
+    const int tiles_j = (ny + TJ - 1) / TJ;
+    const int j0 = (blockIdx.x % tiles_j) * TJ, ib = (blockIdx.x / tiles_j) * CI, ie = min(nx, ib + CI);
+    const int t = threadIdx.x, nt = blockDim.x;
+    const long long sx = (long long)ny * nz;
+
+    auto issue_x = [&](int p) {
+        const unsigned base = (unsigned)__cvta_generic_to_shared(xs + mod_ring(p, kSweepRing) * XR * nz);
+        for (int u = t; u < XR * n4; u += nt) {
+            const int row = u / n4, m = u - row * n4, j = j0 - 2 + row;
+            const bool ok = p >= 0 && p < nx && j >= 0 && j < ny;
+            cp16(base + 16u * (unsigned)(row * n4 + m), ok ? (const void *)(xo + p * sx + (long long)j * nz + 4 * m) : xo, ok);
+        }
+    };
+    auto issue_b = [&](int p) {
+        const unsigned base = (unsigned)__cvta_generic_to_shared(bs + mod_ring(p, kSweepRing) * RR * nz);
+        for (int u = t; u < RR * n4; u += nt) {
+            const int row = u / n4, m = u - row * n4, j = j0 - 1 + row;
+            const bool ok = p >= 0 && p < nx && j >= 0 && j < ny;
+            cp16(base + 16u * (unsigned)(row * n4 + m), ok ? (const void *)(b + p * sx + (long long)j * nz + 4 * m) : b, ok);
+        }
+    };
+    if (zero_init)
+        for (int u = t; u < kSweepRing * XR * n4; u += nt) reinterpret_cast<float4 *>(xs)[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+    else {
+        issue_x(ib - 2);
+        issue_x(ib - 1);
+        issue_x(ib);
+    }
+    issue_b(ib - 1);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+
+    for (int q = ib - 1; q <= ie; ++q) {
+        if (!zero_init) issue_x(q + 2);
+        issue_b(q + 1);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        __syncthreads();
+        // colour c0 at plane q, rows j0-1 .. j0+TJ
+        {
+            const float *xm = xs + mod_ring(q - 1, kSweepRing) * XR * nz;
+            const float *xc = xs + mod_ring(q, kSweepRing) * XR * nz;
+            const float *xp = xs + mod_ring(q + 1, kSweepRing) * XR * nz;
+            const float *bq = bs + mod_ring(q, kSweepRing) * RR * nz;
+            float *dst = rs + mod_ring(q, 3) * RR * nz;
+            const bool qv = q >= 0 && q < nx;
+            float cxm = 0.f, cxp = 0.f, rwx = 0.f, sux = 0.f;
+            if (qv) {
+                cxm = __ldg(L.cm[0] + q); cxp = __ldg(L.cp[0] + q);
+                rwx = __ldg(L.rw[0] + q); sux = __ldg(L.sum[0] + q);
+            }
+            for (int u = t; u < RR * n4; u += nt) {
+                const int rr = u / n4, m = u - rr * n4, j = j0 - 1 + rr, k0 = 4 * m;
+                float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (qv && j >= 0 && j < ny) {
+                    const int xr = rr + 1;
+                    const float4 c = *reinterpret_cast<const float4 *>(xc + xr * nz + k0);
+                    const float4 vxm = *reinterpret_cast<const float4 *>(xm + xr * nz + k0);
+                    const float4 vxp = *reinterpret_cast<const float4 *>(xp + xr * nz + k0);
+                    const float4 vym = *reinterpret_cast<const float4 *>(xc + (xr - 1) * nz + k0);
+                    const float4 vyp = *reinterpret_cast<const float4 *>(xc + (xr + 1) * nz + k0);
+                    const float zlo = k0 > 0 ? xc[xr * nz + k0 - 1] : 0.f;
+                    const float zhi = k0 + 4 < nz ? xc[xr * nz + k0 + 4] : 0.f;
+                    const float4 bv = *reinterpret_cast<const float4 *>(bq + rr * nz + k0);
+                    const float cym = __ldg(L.cm[1] + j), cyp = __ldg(L.cp[1] + j);
+                    const float rxy = rwx * __ldg(L.rw[1] + j), sxy = sux + __ldg(L.sum[1] + j);
+                    const float4 czm = __ldg(reinterpret_cast<const float4 *>(L.cm[2] + k0));
+                    const float4 czp = __ldg(reinterpret_cast<const float4 *>(L.cp[2] + k0));
+                    const float4 rz = __ldg(reinterpret_cast<const float4 *>(L.rw[2] + k0));
+                    const float4 sz = __ldg(reinterpret_cast<const float4 *>(L.sum[2] + k0));
+                    const int e0 = (c0 + q + j) & 1;
+                    const bool odd = e0 != 0;
+                    auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+                    float nA = cxm * pick(vxm.x, vxm.y);
+                    nA = fmaf(cxp, pick(vxp.x, vxp.y), nA);
+                    nA = fmaf(cym, pick(vym.x, vym.y), nA);
+                    nA = fmaf(cyp, pick(vyp.x, vyp.y), nA);
+                    nA = fmaf(pick(czm.x, czm.y), pick(zlo, c.x), nA);
+                    nA = fmaf(pick(czp.x, czp.y), pick(c.y, c.z), nA);
+                    float nB = cxm * pick(vxm.z, vxm.w);
+                    nB = fmaf(cxp, pick(vxp.z, vxp.w), nB);
+                    nB = fmaf(cym, pick(vym.z, vym.w), nB);
+                    nB = fmaf(cyp, pick(vyp.z, vyp.w), nB);
+                    nB = fmaf(pick(czm.z, czm.w), pick(c.y, c.z), nB);
+                    nB = fmaf(pick(czp.z, czp.w), pick(c.w, zhi), nB);
+                    if (zero_init) nA = nB = 0.f;
+                    const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), nA) * __frcp_rn(sxy + pick(sz.x, sz.y));
+                    const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), nB) * __frcp_rn(sxy + pick(sz.z, sz.w));
+                    out = make_float4(odd ? 0.f : vA, odd ? vA : 0.f, odd ? 0.f : vB, odd ? vB : 0.f);
+                }
+                *reinterpret_cast<float4 *>(dst + rr * nz + k0) = out;
+            }
+        }
+        __syncthreads();
+        // colour c1 at plane q - 1, rows j0 .. j0+TJ-1, from the c0 values
+        const int qo = q - 1;
+        if (qo >= ib) {
+            const float *rm = rs + mod_ring(qo - 1, 3) * RR * nz;
+            const float *rc = rs + mod_ring(qo, 3) * RR * nz;
+            const float *rp = rs + mod_ring(qo + 1, 3) * RR * nz;
+            const float *bq = bs + mod_ring(qo, kSweepRing) * RR * nz;
+            const float cxm = __ldg(L.cm[0] + qo), cxp = __ldg(L.cp[0] + qo);
+            const float rwx = __ldg(L.rw[0] + qo), sux = __ldg(L.sum[0] + qo);
+            for (int u = t; u < TJ * n4; u += nt) {
+                const int r = u / n4, m = u - r * n4, j = j0 + r, k0 = 4 * m;
+                if (j >= ny) continue;
+                const int cr = r + 1;
+                const float4 c = *reinterpret_cast<const float4 *>(rc + cr * nz + k0);
+                const float4 vxm = *reinterpret_cast<const float4 *>(rm + cr * nz + k0);
+                const float4 vxp = *reinterpret_cast<const float4 *>(rp + cr * nz + k0);
+                const float4 vym = *reinterpret_cast<const float4 *>(rc + (cr - 1) * nz + k0);
+                const float4 vyp = *reinterpret_cast<const float4 *>(rc + (cr + 1) * nz + k0);
+                const float zlo = k0 > 0 ? rc[cr * nz + k0 - 1] : 0.f;
+                const float zhi = k0 + 4 < nz ? rc[cr * nz + k0 + 4] : 0.f;
+                const float4 bv = *reinterpret_cast<const float4 *>(bq + cr * nz + k0);
+                const float cym = __ldg(L.cm[1] + j), cyp = __ldg(L.cp[1] + j);
+                const float rxy = rwx * __ldg(L.rw[1] + j), sxy = sux + __ldg(L.sum[1] + j);
+                const float4 czm = __ldg(reinterpret_cast<const float4 *>(L.cm[2] + k0));
+                const float4 czp = __ldg(reinterpret_cast<const float4 *>(L.cp[2] + k0));
+                const float4 rz = __ldg(reinterpret_cast<const float4 *>(L.rw[2] + k0));
+                const float4 sz = __ldg(reinterpret_cast<const float4 *>(L.sum[2] + k0));
+                const int e0 = (1 - c0 + qo + j) & 1;  // first c1 cell of the quad
+                const bool odd = e0 != 0;
+                auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+                float nA = cxm * pick(vxm.x, vxm.y);
+                nA = fmaf(cxp, pick(vxp.x, vxp.y), nA);
+                nA = fmaf(cym, pick(vym.x, vym.y), nA);
+                nA = fmaf(cyp, pick(vyp.x, vyp.y), nA);
+                nA = fmaf(pick(czm.x, czm.y), pick(zlo, c.x), nA);
+                nA = fmaf(pick(czp.x, czp.y), pick(c.y, c.z), nA);
+                float nB = cxm * pick(vxm.z, vxm.w);
+                nB = fmaf(cxp, pick(vxp.z, vxp.w), nB);
+                nB = fmaf(cym, pick(vym.z, vym.w), nB);
+                nB = fmaf(cyp, pick(vyp.z, vyp.w), nB);
+                nB = fmaf(pick(czm.z, czm.w), pick(c.y, c.z), nB);
+                nB = fmaf(pick(czp.z, czp.w), pick(c.w, zhi), nB);
+                const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), nA) * __frcp_rn(sxy + pick(sz.x, sz.y));
+                const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), nB) * __frcp_rn(sxy + pick(sz.z, sz.w));
+                // c0 cells keep the values of the first half of the sweep
+                const float4 o = make_float4(odd ? c.x : vA, odd ? vA : c.y, odd ? c.z : vB, odd ? vB : c.w);
+                *reinterpret_cast<float4 *>(xn + qo * sx + (long long)j * nz + k0) = o;
+            }
+        }
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 // a small level's x and b in shared memory, each rounded up to 4 floats so
@@ -346,6 +549,8 @@ __device__ __forceinline__ MgLevel small_view(const MgSmall &S, float *sm, int l
 // the phases.
 __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 {
+    pdl_wait();
+    pdl_allow();
     if (*S.done) return;
     extern __shared__ float4 small_sm4[];
     float *sm = reinterpret_cast<float *>(small_sm4);
@@ -440,6 +645,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 __global__ void __launch_bounds__(kBlock)
 k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, double *partials, unsigned int *counter)
 {
+    pdl_wait();
+    pdl_allow();
     const double nr = (rn2 && *rn2 > 0.0) ? sqrt(*rn2) : 1.0;
     const float s = (float)(1.0 / nr);
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->rhs_scale = nr;
@@ -489,6 +696,8 @@ __global__ void __launch_bounds__(kBlock)
 k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, float *__restrict__ p0, BicgScal *sc,
          double *partials, unsigned int *counter)
 {
+    pdl_wait();
+    pdl_allow();
     if (!p0 && sc->done) return;
     float pa = 0.f;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
@@ -539,6 +748,8 @@ __global__ void __launch_bounds__(kBlock)
 k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float *__restrict__ h,
          const float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter)
 {
+    pdl_wait();
+    pdl_allow();
     if (sc->done) return;
     const float alpha = (float)sc->alpha;
     float pa = 0.f, ps = 0.f;
@@ -746,6 +957,8 @@ int mg_setup(cfd_ctx *c)
     if (G.nlev > 0) return CFD_OK;
     const Geo &g = c->g;
     if (const char *e = std::getenv("CFDGPU_MG_SWEEPS")) G.sweeps = std::atoi(e) > 0 ? std::atoi(e) : 2;
+    G.sweeps0 = G.sweeps;
+    if (const char *e = std::getenv("CFDGPU_MG_SWEEPS0")) G.sweeps0 = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_PAIRS")) G.pairs = std::atoi(e) > 0 ? std::atoi(e) : 1;
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
@@ -817,6 +1030,30 @@ int mg_setup(cfd_ctx *c)
     if (G.small_smem > kMgSmallSmem) return fail(CFD_ERR_STATE, "multigrid: coarsest level too large for shared memory");
     CK(cudaFuncSetAttribute(k_mg_small, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
     CKS(small_image(c, G));
+    // fused sweeps on the grid-wide levels with float4 rows: about 128
+    // threads a block (TJ rows x nz/4 quads), chunks of CI planes sized for
+    // about six blocks per SM, a second x buffer each
+    // off by default: at 512x256x32 a fused pass took 45 us against 2 x 12.4 us
+    // for the two colour launches (the plane march is latency-bound)
+    bool fused = false;
+    if (const char *e = std::getenv("CFDGPU_MG_FUSED")) fused = std::atoi(e) != 0;
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    for (int l = 0; l < G.first_small; ++l) {
+        MgLevel &L = G.lev[l];
+        L.sweep_tj = L.sweep_ci = 0;
+        if (!fused || !L.quads || level_sweeps(G, l) % 2 != 0) continue;
+        const int n4 = L.nz / 4;
+        const int tj = std::max(1, std::min({128 / std::max(n4, 1), L.ny, 1024 / n4}));
+        if (tj * n4 > 1024 || (long long)sweep_smem(tj, L.nz) > kSweepSmemMax) continue;
+        const long long tiles = (L.ny + tj - 1) / tj;
+        const int ci = (int)std::max(4LL, std::min(16LL, (long long)L.nx * tiles / (6LL * std::max(sms, 1))));
+        CKS(dalloc_t(c, &L.xalt, (size_t)L.n));
+        L.sweep_tj = tj;
+        L.sweep_ci = ci;
+    }
+    CK(cudaFuncSetAttribute(k_mg_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSweepSmemMax));
     CKS(dalloc_t(c, &G.never, 1));
     CK(cudaMemset(G.never, 0, sizeof(int)));
     return CFD_OK;
@@ -837,11 +1074,48 @@ static MgSmall small_desc(const Mg &G, const int *done)
     return S;
 }
 
+static void smooth_launch(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s);
+
+// one fused sweep (colour c0 then 1 - c0) of a grid-wide level, xo -> xn
+static void sweep_launch(const MgLevel &L, const float *xo, float *xn, int c0, int zero_init, const int *done,
+                         cudaStream_t s)
+{
+    const int tiles = (L.ny + L.sweep_tj - 1) / L.sweep_tj, chunks = (L.nx + L.sweep_ci - 1) / L.sweep_ci;
+    launch_pdl(k_mg_sweep, dim3(tiles * chunks), dim3(L.sweep_tj * (L.nz / 4)), sweep_smem(L.sweep_tj, L.nz), s, L,
+               (const float *)L.b, xo, xn, c0, zero_init, done);
+}
+
+// the pre-smoothing (c0 = 0, from x = 0) or post-smoothing (c0 = 1, from x) of
+// a grid-wide level: fused sweeps alternate between x and xalt and end in x
+// (an even number of sweeps), else colour launches in place
+static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStream_t s)
+{
+    const MgLevel &L = G.lev[l];
+    const int sweeps = level_sweeps(G, l);
+    if (L.sweep_tj > 0) {
+        const float *src = L.x;
+        for (int q = 0; q < sweeps; ++q) {
+            float *dst = ((sweeps - 1 - q) % 2 == 0) ? L.x : L.xalt;
+            sweep_launch(L, src, dst, pre ? 0 : 1, pre && q == 0, done, s);
+            src = dst;
+        }
+        return;
+    }
+    for (int q = 0; q < sweeps; ++q) {
+        smooth_launch(L, pre ? 0 : 1, pre && q == 0, done, s);
+        smooth_launch(L, pre ? 1 : 0, 0, done, s);
+    }
+}
+
 // one colour of the smoother over a grid-wide level
 static void smooth_launch(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
 {
-    if (L.quads) k_mg_smooth4<<<nblk(L.n / 4), kBlock, 0, s>>>(L, L.b, L.x, color, zero_init, done);
-    else k_mg_smooth<<<nblk((L.nz % 2 == 0) ? L.n / 2 : L.n), kBlock, 0, s>>>(L, L.b, L.x, color, zero_init, done);
+    if (L.quads)
+        launch_pdl(k_mg_smooth4, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
+                   zero_init, done);
+    else
+        launch_pdl(k_mg_smooth, dim3(nblk((L.nz % 2 == 0) ? L.n / 2 : L.n)), dim3(kBlock), 0, s, L,
+                   (const float *)L.b, L.x, color, zero_init, done);
 }
 
 // z = V(h): one V-cycle; every kernel returns at once when *done
@@ -852,22 +1126,18 @@ void mg_vcycle(cfd_ctx *c, const int *done)
     const int fs = G.first_small;
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
-        for (int q = 0; q < G.sweeps; ++q) {
-            smooth_launch(L, 0, q == 0, done, s);
-            smooth_launch(L, 1, 0, done, s);
-        }
-        k_mg_restrict<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], L.b, L.x, G.lev[l + 1].b, done);
+        smooth_phase(G, l, true, done, s);
+        launch_pdl(k_mg_restrict, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1], (const float *)L.b,
+                   (const float *)L.x, G.lev[l + 1].b, done);
     }
-    k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
+    launch_pdl(k_mg_small, dim3(1), dim3(kSmallThreads), G.small_smem, s, small_desc(G, done));
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
-        k_mg_prolong<<<nblk(G.lev[l + 1].n), kBlock, 0, s>>>(L, G.lev[l + 1], G.lev[l + 1].x, L.x, done);
-        for (int q = 0; q < G.sweeps; ++q) {
-            smooth_launch(L, 1, 0, done, s);
-            smooth_launch(L, 0, 0, done, s);
-        }
+        launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1],
+                   (const float *)G.lev[l + 1].x, L.x, done);
+        smooth_phase(G, l, false, done, s);
     }
-    c->launches += (4LL * G.sweeps + 2) * fs + 1;
+    c->launches += mg_vcycle_launches(G);
 }
 
 // one piece of the V-cycle for timing: 0 finest smoothing colour, 1 finest
@@ -882,23 +1152,36 @@ void mg_time_part(cfd_ctx *c, int part)
     else if (part == 1) k_mg_restrict<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], L.b, L.x, G.lev[1].b, done);
     else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
     else if (part == 3) k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
-    else mg_vcycle(c, done);
+    else if (part == 5) {
+        if (L.sweep_tj > 0) sweep_launch(L, L.x, L.xalt, 0, 0, done, s);
+    }
+    else if (part == 4) mg_vcycle(c, done);
+}
+
+// kernel launches of one V-cycle
+long long mg_vcycle_launches(const Mg &G)
+{
+    long long n = 1;
+    for (int l = 0; l < G.first_small; ++l) n += 2 + (G.lev[l].sweep_tj > 0 ? 1LL : 2LL) * 2 * level_sweeps(G, l);
+    return n;
 }
 
 void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc)
 {
     const FvOp<float> F = fv32(c);
-    k_mg_h<<<c->lc.red_blocks, kBlock, 0, c->s>>>(F, h, rn2, sc, c->lc.partials, c->lc.counter);
+    launch_pdl(k_mg_h, dim3(c->lc.red_blocks), dim3(kBlock), 0, c->s, F, h, rn2, sc, c->lc.partials, c->lc.counter);
 }
 
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc)
 {
-    k_mg_rho<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, h, z, p0, sc, c->lc.partials, c->lc.counter);
+    launch_pdl(k_mg_rho, dim3(c->lc.red_blocks), dim3(kBlock), 0, c->s, c->g.n, h, z, p0, sc, c->lc.partials,
+               c->lc.counter);
 }
 
 void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc)
 {
-    k_mg_upd<<<c->lc.red_blocks, kBlock, 0, c->s>>>(c->g.n, e, p, h, q, sc, c->lc.partials, c->lc.counter);
+    launch_pdl(k_mg_upd, dim3(c->lc.red_blocks), dim3(kBlock), 0, c->s, c->g.n, e, p, h, q, sc, c->lc.partials,
+               c->lc.counter);
 }
 
 }  // namespace cfd

@@ -567,6 +567,8 @@ __global__ void __launch_bounds__(kBlock, 5)
 k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p, float *__restrict__ pn,
         float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter, int TK, int ichunk)
 {
+    pdl_wait();
+    pdl_allow();
     if (sc->done) return;
     const SpeOp<float> &A = F.A;
     const int TJ = kBlock / TK, SW = TK + 2;
@@ -746,6 +748,8 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
     using G = CgTile<TK>;
     constexpr int NV = first ? 1 : 2;
     constexpr int MAXH = (G::NHALO + kBlock - 1) / kBlock;  // halo items per thread
+    pdl_wait();
+    pdl_allow();
     if (sc->done) return;
     extern __shared__ unsigned char dsm[];
     const unsigned base = (smem_u32(dsm) + 127u) & ~127u;
@@ -1103,10 +1107,11 @@ static void launch_tma_t(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t
     cg_tma_launch_shape(t, F, ichunk, grid);
     const size_t sm = CgTile<TK>::smem(first ? 1 : 2);
     if (form_z)
-        k_cg_pq_tma<first, TK, true><<<grid, kBlock, sm, c.s>>>(F, *mz, *mp, pn, q, sc, c.partials, c.counter, ichunk);
+        launch_pdl(k_cg_pq_tma<first, TK, true>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, pn, q, sc, c.partials,
+                   c.counter, ichunk);
     else
-        k_cg_pq_tma<first, TK, false><<<grid, kBlock, sm, c.s>>>(F, *mz, *mp, pn, q, sc, c.partials, c.counter,
-                                                                 ichunk);
+        launch_pdl(k_cg_pq_tma<first, TK, false>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, pn, q, sc,
+                   c.partials, c.counter, ichunk);
 }
 
 // z_map: the z vector (or p itself on the first iteration), p_map: p
@@ -1138,11 +1143,11 @@ void launch_cg_pq_mg(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma *tma, 
     }
     const CgShape cs = cg_shape(c, F);
     if (first)
-        k_cg_pq<true><<<cs.grid, kBlock, 0, c.s>>>(F, P[from], P[from], P[from], q, sc, c.partials, c.counter, cs.TK,
-                                                   cs.ichunk);
+        launch_pdl(k_cg_pq<true>, dim3(cs.grid), dim3(kBlock), 0, c.s, F, (const float *)P[from],
+                   (const float *)P[from], P[from], q, sc, c.partials, c.counter, cs.TK, cs.ichunk);
     else
-        k_cg_pq<false><<<cs.grid, kBlock, 0, c.s>>>(F, z, P[from], P[to], q, sc, c.partials, c.counter, cs.TK,
-                                                    cs.ichunk);
+        launch_pdl(k_cg_pq<false>, dim3(cs.grid), dim3(kBlock), 0, c.s, F, (const float *)z, (const float *)P[from],
+                   P[to], q, sc, c.partials, c.counter, cs.TK, cs.ichunk);
 }
 
 void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
@@ -1554,38 +1559,44 @@ void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc
 // FP32 right-hand side of the next inner solve, and the FP64 correction.
 template <class Op, class V>
 __global__ void __launch_bounds__(kBlock)
+// (with bout != null also |b|^2 in the same pass, the defect correction's reference norm)
 k_residual64(Op A, const double *__restrict__ b, const double *__restrict__ x, V *__restrict__ r32,
-             double *partials, unsigned int *counter, double *out)
+             double *partials, unsigned int *counter, double *out, double *bout)
 {
-    double acc[1] = {0.0};
+    double acc[2] = {0.0, 0.0};
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < A.n;
          row += (long long)gridDim.x * blockDim.x) {
-        const double r = b[row] - apply_row(A, x, row);
+        const double bv = b[row];
+        const double r = bv - apply_row(A, x, row);
         r32[row] = (V)r;
         acc[0] += r * r;
+        acc[1] += bv * bv;
     }
-    double tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) *out = tot[0];
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        *out = tot[0];
+        if (bout) *bout = tot[1];
+    }
 }
 
 template <class V>
 void launch_residual64(cfd_launch_ctx &c, const SpeOp<double> &A, const double *b, const double *x,
-                       V *r32, double *norm2_out)
+                       V *r32, double *norm2_out, double *bnorm2_out)
 {
     k_residual64<SpeOp<double>, V><<<c.red_blocks, kBlock, 0, c.s>>>(A, b, x, r32, c.partials,
-                                                                     c.counter, norm2_out);
+                                                                     c.counter, norm2_out, bnorm2_out);
 }
 template <class V>
 void launch_residual64_ell(cfd_launch_ctx &c, const EllOp<double> &A, const double *b,
-                           const double *x, V *r32, double *norm2_out)
+                           const double *x, V *r32, double *norm2_out, double *bnorm2_out)
 {
     k_residual64<EllOp<double>, V><<<c.red_blocks, kBlock, 0, c.s>>>(A, b, x, r32, c.partials,
-                                                                     c.counter, norm2_out);
+                                                                     c.counter, norm2_out, bnorm2_out);
 }
 template void launch_residual64<float>(cfd_launch_ctx &, const SpeOp<double> &, const double *,
-                                       const double *, float *, double *);
+                                       const double *, float *, double *, double *);
 template void launch_residual64_ell<float>(cfd_launch_ctx &, const EllOp<double> &, const double *,
-                                           const double *, float *, double *);
+                                           const double *, float *, double *, double *);
 
 // x += e (FP64 accumulation of an FP32 correction)
 template <class V>

@@ -249,6 +249,7 @@ typedef enum {
     CFD_KERNEL_MG_VCYCLE,    /* multigrid: one whole V-cycle (all its launches) */
     CFD_KERNEL_MG_UPD,       /* multigrid CG: e, h update */
     CFD_KERNEL_MG_RHO,       /* multigrid CG: h.z and the scalar update */
+    CFD_KERNEL_MG_SWEEP,     /* multigrid: one fused red-black sweep on the finest level */
     CFD_KERNEL_COUNT
 } cfd_kernel_id;
 
