@@ -79,6 +79,12 @@ __device__ __forceinline__ float4 tl4(const float *p)
 template <bool SM>
 using Ix = std::conditional_t<SM, int, long long>;
 
+// 1 / diag of the smoother: the approximate reciprocal (2 ulp, one
+// special-function instruction); every smoothing path and the small levels'
+// per-cell tables use this same function, so the V-cycle stays one fixed
+// symmetric operator
+__device__ __forceinline__ float smooth_rcp(float d) { return __fdividef(1.0f, d); }
+
 // the neighbour sum of L at (i, j, k), cell t
 template <bool SM = false>
 __device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict__ x, int i, int j, int k, Ix<SM> t)
@@ -115,23 +121,23 @@ __device__ __forceinline__ void gs_cell(const MgLevel &L, const float *__restric
 {
     const float nb = zero_init ? 0.f : mg_nb<SM>(L, x, i, j, k, t);
     if constexpr (SM) x[t] = fmaf(b[t], L.rv[t], nb) * L.rg[t];
-    else x[t] = fmaf(b[t], mg_rdv<SM>(L, i, j, k), nb) * __frcp_rn(mg_diag<SM>(L, i, j, k));
+    else x[t] = fmaf(b[t], mg_rdv<SM>(L, i, j, k), nb) * smooth_rcp(mg_diag<SM>(L, i, j, k));
 }
 
 // one colour over a level with nz % 4 == 0: one thread per quad of cells
 // k = 4m..4m+3 (float4 rows), updating the two cells of that colour
-template <bool SM = false>
+template <bool SM = false, class I = Ix<SM>>
 __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
-                                             int color, bool zero_init, Ix<SM> t0, Ix<SM> stride)
+                                             int color, bool zero_init, I t0, I stride)
 {
-    const Ix<SM> nq = L.n >> 2;
+    const I nq = (I)(L.n >> 2);
     const int n4 = L.nz >> 2;
-    const Ix<SM> sx = (Ix<SM>)L.ny * L.nz, sy = L.nz;
-    for (Ix<SM> q = t0; q < nq; q += stride) {
+    const I sx = (I)L.ny * L.nz, sy = L.nz;
+    for (I q = t0; q < nq; q += stride) {
         const unsigned u = (unsigned)q;
         const unsigned i = L.fyq.div(u), r = u - i * (unsigned)(L.ny * n4), j = L.fq.div(r);
         const int k0 = 4 * (int)(r - j * (unsigned)n4);
-        const Ix<SM> t = ((Ix<SM>)i * L.ny + j) * L.nz + k0;
+        const I t = ((I)i * L.ny + j) * L.nz + k0;
         const int e0 = (int)((color + i + j) & 1u);  // first updated cell of the quad: e0, then e0 + 2
         const bool odd = e0 != 0;
         // the two cells of the colour sit at quad offsets e0 and e0 + 2:
@@ -154,8 +160,8 @@ __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__re
             const float4 sz = tl4<SM>(L.sum[2] + k0);
             rA = rxy * pick(rz.x, rz.y);
             rB = rxy * pick(rz.z, rz.w);
-            dA = __frcp_rn(sxy + pick(sz.x, sz.y));
-            dB = __frcp_rn(sxy + pick(sz.z, sz.w));
+            dA = smooth_rcp(sxy + pick(sz.x, sz.y));
+            dB = smooth_rcp(sxy + pick(sz.z, sz.w));
         }
         float4 xc = make_float4(0.f, 0.f, 0.f, 0.f);
         float nA = 0.f, nB = 0.f;
@@ -280,7 +286,7 @@ __global__ void k_mg_cell_tables(MgLevel L, float *__restrict__ rv, float *__res
         int i, j, k;
         decomp(L, t, i, j, k);
         rv[t] = mg_rdv(L, i, j, k);
-        rg[t] = __frcp_rn(mg_diag(L, i, j, k));
+        rg[t] = smooth_rcp(mg_diag(L, i, j, k));
     }
 }
 
@@ -294,15 +300,17 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b,
                  (long long)gridDim.x * blockDim.x);
 }
 
-// the float4 form (nz % 4 == 0) as its own kernel
+// the float4 form (nz % 4 == 0) as its own kernel; I = int where every
+// index of the level fits (fewer instructions per quad)
+template <class I>
 __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, const float *b, float *x, int color,
                                                           int zero_init, const int *done)
 {
     pdl_wait();
     pdl_allow();
     if (*done) return;
-    smooth_quads(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
-                 (long long)gridDim.x * blockDim.x);
+    smooth_quads<false, I>(L, b, x, color, zero_init != 0, (I)blockIdx.x * blockDim.x + threadIdx.x,
+                           (I)gridDim.x * blockDim.x);
 }
 
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, const float *bf, const float *xf,
@@ -450,8 +458,8 @@ k_mg_sweep(MgLevel L, const float *__restrict__ b, const float *__restrict__ xo,
                     nB = fmaf(pick(czm.z, czm.w), pick(c.y, c.z), nB);
                     nB = fmaf(pick(czp.z, czp.w), pick(c.w, zhi), nB);
                     if (zero_init) nA = nB = 0.f;
-                    const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), nA) * __frcp_rn(sxy + pick(sz.x, sz.y));
-                    const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), nB) * __frcp_rn(sxy + pick(sz.z, sz.w));
+                    const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), nA) * smooth_rcp(sxy + pick(sz.x, sz.y));
+                    const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), nB) * smooth_rcp(sxy + pick(sz.z, sz.w));
                     out = make_float4(odd ? 0.f : vA, odd ? vA : 0.f, odd ? 0.f : vB, odd ? vB : 0.f);
                 }
                 *reinterpret_cast<float4 *>(dst + rr * nz + k0) = out;
@@ -500,8 +508,8 @@ k_mg_sweep(MgLevel L, const float *__restrict__ b, const float *__restrict__ xo,
                 nB = fmaf(cyp, pick(vyp.z, vyp.w), nB);
                 nB = fmaf(pick(czm.z, czm.w), pick(c.y, c.z), nB);
                 nB = fmaf(pick(czp.z, czp.w), pick(c.w, zhi), nB);
-                const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), nA) * __frcp_rn(sxy + pick(sz.x, sz.y));
-                const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), nB) * __frcp_rn(sxy + pick(sz.z, sz.w));
+                const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), nA) * smooth_rcp(sxy + pick(sz.x, sz.y));
+                const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), nB) * smooth_rcp(sxy + pick(sz.z, sz.w));
                 // c0 cells keep the values of the first half of the sweep
                 const float4 o = make_float4(odd ? c.x : vA, odd ? vA : c.y, odd ? c.z : vB, odd ? vB : c.w);
                 *reinterpret_cast<float4 *>(xn + qo * sx + (long long)j * nz + k0) = o;
@@ -1110,9 +1118,12 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
 // one colour of the smoother over a grid-wide level
 static void smooth_launch(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
 {
-    if (L.quads)
-        launch_pdl(k_mg_smooth4, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
+    if (L.quads && L.n + (long long)L.ny * L.nz < (1LL << 31))
+        launch_pdl(k_mg_smooth4<int>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
                    zero_init, done);
+    else if (L.quads)
+        launch_pdl(k_mg_smooth4<long long>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x,
+                   color, zero_init, done);
     else
         launch_pdl(k_mg_smooth, dim3(nblk((L.nz % 2 == 0) ? L.n / 2 : L.n)), dim3(kBlock), 0, s, L,
                    (const float *)L.b, L.x, color, zero_init, done);
