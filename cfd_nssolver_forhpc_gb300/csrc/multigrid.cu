@@ -657,7 +657,10 @@ k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, do
     pdl_allow();
     const double nr = (rn2 && *rn2 > 0.0) ? sqrt(*rn2) : 1.0;
     const float s = (float)(1.0 / nr);
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->rhs_scale = nr;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->rhs_scale = nr;
+        sc->wait_timeout = 0;  // the solve's bounded waits (TMA pipeline) report here
+    }
     float pa = 0.f, ps = 0.f;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
     const int nz = F.A.nzc, ny = F.A.nyc;
@@ -732,7 +735,6 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
         sc->timestep += 1;
         sc->done = (tot[0] != 0.0 && sc->r0n2 != 0.0) ? BICG_RUNNING : BICG_ZERO_RHS;
         sc->relres = sc->done == BICG_RUNNING ? 1.0 : 0.0;
-        sc->wait_timeout = 0;
         return;
     }
     if (sc->iter + 1 >= sc->maxit) {
