@@ -104,6 +104,7 @@ def lib() -> C.CDLL:
         "cfd_download": ([vp, i, dp, sz], i),
         "cfd_field_count": ([vp, i], sz),
         "cfd_host_register": ([vp, sz], i),
+        "cfd_host_mapped": ([vp], i),
         "cfd_host_unregister": ([vp], i),
         "cfd_init_uniform": ([vp, d, d, d], i),
         "cfd_start": ([vp], i),

@@ -769,6 +769,55 @@ void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b)
     k_convert<A, B><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, b);
 }
 
+// Copy with conversion where one side is a registered host buffer reached
+// through its device mapping (NVLink-C2C on Grace systems): 16-byte vector
+// accesses, four elements per thread step, so many link transactions are in
+// flight; a scalar tail covers n % 4.  Both pointers are 16-byte aligned
+// (checked by the caller).
+template <class A, class B>
+__device__ __forceinline__ void ld4(const A *p, A (&v)[4])
+{
+    if constexpr (sizeof(A) == 8) {
+        const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    } else {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+}
+template <class B>
+__device__ __forceinline__ void st4(B *p, const B (&v)[4])
+{
+    if constexpr (sizeof(B) == 8) {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+    } else {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+template <class A, class B>
+__global__ void __launch_bounds__(kBlock) k_link_copy(long long n, const A *__restrict__ a, B *__restrict__ b)
+{
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    const long long n4 = n >> 2;
+    for (long long q = t0; q < n4; q += st) {
+        A v[4];
+        ld4<A, B>(a + 4 * q, v);
+        B w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) w[e] = (B)v[e];
+        st4<B>(b + 4 * q, w);
+    }
+    for (long long m = 4 * n4 + t0; m < n; m += st) b[m] = (B)a[m];
+}
+
+template <class A, class B>
+void launch_link_copy(cfd_launch_ctx &c, long long n, const A *a, B *b)
+{
+    k_link_copy<A, B><<<blocks_for((n + 3) / 4, c.grid_cap), kBlock, 0, c.s>>>(n, a, b);
+}
+
 #define CFD_FLOW_INSTANTIATE(T)                                                                   \
     template void launch_convdiff<T>(cudaStream_t, const Geo &, const Metrics<T> &, T, T,        \
                                      const T *, const T *, const T *, T *, T *, T *, const T *,  \
@@ -804,5 +853,8 @@ CFD_FLOW_INSTANTIATE(double)
 CFD_FLOW_INSTANTIATE(float)
 template void launch_convert<double, float>(cfd_launch_ctx &, long long, const double *, float *);
 template void launch_convert<float, double>(cfd_launch_ctx &, long long, const float *, double *);
+template void launch_link_copy<double, float>(cfd_launch_ctx &, long long, const double *, float *);
+template void launch_link_copy<float, double>(cfd_launch_ctx &, long long, const float *, double *);
+template void launch_link_copy<double, double>(cfd_launch_ctx &, long long, const double *, double *);
 
 }  // namespace cfd

@@ -72,6 +72,10 @@ template <class T>
 void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val);
 template <class A, class B>
 void launch_convert(cfd_launch_ctx &c, long long n, const A *a, B *b);
+// element copy with conversion where a or b is the device mapping of a
+// registered host buffer (16-byte aligned)
+template <class A, class B>
+void launch_link_copy(cfd_launch_ctx &c, long long n, const A *a, B *b);
 
 // ---- poisson.cu ----
 

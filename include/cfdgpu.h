@@ -156,9 +156,16 @@ int cfd_set_metrics(cfd_ctx *ctx, const double *X, const double *Y, const double
 int cfd_upload(cfd_ctx *ctx, int field, const double *host, size_t count);
 int cfd_download(cfd_ctx *ctx, int field, double *host, size_t count);
 size_t cfd_field_count(cfd_ctx *ctx, int field);
-/* Page-lock a host buffer for faster uploads/downloads (cudaHostRegister). */
+/* Page-lock and map a host buffer (cudaHostRegister, mapped).  cfd_upload
+   reads a host buffer the GPU can address (registered and mapped, or any host
+   memory on systems with address translation such as Grace) that starts on a
+   16-byte boundary with one kernel over the host link, conversion to FP32
+   fields included; other buffers, and every download, go through copies.
+   Both forms give identical data. */
 int cfd_host_register(void *host, size_t bytes);
 int cfd_host_unregister(void *host);
+/* 1 when cfd_upload reads this buffer by the direct kernel path, else 0. */
+int cfd_host_mapped(const void *host);
 /* velocity::iniU (physicalVariables.hpp:53) on T0, T1, T3 and p = 0
    (RUN_CPU_PC_METHOD.hpp:84-89) */
 int cfd_init_uniform(cfd_ctx *ctx, double ui, double vi, double wi);
