@@ -48,7 +48,7 @@ class CfdConfig(C.Structure):
                 ("aligned_source", C.c_int), ("compat_rhs", C.c_int),
                 ("bc_dir", (C.c_double * 3) * 6), ("bc_num", (C.c_double * 3) * 6),
                 ("check_every", C.c_int), ("inner_tol", C.c_double), ("max_outer", C.c_int),
-                ("inner_solver", C.c_int), ("les_smagorinsky", C.c_int)]
+                ("inner_solver", C.c_int), ("les_smagorinsky", C.c_int), ("conv_outflow_uc", C.c_double)]
 
 
 class CfdStepInfo(C.Structure):

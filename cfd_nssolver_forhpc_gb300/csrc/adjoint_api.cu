@@ -342,6 +342,8 @@ int cfd_adj_enable(cfd_ctx *c, int tape_len)
     if (c->cfg.solver == CFD_SOLVER_SOR_RB)
         return fail(CFD_ERR_ARG, "the adjoint needs a Krylov pressure solver (SPE or ELL)");
     if (c->cfg.les_smagorinsky) return fail(CFD_ERR_ARG, "the adjoint does not cover the Smagorinsky model");
+    if (c->cfg.conv_outflow_uc > 0.0)
+        return fail(CFD_ERR_ARG, "the adjoint does not cover the convective outflow condition");
     if (tape_len < 1) return fail(CFD_ERR_ARG, "tape_len must be at least 1");
     if (c->adj) {
         if (tape_len > c->adj->tape_len) CKS(alloc_tape(c, tape_len));

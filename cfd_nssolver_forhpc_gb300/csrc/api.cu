@@ -506,9 +506,17 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
         CK(cudaGetLastError());
     }
     const size_t bytes = (size_t)g.ng * sizeof(T);
+    const bool conv = c->cfg.conv_outflow_uc > 0.0;
+    if (conv) {  // convective outflow from the old T0 into T3, before T0 <- T3
+        launch_bc_convective<T>(c->lc, g, metrics_of<double>(c), c->cfg.dt, c->cfg.conv_outflow_uc, u0, v0, w0,
+                                u3, v3, w3, c->dscal + 6);
+        c->launches += 2;
+        CK(cudaGetLastError());
+    }
     for (int q = 0; q < 3; ++q)
         CK(cudaMemcpyAsync(c->vel[0][q], c->vel[2][q], bytes, cudaMemcpyDeviceToDevice, c->s));
-    const BcTab bc = bc_tab(c);
+    BcTab bc = bc_tab(c);
+    bc.skip_outflow = conv ? 1 : 0;
     launch_bc_main<T>(c->s, g, bc, u0, v0, w0, c->p);
     launch_bc_copy<T>(c->s, g, u0, v0, w0, u1, v1, w1);
     launch_cdcl<T>(c->lc, g, metrics_of<double>(c), c->cfg.lz, f, c->dscal + 1);
@@ -693,6 +701,7 @@ int cfd_config_default(cfd_config *cfg, int nx, int ny, int nz)
     cfg->inner_tol = 1e-3;
     cfg->inner_solver = CFD_INNER_MG;
     cfg->max_outer = 30;
+    cfg->conv_outflow_uc = 0.0;
     cfg->les_smagorinsky = 0;
     return CFD_OK;
 }
@@ -719,6 +728,10 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (k.les_smagorinsky != 0 && k.les_smagorinsky != 1) return fail(CFD_ERR_ARG, "les_smagorinsky must be 0 or 1");
     if (k.inner_solver != CFD_INNER_CG && k.inner_solver != CFD_INNER_BICGSTAB && k.inner_solver != CFD_INNER_MG)
         return fail(CFD_ERR_ARG, "unknown inner solver");
+    if (!(k.conv_outflow_uc >= 0.0) || !std::isfinite(k.conv_outflow_uc))
+        return fail(CFD_ERR_ARG, "conv_outflow_uc must be finite and >= 0");
+    if (k.conv_outflow_uc > 0.0 && !(k.conv_outflow_uc * k.dt <= 0.5 * 1e300))
+        return fail(CFD_ERR_ARG, "conv_outflow_uc out of range");
     if (k.precision == CFD_PREC_MIXED && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
         return fail(CFD_ERR_ARG, "mixed precision needs 0 < inner_tol < 1 and max_outer >= 1");
 

@@ -273,6 +273,7 @@ inline BcTab bc_tab(const cfd_ctx *c)
         bc.num[q] = c->cfg.bc_num[q / 3][q % 3];
     }
     bc.inflow = c->inflow;
+    bc.skip_outflow = 0;
     return bc;
 }
 

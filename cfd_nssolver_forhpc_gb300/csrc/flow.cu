@@ -375,9 +375,11 @@ __global__ void k_bc_main(Geo g, BcTab bc, int phase, T *__restrict__ u, T *__re
         u[I(1)] = x; u[I(0)] = x;
         x = bc_tan<T>(bc, 0, 1, v[I(2)]); v[I(1)] = x; v[I(0)] = x;
         x = bc_tan<T>(bc, 0, 2, w[I(2)]); w[I(1)] = x; w[I(0)] = x;
-        x = bc_norm<T>(bc, 1, 0, u[I(nx - 4)]); u[I(nx - 3)] = x; u[I(nx - 2)] = x; u[I(nx - 1)] = x;
-        x = bc_tan<T>(bc, 1, 1, v[I(nx - 3)]); v[I(nx - 2)] = x; v[I(nx - 1)] = x;
-        x = bc_tan<T>(bc, 1, 2, w[I(nx - 3)]); w[I(nx - 2)] = x; w[I(nx - 1)] = x;
+        if (!bc.skip_outflow) {
+            x = bc_norm<T>(bc, 1, 0, u[I(nx - 4)]); u[I(nx - 3)] = x; u[I(nx - 2)] = x; u[I(nx - 1)] = x;
+            x = bc_tan<T>(bc, 1, 1, v[I(nx - 3)]); v[I(nx - 2)] = x; v[I(nx - 1)] = x;
+            x = bc_tan<T>(bc, 1, 2, w[I(nx - 3)]); w[I(nx - 2)] = x; w[I(nx - 1)] = x;
+        }
         double q = p[I(2)]; p[I(1)] = q; p[I(0)] = q;
         q = p[I(nx - 3)]; p[I(nx - 2)] = q; p[I(nx - 1)] = q;
     } else if (phase == 1) {
@@ -403,6 +405,63 @@ __global__ void k_bc_main(Geo g, BcTab bc, int phase, T *__restrict__ u, T *__re
         double q = p[K(2)]; p[K(1)] = q; p[K(0)] = q;
         q = p[K(nz - 3)]; p[K(nz - 2)] = q; p[K(nz - 1)] = q;
     }
+}
+
+// Convective outflow (extension): per interior (j, k) of the x-max face,
+//   u_b = u0_b - C (u0_b - u0_{b-1}),  C = uc dt / Dx[nx-3]   (face nx-3)
+//   v_g = v0_g - Ct (v0_g - v0_{g-1}), Ct = uc dt / Dxs[nx-3] (ghost nx-2)
+// (w as v), written into the new field; the flux sums of the inflow face
+// (u0 at face 1) and of the new outflow face give the scale of the second
+// kernel, which also fills the outer ghosts.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_bc_conv(Geo g, Metrics<double> m, double dt, double uc, const T *__restrict__ u0, const T *__restrict__ v0,
+          const T *__restrict__ w0, T *__restrict__ u3, T *__restrict__ v3, T *__restrict__ w3, double *partials,
+          unsigned int *counter, double *scale_out)
+{
+    const int nx = g.nx;
+    const double C = uc * dt / m.x(AX_D, nx - 3), Ct = uc * dt / m.x(AX_DS, nx - 3);
+    double acc[2] = {0.0, 0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < (long long)g.nyc * g.nzc;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(t / g.nzc) + GC, k = (int)(t % g.nzc) + GC;
+        auto I = [&](int i) { return icel(g, i, j, k); };
+        const double ub = (double)u0[I(nx - 3)] - C * ((double)u0[I(nx - 3)] - (double)u0[I(nx - 4)]);
+        const double vg = (double)v0[I(nx - 2)] - Ct * ((double)v0[I(nx - 2)] - (double)v0[I(nx - 3)]);
+        const double wg = (double)w0[I(nx - 2)] - Ct * ((double)w0[I(nx - 2)] - (double)w0[I(nx - 3)]);
+        u3[I(nx - 3)] = (T)ub;
+        v3[I(nx - 2)] = (T)vg; v3[I(nx - 1)] = (T)vg;
+        w3[I(nx - 2)] = (T)wg; w3[I(nx - 1)] = (T)wg;
+        const double area = m.y(AX_D, j) * m.z(AX_D, k);
+        acc[0] += (double)u0[I(1)] * area;
+        acc[1] += (double)(T)ub * area;
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0)
+        *scale_out = tot[1] != 0.0 ? tot[0] / tot[1] : 1.0;
+}
+
+template <class T>
+__global__ void k_bc_conv_scale(Geo g, const double *__restrict__ scale, T *__restrict__ u3)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.nyc * g.nzc) return;
+    const int j = (int)(t / g.nzc) + GC, k = (int)(t % g.nzc) + GC, nx = g.nx;
+    const long long b = icel(g, nx - 3, j, k);
+    const T x = (T)((double)u3[b] * *scale);
+    u3[b] = x;
+    u3[b + g.sx] = x;
+    u3[b + 2 * g.sx] = x;
+}
+
+template <class T>
+void launch_bc_convective(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double dt, double uc,
+                          const T *u0, const T *v0, const T *w0, T *u3, T *v3, T *w3, double *scale_out)
+{
+    k_bc_conv<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, dt, uc, u0, v0, w0, u3, v3, w3, c.partials, c.counter,
+                                                  scale_out);
+    const int blocks = (int)(((long long)g.nyc * g.nzc + kBlock - 1) / kBlock);
+    k_bc_conv_scale<T><<<blocks, kBlock, 0, c.s>>>(g, scale_out, u3);
 }
 
 // BC_staggered_copy (updateBC.hpp:6-111): the three face sets are disjoint,
@@ -836,6 +895,9 @@ void launch_link_copy(cfd_launch_ctx &c, long long n, const A *a, B *b)
                                  const T *, double *);                                           \
     template void launch_bc_main<T>(cudaStream_t, const Geo &, const BcTab &, T *, T *, T *,     \
                                     double *);                                                   \
+    template void launch_bc_convective<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double,  \
+                                          double, const T *, const T *, const T *, T *, T *, T *,  \
+                                          double *);                                               \
     template void launch_bc_copy<T>(cudaStream_t, const Geo &, const T *, const T *, const T *,  \
                                     T *, T *, T *);                                              \
     template void launch_div_inf<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,      \

@@ -15,6 +15,9 @@ struct BcTab {
     // optional per-j Dirichlet value of u on the x-min face (interior j,
     // nyc entries) replacing dir[0]
     const double *inflow;
+    // 1: the x-max face's velocities were set by the convective outflow
+    // condition (k_bc_conv), so the table leaves them alone
+    int skip_outflow;
 };
 
 // What a launcher needs besides its arguments: the stream, the fixed shape
@@ -134,6 +137,15 @@ template <class V>
 struct BicgVecs {
     V *r0, *r1, *p1, *s1, *ap, *as;
 };
+
+// convective outflow at the x-max face (extension; the reference has only the
+// Dirichlet/Neumann table): from the old field (u0, v0, w0) the outflow face
+// u and the ghost v, w move by first-order upwind with speed uc, into the new
+// field (u3, v3, w3); then u on that face is scaled so that its flux equals
+// the inflow face's (scale_out = flux in / flux out)
+template <class T>
+void launch_bc_convective(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double dt, double uc,
+                          const T *u0, const T *v0, const T *w0, T *u3, T *v3, T *w3, double *scale_out);
 
 // the WHILE condition of a solve loop inside one CUDA graph: continue while
 // sc->done is BICG_RUNNING, no bounded wait gave up and the body has run

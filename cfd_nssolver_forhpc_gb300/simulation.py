@@ -37,7 +37,8 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
                 precision: int = capi.PREC_FP64, tol: float | None = None, maxit: int = 5000,
                 omega: float | None = None, sor_maxit: int = 5000, aligned_source: bool = False,
                 compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-3,
-                max_outer: int = 30, inner_solver: int = capi.INNER_MG, les: bool = False) -> capi.CfdConfig:
+                max_outer: int = 30, inner_solver: int = capi.INNER_MG, les: bool = False,
+                conv_outflow_uc: float = 0.0) -> capi.CfdConfig:
     cfg = capi.CfdConfig()
     check(lib().cfd_config_default(C.byref(cfg), w.nxc, w.nyc, w.nzc))
     cfg.lx, cfg.ly, cfg.lz = w.lx, w.ly, w.lz
@@ -58,6 +59,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
     cfg.max_outer = max_outer
     cfg.inner_solver = inner_solver
     cfg.les_smagorinsky = int(les)
+    cfg.conv_outflow_uc = conv_outflow_uc
     return cfg
 
 

@@ -125,6 +125,10 @@ typedef struct {
     int inner_solver;           /* mixed precision: cfd_inner_solver */
     int les_smagorinsky;        /* 1: Smagorinsky eddy viscosity added to nu in the diffusion
                                    (source/smagorinskyModel.hpp:31, TERBULENCE_SMAGORINSKY) */
+    double conv_outflow_uc;     /* > 0: convective outflow at the x-max face with this speed
+                                   (first-order upwind of u on the face and of v, w in the ghost
+                                   cells, outflow flux scaled to the inflow flux at the end of
+                                   every step); 0: the Dirichlet/Neumann table (the reference's) */
 } cfd_config;
 
 typedef struct {

@@ -787,6 +787,12 @@ void og_cdcl(const og_grid *g, const double *f, double *cd, double *cl)
 void og_bc_main(const og_grid *g, const double *dir, const double *num,
                 double *u, double *v, double *w, double *p)
 {
+    og_bc_main_ex(g, dir, num, u, v, w, p, 0);
+}
+
+void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, double *u, double *v,
+                   double *w, double *p, int skip_outflow)
+{
     const int nx = g->nx, ny = g->ny, nz = g->nz;
 #define DIR(b, c) dir[(b) * 3 + (c)]
 #define NUM(b, c) num[(b) * 3 + (c)]
@@ -798,7 +804,7 @@ void og_bc_main(const og_grid *g, const double *dir, const double *num,
             w[icel(g, 1, j, k)] = w[icel(g, 0, j, k)] =
                 DIR(0, 2) * 2. + (2.0 * NUM(0, 2) - 1.0) * w[icel(g, 2, j, k)];
         }
-    for (int j = GC; j < ny - GC; ++j)
+    for (int j = GC; j < ny - GC && !skip_outflow; ++j)
         for (int k = GC; k < nz - GC; ++k) { /* BC_1 */
             u[icel(g, nx - 1, j, k)] = u[icel(g, nx - 2, j, k)] = u[icel(g, nx - 3, j, k)] =
                 DIR(1, 0) + NUM(1, 0) * u[icel(g, nx - 4, j, k)];
@@ -858,6 +864,34 @@ void og_bc_main(const og_grid *g, const double *dir, const double *num,
         for (int j = GC; j < ny - GC; ++j) {
             p[icel(g, i, j, 1)] = p[icel(g, i, j, 0)] = p[icel(g, i, j, 2)];
             p[icel(g, i, j, nz - 2)] = p[icel(g, i, j, nz - 1)] = p[icel(g, i, j, nz - 3)];
+        }
+}
+
+void og_bc_convective(const og_grid *g, double dt, double uc, const double *u0, const double *v0,
+                      const double *w0, double *u3, double *v3, double *w3)
+{
+    const int nx = g->nx, ny = g->ny, nz = g->nz;
+    const double C = uc * dt / g->Dx[nx - 3], Ct = uc * dt / g->Dxs[nx - 3];
+    double qin = 0.0, qout = 0.0;
+    for (int j = GC; j < ny - GC; ++j)
+        for (int k = GC; k < nz - GC; ++k) {
+            const long long b = icel(g, nx - 3, j, k), gc = icel(g, nx - 2, j, k);
+            const double ub = u0[b] - C * (u0[b] - u0[icel(g, nx - 4, j, k)]);
+            const double vg = v0[gc] - Ct * (v0[gc] - v0[b]);
+            const double wg = w0[gc] - Ct * (w0[gc] - w0[b]);
+            u3[b] = ub;
+            v3[gc] = v3[icel(g, nx - 1, j, k)] = vg;
+            w3[gc] = w3[icel(g, nx - 1, j, k)] = wg;
+            const double area = g->Dy[j] * g->Dz[k];
+            qin += u0[icel(g, 1, j, k)] * area;
+            qout += ub * area;
+        }
+    const double scale = qout != 0.0 ? qin / qout : 1.0;
+    for (int j = GC; j < ny - GC; ++j)
+        for (int k = GC; k < nz - GC; ++k) {
+            const long long b = icel(g, nx - 3, j, k);
+            const double x = u3[b] * scale;
+            u3[b] = u3[icel(g, nx - 2, j, k)] = u3[icel(g, nx - 1, j, k)] = x;
         }
 }
 
@@ -1208,8 +1242,10 @@ int og_sim_step(og_sim *s, int *iters4, double *err4, double *cd, double *cl)
         if (err4) err4[pass] = er;
     }
     size_t bytes = (size_t)s->ng * sizeof(double);
+    const int conv = s->cfg.conv_uc > 0.0;
+    if (conv) og_bc_convective(g, dt, s->cfg.conv_uc, F[0], F[1], F[2], F[6], F[7], F[8]);
     for (int c = 0; c < 3; ++c) memcpy(F[c], F[6 + c], bytes);
-    og_bc_main(g, s->dir, s->num, F[0], F[1], F[2], F[9]);
+    og_bc_main_ex(g, s->dir, s->num, F[0], F[1], F[2], F[9], conv);
     og_bc_copy(g, F[0], F[1], F[2], F[3], F[4], F[5]);
     og_cdcl(g, F[11], cd, cl);
     s->loop++;

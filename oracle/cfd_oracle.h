@@ -139,7 +139,22 @@ typedef struct {
     int compat;        /* subtract the volume-weighted RHS mean before each solve */
     double dt, nu, tol, omega;
     int maxit, sor_maxit;
+    double conv_uc;    /* > 0: convective outflow at the x-max face (extension, see og_bc_convective) */
 } og_step_cfg;
+
+/* Convective outflow at the x-max face (an extension: the reference has only
+   the Dirichlet/Neumann table).  For every interior (j, k), from the old field
+   (u0, v0, w0): u on the outflow face nx-3 moves by first-order upwind,
+   u_b - C (u_b - u_{b-1}) with C = uc dt / Dx[nx-3], and v, w in the ghost
+   cell nx-2 likewise with C = uc dt / Dxs[nx-3]; results go to the new field
+   (u3, v3, w3).  Then u on the face is scaled by (inflow flux) / (outflow
+   flux), the fluxes being sums of u times Dy Dz over the inflow face (u0 at
+   face 1) and the outflow face, and the outer ghosts take the face values. */
+void og_bc_convective(const og_grid *g, double dt, double uc, const double *u0, const double *v0,
+                      const double *w0, double *u3, double *v3, double *w3);
+/* og_bc_main that leaves the x-max face's velocities alone when skip_outflow */
+void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, double *u, double *v,
+                   double *w, double *p, int skip_outflow);
 
 typedef struct og_sim og_sim;
 og_sim *og_sim_create(const og_grid *g, const og_step_cfg *cfg, const double *dir,

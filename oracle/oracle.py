@@ -63,7 +63,7 @@ class OgStepCfg(C.Structure):
     _fields_ = [("method", C.c_int), ("solver", C.c_int), ("aligned_src", C.c_int),
                 ("compat", C.c_int), ("dt", C.c_double), ("nu", C.c_double),
                 ("tol", C.c_double), ("omega", C.c_double), ("maxit", C.c_int),
-                ("sor_maxit", C.c_int)]
+                ("sor_maxit", C.c_int), ("conv_uc", C.c_double)]
 
 
 class Grid:
@@ -127,6 +127,7 @@ class Oracle:
         L.og_sim_step.argtypes = [C.c_void_p, _ip, _dp, _dp, _dp]
         L.og_sim_loop.restype = C.c_longlong
         L.og_sim_loop.argtypes = [C.c_void_p]
+        L.og_bc_convective.argtypes = [C.c_void_p, d, d] + [_dp] * 6
         del v
 
     # -- single kernels -------------------------------------------------
@@ -208,6 +209,10 @@ class Oracle:
         n = np.ascontiguousarray(bc_num, dtype=np.float64).ravel()
         self.lib.og_bc_main(g.ref(), p(d), p(n), p(u), p(v), p(w), p(pr))
 
+    def bc_convective(self, g, dt, uc, u0, v0, w0, u3, v3, w3):
+        """Convective outflow at the x-max face (extension; og_bc_convective)."""
+        self.lib.og_bc_convective(g.ref(), dt, uc, p(u0), p(v0), p(w0), p(u3), p(v3), p(w3))
+
     def bc_copy(self, g, uo, vo, wo, u, v, w):
         self.lib.og_bc_copy(g.ref(), p(uo), p(vo), p(wo), p(u), p(v), p(w))
 
@@ -287,11 +292,12 @@ class Oracle:
                   "w3": 8, "p": 9, "eta": 10, "f": 11, "src": 12, "x": 13, "b": 14, "jp": 15}
 
         def __init__(self, orc, g, *, method=0, solver=0, aligned_src=False, compat=False,
-                     dt, nu, tol, omega=1.7, maxit=5000, sor_maxit=5000, bc_dir, bc_num, eta):
+                     dt, nu, tol, omega=1.7, maxit=5000, sor_maxit=5000, bc_dir, bc_num, eta,
+                     conv_uc=0.0):
             self.L = orc.lib
             self.g = g
             cfg = OgStepCfg(method, solver, int(aligned_src), int(compat), dt, nu, tol, omega,
-                            maxit, sor_maxit)
+                            maxit, sor_maxit, conv_uc)
             d = np.ascontiguousarray(bc_dir, dtype=np.float64).ravel()
             n = np.ascontiguousarray(bc_num, dtype=np.float64).ravel()
             self.h = self.L.og_sim_create(C.addressof(g.c), C.addressof(cfg), p(d), p(n), p(eta))
