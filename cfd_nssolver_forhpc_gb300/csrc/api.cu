@@ -1249,11 +1249,11 @@ int cfd_copy_velocity(cfd_ctx *c, int from_slot, int to_slot)
 int cfd_eta_cylinder_z(cfd_ctx *c, double cx, double cy, double radius, int nsub)
 {
     CKS(need_metrics(c));
-    if (nsub < 1 || nsub > 4096 || !(radius > 0)) return fail(CFD_ERR_ARG, "bad cylinder parameters");
+    if (nsub < 0 || nsub > 4096 || !(radius > 0)) return fail(CFD_ERR_ARG, "bad cylinder parameters");
     double *eta64 = c->fp32 ? c->staging : static_cast<double *>(c->eta);
     CK(cudaMemsetAsync(eta64, 0, (size_t)c->g.ng * sizeof(double), c->s));
     launch_eta_cylinder_z(c->s, c->g, c->rawp[0], c->rawp[1], c->rawp[3], c->rawp[4], cx, cy, radius, nsub,
-                          std::pow((double)nsub, -2.0), eta64);
+                          nsub > 0 ? std::pow((double)nsub, -2.0) : 0.0, eta64);
     if (c->fp32) launch_convert<double, float>(c->lc, c->g.ng, eta64, static_cast<float *>(c->eta));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->s));

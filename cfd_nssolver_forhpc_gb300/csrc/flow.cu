@@ -537,6 +537,74 @@ __global__ void k_eta_plane(Geo g, const double *__restrict__ X, const double *_
     }
 }
 
+// Exact-area option (nsub == 0; an extension of the sub-sampling): area of
+// the disc of radius r at the origin inside [x0, x1] x [y0, y1], the integral
+// over t of (min(y1, s) - max(y0, -s))+ with s = sqrt(r^2 - t^2), split where
+// s crosses |y0| or |y1|; S(t) = (t s + r^2 asin(t / r)) / 2 integrates s.
+__device__ double disc_prim(double t, double r)
+{
+    const double u = fmax(-1.0, fmin(1.0, t / r));
+    return 0.5 * (t * sqrt(fmax(r * r - t * t, 0.0)) + r * r * asin(u));
+}
+
+__device__ double disc_rect_area(double x0, double x1, double y0, double y1, double r)
+{
+    const double a = fmax(x0, -r), b = fmin(x1, r);
+    if (!(a < b)) return 0.0;
+    double t[6];
+    int n = 0;
+    t[n++] = a;
+    t[n++] = b;
+    const double ys[2] = {y0, y1};
+    for (int q = 0; q < 2; ++q) {
+        const double y = fabs(ys[q]);
+        if (y < r) {
+            const double c = sqrt(r * r - y * y);
+            if (c > a && c < b) t[n++] = c;
+            if (-c > a && -c < b) t[n++] = -c;
+        }
+    }
+    for (int q = 1; q < n; ++q)
+        for (int m = q; m > 0 && t[m - 1] > t[m]; --m) {
+            const double tmp = t[m - 1];
+            t[m - 1] = t[m];
+            t[m] = tmp;
+        }
+    double area = 0.0;
+    for (int q = 0; q + 1 < n; ++q) {
+        const double lo = t[q], hi = t[q + 1];
+        if (!(hi > lo)) continue;
+        const double mid = 0.5 * (lo + hi), sm = sqrt(fmax(r * r - mid * mid, 0.0));
+        const bool top_s = sm < y1, bot_s = -sm > y0;
+        const double top = top_s ? sm : y1, bot = bot_s ? -sm : y0;
+        if (!(top > bot)) continue;
+        const double is = disc_prim(hi, r) - disc_prim(lo, r);
+        area += (top_s ? is : y1 * (hi - lo)) - (bot_s ? -is : y0 * (hi - lo));
+    }
+    return area;
+}
+
+// the k = 0 plane with exact areas: one thread per interior (i, j); the
+// inside / outside classification of the sub-sampled form (which is exact)
+__global__ void k_eta_plane_exact(Geo g, const double *__restrict__ X, const double *__restrict__ Y,
+                                  const double *__restrict__ Dx, const double *__restrict__ Dy, double cx,
+                                  double cy, double radius, double *__restrict__ eta)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.nxc * g.nyc) return;
+    const int i = (int)(t / g.nyc) + GC, j = (int)(t % g.nyc) + GC;
+    const long long ic = icel(g, i, j, 0);
+    const double diag = sqrt(Dx[i] * Dx[i] + Dy[j] * Dy[j]) * 0.5;
+    const double ex = (X[i] + X[i + 1]) * 0.5 - cx, ey = (Y[j] + Y[j + 1]) * 0.5 - cy;
+    const double dist = sqrt(ex * ex + ey * ey);
+    if (fabs(dist - radius) < diag) {
+        const double x0 = X[i] - cx, y0 = Y[j] - cy;
+        eta[ic] = disc_rect_area(x0, x0 + Dx[i], y0, y0 + Dy[j], radius) / (Dx[i] * Dy[j]);
+    } else {
+        eta[ic] = dist > radius ? 0.0 : 1.0;
+    }
+}
+
 // eta(i,j,k) = eta(i,j,0) for i < nx-1, j < ny-1, 1 <= k < nz-1 (setEta.hpp:200-203)
 __global__ void k_eta_extrude(Geo g, double *__restrict__ eta)
 {
@@ -781,8 +849,12 @@ void launch_eta_cylinder_z(cudaStream_t s, const Geo &g, const double *X, const 
                            const double *Dx, const double *Dy, double cx, double cy, double radius,
                            int nsub, double scale, double *eta)
 {
-    dim3 grid(g.nxc, g.nyc);
-    k_eta_plane<<<grid, kBlock, 0, s>>>(g, X, Y, Dx, Dy, cx, cy, radius, nsub, scale, eta);
+    if (nsub == 0) {
+        k_eta_plane_exact<<<nblk((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, X, Y, Dx, Dy, cx, cy, radius, eta);
+    } else {
+        dim3 grid(g.nxc, g.nyc);
+        k_eta_plane<<<grid, kBlock, 0, s>>>(g, X, Y, Dx, Dy, cx, cy, radius, nsub, scale, eta);
+    }
     const long long n = (long long)(g.nx - 1) * (g.ny - 1) * (g.nz - 2);
     k_eta_extrude<<<nblk(n), kBlock, 0, s>>>(g, eta);
 }

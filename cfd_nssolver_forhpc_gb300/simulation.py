@@ -197,6 +197,7 @@ class Simulation:
         check(lib().cfd_copy_velocity(self._h, src, dst))
 
     def DFIB_CylinderZ(self, cx, cy, radius=0.5, nsub=100):
+        """nsub >= 1: the reference's sub-sampling; nsub = 0: exact cut-cell areas."""
         check(lib().cfd_eta_cylinder_z(self._h, cx, cy, radius, nsub))
 
     def div_inf(self, slot=T0) -> float:

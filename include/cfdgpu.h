@@ -212,7 +212,9 @@ int cfd_bc_main(cfd_ctx *ctx, int slot);
 int cfd_bc_copy(cfd_ctx *ctx, int from_slot, int to_slot);
 /* velocity::copy_omp (physicalVariables.hpp:84-102) */
 int cfd_copy_velocity(cfd_ctx *ctx, int from_slot, int to_slot);
-/* DFIB_CylinderZ (setEta.hpp:136-204) with explicit centre and radius */
+/* DFIB_CylinderZ (setEta.hpp:136-204) with explicit centre and radius: cut
+   cells sub-sampled nsub x nsub as the reference does (nsub >= 1), or their
+   exact area fraction (nsub == 0, an extension) */
 int cfd_eta_cylinder_z(cfd_ctx *ctx, double cx, double cy, double radius, int nsub);
 /* One iteration of the main loop of the configured driver
    (RUN_CPU_PC_METHOD.hpp:287-627 or RUN_CPU.hpp:290-462, without IO). */

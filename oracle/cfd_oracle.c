@@ -937,9 +937,78 @@ void og_bc_copy(const og_grid *g, const double *uo, const double *vo, const doub
  * z-aligned cylinder; cut cells are sampled on nsub x nsub sub-cell centres.
  * eta must be zero on entry (the driver fills it with 0, RUN_CPU_PC_METHOD.hpp:258).
  * Centre and radius are parameters here (hard-coded at setEta.hpp:145-147). */
+/* Exact-area option of the cut-cell fraction (an extension: the reference
+ * sub-samples nsub x nsub points).  Area of the disc of radius r centred at
+ * the origin inside [x0, x1] x [y0, y1]: the integral over t of
+ * (min(y1, s) - max(y0, -s))+ with s(t) = sqrt(r^2 - t^2), split where s
+ * crosses |y0| or |y1|; on each piece the bounds are constants or +-s, and
+ * the integral of s is S(t) = (t s(t) + r^2 asin(t / r)) / 2. */
+static double disc_prim(double t, double r)
+{
+    const double u = fmax(-1.0, fmin(1.0, t / r));
+    return 0.5 * (t * sqrt(fmax(r * r - t * t, 0.0)) + r * r * asin(u));
+}
+
+double og_disc_rect_area(double x0, double x1, double y0, double y1, double r)
+{
+    const double a = fmax(x0, -r), b = fmin(x1, r);
+    if (!(a < b)) return 0.0;
+    double t[6];
+    int n = 0;
+    t[n++] = a;
+    t[n++] = b;
+    const double ys[2] = {y0, y1};
+    for (int q = 0; q < 2; ++q) {
+        const double y = fabs(ys[q]);
+        if (y < r) {
+            const double c = sqrt(r * r - y * y);
+            if (c > a && c < b) t[n++] = c;
+            if (-c > a && -c < b) t[n++] = -c;
+        }
+    }
+    for (int q = 1; q < n; ++q) /* insertion sort of at most 6 */
+        for (int m = q; m > 0 && t[m - 1] > t[m]; --m) {
+            const double tmp = t[m - 1];
+            t[m - 1] = t[m];
+            t[m] = tmp;
+        }
+    double area = 0.0;
+    for (int q = 0; q + 1 < n; ++q) {
+        const double lo = t[q], hi = t[q + 1];
+        if (!(hi > lo)) continue;
+        const double mid = 0.5 * (lo + hi), sm = sqrt(fmax(r * r - mid * mid, 0.0));
+        const int top_s = sm < y1, bot_s = -sm > y0;
+        const double top = top_s ? sm : y1, bot = bot_s ? -sm : y0;
+        if (!(top > bot)) continue;
+        const double is = disc_prim(hi, r) - disc_prim(lo, r);
+        area += (top_s ? is : y1 * (hi - lo)) - (bot_s ? -is : y0 * (hi - lo));
+    }
+    return area;
+}
+
 void og_eta_cylinder_z(const og_grid *g, double cx, double cy, double radius, int nsub,
                        double *eta)
 {
+    if (nsub == 0) { /* exact areas, same cells and z copy as the sub-sampled form */
+        const int nx = g->nx, ny = g->ny, nz = g->nz;
+        for (int i = GC; i < nx - GC; ++i)
+            for (int j = GC; j < ny - GC; ++j) {
+                const long long ic = icel(g, i, j, 0);
+                const double diagonal = sqrt(g->Dx[i] * g->Dx[i] + g->Dy[j] * g->Dy[j]) * 0.5;
+                const double ex = ((g->X[i] + g->X[i + 1]) * 0.5) - cx, ey = ((g->Y[j] + g->Y[j + 1]) * 0.5) - cy;
+                const double distance = sqrt(ex * ex + ey * ey);
+                if (fabs(distance - radius) < diagonal) {
+                    const double x0 = g->X[i] - cx, y0 = g->Y[j] - cy;
+                    eta[ic] = og_disc_rect_area(x0, x0 + g->Dx[i], y0, y0 + g->Dy[j], radius) / (g->Dx[i] * g->Dy[j]);
+                } else {
+                    eta[ic] = distance > radius ? 0.0 : 1.0;
+                }
+            }
+        for (int i = 0; i < nx - 1; ++i)
+            for (int j = 0; j < ny - 1; ++j)
+                for (int k = 1; k < nz - 1; ++k) eta[icel(g, i, j, k)] = eta[icel(g, i, j, 0)];
+        return;
+    }
     const int nx = g->nx, ny = g->ny, nz = g->nz;
     const double *X = g->X, *Y = g->Y, *Dx = g->Dx, *Dy = g->Dy;
     const double scale = pow((double)nsub, -2.0);

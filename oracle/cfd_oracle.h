@@ -101,8 +101,12 @@ void og_bc_copy(const og_grid *g, const double *uo, const double *vo, const doub
                 double *u, double *v, double *w);
 
 /* ---- immersed body (setEta.hpp) ---- */
+/* nsub >= 1: the reference's nsub x nsub sub-sampling of cut cells;
+   nsub == 0: the exact area fraction (extension, og_disc_rect_area) */
 void og_eta_cylinder_z(const og_grid *g, double cx, double cy, double radius, int nsub,
                        double *eta);
+/* area of the disc of radius r at the origin inside [x0, x1] x [y0, y1] */
+double og_disc_rect_area(double x0, double x1, double y0, double y1, double r);
 
 /* ---- diagnostics ---- */
 double og_div_inf(const og_grid *g, const double *u, const double *v, const double *w);
