@@ -126,6 +126,12 @@ class Dist:
             self.pg.destroy_process_group()
 
 
+def whole_job_rate(n_cells: int, steps: int, world: int, seconds_max: float) -> float:
+    """Mcell-steps/s of the whole job: every rank advances its own replica of
+    n_cells by `steps`, the job takes as long as its slowest rank."""
+    return n_cells * steps * world / seconds_max / 1e6
+
+
 # ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
@@ -497,7 +503,7 @@ def main():
         sec, infos, launches = timed_steps(S, K, dist)
     clocks = clk.summary()
     sec_max = dist.max(sec)
-    value = w.n_cells * K * dist.world / sec_max / 1e6
+    value = whole_job_rate(w.n_cells, K, dist.world, sec_max)
     mixed = args.precision == "mixed"
     rl = roofline(S, w, infos, args.precision, sec_max / K * 1e3)
     cd64 = infos[-1]["cd"]
@@ -506,7 +512,7 @@ def main():
     if not args.no_e2e:
         dev_s, wall_s, nbytes = e2e_steps(S, K, dist)
         wall_s = dist.max(wall_s)
-        e2e = {"value": round(w.n_cells * K * dist.world / wall_s / 1e6, 4), "unit": UNIT,
+        e2e = {"value": round(whole_job_rate(w.n_cells, K, dist.world, wall_s), 4), "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "seconds": round(wall_s, 4)}
     S.close()
@@ -520,7 +526,7 @@ def main():
             M.step(allow_noconv=True)
         msec, minfos, mlaunch = timed_steps(M, K, dist)
         msec = dist.max(msec)
-        mval = w.n_cells * K * dist.world / msec / 1e6
+        mval = whole_job_rate(w.n_cells, K, dist.world, msec)
         mixed_v, fp64_v = (value, mval) if mixed else (mval, value)
         other = {"precision": other_prec, "value": round(mval, 4), "unit": UNIT,
                  "dtype": "f64" if mixed else "f32+f64", "ms_per_step": round(msec / K * 1e3, 3),
