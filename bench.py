@@ -332,6 +332,10 @@ def roofline(S, w, infos, precision, ms_step):
     out["shares"]["other"] = round(max(0.0, 1.0 - sum(shares.values()) / total), 3)
     if "mg_vcycle" in ms:
         out["mg_vcycle_ms"] = round(ms["mg_vcycle"], 5)
+    if top == "mg_smooth":
+        out["note"] = ("launch time from back-to-back launches on the finest level, whose x and b "
+                       "(8 B/cell) stay in L2 between passes as they do inside the V-cycle; the ncu "
+                       "capture with caches flushed (profiles/k_mg_smooth4_c2.md) is the cold figure")
     if precision != "mixed":
         # the FP64 Krylov kernels are bound by the FP64 pipe: FP64 operations
         # per row (SpMV 7, each dot 1, updates as written) / measured DFMA rate
