@@ -71,6 +71,9 @@ def _cfg(L, **kw):
     (dict(precision=5), "unknown precision"),
     (dict(check_every=0), "check_every"),
     (dict(precision=1, inner_tol=2.0), "inner_tol"),
+    (dict(conv_outflow_uc=-1.0), "conv_outflow_uc"),
+    (dict(conv_outflow_uc=float("nan")), "conv_outflow_uc"),
+    (dict(conv_outflow_uc=float("inf")), "conv_outflow_uc"),
 ])
 def test_create_rejects_bad_config(L, kw, needle):
     cfg = _cfg(L, **kw)
@@ -88,6 +91,7 @@ def test_null_arguments_rejected(L):
     assert L.cfd_upload(None, 0, None, 0) == -1
     assert L.cfd_destroy(None) == 0
     assert L.cfd_host_register(None, 0) == -1
+    assert L.cfd_host_mapped(None) == 0
 
 
 def test_build_is_sm103a_only():
