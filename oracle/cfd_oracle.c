@@ -214,11 +214,12 @@ void og_convdiff_les(const og_grid *g, double dt, double nu_mol, const double *v
                 v1[ic] = v0[ic] + convection + difussion;
             }
 
-    /* w: lines 360-434 */
+    /* w: lines 360-434 (periodic z: also the top face, the same face as the bottom one) */
+    const int wkend = nz - GC - (g->periodic_z ? 0 : 1);
 #pragma omp parallel for schedule(static)
     for (int i = GC; i < nx - GC; ++i)
         for (int j = GC; j < ny - GC; ++j)
-            for (int k = GC; k < nz - GC - 1; ++k) {
+            for (int k = GC; k < wkend; ++k) {
                 long long ic = icel(g, i, j, k);
                 long long xm = ic - sx, xp = ic + sx, ym = ic - sy, yp = ic + sy, zm = ic - sz,
                           zp = ic + sz;
@@ -369,14 +370,39 @@ void og_spe_setup(const og_grid *g, double *xm, double *xp, double *ym, double *
                 if (i == nx - 1) ijk -= xp[i];
                 if (j == 0) ijk -= ym[j];
                 if (j == ny - 1) ijk -= yp[j];
-                if (k == 0) ijk -= zm[k];
-                if (k == nz - 1) ijk -= zp[k];
+                if (k == 0 && !g->periodic_z) ijk -= zm[k];
+                if (k == nz - 1 && !g->periodic_z) ijk -= zp[k];
                 val[ic] = ijk;
                 jp[ic] = 1.0 / ijk;
             }
 }
 
-/* SPE_matrix1::spmv_ompJP (SPE_sparseMatrix1.hpp:126-144) */
+/* SPE_matrix1::spmv_ompJP (SPE_sparseMatrix1.hpp:126-144); periodic_z wraps
+   the z neighbours of the first and last k (extension) */
+static void spe_spmv_ex(int nx, int ny, int nz, const double *xm, const double *xp, const double *ym,
+                        const double *yp, const double *zm, const double *zp, const double *jp,
+                        const double *x, double *r, int periodic_z)
+{
+    const long long nynz = (long long)ny * nz;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                long long ic = k + (long long)j * nz + (long long)i * nynz;
+                double sum = 0.0;
+                if (i != 0) sum += -xm[i] * jp[ic] * x[ic - nynz];
+                if (j != 0) sum += -ym[j] * jp[ic] * x[ic - nz];
+                if (k != 0) sum += -zm[k] * jp[ic] * x[ic - 1];
+                else if (periodic_z) sum += -zm[k] * jp[ic] * x[ic + nz - 1];
+                sum += x[ic];
+                if (k != nz - 1) sum += -zp[k] * jp[ic] * x[ic + 1];
+                else if (periodic_z) sum += -zp[k] * jp[ic] * x[ic - (nz - 1)];
+                if (j != ny - 1) sum += -yp[j] * jp[ic] * x[ic + nz];
+                if (i != nx - 1) sum += -xp[i] * jp[ic] * x[ic + nynz];
+                r[ic] = sum;
+            }
+}
+
 void og_spe_spmv(int nx, int ny, int nz, const double *xm, const double *xp, const double *ym,
                  const double *yp, const double *zm, const double *zp, const double *jp,
                  const double *x, double *r)
@@ -425,8 +451,8 @@ void og_ell_assemble(const og_grid *g, int *cols, double *vals, double *jp)
                 if (i == xEnd) aa = -xp;
                 if (j == yBeg) bb = -ym;
                 if (j == yEnd) bb = -yp;
-                if (k == zBeg) cc = -zm;
-                if (k == zEnd) cc = -zp;
+                if (k == zBeg && !g->periodic_z) cc = -zm;
+                if (k == zEnd && !g->periodic_z) cc = -zp;
                 long long row = icelcal(g, i, j, k);
                 double val = xm + xp + ym + yp + zm + zp + aa + bb + cc;
                 double jpr = 1. / val;
@@ -440,7 +466,9 @@ void og_ell_assemble(const og_grid *g, int *cols, double *vals, double *jp)
                 if (j != yBeg) { c[s] = (int)icelcal(g, i, j - 1, k); v[s++] = -ym * jpr; }
                 if (j != yEnd) { c[s] = (int)icelcal(g, i, j + 1, k); v[s++] = -yp * jpr; }
                 if (k != zBeg) { c[s] = (int)icelcal(g, i, j, k - 1); v[s++] = -zm * jpr; }
+                else if (g->periodic_z) { c[s] = (int)icelcal(g, i, j, zEnd); v[s++] = -zm * jpr; }
                 if (k != zEnd) { c[s] = (int)icelcal(g, i, j, k + 1); v[s++] = -zp * jpr; }
+                else if (g->periodic_z) { c[s] = (int)icelcal(g, i, j, zBeg); v[s++] = -zp * jpr; }
                 for (; s < 7; ++s) { c[s] = (int)(N - 1); v[s] = 0.0; }
             }
 }
@@ -474,6 +502,7 @@ struct og_bicg {
     const double *xm, *xp, *ym, *yp, *zm, *zp, *jp;
     const int *cols;
     const double *vals;
+    int periodic_z;  /* the SPE operator wraps in z */
 };
 
 og_bicg *og_bicg_create(long long n, double tol, int maxit)
@@ -512,10 +541,13 @@ void og_bicg_set_ell(og_bicg *s, const int *cols, const double *vals)
     s->vals = vals;
 }
 
+void og_bicg_set_periodic_z(og_bicg *s, int periodic_z) { s->periodic_z = periodic_z; }
+
 static void bicg_apply(og_bicg *s, const double *x, double *r)
 {
     if (s->kind == 0)
-        og_spe_spmv(s->nxc, s->nyc, s->nzc, s->xm, s->xp, s->ym, s->yp, s->zm, s->zp, s->jp, x, r);
+        spe_spmv_ex(s->nxc, s->nyc, s->nzc, s->xm, s->xp, s->ym, s->yp, s->zm, s->zp, s->jp, x, r,
+                    s->periodic_z);
     else
         og_ell_spmv(s->n, s->cols, s->vals, x, r);
 }
@@ -747,10 +779,11 @@ void og_update_uf(const og_grid *g, double dt, const double *p, const double *et
                 v3[ic] = eta[ic] * vS + (1.0 - et) * T2v;
                 f[icelcal(g, i, j, k) + N] = (v3[ic] - T2v) / dt;
             }
+    const int wkend = g->nz - GC - (g->periodic_z ? 0 : 1);
 #pragma omp parallel for schedule(static)
     for (int i = GC; i < g->nx - GC; ++i)
         for (int j = GC; j < g->ny - GC; ++j)
-            for (int k = GC; k < g->nz - GC - 1; ++k) {
+            for (int k = GC; k < wkend; ++k) {
                 long long ic = icel(g, i, j, k), icP = ic + 1;
                 double T2w = w1[ic] - dt * (p[icP] - p[ic]) / g->Dzs[k];
                 double et = eta[ic] + (eta[icP] - eta[ic]) * ((g->Dzs[k] * 0.5) / g->Dz[k]);
@@ -788,6 +821,18 @@ void og_bc_main(const og_grid *g, const double *dir, const double *num,
                 double *u, double *v, double *w, double *p)
 {
     og_bc_main_ex(g, dir, num, u, v, w, p, 0);
+}
+
+void og_periodic_z(const og_grid *g, double *a)
+{
+    const int nz = g->nz, nzc = g->nzc;
+    for (int i = 0; i < g->nx; ++i)
+        for (int j = 0; j < g->ny; ++j) {
+            a[icel(g, i, j, 0)] = a[icel(g, i, j, nzc)];
+            a[icel(g, i, j, 1)] = a[icel(g, i, j, 1 + nzc)];
+            a[icel(g, i, j, nz - 2)] = a[icel(g, i, j, nz - 2 - nzc)];
+            a[icel(g, i, j, nz - 1)] = a[icel(g, i, j, nz - 1 - nzc)];
+        }
 }
 
 void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, double *u, double *v,
@@ -830,7 +875,7 @@ void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, doubl
             w[icel(g, i, ny - 1, k)] = w[icel(g, i, ny - 2, k)] =
                 DIR(3, 2) * 2. + (2.0 * NUM(3, 2) - 1.0) * w[icel(g, i, ny - 3, k)];
         }
-    for (int i = GC; i < nx - GC; ++i)
+    for (int i = GC; i < nx - GC && !g->periodic_z; ++i)
         for (int j = GC; j < ny - GC; ++j) { /* BC_4 */
             u[icel(g, i, j, 1)] = u[icel(g, i, j, 0)] =
                 DIR(4, 0) * 2. + (2.0 * NUM(4, 0) - 1.0) * u[icel(g, i, j, 2)];
@@ -838,7 +883,7 @@ void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, doubl
                 DIR(4, 1) * 2. + (2.0 * NUM(4, 1) - 1.0) * v[icel(g, i, j, 2)];
             w[icel(g, i, j, 1)] = w[icel(g, i, j, 0)] = DIR(4, 2) + NUM(4, 2) * w[icel(g, i, j, 2)];
         }
-    for (int i = GC; i < nx - GC; ++i)
+    for (int i = GC; i < nx - GC && !g->periodic_z; ++i)
         for (int j = GC; j < ny - GC; ++j) { /* BC_5 */
             w[icel(g, i, j, nz - 1)] = w[icel(g, i, j, nz - 2)] = w[icel(g, i, j, nz - 3)] =
                 DIR(5, 2) + NUM(5, 2) * w[icel(g, i, j, nz - 4)];
@@ -849,6 +894,11 @@ void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, doubl
         }
 #undef DIR
 #undef NUM
+    if (g->periodic_z) { /* z faces periodic instead of BC_4 / BC_5 (extension) */
+        og_periodic_z(g, u);
+        og_periodic_z(g, v);
+        og_periodic_z(g, w);
+    }
     /* pressure ghosts: zero normal gradient (lines 145-171) */
     for (int j = GC; j < ny - GC; ++j)
         for (int k = GC; k < nz - GC; ++k) {
@@ -860,6 +910,10 @@ void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, doubl
             p[icel(g, i, 1, k)] = p[icel(g, i, 0, k)] = p[icel(g, i, 2, k)];
             p[icel(g, i, ny - 2, k)] = p[icel(g, i, ny - 1, k)] = p[icel(g, i, ny - 3, k)];
         }
+    if (g->periodic_z) {
+        og_periodic_z(g, p);
+        return;
+    }
     for (int i = GC; i < nx - GC; ++i)
         for (int j = GC; j < ny - GC; ++j) {
             p[icel(g, i, j, 1)] = p[icel(g, i, j, 0)] = p[icel(g, i, j, 2)];
@@ -1193,6 +1247,7 @@ struct og_sim {
 og_sim *og_sim_create(const og_grid *g, const og_step_cfg *cfg, const double *dir,
                       const double *num, const double *eta)
 {
+    if (g->periodic_z && cfg->solver >= 2) return NULL; /* periodic z: the Krylov solvers only */
     og_sim *s = (og_sim *)calloc(1, sizeof(og_sim));
     s->g = *g;
     s->cfg = *cfg;
@@ -1214,6 +1269,7 @@ og_sim *og_sim_create(const og_grid *g, const og_step_cfg *cfg, const double *di
     s->zp = (double *)calloc((size_t)g->nzc, sizeof(double));
     s->val = (double *)calloc((size_t)s->n, sizeof(double));
     s->bicg = og_bicg_create(s->n, cfg->tol, cfg->maxit);
+    og_bicg_set_periodic_z(s->bicg, g->periodic_z);
     if (cfg->solver == 1) {
         s->cols = (int *)calloc((size_t)(7 * s->n), sizeof(int));
         s->vals = (double *)calloc((size_t)(7 * s->n), sizeof(double));
@@ -1304,7 +1360,10 @@ int og_sim_step(og_sim *s, int *iters4, double *err4, double *cd, double *cl)
         double er = 0.0;
         og_convdiff(g, dt, s->cfg.nu, F[0], F[1], F[2], F[3], F[4], F[5]);
         if (s->cfg.method == 0) og_src_add(g, s->cfg.aligned_src, F[3], F[4], F[5], F[12]);
+        if (g->periodic_z) /* the divergence at the first cell reads w on face 1 = face nz-3 */
+            for (int c = 3; c < 6; ++c) og_periodic_z(g, F[c]);
         if (s->loop > 1) sim_pressure(s, &it, &er);
+        if (g->periodic_z) og_periodic_z(g, F[9]); /* the top w face's gradient reads p above it */
         og_update_uf(g, dt, F[9], F[10], F[3], F[4], F[5], F[6], F[7], F[8], F[11]);
         if (s->cfg.method == 0 && pass < 3) og_src_accumulate(g, dt, F[12], F[11]);
         if (iters4) iters4[pass] = it;

@@ -30,6 +30,8 @@ typedef struct {
     const double *X, *Y, *Z;     /* node coordinates, length n+1 */
     const double *Dx, *Dy, *Dz;  /* cell widths, ghosted length */
     const double *Dxs, *Dys, *Dzs; /* staggered widths, ghosted length */
+    int periodic_z;              /* 1: periodic in z (extension; the reference is Neumann-only
+                                    in z); z spacing uniform across the periodic face */
 } og_grid;
 
 /* ---- grid generation (structureGrid.hpp:409-440, :326-405, :506-559) ---- */
@@ -74,6 +76,8 @@ void og_bicg_set_spe(og_bicg *s, int nxc, int nyc, int nzc,
                      const double *xm, const double *xp, const double *ym, const double *yp,
                      const double *zm, const double *zp, const double *jp);
 void og_bicg_set_ell(og_bicg *s, const int *cols, const double *vals);
+/* the SPE operator wraps in z (periodic z, extension) */
+void og_bicg_set_periodic_z(og_bicg *s, int periodic_z);
 int og_bicg_solve(og_bicg *s, const double *b, double *x, int *iters, double *relres);
 void og_bicg_counters(const og_bicg *s, int *timestep, int *total_iters, int *restarts,
                       int *resets);
@@ -156,6 +160,10 @@ typedef struct {
    face 1) and the outflow face, and the outer ghosts take the face values. */
 void og_bc_convective(const og_grid *g, double dt, double uc, const double *u0, const double *v0,
                       const double *w0, double *u3, double *v3, double *w3);
+/* periodic z (g->periodic_z): ghost planes k = 0, 1 take planes k + nzc and
+   k = nz-2, nz-1 take k - nzc, over the whole x-y plane; for w, a face
+   variable, face nz-3 is the same face as face 1 and is an unknown */
+void og_periodic_z(const og_grid *g, double *a);
 /* og_bc_main that leaves the x-max face's velocities alone when skip_outflow */
 void og_bc_main_ex(const og_grid *g, const double *dir, const double *num, double *u, double *v,
                    double *w, double *p, int skip_outflow);

@@ -56,7 +56,7 @@ class OgGrid(C.Structure):
                 ("lx", C.c_double), ("ly", C.c_double), ("lz", C.c_double),
                 ("X", _dp), ("Y", _dp), ("Z", _dp),
                 ("Dx", _dp), ("Dy", _dp), ("Dz", _dp),
-                ("Dxs", _dp), ("Dys", _dp), ("Dzs", _dp)]
+                ("Dxs", _dp), ("Dys", _dp), ("Dzs", _dp), ("periodic_z", C.c_int)]
 
 
 class OgStepCfg(C.Structure):
@@ -69,7 +69,7 @@ class OgStepCfg(C.Structure):
 class Grid:
     """Uniform staggered grid metrics (numpy) plus the C view of them."""
 
-    def __init__(self, nxc, nyc, nzc, lx, ly, lz, oracle=None, metrics=None):
+    def __init__(self, nxc, nyc, nzc, lx, ly, lz, oracle=None, metrics=None, periodic_z=False):
         self.nxc, self.nyc, self.nzc = nxc, nyc, nzc
         self.nx, self.ny, self.nz = nxc + 4, nyc + 4, nzc + 4
         self.lx, self.ly, self.lz = lx, ly, lz
@@ -84,12 +84,14 @@ class Grid:
                 nxc, nyc, nzc, C.c_double(lx), C.c_double(ly), C.c_double(lz),
                 *[p(metrics[k]) for k in ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")])
         self.m = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in metrics.items()}
+        self.periodic_z = bool(periodic_z)
         self.c = OgGrid(nxc, nyc, nzc, self.nx, self.ny, self.nz, lx, ly, lz,
-                        *[p(self.m[k]) for k in ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")])
+                        *[p(self.m[k]) for k in ("X", "Y", "Z", "Dx", "Dy", "Dz", "Dxs", "Dys", "Dzs")],
+                        int(self.periodic_z))
 
     @classmethod
-    def of(cls, w, oracle=None):
-        return cls(w.nxc, w.nyc, w.nzc, w.lx, w.ly, w.lz, oracle=oracle)
+    def of(cls, w, oracle=None, periodic_z=False):
+        return cls(w.nxc, w.nyc, w.nzc, w.lx, w.ly, w.lz, oracle=oracle, periodic_z=periodic_z)
 
     def ref(self):
         return C.byref(self.c)
@@ -301,6 +303,8 @@ class Oracle:
             d = np.ascontiguousarray(bc_dir, dtype=np.float64).ravel()
             n = np.ascontiguousarray(bc_num, dtype=np.float64).ravel()
             self.h = self.L.og_sim_create(C.addressof(g.c), C.addressof(cfg), p(d), p(n), p(eta))
+            if not self.h:
+                raise ValueError("og_sim_create refused the configuration (periodic z needs a Krylov solver)")
 
         def field(self, name):
             k = self.FIELDS[name]
