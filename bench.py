@@ -87,6 +87,14 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward ratio leg")
     ap.add_argument("--adj-workload", default="c4")
     ap.add_argument("--adj-steps", type=int, default=20, help="steps of the bounded adjoint sample")
+    ap.add_argument("--fp64-maxit", type=int, default=20000,
+                    help="BiCGSTAB iteration cap per solve of the FP64 leg (the reference's is 5000; "
+                         "at tolerance 1e-10 some of its solves need more)")
+    ap.add_argument("--leg", default=None, choices=["c3", "c5"],
+                    help="run one of the large-workload legs instead of the headline: c3 = mixed vs FP64 "
+                         "at 1024x512x64 (bounded steps, per-field errors); c5 = memory plan and one "
+                         "forward + adjoint segment at 1536x768x96")
+    ap.add_argument("--leg-steps", type=int, default=3, help="steps of the large-workload leg")
     ap.add_argument("--cpu-worker", default=None, help=argparse.SUPPRESS)
     return ap.parse_args()
 
@@ -213,7 +221,8 @@ def build_sim(args, w, precision):
     from cfd_nssolver_forhpc_gb300.simulation import Simulation
     solver = {"spe": capi.SOLVER_BICG_SPE, "ell": capi.SOLVER_BICG_ELL, "sor": capi.SOLVER_SOR_RB}[args.solver]
     prec = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
-    S = Simulation(w, solver=solver, precision=prec, tol=w.tol, check_every=16)
+    maxit = args.fp64_maxit if precision == "fp64" else 5000
+    S = Simulation(w, solver=solver, precision=prec, tol=w.tol, check_every=16, maxit=maxit)
     S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
     return S
 
@@ -334,8 +343,8 @@ def roofline(S, w, infos, precision, ms_step):
         out["mg_vcycle_ms"] = round(ms["mg_vcycle"], 5)
     if top == "mg_smooth":
         out["note"] = ("launch time from back-to-back launches on the finest level, whose x and b "
-                       "(8 B/cell) stay in L2 between passes as they do inside the V-cycle; the ncu "
-                       "capture with caches flushed (profiles/k_mg_smooth4_c2.md) is the cold figure")
+                       "(8 B/cell) stay in L2 between passes as they do inside the V-cycle; an ncu "
+                       "capture with caches flushed gives the cold figure")
     if precision != "mixed":
         # the FP64 Krylov kernels are bound by the FP64 pipe: FP64 operations
         # per row (SpMV 7, each dot 1, updates as written) / measured DFMA rate
@@ -362,7 +371,8 @@ def cpu_worker(spec: str):
     kind = None
     try:
         from oracle.oracle import RefHarness
-        R = RefHarness(w.name, build=False)
+        R = RefHarness(w.name, build=False, fast=True)
+        flags = R.flags
         R.setup(w.dt, w.re, w.tol, True)
         R.pc_start(u0, v0, w0)
         kind = "reference"
@@ -383,6 +393,7 @@ def cpu_worker(spec: str):
         sim.field("w0")[:] = w0
         sim.start()
         kind = "port"
+        flags = "-O2 -ffp-contract=off"
 
         def run(n):
             walls, its = [], []
@@ -394,7 +405,7 @@ def cpu_worker(spec: str):
             return walls, its
     run(warm)
     walls, its = run(steps)
-    print(json.dumps({"kind": kind, "walls": walls, "iters": its}))
+    print(json.dumps({"kind": kind, "walls": walls, "iters": its, "flags": flags}))
 
 
 def cpu_baseline(args, w, warmup, steps, budget_s=600):
@@ -416,7 +427,7 @@ def cpu_baseline(args, w, warmup, steps, budget_s=600):
     return {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": d["kind"],
             "sample": (f"{w.name} {w.nxc}x{w.nyc}x{w.nzc} predictor-corrector steps "
                        f"{warmup + 1}..{warmup + steps} (after {warmup} untimed), BiCGSTAB tol {w.tol:g}, "
-                       f"{its} solver iterations per step, {t:.1f} s"),
+                       f"{its} solver iterations per step, {t:.1f} s, g++ {d.get('flags', '?')}"),
             "s_per_step": round(t / len(d["walls"]), 3)}
 
 
@@ -462,10 +473,160 @@ def adjoint_leg(args, dist):
     return out
 
 
+def div_check(S, tol):
+    """Divergence of the last projection of the last step, measured inside
+    the step (after the solve, before the boundary update): T2 = u* - dt grad p
+    (updateUandF.hpp:136, 158, 179).  dev_inf = max |div T2 + dt m| (m: the RHS
+    mean the compatibility projection removed) is the part a converged solve
+    answers for; dev_rel divides it by max |div u*|, the divergence the
+    projection had to remove."""
+    S.divergence_check(True)
+    S.step(allow_noconv=True)
+    d = S.step_divergence()
+    S.divergence_check(False)
+    dev, du = d["dev_inf"], d["div_ustar_inf"]
+    return {"dev_inf": dev, "div_T2_inf": d["div_T2_inf"], "div_ustar_inf": du,
+            "dev_rel": dev / du if du > 0 else 0.0, "dev_inf_below_1e-10": bool(dev < 1e-10),
+            "dev_rel_below_1e-10": bool(dev < 1e-10 * du), "solver_tol": tol,
+            "measured": "one extra step after the timed ones"}
+
+
+def snapshot(S):
+    return {k: S.download(k) for k in ("U0", "V0", "W0", "P")}
+
+
+def field_errors(a: dict, b: dict) -> dict:
+    """Per-field max and L2 error of a against b, relative to b's max / L2.
+    The pressure of the all-Neumann problem is defined up to a constant, so
+    p is compared with its mean removed."""
+    import numpy as np
+    out = {}
+    for k in a:
+        if k == "P":
+            a = dict(a, P=a[k] - a[k].mean())
+            b = dict(b, P=b[k] - b[k].mean())
+        d = a[k] - b[k]
+        out[k] = {"max_rel": float(np.abs(d).max() / max(np.abs(b[k]).max(), 1e-300)),
+                  "l2_rel": float(np.linalg.norm(d) / max(np.linalg.norm(b[k]), 1e-300))}
+    return out
+
+
+def cap_hits(infos, tol):
+    """Solves whose final relative residual did not reach the tolerance (the
+    first step solves nothing)."""
+    return sum(1 for i in infos[1:] for r in i["relres"] if not r < tol)
+
+
+def leg_c3(args):
+    """Mixed precision against FP64 on the GPU at 1024x512x64 (Re 150, dt
+    5e-4, tolerance 1e-10): the same seeded start, leg-steps steps each, the
+    per-field max/L2 errors of u, v, w, p (p without its mean), drag and lift,
+    the projected divergence of the last step, and both step rates."""
+    from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+    w = WORKLOADS["c3"]
+    K = max(2, args.leg_steps)
+    out = {"leg": "c3", "workload": f"{w.name}: cylinder wake {w.nxc}x{w.nyc}x{w.nzc} ({w.n_cells} cells), Re {w.re:g}, "
+                                    f"dt {w.dt:g}, tol {w.tol:g}, {K} steps (the first solves no Poisson equation)"}
+    fields, legs = {}, {}
+    for prec in ("mixed", "fp64"):
+        S = build_sim(args, w, prec)
+        t0 = time.perf_counter()
+        infos = [S.step(allow_noconv=True) for _ in range(K - 1)]
+        S.divergence_check(True)
+        infos.append(S.step(allow_noconv=True))
+        wall = time.perf_counter() - t0
+        fields[prec] = snapshot(S)
+        legs[prec] = {"s_per_solved_step": round(wall / max(1, K - 1), 3),
+                      "iters_per_step": [sum(i["iters"]) for i in infos],
+                      "outer_per_step": [sum(i["outer"]) for i in infos],
+                      "max_relres": max(r for i in infos[1:] for r in i["relres"]),
+                      "solves_above_tol": cap_hits(infos, w.tol),
+                      "cd": [i["cd"] for i in infos], "cl": [i["cl"] for i in infos],
+                      "divergence": S.step_divergence()}
+        S.close()
+    out.update(legs)
+    cd_m, cd_f = legs["mixed"]["cd"][-1], legs["fp64"]["cd"][-1]
+    out["cd_rel_mixed_vs_fp64"] = abs(cd_m / cd_f - 1.0)
+    out["cl_diff_rel_to_cd"] = abs(legs["mixed"]["cl"][-1] - legs["fp64"]["cl"][-1]) / abs(cd_f)
+    out["fields_mixed_vs_fp64"] = field_errors(fields["mixed"], fields["fp64"])
+    return out
+
+
+def leg_c5(args):
+    """Memory plan and one bounded forward + adjoint segment at 1536x768x96
+    (Re 200, dt 5e-4, mixed forward): device memory of the context with the
+    adjoint state and a tape of `interval` steps, of each checkpoint, and the
+    checkpoint interval that fits the full 400-step run (J over its last 200
+    steps, every step reversed) in the GPU's memory."""
+    import torch
+
+    import numpy as np
+
+    from cfd_nssolver_forhpc_gb300 import capi
+    from cfd_nssolver_forhpc_gb300.adjoint import MeanDrag
+    from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+    w = WORKLOADS["c5"]
+    n = max(4, args.leg_steps)
+    interval = max(1, n // 2)
+    dev = torch.device("cuda", 0)
+    torch.cuda.synchronize()
+    free0, total = torch.cuda.mem_get_info(dev)
+    m = MeanDrag(w, n // 2, n, interval, precision=capi.PREC_MIXED, tol=w.tol)
+    try:
+        eta = m.default_eta().numpy()
+        prof = np.full(w.nyc, float(w.bc_dir[0][0]))
+        free1 = torch.cuda.mem_get_info(dev)[0]
+        J = m.objective(prof, eta)
+        free2 = torch.cuda.mem_get_info(dev)[0]
+        g_in, g_eta = m.gradient()
+        free3 = torch.cuda.mem_get_info(dev)[0]
+        run = m.last_run
+    finally:
+        m.close()
+    ng, nc = w.n_ghosted, w.n_cells
+    tape_step = 3 * ng * 4 + 4 * nc * 8  # T0 (FP32) and the pressure of the four passes (FP64)
+    nck = run.get("checkpoints") or -(-n // interval)
+    ck_bytes = (free1 - free2) / max(1, nck) if free2 < free1 else None
+    base = (free0 - free1) - interval * tape_step
+    full_steps = 400
+    plan = None
+    if ck_bytes:
+        budget = 0.92 * total
+        best = None
+        for I in range(1, full_steps + 1):
+            tot = base + I * tape_step + -(-full_steps // I) * ck_bytes
+            if tot <= budget and (best is None or tot < best[1]):
+                best = (I, tot)
+        if best:
+            plan = {"interval": best[0], "checkpoints": -(-full_steps // best[0]),
+                    "device_bytes": int(best[1]), "of_total": round(best[1] / total, 3)}
+    return {"leg": "c5",
+            "workload": f"{w.name}: cylinder wake {w.nxc}x{w.nyc}x{w.nzc} ({w.n_cells} cells), Re {w.re:g}, "
+                        f"dt {w.dt:g}, tol {w.tol:g}, mixed forward",
+            "segment": {"steps": n, "objective": f"mean Cd over steps {n // 2}..{n}", "interval": interval,
+                        "J": J, "forward_seconds": round(run["forward_seconds"], 3),
+                        "adjoint_seconds": round(run["adjoint_seconds"], 3),
+                        "ratio": round(run["adjoint_seconds"] / run["forward_seconds"], 3),
+                        "grad_inflow_norm": float(np.linalg.norm(g_in)),
+                        "grad_eta_norm": float(np.linalg.norm(g_eta))},
+            "memory": {"gpu_total_bytes": int(total),
+                       "context_adjoint_and_tape_bytes": int(free0 - free1),
+                       "tape_step_bytes": int(tape_step), "checkpoint_bytes": int(ck_bytes) if ck_bytes else None,
+                       "base_bytes": int(base), "peak_used_bytes": int(free0 - min(free2, free3))},
+            "plan_400_steps": plan}
+
+
 def main():
     args = parse()
     if args.cpu_worker:
         cpu_worker(args.cpu_worker)
+        return
+    if args.leg:
+        from cfd_nssolver_forhpc_gb300.build import build
+        build()
+        import torch
+        torch.cuda.init()
+        print(json.dumps(leg_c3(args) if args.leg == "c3" else leg_c5(args)))
         return
     from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
     w = WORKLOADS[args.workload]
@@ -511,7 +672,9 @@ def main():
     mixed = args.precision == "mixed"
     rl = roofline(S, w, infos, args.precision, sec_max / K * 1e3)
     cd64 = infos[-1]["cd"]
-    div = S.div_inf(0)
+    cl64 = infos[-1]["cl"]
+    fields = snapshot(S) if not args.no_compare and args.solver != "sor" else None
+    div = div_check(S, w.tol)
     e2e = None
     if not args.no_e2e:
         dev_s, wall_s, nbytes = e2e_steps(S, K, dist)
@@ -532,12 +695,21 @@ def main():
         msec = dist.max(msec)
         mval = whole_job_rate(w.n_cells, K, dist.world, msec)
         mixed_v, fp64_v = (value, mval) if mixed else (mval, value)
+        mfields = snapshot(M)
+        mixed_f, fp64_f = (fields, mfields) if mixed else (mfields, fields)
+        mdiv = div_check(M, w.tol)
         other = {"precision": other_prec, "value": round(mval, 4), "unit": UNIT,
                  "dtype": "f64" if mixed else "f32+f64", "ms_per_step": round(msec / K * 1e3, 3),
                  "iters_per_step": [sum(i["iters"]) for i in minfos],
                  "max_relres": max(r for i in minfos[1:] or minfos for r in i["relres"]),
+                 "solves_above_tol": cap_hits(minfos, w.tol),
+                 "maxit": args.fp64_maxit if other_prec == "fp64" else 5000,
                  "cd_last": minfos[-1]["cd"], "cd_rel_vs_headline": abs(minfos[-1]["cd"] / cd64 - 1.0),
-                 "div_inf_T0": M.div_inf(0), "gpu_launches": mlaunch,
+                 "cl_last": minfos[-1]["cl"],
+                 "cl_diff_rel_to_cd": abs(minfos[-1]["cl"] - cl64) / abs(cd64),
+                 "divergence": mdiv, "gpu_launches": mlaunch,
+                 "fields_mixed_vs_fp64": field_errors(mixed_f, fp64_f),
+                 "fields_after_steps": W + K,
                  "roofline": roofline(M, w, minfos, other_prec, msec / K * 1e3),
                  "ratio_mixed_vs_fp64": round(mixed_v / fp64_v, 3)}
         M.close()
@@ -560,7 +732,8 @@ def main():
                        "l2": "working set larger than L2 (no flush needed)"},
             "iters_per_step": [sum(i["iters"]) for i in infos],
             "max_relres": max(r for i in infos[1:] or infos for r in i["relres"]),
-            "cd_last": infos[-1]["cd"], "div_inf_T0": div,
+            "solves_above_tol": cap_hits(infos, w.tol),
+            "cd_last": infos[-1]["cd"], "divergence": div,
             "roofline": rl, "cpu_baseline": cpu, "clocks": clocks, "e2e": e2e,
             "gpu_launches": launches,
         }

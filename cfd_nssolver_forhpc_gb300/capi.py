@@ -19,7 +19,7 @@ STATUS = {0: "CFD_OK", -1: "CFD_ERR_ARG", -2: "CFD_ERR_CUDA", -3: "CFD_ERR_NOMEM
 
 SOLVER_BICG_SPE, SOLVER_BICG_ELL, SOLVER_SOR_RB = 0, 1, 3
 METHOD_PC, METHOD_PLAIN = 0, 1
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_FP64_DC = 0, 1, 2
 INNER_CG, INNER_BICGSTAB, INNER_MG = 0, 1, 2
 T0, T1, T3 = 0, 1, 3
 KERNELS = ["bicg_ap", "bicg_s", "bicg_as", "bicg_xr", "bicg_p", "convdiff", "update_uf", "rhs",
@@ -48,7 +48,8 @@ class CfdConfig(C.Structure):
                 ("aligned_source", C.c_int), ("compat_rhs", C.c_int),
                 ("bc_dir", (C.c_double * 3) * 6), ("bc_num", (C.c_double * 3) * 6),
                 ("check_every", C.c_int), ("inner_tol", C.c_double), ("max_outer", C.c_int),
-                ("inner_solver", C.c_int), ("les_smagorinsky", C.c_int), ("conv_outflow_uc", C.c_double)]
+                ("inner_solver", C.c_int), ("les_smagorinsky", C.c_int), ("conv_outflow_uc", C.c_double),
+                ("periodic_z", C.c_int)]
 
 
 class CfdStepInfo(C.Structure):
@@ -105,6 +106,12 @@ def lib() -> C.CDLL:
         "cfd_field_count": ([vp, i], sz),
         "cfd_host_register": ([vp, sz], i),
         "cfd_host_mapped": ([vp], i),
+        "cfd_host_mapped_range": ([vp, sz], i),
+        "cfd_set_test_limits": ([vp, i, C.c_longlong], i),
+        "cfd_set_step_divergence_check": ([vp, i], i),
+        "cfd_set_clock": ([vp, C.c_longlong, d], i),
+        "cfd_get_clock": ([vp, C.POINTER(C.c_longlong), dp], i),
+        "cfd_step_divergence": ([vp, dp], i),
         "cfd_host_unregister": ([vp], i),
         "cfd_init_uniform": ([vp, d, d, d], i),
         "cfd_start": ([vp], i),
@@ -122,6 +129,7 @@ def lib() -> C.CDLL:
         "cfd_bc_main": ([vp, i], i),
         "cfd_bc_copy": ([vp, i, i], i),
         "cfd_copy_velocity": ([vp, i, i], i),
+        "cfd_sync_periodic_z": ([vp, i], i),
         "cfd_eta_cylinder_z": ([vp, d, d, d, i], i),
         "cfd_step": ([vp, C.POINTER(CfdStepInfo)], i),
         "cfd_div_inf": ([vp, i, dp], i),

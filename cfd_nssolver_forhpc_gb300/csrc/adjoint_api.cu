@@ -344,6 +344,7 @@ int cfd_adj_enable(cfd_ctx *c, int tape_len)
     if (c->cfg.les_smagorinsky) return fail(CFD_ERR_ARG, "the adjoint does not cover the Smagorinsky model");
     if (c->cfg.conv_outflow_uc > 0.0)
         return fail(CFD_ERR_ARG, "the adjoint does not cover the convective outflow condition");
+    if (c->cfg.periodic_z) return fail(CFD_ERR_ARG, "the adjoint does not cover periodic z");
     if (tape_len < 1) return fail(CFD_ERR_ARG, "tape_len must be at least 1");
     if (c->adj) {
         if (tape_len > c->adj->tape_len) CKS(alloc_tape(c, tape_len));

@@ -67,6 +67,15 @@ void *field_ptr(cfd_ctx *c, int field, bool &is_t)
 
 // ---- solvers ----------------------------------------------------------------
 
+// Trip cap of a solve loop: enough body runs for the iteration cap, lowered
+// by cfd_set_test_limits.
+int trip_cap(const cfd_ctx *c, long long want)
+{
+    long long cap = std::min<long long>(want, 1 << 30);
+    if (c->test_trip_cap > 0) cap = std::min<long long>(cap, c->test_trip_cap);
+    return (int)cap;
+}
+
 // One CUDA graph per solve: head() (the solve's set-up and first steps),
 // then a WHILE node whose body is body() followed by the loop condition
 // (k_loop_cond), so the whole solve runs on the device and the host waits
@@ -156,7 +165,7 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
              BicgScal *sc, int which_graph)
 {
     const int batch = c->cfg.check_every;
-    const int cap = (int)std::min<long long>((long long)c->cfg.p_iter_max / batch + 3, 1 << 30);
+    const int cap = trip_cap(c, (long long)c->cfg.p_iter_max / batch + 3);
     auto iterations = [&] { for (int q = 0; q < batch; ++q) launch_bicg_iteration<Op, V>(c->lc, A, x, w, sc); };
     if (c->use_graphs && c->device_loops) {
         CKS(while_graph(
@@ -197,7 +206,7 @@ int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int
               int launches_pair, int pairs_req = 0)
 {
     const int pairs = pairs_req > 0 ? pairs_req : (c->cfg.check_every + 1) / 2;
-    const int cap = (int)std::min<long long>((long long)c->cfg.p_iter_max / (2 * pairs) + 3, 1 << 30);
+    const int cap = trip_cap(c, (long long)c->cfg.p_iter_max / (2 * pairs) + 3);
     auto body = [&] {
         for (int q = 0; q < pairs; ++q) {
             pair(0);
@@ -395,8 +404,9 @@ int poisson_solve(cfd_ctx *c, int *iters, double *relres, int *outer)
 {
     if (outer) *outer = 0;
     const bool ell = c->cfg.solver == CFD_SOLVER_BICG_ELL;
-    if (c->cfg.precision == CFD_PREC_MIXED) {
+    if (c->cfg.precision == CFD_PREC_MIXED || c->cfg.precision == CFD_PREC_FP64_DC) {
         const int inner = c->cfg.inner_solver;
+        if (c->cfg.precision == CFD_PREC_FP64_DC) CKS(ensure_fp32_solver(c));
         if (inner == CFD_INNER_MG) CKS(mg_setup(c));
         if (ell) return solve_mixed(c, ell64(c), ell32(c), c->b, c->x, c->w64.r0, inner, iters, relres, outer);
         return solve_mixed(c, spe64(c), spe32(c), c->b, c->x, c->w64.r0, inner, iters, relres, outer);
@@ -440,17 +450,20 @@ int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
     return CFD_OK;
 }
 
+// rhs_done: the pass kernel already formed b (and its compatibility projection)
 template <class T>
-int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer)
+int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer, bool rhs_done = false)
 {
     const Geo &g = c->g;
     if (c->cfg.solver == CFD_SOLVER_SOR_RB) {
         if (outer) *outer = 0;
         return sor_solve_t<T>(c, si, iters, relres);
     }
-    launch_rhs<T>(c->lc, g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, si, 0),
-                  dv<T>(c, si, 1), dv<T>(c, si, 2), c->b, c->cfg.compat_rhs != 0, c->dscal + 0);
-    c->launches += c->cfg.compat_rhs ? 2 : 1;
+    if (!rhs_done) {
+        launch_rhs<T>(c->lc, g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, si, 0),
+                      dv<T>(c, si, 1), dv<T>(c, si, 2), c->b, c->cfg.compat_rhs != 0, c->dscal + 0);
+        c->launches += c->cfg.compat_rhs ? 2 : 1;
+    }
     CK(cudaGetLastError());
     int st = poisson_solve(c, iters, relres, outer);
     if (st != CFD_OK && st != CFD_ERR_NOCONV) return st;
@@ -484,25 +497,79 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
         launch_smagorinsky<T>(c->s, g, metrics_of<double>(c), u0, v0, w0, vis);
         c->launches += 1;
     }
+    // predictor-corrector: every pass starts with ConvectionDifussion(T0 -> T1)
+    // of the same T0 (RUN_CPU_PC_METHOD.hpp:304, 455); it is evaluated once
+    T *C[3] = {static_cast<T *>(c->cdbuf[0]), static_cast<T *>(c->cdbuf[1]), static_cast<T *>(c->cdbuf[2])};
+    if (pc) {
+        launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, C[0], C[1], C[2], nullptr, vis, (T)(1.0 / c->cfg.re));
+        c->launches += 1;
+    }
+    const bool krylov = c->cfg.solver != CFD_SOLVER_SOR_RB;
     for (int pass = 0; pass < npass; ++pass) {
-        launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, u1, v1, w1,
-                           (pc && aligned && pass > 0) ? src : nullptr, vis, (T)(1.0 / c->cfg.re));
-        if (pc && !aligned) launch_src_add<T>(c->lc, g, 0, u1, v1, w1, src);
-        c->launches += (pc && !aligned) ? 2 : 1;
+        bool rhs_done = false;
+        if (pc) {
+            // T1 = C + source, and the pass's Poisson right-hand side
+            PassArgs<T> A{};
+            for (int q = 0; q < 3; ++q) A.C[q] = C[q];
+            A.T1[0] = u1; A.T1[1] = v1; A.T1[2] = w1;
+            A.src = src;
+            A.src_mode = pass == 0 ? 0 : (aligned ? 2 : 1);
+            A.jp = c->jp;
+            A.jph = c->jp32;
+            A.jpl = c->jp32lo;
+            A.ddt = 1.0 / c->cfg.dt;
+            rhs_done = krylov && c->loop > 1;
+            A.b = rhs_done ? c->b : nullptr;
+            A.partials = rhs_done && c->cfg.compat_rhs ? c->lc.partials : nullptr;
+            A.counter = c->lc.counter;
+            A.mean = c->dscal + 0;
+            const bool ghosts = !aligned && pass > 0;
+            launch_pass<T>(c->lc, g, metrics_of<double>(c), metrics_of<float>(c), A, ghosts);
+            c->launches += 1 + (ghosts ? 1 : 0) + (A.partials ? 1 : 0);
+        } else {
+            launch_convdiff<T>(c->s, g, m, dt, nudt, u0, v0, w0, u1, v1, w1, nullptr, vis, (T)(1.0 / c->cfg.re));
+            c->launches += 1;
+        }
+        if (g.pz) {  // the divergence at the first cell reads w on face 1 = the top face
+            launch_sync_z<T>(c->s, g, u1, v1, w1);
+            c->launches += 1;
+        }
         CK(cudaGetLastError());
         if (c->loop > 1) {
-            int s2 = pressure_step<T>(c, 1, &loc.iters[pass], &loc.relres[pass], &loc.outer[pass]);
+            int s2 = pressure_step<T>(c, 1, &loc.iters[pass], &loc.relres[pass], &loc.outer[pass], rhs_done);
             if (s2 != CFD_OK && s2 != CFD_ERR_NOCONV) return s2;
             if (s2 != CFD_OK) st = s2;
+        }
+        if (g.pz) {  // the top w face's pressure gradient reads p above it
+            launch_sync_z<double>(c->s, g, c->p, nullptr, nullptr);
+            c->launches += 1;
         }
         if (rec) {
             launch_gather_interior(c->s, g, c->p, rec->x[pass]);
             c->launches += 1;
         }
-        launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
-                            u1, v1, w1, u3, v3, w3, f);
-        if (pc && pass < 3) launch_src_accumulate<T>(c->lc, 3 * g.n, dt, src, f);
-        c->launches += (pc && pass < 3) ? 2 : 1;
+        if (c->div_check && pass == npass - 1 && c->loop > 1) {
+            // T2 = u* - dt grad p of the last pass, before the boundary update
+            // rewrites T1's faces
+            CK(cudaMemsetAsync(c->dmax, 0, 3 * sizeof(unsigned long long), c->s));
+            launch_div_projected<T>(c->lc, g, metrics_of<double>(c), c->cfg.dt, c->p, u1, v1, w1,
+                                    c->cfg.compat_rhs ? c->dscal + 0 : nullptr, c->dmax, true);
+            CK(cudaMemcpyAsync(c->h_max, c->dmax, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->s));
+            c->launches += 1;
+        }
+        if (pc) {
+            // the predictor passes feed f into the source; the final pass
+            // stores f and reduces the drag and lift
+            const bool last = pass == npass - 1;
+            launch_update_pass<T>(c->lc, g, m, metrics_of<double>(c), c->cfg.dt, c->p, static_cast<T *>(c->eta),
+                                  u1, v1, w1, u3, v3, w3, f, last, last ? nullptr : src, c->cfg.lz,
+                                  last ? c->dscal + 1 : nullptr);
+            c->launches += 1;
+        } else {
+            launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
+                                u1, v1, w1, u3, v3, w3, f);
+            c->launches += 1;
+        }
         CK(cudaGetLastError());
     }
     const size_t bytes = (size_t)g.ng * sizeof(T);
@@ -519,13 +586,14 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
     bc.skip_outflow = conv ? 1 : 0;
     launch_bc_main<T>(c->s, g, bc, u0, v0, w0, c->p);
     launch_bc_copy<T>(c->s, g, u0, v0, w0, u1, v1, w1);
-    launch_cdcl<T>(c->lc, g, metrics_of<double>(c), c->cfg.lz, f, c->dscal + 1);
-    c->launches += 3 + 1 + 1;
+    if (!pc) launch_cdcl<T>(c->lc, g, metrics_of<double>(c), c->cfg.lz, f, c->dscal + 1);
+    c->launches += 3 + 1 + (pc ? 0 : 1);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(c->h_scal, c->dscal, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
     loc.cd = c->h_scal[1];
     loc.cl = c->h_scal[2];
+    if (c->div_check && c->loop > 1) std::memcpy(c->last_div, c->h_max, sizeof(c->last_div));
     c->loop += 1;
     c->time += c->cfg.dt;
     loc.loop = c->loop;
@@ -641,6 +709,7 @@ int build_tables(cfd_ctx *c)
             if (c->fv_sum[a]) launch_fv_axes(c->s, na, c->spe_c32[a], fv_width_src(c, a), c->fv_sum[a]);
         }
         launch_convert<double, float>(c->lc, g.n, c->jp, c->jp32);
+        if (c->jp32lo) launch_split_lo(c->lc, g.n, c->jp, c->jp32lo);
         if (c->cg_ip) launch_cg_ip(c->lc, fv32(c), c->cg_ip);
         if (c->cfg.solver == CFD_SOLVER_BICG_ELL)
             launch_convert<double, float>(c->lc, 7 * g.n, c->ell_vals, c->ell_vals32);
@@ -722,7 +791,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (k.solver != CFD_SOLVER_BICG_SPE && k.solver != CFD_SOLVER_BICG_ELL && k.solver != CFD_SOLVER_SOR_RB)
         return fail(CFD_ERR_ARG, "unknown solver");
     if (k.method != CFD_METHOD_PC && k.method != CFD_METHOD_PLAIN) return fail(CFD_ERR_ARG, "unknown method");
-    if (k.precision != CFD_PREC_FP64 && k.precision != CFD_PREC_MIXED)
+    if (k.precision != CFD_PREC_FP64 && k.precision != CFD_PREC_MIXED && k.precision != CFD_PREC_FP64_DC)
         return fail(CFD_ERR_ARG, "unknown precision");
     if (k.check_every < 1 || k.check_every > 4096) return fail(CFD_ERR_ARG, "check_every out of range");
     if (k.les_smagorinsky != 0 && k.les_smagorinsky != 1) return fail(CFD_ERR_ARG, "les_smagorinsky must be 0 or 1");
@@ -732,8 +801,13 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         return fail(CFD_ERR_ARG, "conv_outflow_uc must be finite and >= 0");
     if (k.conv_outflow_uc > 0.0 && !(k.conv_outflow_uc * k.dt <= 0.5 * 1e300))
         return fail(CFD_ERR_ARG, "conv_outflow_uc out of range");
-    if (k.precision == CFD_PREC_MIXED && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
+    if (k.precision != CFD_PREC_FP64 && (!(k.inner_tol > 0 && k.inner_tol < 1) || k.max_outer < 1))
         return fail(CFD_ERR_ARG, "mixed precision needs 0 < inner_tol < 1 and max_outer >= 1");
+    if (k.precision == CFD_PREC_FP64_DC && k.solver != CFD_SOLVER_BICG_SPE)
+        return fail(CFD_ERR_ARG, "CFD_PREC_FP64_DC solves with the matrix-free SPE operator only");
+    if (k.periodic_z != 0 && k.periodic_z != 1) return fail(CFD_ERR_ARG, "periodic_z must be 0 or 1");
+    if (k.periodic_z && k.solver == CFD_SOLVER_SOR_RB)
+        return fail(CFD_ERR_ARG, "periodic z needs a Krylov solver (SPE or ELL), not SOR");
 
     cfd_ctx *c = new cfd_ctx();
     c->cfg = k;
@@ -747,6 +821,9 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     g.n = n;
     g.fsxc = FastDiv((unsigned int)g.sxc);
     g.fsyc = FastDiv((unsigned int)g.syc);
+    g.fsx = FastDiv((unsigned int)g.sx);
+    g.fsy = FastDiv((unsigned int)g.sy);
+    g.pz = k.periodic_z;
     if (const char *e = std::getenv("CFDGPU_NO_GRAPH")) c->use_graphs = !(e[0] == '1');
     if (const char *e = std::getenv("CFDGPU_SOLVE_LOOP")) c->device_loops = std::strcmp(e, "host") != 0;
     if (const char *e = std::getenv("CFDGPU_DEBUG")) c->debug = std::atoi(e);
@@ -765,6 +842,8 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if ((st = dalloc(c, reinterpret_cast<void **>(&(ptr)), (bytes))) != CFD_OK) return bail(st)
     for (int sl = 0; sl < 3; ++sl)
         for (int q = 0; q < 3; ++q) AL(c->vel[sl][q], (size_t)g.ng * ts);
+    if (k.method == CFD_METHOD_PC)
+        for (int q = 0; q < 3; ++q) AL(c->cdbuf[q], (size_t)g.ng * ts);
     AL(c->eta, (size_t)g.ng * ts);
     AL(c->f, (size_t)(3 * n) * ts);
     AL(c->src, (size_t)(3 * n) * ts);
@@ -805,6 +884,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         for (int a = 0; a < 3; ++a) AL(c->fv_sum[a], 2 * (size_t)nc[a] * sizeof(float));
         AL(c->cg_ip, n * 4);
         AL(c->jp32, n * 4);
+        AL(c->jp32lo, n * 4);
         if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
     }
     if (!bicg) {
@@ -819,16 +899,17 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     AL(c->dscal, 8 * sizeof(double));
     AL(c->mon, 8 * sizeof(double));
     if (k.les_smagorinsky) AL(c->vis, (size_t)n * ts);
-    AL(c->dmax, 2 * sizeof(unsigned long long));
+    AL(c->dmax, 3 * sizeof(unsigned long long));
     const int red_blocks = blocks_for(n, sms * 8);
     AL(c->lc.partials, (size_t)kMaxReduce * red_blocks * sizeof(double));
     AL(c->lc.counter, sizeof(unsigned int));
-    if (c->fp32) AL(c->staging, (size_t)g.ng * sizeof(double));
+    // the largest field crossing the boundary: ghosted, or f / src (3 x compact)
+    if (c->fp32) AL(c->staging, (size_t)std::max<long long>(g.ng, 3 * g.n) * sizeof(double));
 #undef AL
     if (cudaMallocHost(reinterpret_cast<void **>(&c->h_sc), sizeof(BicgScal)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_scal), 8 * sizeof(double)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_sor_state), 4 * sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(reinterpret_cast<void **>(&c->h_max), 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMallocHost(reinterpret_cast<void **>(&c->h_max), 3 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(CFD_ERR_NOMEM, "pinned host allocation failed"));
     }
@@ -925,17 +1006,22 @@ size_t cfd_field_count(cfd_ctx *c, int field)
     return field_count(c, field);
 }
 
-// the device address of a host buffer that starts on a 16-byte boundary and
-// that the GPU can address (registered and mapped, or any memory on systems
-// with address translation such as Grace), else null
-static void *mapped_host(const void *host)
+// the device address of a host buffer of `bytes` bytes that starts on a
+// 16-byte boundary and that the GPU can address as a whole (registered and
+// mapped, or any memory on systems with address translation such as Grace),
+// else null.  The first and the last byte must both map, contiguously: a
+// buffer of which only the head lies in a registration goes through copies.
+static void *mapped_host(const void *host, size_t bytes)
 {
-    if ((reinterpret_cast<uintptr_t>(host) & 15u) != 0) return nullptr;
-    void *dev = nullptr;
-    if (cudaHostGetDevicePointer(&dev, const_cast<void *>(host), 0) != cudaSuccess) {
+    if ((reinterpret_cast<uintptr_t>(host) & 15u) != 0 || bytes == 0) return nullptr;
+    void *dev = nullptr, *dev_last = nullptr;
+    const char *last = static_cast<const char *>(host) + (bytes - 1);
+    if (cudaHostGetDevicePointer(&dev, const_cast<void *>(host), 0) != cudaSuccess ||
+        cudaHostGetDevicePointer(&dev_last, const_cast<char *>(last), 0) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
+    if (static_cast<char *>(dev_last) - static_cast<char *>(dev) != (ptrdiff_t)(bytes - 1)) return nullptr;
     return (reinterpret_cast<uintptr_t>(dev) & 15u) == 0 ? dev : nullptr;
 }
 
@@ -949,7 +1035,7 @@ int cfd_upload(cfd_ctx *c, int field, const double *host, size_t count)
         return fail(CFD_ERR_ARG, "element count " + std::to_string(count) + " != " + std::to_string(want));
     bool is_t;
     void *d = field_ptr(c, field, is_t);
-    if (const double *hd = static_cast<const double *>(mapped_host(host))) {
+    if (const double *hd = static_cast<const double *>(mapped_host(host, count * sizeof(double)))) {
         // host buffer the GPU addresses directly: one kernel reads it over the
         // host link (190 GB/s on GB300), converting on the way
         if (is_t && c->fp32) launch_link_copy<double, float>(c->lc, (long long)count, hd, static_cast<float *>(d));
@@ -998,7 +1084,12 @@ int cfd_host_register(void *host, size_t bytes)
 
 int cfd_host_mapped(const void *host)
 {
-    return mapped_host(host) ? 1 : 0;
+    return mapped_host(host, 1) ? 1 : 0;
+}
+
+int cfd_host_mapped_range(const void *host, size_t bytes)
+{
+    return mapped_host(host, bytes) ? 1 : 0;
 }
 
 int cfd_host_unregister(void *host)
@@ -1378,6 +1469,74 @@ int cfd_steady_max(cfd_ctx *c, int slot_new, int slot_old, double *out)
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, c->mon, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_sync_periodic_z(cfd_ctx *c, int slot)
+{
+    CKS(check_ctx(c));
+    if (!c->g.pz) return fail(CFD_ERR_STATE, "the context is not periodic in z");
+    if (slot == -1) {
+        launch_sync_z<double>(c->s, c->g, c->p, nullptr, nullptr);
+    } else {
+        CKS(check_slot(slot));
+        const int a = slot_index(slot);
+        dispatch(c, [&](auto tag) {
+            using T = typename decltype(tag)::type;
+            launch_sync_z<T>(c->s, c->g, dv<T>(c, a, 0), dv<T>(c, a, 1), dv<T>(c, a, 2));
+            return 0;
+        });
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->s));
+    return CFD_OK;
+}
+
+int cfd_set_clock(cfd_ctx *c, long long loop, double time)
+{
+    CKS(check_ctx(c));
+    if (loop < 1 || !std::isfinite(time)) return fail(CFD_ERR_ARG, "loop must be >= 1 and time finite");
+    c->loop = loop;
+    c->time = time;
+    return CFD_OK;
+}
+
+int cfd_get_clock(cfd_ctx *c, long long *loop, double *time)
+{
+    CKS(check_ctx(c));
+    if (loop) *loop = c->loop;
+    if (time) *time = c->time;
+    return CFD_OK;
+}
+
+int cfd_set_step_divergence_check(cfd_ctx *c, int on)
+{
+    CKS(check_ctx(c));
+    c->div_check = on != 0;
+    for (double &v : c->last_div) v = -1.0;
+    return CFD_OK;
+}
+
+int cfd_step_divergence(cfd_ctx *c, double *out3)
+{
+    CKS(check_ctx(c));
+    if (!out3) return fail(CFD_ERR_ARG, "null output");
+    if (!c->div_check) return fail(CFD_ERR_STATE, "the step divergence check is off");
+    std::memcpy(out3, c->last_div, sizeof(c->last_div));
+    return CFD_OK;
+}
+
+int cfd_set_test_limits(cfd_ctx *c, int loop_trip_cap, long long tma_wait_limit)
+{
+    CKS(check_ctx(c));
+    c->test_trip_cap = loop_trip_cap > 0 ? loop_trip_cap : 0;
+    c->cgtma.wait_limit = tma_wait_limit >= 0 ? tma_wait_limit : (1LL << 24);
+    // the cached solve graphs hold the old cap and limit as launch arguments
+    for (int q = 0; q < 5; ++q) {
+        if (c->graph[q]) cudaGraphExecDestroy(c->graph[q]);
+        c->graph[q] = nullptr;
+        c->graph_batch[q] = 0;
+    }
     return CFD_OK;
 }
 

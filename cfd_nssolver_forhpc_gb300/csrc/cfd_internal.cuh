@@ -84,6 +84,8 @@ struct Geo {
     int syc;              // compact j stride = nzc
     long long ng, n;      // ghosted and compact element counts
     FastDiv fsxc, fsyc;   // division by sxc and syc (n < 2^31)
+    int pz;               // 1: periodic in z (the top w face is an unknown, z ghosts wrap)
+    FastDiv fsx, fsy;     // division by the ghosted strides sx and sy (ng < 2^31 when used)
 };
 
 __host__ __device__ __forceinline__ long long icel(const Geo &g, int i, int j, int k)
@@ -112,6 +114,8 @@ enum AxRow {
     AX_CBNN,    //             Un <= 0: 0.125*Ds[i-1]*Ds[i-1]/D[i]
     AX_PM,      // Poisson -face coefficient 1/D[i]/Ds[i-1], zero on the first cell
     AX_PP,      // Poisson +face coefficient 1/D[i]/Ds[i],   zero on the last cell
+    AX_RDL,     // 1 / Dx - (float)(1 / Dx): with the FP32 AX_RD row, 1 / Dx as a float pair
+    AX_DL,      // Dx - (float)Dx: with the FP32 AX_D row, Dx as a float pair
     AX_ROWS
 };
 
@@ -126,6 +130,55 @@ template <class T>
 struct Metrics {
     Axis<T> x, y, z;
 };
+
+// ---- float-float arithmetic ------------------------------------------------
+// A value hi + lo of two FP32 numbers with |lo| <= ulp(hi) / 2 carries about
+// 48 significant bits.  GB300 issues FP32 operations at many times its FP64
+// rate, so kernels of the mixed-precision path that need more than FP32
+// accuracy (the Poisson right-hand side, whose divergence of FP32 velocities
+// must not lose the digits the FP64 defect correction solves for) use these
+// error-free transformations (Knuth's two-sum, the fused multiply-add form of
+// Dekker's two-product).  Every rounding step is an explicit _rn intrinsic,
+// so the compiler cannot contract or reorder them.
+struct ff {
+    float hi, lo;
+};
+// the exact sum a + b as hi + lo
+__device__ __forceinline__ ff ff_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+// the exact difference a - b
+__device__ __forceinline__ ff ff_two_diff(float a, float b) { return ff_two_sum(a, -b); }
+// renormalise s + t when |s| >= |t| (or s == 0)
+__device__ __forceinline__ ff ff_fast(float s, float t)
+{
+    const float h = __fadd_rn(s, t);
+    return {h, __fsub_rn(t, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    const ff s = ff_two_sum(a.hi, b.hi);
+    return ff_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);  // the exact error of p
+    const float t = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return ff_fast(p, t);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+// a double split into its nearest float and the float nearest the rest
+__host__ __device__ inline ff ff_of(double v)
+{
+    const float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
 
 // ---- deterministic grid reductions --------------------------------------
 // Each block reduces NV values (warp shuffles, then warps in index order),

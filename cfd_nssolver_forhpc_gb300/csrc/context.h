@@ -77,6 +77,7 @@ struct cfd_ctx {
 
     // state (velocity type T = double or float)
     void *vel[3][3] = {};  // [slot 0/1/2 = T0/T1/T3][component]
+    void *cdbuf[3] = {};   // the step's one convection-diffusion of T0 (predictor-corrector method)
     void *eta = nullptr, *f = nullptr, *src = nullptr;
     double *p = nullptr, *x = nullptr, *b = nullptr, *jp = nullptr;
     double *staging = nullptr;  // FP64 staging for conversions (mixed precision)
@@ -93,6 +94,7 @@ struct cfd_ctx {
     double *spe_c[3] = {};
     float *spe_c32[3] = {};
     float *jp32 = nullptr;
+    float *jp32lo = nullptr;  // jp - jp32 as a float: jp as a float pair (mixed path's right-hand side)
     int *ell_cols = nullptr;
     double *ell_vals = nullptr;
     float *ell_vals32 = nullptr;
@@ -130,6 +132,9 @@ struct cfd_ctx {
     int debug = 0;
     bool fused = true;  // fused FP32 inner iterations (SPE operator)
     long long launches = 0;  // kernels issued by the step and solver paths
+    int test_trip_cap = 0;   // > 0: cap on the body runs of every solve loop (cfd_set_test_limits)
+    bool div_check = false;  // cfd_set_step_divergence_check
+    double last_div[3] = {-1.0, -1.0, -1.0};  // its result for the last step
 
     // inflow profile: per-j Dirichlet value of u on the x-min face (nullptr:
     // the scalar bc_dir[0][0]); a parameter of the adjoint
@@ -201,14 +206,15 @@ inline SpeOp<double> spe64(cfd_ctx *c)
 {
     const Geo &g = c->g;
     return {c->spe_c[0], c->spe_c[0] + g.nxc, c->spe_c[1], c->spe_c[1] + g.nyc, c->spe_c[2],
-            c->spe_c[2] + g.nzc, c->jp, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc, FastDiv((unsigned int)g.nzc)};
+            c->spe_c[2] + g.nzc, c->jp, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc, FastDiv((unsigned int)g.nzc),
+            g.pz};
 }
 inline SpeOp<float> spe32(cfd_ctx *c)
 {
     const Geo &g = c->g;
     return {c->spe_c32[0], c->spe_c32[0] + g.nxc, c->spe_c32[1], c->spe_c32[1] + g.nyc, c->spe_c32[2],
             c->spe_c32[2] + g.nzc, c->jp32, g.nxc, g.nyc, g.nzc, g.sxc, g.n, g.fsxc,
-            FastDiv((unsigned int)g.nzc)};
+            FastDiv((unsigned int)g.nzc), g.pz};
 }
 // interior cell widths of axis a (FP32 metric table row AX_D from the first
 // interior cell)
@@ -261,6 +267,9 @@ inline std::vector<double> axis_table(const std::vector<double> &D, const std::v
         }
         T(AX_CANN, i) = 0.125 * D[i] * D[i] / Ds[i];
         T(AX_CBPP, i) = 0.125 * Ds[i] * Ds[i] / D[i];
+        // low parts of 1 / D and D (float-float arithmetic of the mixed path)
+        T(AX_RDL, i) = (double)(float)(T(AX_RD, i) - (double)(float)T(AX_RD, i));
+        T(AX_DL, i) = (double)(float)(D[i] - (double)(float)D[i]);
     }
     return t;
 }

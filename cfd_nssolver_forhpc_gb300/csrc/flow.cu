@@ -157,7 +157,7 @@ k_convdiff(Geo g, Metrics<T> m, T dt, T nudt, const T *__restrict__ u0, const T 
         if (src) r += src[g.n + t];
         v1[ic] = r;
     }
-    if (k < g.nz - GC - 1) {  // ---- w, lines 360-434
+    if (k < g.nz - GC - 1 + g.pz) {  // ---- w, lines 360-434 (periodic z: the top face too)
         const T IT = Z(AX_IT, k);
         const T Wp = T(0.5) * (w_zp + wc), Wn = T(0.5) * (w_zm + wc);
         const T Up = uc + (__ldg(u0 + ic + 1) - uc) * IT;
@@ -260,6 +260,199 @@ __global__ void k_rhs_compat(long long n, const double *__restrict__ jp, const d
         b[t] = b[t] - jp[t] * mu;
 }
 
+// ---------------------------------------------------------------------------
+// One predictor-corrector pass without re-evaluating the convection-
+// diffusion.  Every pass of RUN_CPU_PC_METHOD.hpp:287-627 starts with
+// ConvectionDifussion(T0 -> T1) of the same T0 (lines 304, 455), so the
+// step evaluates it once into C and each pass forms
+//   T1 = C + src     at the faces the convection-diffusion writes,
+//   T1 = T1 + src    at the other elements m < N (reference index convention:
+//                    element m of the ghosted array gets src[m], lines 309-316),
+// which is bit for bit what ConvectionDifussion followed by the source
+// coupling leaves in T1.  The same pass then evaluates createBMatrix_omp
+// (b_matrix.hpp:76-79) from those T1 values and, for the compatibility
+// projection, the volume-weighted sum of the unscaled right-hand side.
+
+// the faces ConvectionDifussion writes: interior cells, the normal
+// component's last face skipped (periodic z: the top w face included)
+__device__ __forceinline__ bool cd_writes(const Geo &g, int c, int i, int j, int k)
+{
+    if (i < GC || j < GC || k < GC || i >= g.nx - GC || j >= g.ny - GC || k >= g.nz - GC) return false;
+    if (c == 0) return i < g.nx - GC - 1;
+    if (c == 1) return j < g.ny - GC - 1;
+    return k < g.nz - GC - 1 + g.pz;
+}
+
+// T1 += src at the elements m < N the convection-diffusion does not write
+// (reference index convention); runs before k_pass, which reads them
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_pass_ghosts(Geo g, T *__restrict__ u1, T *__restrict__ v1, T *__restrict__ w1, const T *__restrict__ src)
+{
+    for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < g.n;
+         m += (long long)gridDim.x * blockDim.x) {
+        const unsigned q = (unsigned)m;
+        const unsigned i = g.fsx.div(q), r = q - i * (unsigned)g.sx, j = g.fsy.div(r);
+        const int k = (int)(r - j * (unsigned)g.sy);
+        if (!cd_writes(g, 0, (int)i, (int)j, k)) u1[m] += src[m];
+        if (!cd_writes(g, 1, (int)i, (int)j, k)) v1[m] += src[g.n + m];
+        if (!cd_writes(g, 2, (int)i, (int)j, k)) w1[m] += src[2 * g.n + m];
+    }
+}
+
+// Pass arguments (PassArgs, kernels.h).  src_mode: 0 no source (the first
+// pass), 1 the reference's index convention, 2 aligned (the source of the
+// cell).  b == nullptr: no right-hand side (the first step, or the SOR
+// solver, which forms its own).
+template <class T>
+__device__ __forceinline__ T pass_value(const Geo &g, const PassArgs<T> &A, int c, int i, int j, int k)
+{
+    if (g.pz && k < GC) k += g.nzc;  // the periodic image of a bottom ghost face
+    const long long q = icel(g, i, j, k);
+    if (!cd_writes(g, c, i, j, k)) return A.T1[c][q];  // as k_pass_ghosts left it
+    T v = A.C[c][q];
+    if (A.src_mode == 1) {
+        if (q < g.n) v += A.src[c * g.n + q];
+    } else if (A.src_mode == 2) {
+        v += A.src[c * g.n + icelcal(g, i, j, k)];
+    }
+    return v;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_pass(Geo g, Metrics<double> m, Metrics<float> m32, PassArgs<T> A)
+{
+    double acc[2] = {0.0, 0.0};
+    ff accf[2] = {{0.f, 0.f}, {0.f, 0.f}};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        const T ue = pass_value(g, A, 0, i, j, k), vn = pass_value(g, A, 1, i, j, k),
+                wt = pass_value(g, A, 2, i, j, k);
+        if (cd_writes(g, 0, i, j, k)) A.T1[0][ic] = ue;
+        if (cd_writes(g, 1, i, j, k)) A.T1[1][ic] = vn;
+        if (cd_writes(g, 2, i, j, k)) A.T1[2][ic] = wt;
+        if (!A.b) continue;
+        const T uw = pass_value(g, A, 0, i - 1, j, k), vs = pass_value(g, A, 1, i, j - 1, k),
+                wb = pass_value(g, A, 2, i, j, k - 1);
+        if constexpr (sizeof(T) == sizeof(double)) {
+            // createBMatrix_omp in FP64, the arithmetic of k_rhs
+            const double div = ((double)ue - (double)uw) * m.x(AX_RD, i) + ((double)vn - (double)vs) * m.y(AX_RD, j)
+                             + ((double)wt - (double)wb) * m.z(AX_RD, k);
+            A.b[t] = -A.jp[t] * A.ddt * div;
+            if (A.partials) {
+                const double vol = m.x(AX_D, i) * m.y(AX_D, j) * m.z(AX_D, k);
+                acc[0] += vol * (-A.ddt * div);
+                acc[1] += vol;
+            }
+        } else {
+            // FP32 velocities: their differences are exact as float pairs and the
+            // rest runs in float-float, so b keeps the digits FP64 would
+            auto rd = [](const Axis<float> &a, int x) { return ff{a(AX_RD, x), a(AX_RDL, x)}; };
+            const ff div = ff_add(ff_add(ff_mul(ff_two_diff((float)ue, (float)uw), rd(m32.x, i)),
+                                         ff_mul(ff_two_diff((float)vn, (float)vs), rd(m32.y, j))),
+                                  ff_mul(ff_two_diff((float)wt, (float)wb), rd(m32.z, k)));
+            const ff d = ff_mul(div, ff_of(-A.ddt));  // the unscaled right-hand side
+            A.b[t] = ff_to_double(ff_mul(ff{__ldg(A.jph + t), __ldg(A.jpl + t)}, d));
+            if (A.partials) {
+                auto wd = [](const Axis<float> &a, int x) { return ff{a(AX_D, x), a(AX_DL, x)}; };
+                const ff vol = ff_mul(ff_mul(wd(m32.x, i), wd(m32.y, j)), wd(m32.z, k));
+                accf[0] = ff_add(accf[0], ff_mul(vol, d));
+                accf[1] = ff_add(accf[1], vol);
+            }
+        }
+    }
+    if (!A.partials) return;
+    if constexpr (sizeof(T) != sizeof(double)) {
+        acc[0] = ff_to_double(accf[0]);
+        acc[1] = ff_to_double(accf[1]);
+    }
+    double tot[2];
+    if (grid_reduce<2>(acc, A.partials, A.counter, tot) && threadIdx.x == 0) *A.mean = tot[0] / tot[1];
+}
+
+// update_UandF_omp (updateUandF.hpp:95-190) of one pass with the step's
+// other uses of f fused: src += dt f in the predictor passes
+// (RUN_CPU_PC_METHOD.hpp:393-401; f itself is then not stored, nothing
+// reads it), f stored and reduced to Cd and Cl in the final pass
+// (virtualF_Int, virtualForceIntergrator.hpp:26-32, with k_cdcl's launch
+// shape and summation order).  The faces update_UandF skips keep the f they
+// had (it never writes them), which is what the source and the sums read.
+template <class T>
+__global__ void __launch_bounds__(kBlock)
+k_update_pass(Geo g, Metrics<T> m, Metrics<double> m64, double dt, T rdt, const double *__restrict__ p,
+              const T *__restrict__ eta, const T *__restrict__ u1, const T *__restrict__ v1,
+              const T *__restrict__ w1, T *__restrict__ u3, T *__restrict__ v3, T *__restrict__ w3,
+              T *__restrict__ f, int store_f, T *__restrict__ src, T srcdt, double lz, double *partials,
+              unsigned int *counter, double *cdcl)
+{
+    double acc[2] = {0.0, 0.0};
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
+         t += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_of(g, t, i, j, k);
+        const long long ic = icel(g, i, j, k);
+        const double pc = p[ic];
+        const T ec = eta[ic];
+        T fv[3] = {T(0), T(0), T(0)};
+        if (i < g.nx - GC - 1) {
+            const T T2 = u1[ic] - (T)(dt * (p[ic + g.sx] - pc)) * m.x(AX_RDS, i);
+            const T ef = ec + (eta[ic + g.sx] - ec) * m.x(AX_IT, i);
+            const T un = (T(1) - ef) * T2;
+            u3[ic] = un;
+            fv[0] = (un - T2) * rdt;
+        }
+        if (j < g.ny - GC - 1) {
+            const T T2 = v1[ic] - (T)(dt * (p[ic + g.sy] - pc)) * m.y(AX_RDS, j);
+            const T ef = ec + (eta[ic + g.sy] - ec) * m.y(AX_IT, j);
+            const T vn = (T(1) - ef) * T2;
+            v3[ic] = vn;
+            fv[1] = (vn - T2) * rdt;
+        }
+        if (k < g.nz - GC - 1 + g.pz) {
+            const T T2 = w1[ic] - (T)(dt * (p[ic + 1] - pc)) * m.z(AX_RDS, k);
+            const T ef = ec + (eta[ic + 1] - ec) * m.z(AX_IT, k);
+            const T wn = (T(1) - ef) * T2;
+            w3[ic] = wn;
+            fv[2] = (wn - T2) * rdt;
+        }
+        if (store_f) {
+            if (i < g.nx - GC - 1) f[t] = fv[0];
+            if (j < g.ny - GC - 1) f[g.n + t] = fv[1];
+            if (k < g.nz - GC - 1 + g.pz) f[2 * g.n + t] = fv[2];
+        }
+        if (src) {
+            const T f0 = i < g.nx - GC - 1 ? fv[0] : f[t];
+            const T f1 = j < g.ny - GC - 1 ? fv[1] : f[g.n + t];
+            const T f2 = k < g.nz - GC - 1 + g.pz ? fv[2] : f[2 * g.n + t];
+            src[t] += srcdt * f0;
+            src[g.n + t] += srcdt * f1;
+            src[2 * g.n + t] += srcdt * f2;
+        }
+        if (cdcl) {
+            const double vol = m64.x(AX_D, i) * m64.y(AX_D, j) * m64.z(AX_D, k);
+            acc[0] += (double)(i < g.nx - GC - 1 ? fv[0] : f[t]) * vol;
+            acc[1] += (double)(j < g.ny - GC - 1 ? fv[1] : f[g.n + t]) * vol;
+        }
+    }
+    if (!cdcl) return;
+    double tot[2];
+    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+        cdcl[0] = -2.0 * tot[0] / lz;
+        cdcl[1] = -2.0 * tot[1] / lz;
+    }
+}
+
+__global__ void k_split_lo(long long n, const double *__restrict__ a, float *__restrict__ lo)
+{
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x)
+        lo[t] = ff_of(a[t]).lo;
+}
+
 // Pressure_transform_X_result (Transform.hpp:8-24)
 __global__ void k_transform(Geo g, const double *__restrict__ x, double *__restrict__ p)
 {
@@ -301,7 +494,7 @@ k_update_uf(Geo g, Metrics<T> m, double dt, T rdt, const double *__restrict__ p,
         v3[ic] = vn;
         f[g.n + t] = (vn - T2) * rdt;
     }
-    if (k < g.nz - GC - 1) {
+    if (k < g.nz - GC - 1 + g.pz) {  // periodic z: the top face is an unknown too
         const T T2 = w1[ic] - (T)(dt * (p[ic + 1] - pc)) * m.z(AX_RDS, k);
         const T ef = ec + (eta[ic + 1] - ec) * m.z(AX_IT, k);
         const T wn = (T(1) - ef) * T2;
@@ -356,6 +549,36 @@ template <class T>
 __device__ __forceinline__ T bc_tan(const BcTab &bc, int b, int c, T x)
 {   // tangential component: 2 Dir + (2 Num - 1) * interior
     return add_rn((T)(bc.dir[b * 3 + c] * 2.), mul_rn((T)(2.0 * bc.num[b * 3 + c] - 1.0), x));
+}
+
+// Periodic z (an extension; the reference's table has no periodic face): the
+// two ghost planes at each z end take the interior planes one period away,
+// over the whole (i, j) range including the x and y ghosts.  The sources
+// are interior planes, so the four copies of a column are independent.
+template <class T>
+__global__ void k_sync_z(Geo g, T *__restrict__ a0, T *__restrict__ a1, T *__restrict__ a2)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.nx * g.ny) return;
+    const long long base = t * g.nz;  // icel(i, j, 0) of column t = i ny + j
+    const int nzc = g.nzc, nz = g.nz;
+    auto col = [&](T *f) {
+        if (!f) return;
+        f[base + 0] = f[base + nzc];
+        f[base + 1] = f[base + 1 + nzc];
+        f[base + nz - 2] = f[base + nz - 2 - nzc];
+        f[base + nz - 1] = f[base + nz - 1 - nzc];
+    };
+    col(a0);
+    col(a1);
+    col(a2);
+}
+
+template <class T>
+void launch_sync_z(cudaStream_t s, const Geo &g, T *a0, T *a1, T *a2)
+{
+    const long long cols = (long long)g.nx * g.ny;
+    k_sync_z<T><<<(int)((cols + kBlock - 1) / kBlock), kBlock, 0, s>>>(g, a0, a1, a2);
 }
 
 template <class T>
@@ -648,10 +871,10 @@ template <class T>
 __global__ void __launch_bounds__(kBlock)
 k_div_projected(Geo g, Metrics<double> m, double dt, const double *__restrict__ p,
                 const T *__restrict__ u1, const T *__restrict__ v1, const T *__restrict__ w1,
-                const double *__restrict__ mean, unsigned long long *slot)
+                const double *__restrict__ mean, unsigned long long *slot, bool slot3)
 {
     const double c = -dt * (mean ? *mean : 0.0);
-    double mx = 0.0, md = 0.0;
+    double mx = 0.0, md = 0.0, mu = 0.0;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
@@ -665,16 +888,27 @@ k_div_projected(Geo g, Metrics<double> m, double dt, const double *__restrict__ 
         if (j < g.ny - GC - 1) vn -= dt * (p[ic + g.sy] - pc) * m.y(AX_RDS, j);
         if (j > GC) vs -= dt * (pc - p[ic - g.sy]) * m.y(AX_RDS, j - 1);
         double wt = (double)w1[ic], wb = (double)w1[ic - 1];
-        if (k < g.nz - GC - 1) wt -= dt * (p[ic + 1] - pc) * m.z(AX_RDS, k);
-        if (k > GC) wb -= dt * (pc - p[ic - 1]) * m.z(AX_RDS, k - 1);
+        if (k < g.nz - GC - 1 + g.pz) wt -= dt * (p[ic + 1] - pc) * m.z(AX_RDS, k);
+        if (k > GC || g.pz) wb -= dt * (pc - p[ic - 1]) * m.z(AX_RDS, k - 1);
         const double d = (ue - uw) * m.x(AX_RD, i) + (vn - vs) * m.y(AX_RD, j) + (wt - wb) * m.z(AX_RD, k);
         const double a = fabs(d), b = fabs(d - c);
         mx = (a > mx || a != a) ? a : mx;
         md = (b > md || b != b) ? b : md;
+        if (slot3) {  // the divergence of u* itself
+            const double du = ((double)u1[ic] - (double)u1[ic - g.sx]) * m.x(AX_RD, i)
+                            + ((double)v1[ic] - (double)v1[ic - g.sy]) * m.y(AX_RD, j)
+                            + ((double)w1[ic] - (double)w1[ic - 1]) * m.z(AX_RD, k);
+            const double e = fabs(du);
+            mu = (e > mu || e != e) ? e : mu;
+        }
     }
     grid_max_nonneg(mx, slot);
     __syncthreads();
     grid_max_nonneg(md, slot + 1);
+    if (slot3) {
+        __syncthreads();
+        grid_max_nonneg(mu, slot + 2);
+    }
 }
 
 template <class T>
@@ -806,6 +1040,36 @@ void launch_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, doubl
     }
 }
 
+template <class T>
+void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const Metrics<float> &m32,
+                 const PassArgs<T> &A, bool ghosts)
+{
+    if (ghosts) k_pass_ghosts<T><<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g, A.T1[0], A.T1[1], A.T1[2], A.src);
+    // the compatibility sums need the reduction's fixed launch shape
+    const int grid = A.partials ? c.red_blocks : blocks_for(g.n, c.grid_cap);
+    k_pass<T><<<grid, kBlock, 0, c.s>>>(g, m, m32, A);
+    if (A.partials) {
+        const double *jp = A.jp;
+        if (jp) k_rhs_compat<<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g.n, jp, A.mean, A.b);
+    }
+}
+
+template <class T>
+void launch_update_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<T> &m, const Metrics<double> &m64, double dt,
+                        const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3, T *v3, T *w3,
+                        T *f, bool store_f, T *src, double lz, double *cdcl)
+{
+    // the drag/lift sums need k_cdcl's launch shape (the same sums, bit for bit)
+    const int grid = cdcl ? c.red_blocks : (int)((g.n + kBlock - 1) / kBlock);
+    k_update_pass<T><<<grid, kBlock, 0, c.s>>>(g, m, m64, dt, (T)(1.0 / dt), p, eta, u1, v1, w1, u3, v3, w3, f,
+                                               store_f ? 1 : 0, src, (T)dt, lz, c.partials, c.counter, cdcl);
+}
+
+void launch_split_lo(cfd_launch_ctx &c, long long n, const double *a, float *lo)
+{
+    k_split_lo<<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, lo);
+}
+
 void launch_transform(cudaStream_t s, const Geo &g, const double *x, double *p)
 {
     k_transform<<<nblk(g.n), kBlock, 0, s>>>(g, x, p);
@@ -831,6 +1095,11 @@ void launch_bc_main(cudaStream_t s, const Geo &g, const BcTab &bc, T *u, T *v, T
 {
     k_bc_main<T><<<nblk((long long)g.nyc * g.nzc), kBlock, 0, s>>>(g, bc, 0, u, v, w, p);
     k_bc_main<T><<<nblk((long long)g.nxc * g.nzc), kBlock, 0, s>>>(g, bc, 1, u, v, w, p);
+    if (g.pz) {  // periodic z replaces faces 4 and 5, after the x and y faces
+        launch_sync_z<T>(s, g, u, v, w);
+        launch_sync_z<double>(s, g, p, nullptr, nullptr);
+        return;
+    }
     k_bc_main<T><<<nblk((long long)g.nxc * g.nyc), kBlock, 0, s>>>(g, bc, 2, u, v, w, p);
 }
 
@@ -869,9 +1138,9 @@ void launch_div_inf(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, c
 template <class T>
 void launch_div_projected(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double dt,
                           const double *p, const T *u1, const T *v1, const T *w1, const double *mean,
-                          unsigned long long *slot2)
+                          unsigned long long *slot2, bool with_ustar)
 {
-    k_div_projected<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, dt, p, u1, v1, w1, mean, slot2);
+    k_div_projected<T><<<c.red_blocks, kBlock, 0, c.s>>>(g, m, dt, p, u1, v1, w1, mean, slot2, with_ustar);
 }
 
 template <class T>
@@ -965,6 +1234,13 @@ void launch_link_copy(cfd_launch_ctx &c, long long n, const A *a, B *b)
                                       T *, T *, T *, T *);                                       \
     template void launch_cdcl<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double, \
                                  const T *, double *);                                           \
+    template void launch_sync_z<T>(cudaStream_t, const Geo &, T *, T *, T *);                    \
+    template void launch_pass<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,          \
+                                 const Metrics<float> &, const PassArgs<T> &, bool);             \
+    template void launch_update_pass<T>(cfd_launch_ctx &, const Geo &, const Metrics<T> &,        \
+                                        const Metrics<double> &, double, const double *, const T *, \
+                                        const T *, const T *, const T *, T *, T *, T *, T *, bool, \
+                                        T *, double, double *);                                   \
     template void launch_bc_main<T>(cudaStream_t, const Geo &, const BcTab &, T *, T *, T *,     \
                                     double *);                                                   \
     template void launch_bc_convective<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double,  \
@@ -981,7 +1257,7 @@ void launch_link_copy(cfd_launch_ctx &c, long long n, const A *a, B *b)
                                        const T *, const T *, const T *, double *);                \
     template void launch_div_projected<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &,  \
                                           double, const double *, const T *, const T *, const T *, \
-                                          const double *, unsigned long long *);
+                                          const double *, unsigned long long *, bool);
 
 CFD_FLOW_INSTANTIATE(double)
 CFD_FLOW_INSTANTIATE(float)

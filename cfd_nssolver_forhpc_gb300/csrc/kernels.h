@@ -44,6 +44,34 @@ template <class T>
 void launch_src_add(cfd_launch_ctx &c, const Geo &g, int aligned, T *u1, T *v1, T *w1, const T *src);
 template <class T>
 void launch_src_accumulate(cfd_launch_ctx &c, long long n3, T dt, T *src, const T *f);
+// One predictor-corrector pass from the step's single convection-diffusion
+// C: T1 = C (+ the source), and (b != nullptr) the Poisson right-hand side
+// with the compatibility projection (partials != nullptr); flow.cu.
+template <class T>
+struct PassArgs {
+    const T *C[3];
+    T *T1[3];
+    const T *src;
+    int src_mode;            // 0 none, 1 the reference's index convention, 2 aligned
+    const double *jp;
+    const float *jph, *jpl;  // mixed path: jp as a float pair
+    double ddt;
+    double *b;
+    double *partials;
+    unsigned int *counter;
+    double *mean;
+};
+template <class T>
+void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const Metrics<float> &m32,
+                 const PassArgs<T> &A, bool ghosts);
+// update_UandF of one pass with src += dt f (src != nullptr), f stored
+// (store_f) and Cd/Cl reduced into cdcl[0..1] (cdcl != nullptr)
+template <class T>
+void launch_update_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<T> &m, const Metrics<double> &m64, double dt,
+                        const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3, T *v3, T *w3,
+                        T *f, bool store_f, T *src, double lz, double *cdcl);
+// lo[t] = the low float of a[t] as a float pair
+void launch_split_lo(cfd_launch_ctx &c, long long n, const double *a, float *lo);
 template <class T>
 void launch_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double ddt,
                 const double *jp, const T *u1, const T *v1, const T *w1, double *b, bool compat,
@@ -70,7 +98,7 @@ void launch_div_inf(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, c
 template <class T>
 void launch_div_projected(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, double dt,
                           const double *p, const T *u1, const T *v1, const T *w1, const double *mean,
-                          unsigned long long *slot2);
+                          unsigned long long *slot2, bool with_ustar = false);
 template <class T>
 void launch_fill(cfd_launch_ctx &c, long long n, T *a, T val);
 template <class A, class B>
@@ -94,6 +122,8 @@ struct SpeOp {
     long long sxc;
     long long n;
     FastDiv fsxc, fnzc;                           // division by sxc and nzc
+    int pz;                                       // 1: the z neighbours wrap (periodic z);
+                                                  // czm[0] and czp[nzc - 1] are then non-zero
 };
 
 // The finite-volume form M = D_V L of the same operator (D_V = cell
@@ -153,6 +183,10 @@ void launch_bc_convective(cfd_launch_ctx &c, const Geo &g, const Metrics<double>
 // trip count)
 void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc, int cap, int first);
 
+// periodic z: the z ghost planes of up to three fields (null fields skipped)
+template <class T>
+void launch_sync_z(cudaStream_t s, const Geo &g, T *a0, T *a1, T *a2);
+
 void launch_spe_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
                       const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
                       double *cx, double *cy, double *cz, double *jp);
@@ -186,6 +220,7 @@ struct CgTma {
     int TK = 0, TJ = 0, grid = 0;
     size_t smem = 0;
     bool form_z = false;     // z = h / P formed in the stencil kernel (no z vector)
+    long long wait_limit = 1LL << 24;  // try-waits before a pipeline wait gives up
     CUtensorMap zh, p, palt;  // z (or the residual h when form_z), p, p_alt
     CUtensorMap zv;           // the z vector (read by the multigrid-preconditioned CG)
 };
@@ -300,6 +335,7 @@ struct MgLevel {
     float *xalt;           // second x buffer of a grid-wide level (fused sweeps ping-pong)
     int sweep_tj, sweep_ci;  // fused sweep tiling: j rows and i planes per block (0: not fused)
     bool quads;           // the float4 smoother applies (nz % 4 == 0, aligned arrays)
+    int pz;               // 1: periodic in z (nz even: red-black stays a two-colouring)
 };
 constexpr int kMgSmallSmem = 200 * 1024;  // shared-memory bytes for the small levels' x and b
 struct MgSmall {
@@ -318,6 +354,8 @@ struct Mg {
     int nlev = 0, first_small = 0;
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
     int sweeps0 = 2; // ... on the finest level
+    bool fuse_ends = true;  // the first pre-sweep from zero and the prolongation + first
+                            // post-colour each in one pass (float4 levels)
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve
     float *cinv = nullptr;
     bool usable = false;

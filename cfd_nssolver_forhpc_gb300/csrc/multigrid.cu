@@ -96,7 +96,9 @@ __device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict
     if (j > 0) s = fmaf(tl<SM>(L.cm[1] + j), x[t - sy], s);
     if (j < L.ny - 1) s = fmaf(tl<SM>(L.cp[1] + j), x[t + sy], s);
     if (k > 0) s = fmaf(tl<SM>(L.cm[2] + k), x[t - 1], s);
+    else if (L.pz) s = fmaf(tl<SM>(L.cm[2] + k), x[t + (L.nz - 1)], s);
     if (k < L.nz - 1) s = fmaf(tl<SM>(L.cp[2] + k), x[t + 1], s);
+    else if (L.pz) s = fmaf(tl<SM>(L.cp[2] + k), x[t - (L.nz - 1)], s);
     return s;
 }
 
@@ -172,7 +174,8 @@ __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__re
             if ((int)i < L.nx - 1) xp = *reinterpret_cast<const float4 *>(x + t + sx);
             if (j > 0) ym = *reinterpret_cast<const float4 *>(x + t - sy);
             if ((int)j < L.ny - 1) yp = *reinterpret_cast<const float4 *>(x + t + sy);
-            const float zlo = k0 > 0 ? x[t - 1] : 0.f, zhi = k0 + 4 < L.nz ? x[t + 4] : 0.f;
+            const float zlo = k0 > 0 ? x[t - 1] : (L.pz ? x[t + (L.nz - 1)] : 0.f);
+            const float zhi = k0 + 4 < L.nz ? x[t + 4] : (L.pz ? x[t + 4 - L.nz] : 0.f);
             const float cxm = tl<SM>(L.cm[0] + i), cxp = tl<SM>(L.cp[0] + i);
             const float cym = tl<SM>(L.cm[1] + j), cyp = tl<SM>(L.cp[1] + j);
             const float4 czm = tl4<SM>(L.cm[2] + k0);
@@ -198,6 +201,172 @@ __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__re
         xo[2] = odd ? xc.z : vB;
         xo[3] = odd ? vB : xc.w;
         *reinterpret_cast<float4 *>(x + t) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+    }
+}
+
+// quad decomposition of smooth_quads: thread index q -> (i, j, k0), cell t
+template <class I>
+__device__ __forceinline__ void quad_of(const MgLevel &L, I q, unsigned &i, unsigned &j, int &k0, I &t)
+{
+    const int n4 = L.nz >> 2;
+    const unsigned u = (unsigned)q;
+    i = L.fyq.div(u);
+    const unsigned r = u - i * (unsigned)(L.ny * n4);
+    j = L.fq.div(r);
+    k0 = 4 * (int)(r - j * (unsigned)n4);
+    t = ((I)i * L.ny + j) * L.nz + k0;
+}
+
+// the colour-`color` update of the two cells of a quad (offsets e0, e0 + 2)
+// from the quad's and its neighbours' values: smooth_quads' arithmetic, term
+// for term
+__device__ __forceinline__ void quad_update(const MgLevel &L, unsigned i, unsigned j, int k0, const float4 &bv,
+                                            const float4 &xc, const float4 &xm, const float4 &xp, const float4 &ym,
+                                            const float4 &yp, float zlo, float zhi, int color, float4 &out)
+{
+    const int e0 = (int)((color + i + j) & 1u);
+    const bool odd = e0 != 0;
+    auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+    const float bA = pick(bv.x, bv.y), bB = pick(bv.z, bv.w);
+    const float rxy = __ldg(L.rw[0] + i) * __ldg(L.rw[1] + j);
+    const float sxy = __ldg(L.sum[0] + i) + __ldg(L.sum[1] + j);
+    const float4 rz = __ldg(reinterpret_cast<const float4 *>(L.rw[2] + k0));
+    const float4 sz = __ldg(reinterpret_cast<const float4 *>(L.sum[2] + k0));
+    const float rA = rxy * pick(rz.x, rz.y), rB = rxy * pick(rz.z, rz.w);
+    const float dA = smooth_rcp(sxy + pick(sz.x, sz.y)), dB = smooth_rcp(sxy + pick(sz.z, sz.w));
+    const float cxm = __ldg(L.cm[0] + i), cxp = __ldg(L.cp[0] + i);
+    const float cym = __ldg(L.cm[1] + j), cyp = __ldg(L.cp[1] + j);
+    const float4 czm = __ldg(reinterpret_cast<const float4 *>(L.cm[2] + k0));
+    const float4 czp = __ldg(reinterpret_cast<const float4 *>(L.cp[2] + k0));
+    float nA = cxm * pick(xm.x, xm.y);
+    nA = fmaf(cxp, pick(xp.x, xp.y), nA);
+    nA = fmaf(cym, pick(ym.x, ym.y), nA);
+    nA = fmaf(cyp, pick(yp.x, yp.y), nA);
+    nA = fmaf(pick(czm.x, czm.y), pick(zlo, xc.x), nA);
+    nA = fmaf(pick(czp.x, czp.y), pick(xc.y, xc.z), nA);
+    float nB = cxm * pick(xm.z, xm.w);
+    nB = fmaf(cxp, pick(xp.z, xp.w), nB);
+    nB = fmaf(cym, pick(ym.z, ym.w), nB);
+    nB = fmaf(cyp, pick(yp.z, yp.w), nB);
+    nB = fmaf(pick(czm.z, czm.w), pick(xc.y, xc.z), nB);
+    nB = fmaf(pick(czp.z, czp.w), pick(xc.w, zhi), nB);
+    const float vA = fmaf(bA, rA, nA) * dA, vB = fmaf(bB, rB, nB) * dB;
+    out = make_float4(odd ? xc.x : vA, odd ? vA : xc.y, odd ? xc.z : vB, odd ? vB : xc.w);
+}
+
+// The first pre-smoothing sweep from x = 0 in one pass.  Colour 0 from zero
+// gives x = (b / dV) / diag at the colour-0 cells and 0 at the others;
+// colour 1 then reads colour-0 neighbours only, and each thread forms those
+// values from b itself.  The result equals the two colour launches bit for
+// bit (k_mg_smooth4 with zero_init, then colour 1).
+template <class I>
+__global__ void __launch_bounds__(kBlock) k_mg_first4(MgLevel L, const float *__restrict__ b, float *__restrict__ x,
+                                                         const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    const I nq = (I)(L.n >> 2);
+    const I sx = (I)L.ny * L.nz, sy = L.nz;
+    // the zero-start colour-0 values of the quad at (ii, jj, k0), index tt;
+    // cells of colour 1 read as 0 (as the colour-0 launch leaves them)
+    auto zero_start = [&](int ii, int jj, int k0, I tt) -> float4 {
+        const float4 bv = *reinterpret_cast<const float4 *>(b + tt);
+        const int e0 = (int)((ii + jj) & 1);
+        const bool odd = e0 != 0;
+        auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+        const float rxy = __ldg(L.rw[0] + ii) * __ldg(L.rw[1] + jj);
+        const float sxy = __ldg(L.sum[0] + ii) + __ldg(L.sum[1] + jj);
+        const float4 rz = __ldg(reinterpret_cast<const float4 *>(L.rw[2] + k0));
+        const float4 sz = __ldg(reinterpret_cast<const float4 *>(L.sum[2] + k0));
+        const float vA = fmaf(pick(bv.x, bv.y), rxy * pick(rz.x, rz.y), 0.f) * smooth_rcp(sxy + pick(sz.x, sz.y));
+        const float vB = fmaf(pick(bv.z, bv.w), rxy * pick(rz.z, rz.w), 0.f) * smooth_rcp(sxy + pick(sz.z, sz.w));
+        return make_float4(odd ? 0.f : vA, odd ? vA : 0.f, odd ? 0.f : vB, odd ? vB : 0.f);
+    };
+    // one cell's zero-start value (for the z neighbours across the quad ends)
+    auto zero_cell = [&](int ii, int jj, int kk, I tt) -> float {
+        if (((ii + jj + kk) & 1) != 0) return 0.f;
+        const float r = (__ldg(L.rw[0] + ii) * __ldg(L.rw[1] + jj)) * __ldg(L.rw[2] + kk);
+        const float d = smooth_rcp((__ldg(L.sum[0] + ii) + __ldg(L.sum[1] + jj)) + __ldg(L.sum[2] + kk));
+        return fmaf(b[tt], r, 0.f) * d;
+    };
+    for (I q = (I)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (I)gridDim.x * blockDim.x) {
+        unsigned i, j;
+        int k0;
+        I t;
+        quad_of<I>(L, q, i, j, k0, t);
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 xc = zero_start((int)i, (int)j, k0, t);
+        const float4 xm = i > 0 ? zero_start((int)i - 1, (int)j, k0, t - sx) : zero;
+        const float4 xp = (int)i < L.nx - 1 ? zero_start((int)i + 1, (int)j, k0, t + sx) : zero;
+        const float4 ym = j > 0 ? zero_start((int)i, (int)j - 1, k0, t - sy) : zero;
+        const float4 yp = (int)j < L.ny - 1 ? zero_start((int)i, (int)j + 1, k0, t + sy) : zero;
+        const float zlo = k0 > 0 ? zero_cell((int)i, (int)j, k0 - 1, t - 1)
+                                 : (L.pz ? zero_cell((int)i, (int)j, L.nz - 1, t + (L.nz - 1)) : 0.f);
+        const float zhi = k0 + 4 < L.nz ? zero_cell((int)i, (int)j, k0 + 4, t + 4)
+                                        : (L.pz ? zero_cell((int)i, (int)j, 0, t + 4 - L.nz) : 0.f);
+        const float4 bv = *reinterpret_cast<const float4 *>(b + t);
+        float4 out;
+        quad_update(L, i, j, k0, bv, xc, xm, xp, ym, yp, zlo, zhi, 1, out);
+        *reinterpret_cast<float4 *>(x + t) = out;
+    }
+}
+
+// The prolongation and the first post-smoothing colour (colour 1) in one
+// pass: the colour-0 cells around each colour-1 cell are read as x + the
+// coarse correction of their parent (the value k_mg_prolong would store) and
+// the colour-1 cells get their Gauss-Seidel update.  Only colour-1 cells are
+// stored: the colour-0 cells, which other threads read here, keep x, and the
+// colour-0 pass that follows overwrites them without reading them (their
+// update depends on their colour-1 neighbours only).  So after that pass the
+// level equals k_mg_prolong, colour 1, colour 0 bit for bit.
+template <class I>
+__global__ void __launch_bounds__(kBlock) k_mg_prolong_first4(MgLevel L, MgLevel C, const float *__restrict__ b,
+                                                                 float *__restrict__ x, const float *__restrict__ xc_,
+                                                                 const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    const I nq = (I)(L.n >> 2);
+    const I sx = (I)L.ny * L.nz, sy = L.nz;
+    const int fx = L.nx / C.nx, fy = L.ny / C.ny, fz = L.nz / C.nz;
+    auto corr = [&](int ii, int jj, int kk) -> float {
+        return __ldg(xc_ + ((long long)(ii / fx) * C.ny + jj / fy) * C.nz + kk / fz);
+    };
+    auto quad = [&](int ii, int jj, int k0, I tt) -> float4 {
+        const float4 v = *reinterpret_cast<const float4 *>(x + tt);
+        return make_float4(v.x + corr(ii, jj, k0), v.y + corr(ii, jj, k0 + 1), v.z + corr(ii, jj, k0 + 2),
+                           v.w + corr(ii, jj, k0 + 3));
+    };
+    for (I q = (I)blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += (I)gridDim.x * blockDim.x) {
+        unsigned i, j;
+        int k0;
+        I t;
+        quad_of<I>(L, q, i, j, k0, t);
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 raw = *reinterpret_cast<const float4 *>(x + t);
+        const float4 xc = quad((int)i, (int)j, k0, t);
+        const float4 xm = i > 0 ? quad((int)i - 1, (int)j, k0, t - sx) : zero;
+        const float4 xp = (int)i < L.nx - 1 ? quad((int)i + 1, (int)j, k0, t + sx) : zero;
+        const float4 ym = j > 0 ? quad((int)i, (int)j - 1, k0, t - sy) : zero;
+        const float4 yp = (int)j < L.ny - 1 ? quad((int)i, (int)j + 1, k0, t + sy) : zero;
+        const float zlo = k0 > 0 ? x[t - 1] + corr((int)i, (int)j, k0 - 1)
+                                 : (L.pz ? x[t + (L.nz - 1)] + corr((int)i, (int)j, L.nz - 1) : 0.f);
+        const float zhi = k0 + 4 < L.nz ? x[t + 4] + corr((int)i, (int)j, k0 + 4)
+                                        : (L.pz ? x[t + 4 - L.nz] + corr((int)i, (int)j, 0) : 0.f);
+        const float4 bv = *reinterpret_cast<const float4 *>(b + t);
+        float4 out;
+        quad_update(L, i, j, k0, bv, xc, xm, xp, ym, yp, zlo, zhi, 1, out);
+        // colour 1 at offsets e0, e0 + 2; the colour-0 cells keep x
+        if (((1u + i + j) & 1u) != 0) {
+            out.x = raw.x;
+            out.z = raw.z;
+        } else {
+            out.y = raw.y;
+            out.w = raw.w;
+        }
+        *reinterpret_cast<float4 *>(x + t) = out;
     }
 }
 
@@ -795,15 +964,18 @@ k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float 
     else if (!(rel == rel)) sc->done = BICG_CAPPED;
 }
 
-// per-axis device arrays {cm, cp, cm + cp, w, 1/w} of m entries
-int upload_axis(cfd_ctx *c, const std::vector<double> &W, MgLevel &L, int a)
+// per-axis device arrays {cm, cp, cm + cp, w, 1/w} of m entries; periodic:
+// the end cells couple across the period (centre distance (W[m-1] + W[0]) / 2)
+int upload_axis(cfd_ctx *c, const std::vector<double> &W, MgLevel &L, int a, bool periodic = false)
 {
     const int m = (int)W.size();
     std::vector<float> all((size_t)5 * m, 0.f);
     for (int i = 0; i < m; ++i) {
         float cm = 0.f, cp = 0.f;
         if (i > 0) cm = (float)(1.0 / (W[i] * 0.5 * (W[i - 1] + W[i])));
+        else if (periodic) cm = (float)(1.0 / (W[i] * 0.5 * (W[m - 1] + W[i])));
         if (i < m - 1) cp = (float)(1.0 / (W[i] * 0.5 * (W[i] + W[i + 1])));
+        else if (periodic) cp = (float)(1.0 / (W[i] * 0.5 * (W[i] + W[0])));
         all[i] = cm;
         all[m + i] = cp;
         all[2 * m + i] = cm + cp;
@@ -837,8 +1009,9 @@ void set_divs(MgLevel &L)
 }
 
 // dense (M + a 1 1^T)^-1 of a level given its per-axis widths (Gauss-Jordan
-// in FP64; M symmetric positive semi-definite with constants as null space)
-int coarse_inverse(cfd_ctx *c, const std::vector<double> (&W)[3], float **out)
+// in FP64; M symmetric positive semi-definite with constants as null space);
+// pz: z neighbours wrap
+int coarse_inverse(cfd_ctx *c, const std::vector<double> (&W)[3], float **out, bool pz = false)
 {
     const int nx = (int)W[0].size(), ny = (int)W[1].size(), nz = (int)W[2].size(), n = nx * ny * nz;
     std::vector<double> A((size_t)n * n, 0.0), I((size_t)n * n, 0.0);
@@ -853,7 +1026,8 @@ int coarse_inverse(cfd_ctx *c, const std::vector<double> (&W)[3], float **out)
                 double diag = 0.0;
                 for (int a = 0; a < 3; ++a)
                     for (int side = -1; side <= 1; side += 2) {
-                        const int o = ax[a] + side;
+                        int o = ax[a] + side;
+                        if (a == 2 && pz) o = (o + lim[a]) % lim[a];
                         if (o < 0 || o >= lim[a]) continue;
                         const double cf = dv / (W[a][ax[a]] * 0.5 * (W[a][ax[a]] + W[a][o]));
                         int ii = i, jj = j, kk = k;
@@ -970,6 +1144,7 @@ int mg_setup(cfd_ctx *c)
     G.sweeps0 = G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_SWEEPS0")) G.sweeps0 = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_PAIRS")) G.pairs = std::atoi(e) > 0 ? std::atoi(e) : 1;
+    if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS")) G.fuse_ends = std::atoi(e) != 0;
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
     const FvOp<float> F = fv32(c);
@@ -994,15 +1169,21 @@ int mg_setup(cfd_ctx *c)
     }
     L0.x = c->w32.r0;  // z
     L0.b = c->r32;     // h
+    L0.pz = g.pz;
     set_divs(L0);
     G.lev[0] = L0;
     int nl = 1;
     int n[3] = {g.nxc, g.nyc, g.nzc};
-    while (nl < kMgMaxLevels && (long long)n[0] * n[1] * n[2] > kMgCoarseTarget) {
+    long long target = kMgCoarseTarget;
+    if (const char *e = std::getenv("CFDGPU_MG_COARSE")) target = std::max(8LL, std::min<long long>(kMgCoarsest, std::atoll(e)));
+    while (nl < kMgMaxLevels && (long long)n[0] * n[1] * n[2] > target) {
         int f[3];
         bool any = false;
         for (int a = 0; a < 3; ++a) {
             f[a] = (n[a] % 2 == 0 && n[a] >= 4) ? 2 : 1;
+            // periodic z halves only to an even length, so that red-black
+            // stays a two-colouring across the wrap
+            if (a == 2 && g.pz && n[a] % 4 != 0) f[a] = 1;
             any = any || f[a] == 2;
         }
         if (!any) break;
@@ -1012,8 +1193,9 @@ int mg_setup(cfd_ctx *c)
             for (size_t I = 0; I < Wc.size(); ++I) Wc[I] = f[a] == 2 ? W[a][2 * I] + W[a][2 * I + 1] : W[a][I];
             W[a] = Wc;
             n[a] = (int)Wc.size();
-            CKS(upload_axis(c, W[a], L, a));
+            CKS(upload_axis(c, W[a], L, a, a == 2 && g.pz));
         }
+        L.pz = g.pz;
         L.nx = n[0]; L.ny = n[1]; L.nz = n[2];
         L.n = (long long)n[0] * n[1] * n[2];
         CKS(dalloc_t(c, &L.x, (size_t)L.n));
@@ -1025,7 +1207,7 @@ int mg_setup(cfd_ctx *c)
     const long long ncoarse = G.lev[nl - 1].n;
     G.usable = nl > 1 && ncoarse <= kMgCoarsest;
     if (!G.usable) return CFD_OK;
-    CKS(coarse_inverse(c, W, &G.cinv));
+    CKS(coarse_inverse(c, W, &G.cinv, g.pz != 0));
     // the first small level: at most `small` cells, and all levels from it
     // on fit the small kernel's shared memory; the dense inverse is staged
     // there too when it fits
@@ -1053,7 +1235,7 @@ int mg_setup(cfd_ctx *c)
     for (int l = 0; l < G.first_small; ++l) {
         MgLevel &L = G.lev[l];
         L.sweep_tj = L.sweep_ci = 0;
-        if (!fused || !L.quads || level_sweeps(G, l) % 2 != 0) continue;
+        if (!fused || !L.quads || L.pz || level_sweeps(G, l) % 2 != 0) continue;
         const int n4 = L.nz / 4;
         const int tj = std::max(1, std::min({128 / std::max(n4, 1), L.ny, 1024 / n4}));
         if (tj * n4 > 1024 || (long long)sweep_smem(tj, L.nz) > kSweepSmemMax) continue;
@@ -1098,10 +1280,32 @@ static void sweep_launch(const MgLevel &L, const float *xo, float *xn, int c0, i
 // the pre-smoothing (c0 = 0, from x = 0) or post-smoothing (c0 = 1, from x) of
 // a grid-wide level: fused sweeps alternate between x and xalt and end in x
 // (an even number of sweeps), else colour launches in place
-static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStream_t s)
+// a level whose sweep ends run fused (k_mg_first4, k_mg_prolong_first4)
+static bool fused_ends(const Mg &G, const MgLevel &L) { return G.fuse_ends && L.quads && L.sweep_tj == 0; }
+static bool int_index(const MgLevel &L) { return L.n + (long long)L.ny * L.nz < (1LL << 31); }
+
+// pre: the sweeps before the coarse correction; post_fused: the caller ran
+// the first colour of the post-smoothing with the prolongation
+static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStream_t s, bool post_fused = false)
 {
     const MgLevel &L = G.lev[l];
     const int sweeps = level_sweeps(G, l);
+    if (fused_ends(G, L)) {
+        for (int q = 0; q < sweeps; ++q) {
+            if (pre && q == 0) {
+                if (int_index(L))
+                    launch_pdl(k_mg_first4<int>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x,
+                               done);
+                else
+                    launch_pdl(k_mg_first4<long long>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L,
+                               (const float *)L.b, L.x, done);
+                continue;
+            }
+            if (!(post_fused && q == 0)) smooth_launch(L, pre ? 0 : 1, 0, done, s);
+            smooth_launch(L, pre ? 1 : 0, 0, done, s);
+        }
+        return;
+    }
     if (L.sweep_tj > 0) {
         const float *src = L.x;
         for (int q = 0; q < sweeps; ++q) {
@@ -1146,6 +1350,16 @@ void mg_vcycle(cfd_ctx *c, const int *done)
     launch_pdl(k_mg_small, dim3(1), dim3(kSmallThreads), G.small_smem, s, small_desc(G, done));
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
+        if (fused_ends(G, L)) {
+            if (int_index(L))
+                launch_pdl(k_mg_prolong_first4<int>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
+                           (const float *)L.b, L.x, (const float *)G.lev[l + 1].x, done);
+            else
+                launch_pdl(k_mg_prolong_first4<long long>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
+                           (const float *)L.b, L.x, (const float *)G.lev[l + 1].x, done);
+            smooth_phase(G, l, false, done, s, true);
+            continue;
+        }
         launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1],
                    (const float *)G.lev[l + 1].x, L.x, done);
         smooth_phase(G, l, false, done, s);
@@ -1175,7 +1389,13 @@ void mg_time_part(cfd_ctx *c, int part)
 long long mg_vcycle_launches(const Mg &G)
 {
     long long n = 1;
-    for (int l = 0; l < G.first_small; ++l) n += 2 + (G.lev[l].sweep_tj > 0 ? 1LL : 2LL) * 2 * level_sweeps(G, l);
+    for (int l = 0; l < G.first_small; ++l) {
+        const MgLevel &L = G.lev[l];
+        // pre 2s - 1 (the first sweep in one launch), restriction, the
+        // prolongation with the first post colour, then 2s - 1 colours
+        if (fused_ends(G, L)) n += 4LL * level_sweeps(G, l);
+        else n += 2 + (L.sweep_tj > 0 ? 1LL : 2LL) * 2 * level_sweeps(G, l);
+    }
     return n;
 }
 

@@ -40,8 +40,11 @@ struct NoallocScratch {
 
 static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
 
-// Device address of g_noalloc_scratch per device, looked up once with that
-// device current (the host-side symbol is only a stand-in for it).
+// Device address of g_noalloc_scratch per device, looked up with that
+// device current (the host-side symbol is only a stand-in for it).  The
+// lookup is repeated on every call made outside stream capture, so a device
+// reset (which reloads the module at a new address) cannot leave a stale
+// address behind; a call made during capture uses the last address found.
 std::mutex g_mu;
 NoallocScratch *g_addr[64] = {};
 
@@ -95,10 +98,17 @@ extern "C" int cfd_cdcl_noalloc(int nx_cal, int ny_cal, int nz_cal, double lz, c
         return cfd::set_last_error(CFD_ERR_CUDA, std::string("cfd_cdcl_noalloc: cudaGetDevice: ") +
                                                      cudaGetErrorString(e));
     }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) {
+        return cfd::set_last_error(CFD_ERR_CUDA, std::string("cfd_cdcl_noalloc: cudaStreamIsCapturing: ") +
+                                                     cudaGetErrorString(e));
+    }
     NoallocScratch *s = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
+        if (!g_addr[dev] || cap == cudaStreamCaptureStatusNone) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess || !p) {
@@ -109,7 +119,6 @@ extern "C" int cfd_cdcl_noalloc(int nx_cal, int ny_cal, int nz_cal, double lz, c
         }
         s = g_addr[dev];
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     Geo g{};
     g.nxc = nx_cal; g.nyc = ny_cal; g.nzc = nz_cal;
     g.nx = nx_cal + 2 * GC; g.ny = ny_cal + 2 * GC; g.nz = nz_cal + 2 * GC;

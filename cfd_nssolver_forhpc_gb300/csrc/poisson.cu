@@ -39,8 +39,8 @@ __device__ __forceinline__ V apply_row(const SpeOp<V> &A, const V *__restrict__ 
     const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
     const long long ys = j > 0 ? row - A.nzc : row;
     const long long yn = j < A.nyc - 1 ? row + A.nzc : row;
-    const long long zb = k > 0 ? row - 1 : row;
-    const long long zt = k < A.nzc - 1 ? row + 1 : row;
+    const long long zb = k > 0 ? row - 1 : (A.pz ? row + (A.nzc - 1) : row);
+    const long long zt = k < A.nzc - 1 ? row + 1 : (A.pz ? row - (A.nzc - 1) : row);
     V s = __ldg(A.cxm + i) * x[xw];
     s = fma(__ldg(A.cym + j), x[ys], s);
     s = fma(__ldg(A.czm + k), x[zb], s);
@@ -75,8 +75,8 @@ __device__ __forceinline__ V apply_row_f(const SpeOp<V> &A, long long row, F &&x
     const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
     const long long ys = j > 0 ? row - A.nzc : row;
     const long long yn = j < A.nyc - 1 ? row + A.nzc : row;
-    const long long zb = k > 0 ? row - 1 : row;
-    const long long zt = k < A.nzc - 1 ? row + 1 : row;
+    const long long zb = k > 0 ? row - 1 : (A.pz ? row + (A.nzc - 1) : row);
+    const long long zt = k < A.nzc - 1 ? row + 1 : (A.pz ? row - (A.nzc - 1) : row);
     const V cxm = __ldg(A.cxm + i), cxp = __ldg(A.cxp + i), cym = __ldg(A.cym + j), cyp = __ldg(A.cyp + j);
     const V czm = __ldg(A.czm + k), czp = __ldg(A.czp + k);
     V s = cxm * xat(xw);
@@ -104,13 +104,15 @@ __global__ void __launch_bounds__(kBlock) k_apply(Op A, const double *__restrict
 // reference's summation order, so it is bitwise the reference's jp.
 __device__ __forceinline__ double inv2(double a, double b) { return __ddiv_rn(__ddiv_rn(1.0, a), b); }
 
+// periodic (z of a periodic context): the first cell's minus face and the
+// last cell's plus face couple across the period
 __global__ void k_spe_axes(int n, const double *__restrict__ D, const double *__restrict__ Ds,
-                           double *__restrict__ c)
+                           double *__restrict__ c, int periodic)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    c[i] = i == 0 ? 0.0 : inv2(D[i + GC], Ds[i + GC - 1]);
-    c[n + i] = i == n - 1 ? 0.0 : inv2(D[i + GC], Ds[i + GC]);
+    c[i] = (i == 0 && !periodic) ? 0.0 : inv2(D[i + GC], Ds[i + GC - 1]);
+    c[n + i] = (i == n - 1 && !periodic) ? 0.0 : inv2(D[i + GC], Ds[i + GC]);
 }
 
 __global__ void k_spe_jp(Geo g, const double *__restrict__ Dx, const double *__restrict__ Dy,
@@ -131,8 +133,8 @@ __global__ void k_spe_jp(Geo g, const double *__restrict__ Dx, const double *__r
         if (i == g.nxc - 1) v = __dsub_rn(v, xp);
         if (j == 0) v = __dsub_rn(v, ym);
         if (j == g.nyc - 1) v = __dsub_rn(v, yp);
-        if (k == 0) v = __dsub_rn(v, zm);
-        if (k == g.nzc - 1) v = __dsub_rn(v, zp);
+        if (k == 0 && !g.pz) v = __dsub_rn(v, zm);
+        if (k == g.nzc - 1 && !g.pz) v = __dsub_rn(v, zp);
         jp[row] = __ddiv_rn(1.0, v);
     }
 }
@@ -141,9 +143,9 @@ void launch_spe_setup(cudaStream_t s, const Geo &g, const double *Dx, const doub
                       const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
                       double *cx, double *cy, double *cz, double *jp)
 {
-    k_spe_axes<<<(g.nxc + 127) / 128, 128, 0, s>>>(g.nxc, Dx, Dxs, cx);
-    k_spe_axes<<<(g.nyc + 127) / 128, 128, 0, s>>>(g.nyc, Dy, Dys, cy);
-    k_spe_axes<<<(g.nzc + 127) / 128, 128, 0, s>>>(g.nzc, Dz, Dzs, cz);
+    k_spe_axes<<<(g.nxc + 127) / 128, 128, 0, s>>>(g.nxc, Dx, Dxs, cx, 0);
+    k_spe_axes<<<(g.nyc + 127) / 128, 128, 0, s>>>(g.nyc, Dy, Dys, cy, 0);
+    k_spe_axes<<<(g.nzc + 127) / 128, 128, 0, s>>>(g.nzc, Dz, Dzs, cz, g.pz);
     k_spe_jp<<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, Dx, Dy, Dz, Dxs, Dys, Dzs, jp);
 }
 
@@ -169,8 +171,8 @@ __global__ void k_ell_assemble(Geo g, const double *__restrict__ Dx, const doubl
         if (ic == g.nxc - 1) aa = -xp;
         if (jc == 0) bb = -ym;
         if (jc == g.nyc - 1) bb = -yp;
-        if (kc == 0) cc = -zm;
-        if (kc == g.nzc - 1) cc = -zp;
+        if (kc == 0 && !g.pz) cc = -zm;
+        if (kc == g.nzc - 1 && !g.pz) cc = -zp;
         double v = __dadd_rn(xm, xp);
         v = __dadd_rn(v, ym); v = __dadd_rn(v, yp); v = __dadd_rn(v, zm); v = __dadd_rn(v, zp);
         v = __dadd_rn(v, aa); v = __dadd_rn(v, bb); v = __dadd_rn(v, cc);
@@ -185,7 +187,9 @@ __global__ void k_ell_assemble(Geo g, const double *__restrict__ Dx, const doubl
         if (jc != 0) { c[s] = (int)(row - g.nzc); w[s++] = __dmul_rn(-ym, jr); }
         if (jc != g.nyc - 1) { c[s] = (int)(row + g.nzc); w[s++] = __dmul_rn(-yp, jr); }
         if (kc != 0) { c[s] = (int)(row - 1); w[s++] = __dmul_rn(-zm, jr); }
+        else if (g.pz) { c[s] = (int)(row + g.nzc - 1); w[s++] = __dmul_rn(-zm, jr); }
         if (kc != g.nzc - 1) { c[s] = (int)(row + 1); w[s++] = __dmul_rn(-zp, jr); }
+        else if (g.pz) { c[s] = (int)(row - (g.nzc - 1)); w[s++] = __dmul_rn(-zp, jr); }
         for (; s < 7; ++s) { c[s] = (int)(g.n - 1); w[s] = 0.0; }
 #pragma unroll
         for (int q = 0; q < 7; ++q) {
@@ -504,8 +508,8 @@ __device__ __forceinline__ float fv_apply(const FvOp<float> &F, long long row, i
     const long long xe = i < A.nxc - 1 ? row + A.sxc : row;
     const long long ys = j > 0 ? row - A.nzc : row;
     const long long yn = j < A.nyc - 1 ? row + A.nzc : row;
-    const long long zb = k > 0 ? row - 1 : row;
-    const long long zt = k < A.nzc - 1 ? row + 1 : row;
+    const long long zb = k > 0 ? row - 1 : (A.pz ? row + (A.nzc - 1) : row);
+    const long long zt = k < A.nzc - 1 ? row + 1 : (A.pz ? row - (A.nzc - 1) : row);
     float s = __ldg(A.cxm + i) * xat(xw);
     s = fmaf(__ldg(A.cym + j), xat(ys), s);
     s = fmaf(__ldg(A.czm + k), xat(zb), s);
@@ -595,6 +599,7 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
     auto ld = [&](int i, int jj, int kk, float &zv, float &pv) {
         zv = 0.f;
         pv = 0.f;
+        if (A.pz) kk = kk < 0 ? kk + nzc : (kk >= nzc ? kk - nzc : kk);  // periodic z: wrap the halo
         if (i >= 0 && i < nxc && jj >= 0 && jj < nyc && kk >= 0 && kk < nzc) {
             const long long r = (long long)i * sxc + (jj * nzc + kk);
             zv = z[r];
@@ -676,10 +681,14 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
 // Per plane the block forms pn = z + beta p over the tile and its halo in a
 // shared plane (three rotating buffers), then applies M at the previous plane
 // with its x neighbours held in registers.  The mbarrier waits are bounded:
-// on timeout the block records sc->wait_timeout and carries on, so a lost
-// copy cannot hang the GPU; the host turns the flag into an error.
+// when a wait gives up (wait_limit try-waits), the block records
+// sc->wait_timeout, issues no further copies, waits out the copies it has in
+// flight and skips its remaining work, so a lost copy can neither hang the
+// GPU nor land in shared memory after the block has exited; the host turns
+// the flag into an error.
 constexpr int kCgStages = 4;
-constexpr long long kCgWaitLimit = 1LL << 24;
+constexpr long long kCgWaitLimit = 1LL << 24;   // default try-waits of a pipeline wait
+constexpr long long kCgDrainLimit = 1LL << 24;  // try-waits per copy when draining after a timeout
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
 {
@@ -709,10 +718,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
     return ok != 0;
 }
 
-// bounded wait: false if the phase did not complete within the limit
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+// bounded wait: false if the phase did not complete within `limit` try-waits
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, long long limit)
 {
-    for (long long it = 0; it < kCgWaitLimit; ++it)
+    for (long long it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -743,7 +752,7 @@ template <bool first, int TK, bool FZ>
 __global__ void __launch_bounds__(kBlock)
 k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_constant__ CUtensorMap mp,
             float *__restrict__ pn_out, float *__restrict__ q, BicgScal *sc, double *partials,
-            unsigned int *counter, int ichunk)
+            unsigned int *counter, int ichunk, long long wait_limit)
 {
     using G = CgTile<TK>;
     constexpr int NV = first ? 1 : 2;
@@ -775,8 +784,10 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
     }
     __syncthreads();
 
+    long long issued_hi = 0;  // thread 0: global plane counter of the last plane issued + 1
     // one plane's TMA boxes into the stage of global plane counter g
     auto issue = [&](long long g, int k0, int j0, int ip) {
+        issued_hi = g + 1;
         const int st = (int)(g % kCgStages);
         const unsigned bar = bars + 8 * st;
         mbar_expect_tx(bar, NV * G::BOXB);
@@ -793,7 +804,8 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
     const int cslot = (tj + 1) * G::BX + 4 + 4 * tk4;  // this thread's float4 in a box / pn plane
     float pa = 0.f, pz = 0.f;
     long long g0 = 0;  // planes consumed by this block so far (mbarrier phases)
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    long long g_stop = -1;  // the plane whose wait gave up (-1: none)
+    for (int item = blockIdx.x; item < items && g_stop < 0; item += gridDim.x) {
         const int tile = item % tiles, chunk = item / tiles;
         const int k0 = (tile % tiles_k) * TK, j0 = (tile / tiles_k) * G::TJ;
         const int ib = chunk * ichunk, ie = min(nxc, ib + ichunk);
@@ -849,7 +861,7 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
             const int ip = ib - 1 + tt;
             const bool iv = ip >= 0 && ip < nxc;
             const float wxi = iv ? __ldg(F.wx + ip) : 0.f, sxi = iv ? __ldg(F.sx + ip) : 0.f;
-            if (!mbar_wait(bars + 8 * st, (unsigned)((g / kCgStages) & 1))) bad = 1;
+            const int timed_out = mbar_wait(bars + 8 * st, (unsigned)((g / kCgStages) & 1), wait_limit) ? 0 : 1;
             const float *hs_ = stg + (size_t)(st * NV) * SF;
             const float *ps = stg + (size_t)(st * NV + 1) * SF;
             float *pb = pnb + (size_t)(tt % 3) * SF;
@@ -887,7 +899,11 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
                     else form(row * G::BX + 4 * col, hwyz[m], hsyz[m]);
                 }
             }
-            __syncthreads();
+            // one barrier for the block, and the same verdict in every thread
+            if (__syncthreads_or(timed_out)) {
+                g_stop = g;
+                break;
+            }
             // the stage of plane tt is consumed: refill it with plane tt + kCgStages
             if (t == 0 && tt + kCgStages < np) issue(g + kCgStages, k0, j0, ib - 1 + tt + kCgStages);
             if (tt >= 2 && in) {
@@ -929,6 +945,17 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
         }
         g0 += np;
         __syncthreads();  // the next item rewrites the pn planes
+    }
+    if (g_stop >= 0) {
+        // a wait gave up: no copy was issued after it; wait out the ones in
+        // flight (planes g_stop .. issued_hi - 1, at most one per stage) so
+        // none lands in shared memory after the block has exited
+        if (t == 0) {
+            bad = 1;
+            for (long long g = g_stop; g < issued_hi; ++g)
+                mbar_wait(bars + 8 * (int)(g % kCgStages), (unsigned)((g / kCgStages) & 1), kCgDrainLimit);
+        }
+        __syncthreads();
     }
     if (t == 0 && bad) sc->wait_timeout = 1;
     // pn . q gives alpha; q . z (z as loaded) serves the flexible beta of
@@ -1108,10 +1135,10 @@ static void launch_tma_t(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t
     const size_t sm = CgTile<TK>::smem(first ? 1 : 2);
     if (form_z)
         launch_pdl(k_cg_pq_tma<first, TK, true>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, pn, q, sc, c.partials,
-                   c.counter, ichunk);
+                   c.counter, ichunk, t.wait_limit);
     else
         launch_pdl(k_cg_pq_tma<first, TK, false>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, pn, q, sc,
-                   c.partials, c.counter, ichunk);
+                   c.partials, c.counter, ichunk, t.wait_limit);
 }
 
 // z_map: the z vector (or p itself on the first iteration), p_map: p
@@ -1243,6 +1270,7 @@ bool cg_tma_setup(CgTma &t, const FvOp<float> &F, const float *z, const float *h
     t.ok = false;
     const SpeOp<float> &A = F.A;
     if (A.nzc % 4 != 0) return false;
+    if (A.pz) return false;  // the boxes' zero fill at the z ends is the Neumann halo, not a wrapped one
     if (const char *e = std::getenv("CFDGPU_NO_TMA"))
         if (e[0] == '1') return false;
     t.TK = A.nzc >= 24 ? 32 : (A.nzc >= 12 ? 16 : 8);

@@ -38,7 +38,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
                 omega: float | None = None, sor_maxit: int = 5000, aligned_source: bool = False,
                 compat_rhs: bool = True, check_every: int = 16, inner_tol: float = 1e-3,
                 max_outer: int = 30, inner_solver: int = capi.INNER_MG, les: bool = False,
-                conv_outflow_uc: float = 0.0) -> capi.CfdConfig:
+                conv_outflow_uc: float = 0.0, periodic_z: bool = False) -> capi.CfdConfig:
     cfg = capi.CfdConfig()
     check(lib().cfd_config_default(C.byref(cfg), w.nxc, w.nyc, w.nzc))
     cfg.lx, cfg.ly, cfg.lz = w.lx, w.ly, w.lz
@@ -60,6 +60,7 @@ def make_config(w: Workload, *, method: int = capi.METHOD_PC, solver: int = capi
     cfg.inner_solver = inner_solver
     cfg.les_smagorinsky = int(les)
     cfg.conv_outflow_uc = conv_outflow_uc
+    cfg.periodic_z = int(periodic_z)
     return cfg
 
 
@@ -210,6 +211,44 @@ class Simulation:
         a, b = C.c_double(), C.c_double()
         check(lib().cfd_div_projected(self._h, slot, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    STATE_FIELDS = ("U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "P", "X", "ETA")
+
+    def set_clock(self, loop: int, time: float):
+        """simuClass::loop / ::time (a restart from fields set by upload)."""
+        check(lib().cfd_set_clock(self._h, int(loop), float(time)))
+
+    def clock(self) -> tuple[int, float]:
+        loop, t = C.c_longlong(), C.c_double()
+        check(lib().cfd_get_clock(self._h, C.byref(loop), C.byref(t)))
+        return loop.value, t.value
+
+    def state(self) -> dict:
+        """The fields a restart needs (FP64 host arrays) and the clock."""
+        out = {k: self.download(k) for k in self.STATE_FIELDS}
+        out["clock"] = self.clock()
+        return out
+
+    def restore(self, st: dict):
+        """Continue from state() of any context of the same grid and either
+        precision (FP32 fields widen exactly; FP64 fields round to FP32)."""
+        for k in self.STATE_FIELDS:
+            self.upload(k, st[k])
+        self.set_clock(*st["clock"])
+
+    def sync_periodic_z(self, slot):
+        """Periodic z: ghost planes of velocity slot `slot` (or p for -1)."""
+        check(lib().cfd_sync_periodic_z(self._h, slot))
+
+    def divergence_check(self, on: bool = True):
+        """Measure the projected divergence inside every later step."""
+        check(lib().cfd_set_step_divergence_check(self._h, int(on)))
+
+    def step_divergence(self) -> dict:
+        """Last step's (max |div T2|, max |div T2 + dt m|, max |div u*|)."""
+        out = (C.c_double * 3)()
+        check(lib().cfd_step_divergence(self._h, out))
+        return {"div_T2_inf": out[0], "dev_inf": out[1], "div_ustar_inf": out[2]}
 
     def step(self, allow_noconv=False) -> dict:
         info = capi.CfdStepInfo()

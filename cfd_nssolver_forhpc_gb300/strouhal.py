@@ -64,6 +64,24 @@ def strouhal(t, cl, diameter: float = 1.0, velocity: float = 1.0, settle: float 
             "cl_amplitude": float(0.5 * (x.max() - x.min()))}
 
 
+def _run(S, steps: int, hist: dict) -> float:
+    """steps steps of S, recording time, Cd and Cl; returns wall seconds."""
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h = S.step()
+        hist["t"].append(h["time"])
+        hist["cd"].append(h["cd"])
+        hist["cl"].append(h["cl"])
+    return time.perf_counter() - t0
+
+
+def _summary(hist: dict, w, settle: float, wall: float) -> dict:
+    est = strouhal(hist["t"], hist["cl"], diameter=2.0 * w.radius, velocity=w.bc_dir[0][0], settle=settle)
+    cd = np.asarray(hist["cd"])
+    start = int(settle * cd.size)
+    return {"steps": len(hist["t"]), "wall_s": round(wall, 2), "cd_mean": float(cd[start:].mean()), **est}
+
+
 def main(argv=None):
     from . import capi
     from .configs import WORKLOADS
@@ -77,26 +95,43 @@ def main(argv=None):
     ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
     ap.add_argument("--tol", type=float, default=None)
     ap.add_argument("--settle", type=float, default=0.5, help="fraction of the run treated as transient")
+    ap.add_argument("--compare", type=float, default=0.0,
+                    help="after the run, continue it for this many time units in both precisions from "
+                         "the same state and compare the shedding of the two continuations")
+    ap.add_argument("--history", default=None, help="write the Cd/Cl histories to this .npz")
     a = ap.parse_args(argv)
     w = WORKLOADS[a.workload]
     solver = {"spe": capi.SOLVER_BICG_SPE, "ell": capi.SOLVER_BICG_ELL, "sor": capi.SOLVER_SOR_RB}[a.solver]
-    prec = capi.PREC_MIXED if a.precision == "mixed" else capi.PREC_FP64
-    steps = int(round(a.time / w.dt))
-    t, cl, cd = [], [], []
-    t0 = time.perf_counter()
-    with Simulation(w, solver=solver, precision=prec, tol=w.tol if a.tol is None else a.tol) as S:
+    prec = {"mixed": capi.PREC_MIXED, "fp64": capi.PREC_FP64}
+    tol = w.tol if a.tol is None else a.tol
+    out = {"workload": a.workload, "solver": a.solver, "tol": tol, "dt": w.dt}
+    hists = {}
+    with Simulation(w, solver=solver, precision=prec[a.precision], tol=tol) as S:
         S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
-        for _ in range(steps):
-            h = S.step()
-            t.append(h["time"])
-            cl.append(h["cl"])
-            cd.append(h["cd"])
-    wall = time.perf_counter() - t0
-    est = strouhal(t, cl, diameter=2.0 * w.radius, velocity=w.bc_dir[0][0], settle=a.settle)
-    half = len(cd) // 2
-    print(json.dumps({"workload": a.workload, "precision": a.precision, "solver": a.solver, "steps": steps,
-                      "time_units": a.time, "wall_s": round(wall, 2), "cd_mean": float(np.mean(cd[half:])),
-                      **est}))
+        h = {"t": [], "cd": [], "cl": []}
+        wall = _run(S, int(round(a.time / w.dt)), h)
+        hists["run"] = h
+        out["run"] = {"precision": a.precision, "time_units": a.time, **_summary(h, w, a.settle, wall)}
+        state = S.state() if a.compare > 0 else None
+    if state is not None:
+        # both continuations start from the same fields and clock
+        steps = int(round(a.compare / w.dt))
+        for name in ("mixed", "fp64"):
+            with Simulation(w, solver=solver, precision=prec[name], tol=tol,
+                            maxit=5000 if name == "mixed" else 50000) as S:
+                S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+                S.restore(state)
+                h = {"t": [], "cd": [], "cl": []}
+                wall = _run(S, steps, h)
+                hists[name] = h
+                out[name] = {"time_units": a.compare, **_summary(h, w, 0.0, wall)}
+        m, f = out["mixed"], out["fp64"]
+        if m.get("st") and f.get("st"):
+            out["st_rel_diff_mixed_vs_fp64"] = abs(m["st"] / f["st"] - 1.0)
+        out["cd_mean_rel_diff_mixed_vs_fp64"] = abs(m["cd_mean"] / f["cd_mean"] - 1.0)
+    if a.history:
+        np.savez_compressed(a.history, **{f"{k}_{q}": np.asarray(v[q]) for k, v in hists.items() for q in v})
+    print(json.dumps(out))
 
 
 if __name__ == "__main__":

@@ -59,9 +59,13 @@ typedef enum {
 
 typedef enum {
     CFD_PREC_FP64 = 0,  /* everything in FP64, as the reference */
-    CFD_PREC_MIXED = 1  /* FP32 fields, FP32 convection-diffusion and inner Krylov
+    CFD_PREC_MIXED = 1, /* FP32 fields, FP32 convection-diffusion and inner Krylov
                            iterations; FP64 defect correction of the Poisson
                            residual, FP64 dots and FP64 divergence check */
+    CFD_PREC_FP64_DC = 2 /* FP64 fields and flow kernels, as CFD_PREC_FP64, with the
+                           mixed path's Poisson solve (FP64 defect correction
+                           around the FP32 inner solver): an extension that
+                           separates what FP32 fields buy from what the solver buys */
 } cfd_precision;
 
 /* Inner solver of the mixed-precision defect correction (matrix-free SPE
@@ -129,6 +133,12 @@ typedef struct {
                                    (first-order upwind of u on the face and of v, w in the ghost
                                    cells, outflow flux scaled to the inflow flux at the end of
                                    every step); 0: the Dirichlet/Neumann table (the reference's) */
+    int periodic_z;             /* 1: periodic in z (an extension; the reference's table has
+                                   only Dirichlet/Neumann faces, Boundary_Condition.hpp:4-31):
+                                   the two ghost planes at each z end take the interior planes
+                                   one period away, the top w face is an unknown like the
+                                   others, and the Poisson operators wrap in z.  The Krylov
+                                   solvers only (not SOR); no adjoint. */
 } cfd_config;
 
 typedef struct {
@@ -168,14 +178,24 @@ size_t cfd_field_count(cfd_ctx *ctx, int field);
    Both forms give identical data. */
 int cfd_host_register(void *host, size_t bytes);
 int cfd_host_unregister(void *host);
-/* 1 when cfd_upload reads this buffer by the direct kernel path, else 0. */
+/* 1 when the GPU can address this byte of host memory, else 0. */
 int cfd_host_mapped(const void *host);
+/* 1 when cfd_upload reads a buffer of `bytes` bytes at `host` by the direct
+   kernel path (aligned, first and last byte mapped contiguously), else 0. */
+int cfd_host_mapped_range(const void *host, size_t bytes);
 /* velocity::iniU (physicalVariables.hpp:53) on T0, T1, T3 and p = 0
    (RUN_CPU_PC_METHOD.hpp:84-89) */
 int cfd_init_uniform(cfd_ctx *ctx, double ui, double vi, double wi);
 /* First boundary update: T1 = T3 = T0, BC_staggered_main(T0, p),
    BC_staggered_copy(T0 -> T1)  (RUN_CPU_PC_METHOD.hpp:114-119) */
 int cfd_start(cfd_ctx *ctx);
+
+/* simuClass::loop and simuClass::time (simuClass.hpp:92-94): the step
+   counter (the first step, loop 1, solves no Poisson equation) and the time.
+   Setting them restarts a run from fields uploaded from elsewhere (another
+   context, another precision, a Plot3D file). */
+int cfd_set_clock(cfd_ctx *ctx, long long loop, double time);
+int cfd_get_clock(cfd_ctx *ctx, long long *loop, double *time);
 
 /* ---- the hot-path operators --------------------------------------------- */
 /* ConvectionDifussion(simu, T[src], T[dst]) (convection_and_difussion.hpp:168) */
@@ -212,6 +232,11 @@ int cfd_bc_main(cfd_ctx *ctx, int slot);
 int cfd_bc_copy(cfd_ctx *ctx, int from_slot, int to_slot);
 /* velocity::copy_omp (physicalVariables.hpp:84-102) */
 int cfd_copy_velocity(cfd_ctx *ctx, int from_slot, int to_slot);
+/* Periodic z (cfg.periodic_z): copy the interior planes one period away into
+   the z ghost planes of velocity slot `slot`, or of the pressure when slot is
+   -1.  cfd_step does this after each convection-diffusion pass (T1) and
+   after each pressure transform (p); cfd_bc_main does it for its slot and p. */
+int cfd_sync_periodic_z(cfd_ctx *ctx, int slot);
 /* DFIB_CylinderZ (setEta.hpp:136-204) with explicit centre and radius: cut
    cells sub-sampled nsub x nsub as the reference does (nsub >= 1), or their
    exact area fraction (nsub == 0, an extension) */
@@ -230,12 +255,41 @@ int cfd_div_inf(cfd_ctx *ctx, int slot, double *out);
    divergence a converged pressure solve is responsible for.  FP64. */
 int cfd_div_projected(cfd_ctx *ctx, int slot, double *div_inf, double *dev_inf);
 
+/* Divergence check inside cfd_step (no counterpart in the reference).  With
+   on != 0, every later cfd_step that solves a Poisson equation measures, after
+   the last pass's solve and before the boundary update rewrites T1's faces,
+   what cfd_div_projected measures on T1: out3[0] = max |div T2|, out3[1] =
+   max |div T2 + dt m| (the part a converged solve answers for), and out3[2] =
+   max |div u*|, the divergence the projection had to remove.  One extra FP64
+   reduction per step.  cfd_step_divergence returns the last step's values
+   (-1 before the first such step). */
+int cfd_set_step_divergence_check(cfd_ctx *ctx, int on);
+int cfd_step_divergence(cfd_ctx *ctx, double *out3);
+
 /* ---- instrumentation ---------------------------------------------------- */
 /* Number of kernels the context has issued from the time-step and solver
    paths (cfd_step, cfd_bicgstab, cfd_sor and what they call), counting every
    kernel node of a replayed CUDA graph, including Krylov iterations queued
    past convergence that return at once. */
 int cfd_launch_count(cfd_ctx *ctx, long long *count);
+
+/* Test hooks (no counterpart in the reference).  Every device-side wait of
+   the solvers is bounded, so that a lost copy or a solve that never reports
+   completion ends with CFD_ERR_TIMEOUT instead of hanging the GPU; these
+   lower the bounds so tests can make them run out on purpose:
+     loop_trip_cap > 0   caps the body runs of every device-side solve loop
+                         (a CUDA-graph WHILE node); a solve still running at
+                         the cap returns CFD_ERR_TIMEOUT.  0 restores the
+                         default (enough runs for cfg.p_iter_max iterations).
+     tma_wait_limit >= 0 is the number of try-waits after which a wait of the
+                         TMA pipeline of the FP32 CG stencil gives up (0: at
+                         once).  The block then issues no more copies, waits
+                         out those in flight and skips the rest of its work;
+                         the solve returns CFD_ERR_TIMEOUT.  < 0 restores the
+                         default (2^24).
+   The state of the solve that timed out is undefined; the context stays
+   usable. */
+int cfd_set_test_limits(cfd_ctx *ctx, int loop_trip_cap, long long tma_wait_limit);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that record events
    or order their own work on it. */
@@ -283,13 +337,19 @@ int cfd_time_kernels(cfd_ctx *ctx, int reps, double *ms, int nms);
    entries) and f (3 x compact forcing, DfibArray::f layout); cd and cl are
    host outputs.  The work is ordered on `stream` (a cudaStream_t, NULL for
    the default stream), which is synchronised before returning.
-   Nothing is allocated: the scratch is one file-scope device array of about
-   1 MiB that every GPU that loads the library keeps until the process exits.
-   At most CFD_NOALLOC_MAX_CELLS interior cells; larger grids return
-   CFD_ERR_ARG.  The first call on a device looks up that array's device
-   address with the device current; make that first call before any stream
-   capture.  Every call uses the same scratch: calls that overlap on the GPU
-   (other streams, other host threads) race and must be serialised. */
+   Nothing is allocated by the call: the scratch is one file-scope device
+   array of about 1 MiB that every GPU that loads the library keeps until the
+   process exits.  With lazy module loading (the CUDA default) that array
+   comes into existence when the library's device code is first loaded on a
+   device, which the first call on that device may do; a caller whose pool
+   takes the GPU's memory should make one call (or create any context)
+   before handing the memory to its pool.  At most CFD_NOALLOC_MAX_CELLS
+   interior cells; larger grids return CFD_ERR_ARG.  Each call outside stream
+   capture looks up the array's device address with the device current (a
+   device reset moves it); a call during capture reuses the last address
+   found on that device, so make the first call before any capture.  Every
+   call uses the same scratch: calls that overlap on the GPU (other streams,
+   other host threads) race and must be serialised. */
 #define CFD_NOALLOC_MAX_CELLS 268435456
 int cfd_cdcl_noalloc(int nx_cal, int ny_cal, int nz_cal, double lz, const double *Dx,
                      const double *Dy, const double *Dz, const double *f, double *cd, double *cl,

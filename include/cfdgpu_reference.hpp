@@ -40,10 +40,13 @@ struct CUDAstruct {
     }
 
     // Create the context from the driver's grid and simulation settings and
-    // register which velocity object is T0, T1 and T3.
+    // register which velocity object is T0, T1 and T3.  compat_rhs = 1 adds
+    // the compatibility projection of the Poisson right-hand side (an
+    // extension; needed for tolerances below ~1e-6, see cfd_config).
     template <class Grid, class Simu, class Vel>
     void init(Grid &gA, Simu &simu, const Vel &T0, const Vel &T1, const Vel &T3, int solver,
-              const double dir[6][3], const double num[6][3], int method = CFD_METHOD_PC)
+              const double dir[6][3], const double num[6][3], int method = CFD_METHOD_PC,
+              int compat_rhs = 0)
     {
         cfd_config cfg;
         check(cfd_config_default(&cfg, gA.nxCal, gA.nyCal, gA.nzCal), "cfd_config_default");
@@ -56,6 +59,7 @@ struct CUDAstruct {
         cfg.p_sor_iter_max = (int)simu.p_sor_iter_max;
         cfg.solver = solver;
         cfg.method = method;
+        cfg.compat_rhs = compat_rhs;
         for (int b = 0; b < 6; ++b)
             for (int c = 0; c < 3; ++c) { cfg.bc_dir[b][c] = dir[b][c]; cfg.bc_num[b][c] = num[b][c]; }
         check(cfd_create(&cfg, &ctx), "cfd_create");

@@ -7,7 +7,11 @@ For each workload this script copies the reference's inc/ tree into
 oracle/_ref/<name>/inc (git-ignored), rewrites exactly those lines, and
 compiles oracle/ref_harness.cpp against the copy into
 oracle/_ref/<name>/libref.so with plain g++ (no build system, no -march:
--O2 -fopenmp -ffp-contract=off, so no multiply-add is fused).
+-O2 -fopenmp -ffp-contract=off, so no multiply-add is fused).  That build is
+the parity checker.  build(name, fast=True) compiles the same sources with the
+reference's own optimisation flags (-O3 -march=native, Makefile:18) into
+libref_fast.so: the timed CPU baseline, never a checker (its fused multiply-
+adds change the rounding).
 
 When the reference tree is absent (e.g. on a machine that only received the
 patched copy), an existing oracle/_ref/<name>/inc is compiled as is.
@@ -30,6 +34,8 @@ from cfd_nssolver_forhpc_gb300.configs import WORKLOADS, Workload  # noqa: E402
 
 REFERENCE = Path(os.environ.get("CFD_REFERENCE_ROOT", "/root/reference"))
 OUT = HERE / "_ref"
+# workloads whose reference run is also timed (bench.py's CPU baseline)
+TIMED_WORKLOADS = ("c2",)
 
 
 def _replace_once(path: Path, old: str, new: str) -> None:
@@ -75,12 +81,19 @@ def patch_tree(w: Workload, gridder: str = "uniform", out_name: str | None = Non
     return dst
 
 
-def build(name: str, gridder: str = "uniform", force: bool = False, les: bool = False) -> Path:
+# the reference's own optimisation flags (Makefile:18), tried in this order
+# where the host compiler does not take -march=native
+FAST_FLAGS = (["-O3", "-march=native"], ["-O3", "-mcpu=native"], ["-O3"])
+
+
+def build(name: str, gridder: str = "uniform", force: bool = False, les: bool = False,
+          fast: bool = False) -> Path:
     """les: the reference's Smagorinsky model compiled in
-    (TERBULENCE_SMAGORINSKY), output under oracle/_ref/<name>_les/."""
+    (TERBULENCE_SMAGORINSKY), output under oracle/_ref/<name>_les/.
+    fast: the timing build (libref_fast.so, the reference's -O3 -march=native)."""
     w = WORKLOADS[name]
     out_name = name + ("_les" if les else "")
-    lib = OUT / out_name / "libref.so"
+    lib = OUT / out_name / ("libref_fast.so" if fast else "libref.so")
     inc = OUT / out_name / "inc"
     if REFERENCE.exists() and (force or not inc.exists()):
         patch_tree(w, gridder, out_name)
@@ -89,15 +102,25 @@ def build(name: str, gridder: str = "uniform", force: bool = False, les: bool = 
     src = HERE / "ref_harness.cpp"
     if lib.exists() and lib.stat().st_mtime > max(src.stat().st_mtime, inc.stat().st_mtime) and not force:
         return lib
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-w",
-           "-I", str(inc), str(src), "-o", str(lib)]
+    base = ["g++", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-w", "-I", str(inc), str(src), "-o", str(lib)]
     if les:
-        cmd[1:1] = ["-DTERBULENCE_SMAGORINSKY"]
-    subprocess.run(cmd, check=True)
-    return lib
+        base[1:1] = ["-DTERBULENCE_SMAGORINSKY"]
+    if not fast:
+        subprocess.run(base[:1] + ["-O2", "-ffp-contract=off"] + base[1:], check=True)
+        return lib
+    err = None
+    for flags in FAST_FLAGS:
+        r = subprocess.run(base[:1] + flags + base[1:], capture_output=True, text=True)
+        if r.returncode == 0:
+            (OUT / out_name / "libref_fast.flags").write_text(" ".join(flags) + "\n")
+            return lib
+        err = r.stderr
+    raise RuntimeError(f"reference timing build failed: {err}")
 
 
 if __name__ == "__main__":
     names = sys.argv[1:] or ["g1"]
     for n in names:
         print(build(n, force=True))
+        if n in TIMED_WORKLOADS:
+            print(build(n, fast=True, force=True))

@@ -1299,6 +1299,8 @@ void og_sim_destroy(og_sim *s)
 
 double *og_sim_field(og_sim *s, int which) { return s->fld[which]; }
 long long og_sim_loop(const og_sim *s) { return s->loop; }
+/* restart from fields set through og_sim_field: simuClass::loop of the next step */
+void og_sim_set_loop(og_sim *s, long long loop) { s->loop = loop; }
 
 /* Initial state (RUN_CPU_PC_METHOD.hpp:77-119): T0=T1=T3=(ui,vi,wi), p=0,
  * then the first boundary update of T0 and the copy of its boundary into T1.

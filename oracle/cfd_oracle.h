@@ -182,6 +182,7 @@ void og_sim_start(og_sim *s);
    the last pass's Cd/Cl. */
 int og_sim_step(og_sim *s, int *iters4, double *err4, double *cd, double *cl);
 long long og_sim_loop(const og_sim *s);
+void og_sim_set_loop(og_sim *s, long long loop);
 
 #ifdef __cplusplus
 }

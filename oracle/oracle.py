@@ -129,6 +129,7 @@ class Oracle:
         L.og_sim_step.argtypes = [C.c_void_p, _ip, _dp, _dp, _dp]
         L.og_sim_loop.restype = C.c_longlong
         L.og_sim_loop.argtypes = [C.c_void_p]
+        L.og_sim_set_loop.argtypes = [C.c_void_p, C.c_longlong]
         L.og_bc_convective.argtypes = [C.c_void_p, d, d] + [_dp] * 6
         del v
 
@@ -330,6 +331,10 @@ class Oracle:
         def loop(self):
             return self.L.og_sim_loop(self.h)
 
+        @loop.setter
+        def loop(self, v):
+            self.L.og_sim_set_loop(self.h, C.c_longlong(int(v)))
+
         def __del__(self):
             try:
                 self.L.og_sim_destroy(self.h)
@@ -343,11 +348,20 @@ class Oracle:
 class RefHarness:
     """The reference's own functions (oracle/_ref/<name>/libref.so)."""
 
-    def __init__(self, name: str, build: bool = True):
+    def __init__(self, name: str, build: bool = True, fast: bool = False):
+        """fast: the timing build (the reference's -O3 -march=native), when
+        it exists; self.flags names the flags of the library loaded."""
         lib = HERE / "_ref" / name / "libref.so"
+        self.flags = "-O2 -ffp-contract=off"
         if build:
             from oracle.build_ref import build as _build  # noqa: WPS433
             lib = _build(name)
+        if fast:
+            fl = HERE / "_ref" / name / "libref_fast.so"
+            if fl.exists():
+                lib = fl
+                ff = HERE / "_ref" / name / "libref_fast.flags"
+                self.flags = ff.read_text().strip() if ff.exists() else "-O3"
         if not lib.exists():
             raise FileNotFoundError(lib)
         self.L = L = C.CDLL(str(lib))

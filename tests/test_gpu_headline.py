@@ -1,0 +1,78 @@
+"""The mixed-precision step against the FP64 step at equal accuracy (GPU).
+
+The mixed path keeps u, v, w and the advection-diffusion in FP32 and solves
+the Poisson equation by FP32 multigrid-preconditioned CG inside an FP64
+defect correction to the same relative residual as the FP64 path's
+BiCGSTAB.  Over 50 predictor-corrector steps of the 128x64x8 cylinder wake at
+tolerance 1e-10 the two runs must give the same drag to 1e-6 relative and the
+same lift to 1e-6 of the drag (the lift is near zero before shedding, so a
+relative lift error says nothing), every solve of both runs must reach the
+tolerance, and the per-field errors of u, v, w and p are bounded and printed.
+The projected field T2 = u* - dt grad p of the last pass must be free of the
+divergence a converged solve answers for, to the tolerance times the
+divergence the projection removed."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from cfd_nssolver_forhpc_gb300 import capi
+from cfd_nssolver_forhpc_gb300.configs import WORKLOADS
+from cfd_nssolver_forhpc_gb300.initial import initial_velocity
+from cfd_nssolver_forhpc_gb300.simulation import Simulation
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 50
+TOL = 1e-10
+CD_RTOL = 1e-6          # drag, mixed vs FP64
+CL_TOL_OF_CD = 1e-6     # lift difference relative to |drag|
+FIELD_MAX_RTOL = {"U0": 1e-5, "V0": 1e-4, "W0": 1e-3, "P": 1e-4}
+
+
+def _run(w, **kw):
+    S = Simulation(w, tol=TOL, **kw)
+    S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+    S.divergence_check(True)
+    hist = [S.step() for _ in range(STEPS)]
+    fields = {k: S.download(k) for k in ("U0", "V0", "W0", "P")}
+    d = S.step_divergence()
+    return S, hist, fields, d["dev_inf"], d["div_ustar_inf"]
+
+
+def test_mixed_matches_fp64_drag_lift_and_fields_over_50_steps():
+    w = WORKLOADS["c1"]
+    S64, h64, f64, dev64, du64 = _run(w, maxit=50000)
+    S32, h32, f32, dev32, du32 = _run(w, precision=capi.PREC_MIXED)
+    S64.close()
+    S32.close()
+    for h in h64[1:] + h32[1:]:
+        assert all(r < TOL for r in h["relres"]), h["relres"]
+    cd64 = np.array([h["cd"] for h in h64])
+    cd32 = np.array([h["cd"] for h in h32])
+    cl64 = np.array([h["cl"] for h in h64])
+    cl32 = np.array([h["cl"] for h in h32])
+    cd_err = np.abs(cd32 / cd64 - 1.0)
+    cl_err = np.abs(cl32 - cl64) / np.abs(cd64)
+    errs = {}
+    for k in ("P",):  # the pressure is defined up to a constant
+        f64[k] = f64[k] - f64[k].mean()
+        f32[k] = f32[k] - f32[k].mean()
+    for k in f64:
+        d = f32[k] - f64[k]
+        errs[k] = (float(np.abs(d).max() / np.abs(f64[k]).max()),
+                   float(np.linalg.norm(d) / np.linalg.norm(f64[k])))
+    print(f"\nc1 {STEPS} steps, tol {TOL:g}: max drag rel err {cd_err.max():.3e}, "
+          f"max lift err / |drag| {cl_err.max():.3e}")
+    for k, (mx, l2) in errs.items():
+        print(f"  {k}: max rel {mx:.3e}  L2 rel {l2:.3e}")
+    print(f"  projected divergence dev_inf: FP64 {dev64:.3e} (of max|div u*| {du64:.3e}), "
+          f"mixed {dev32:.3e} (of {du32:.3e})")
+    assert cd_err.max() < CD_RTOL
+    assert cl_err.max() < CL_TOL_OF_CD
+    for k, (mx, _) in errs.items():
+        assert mx < FIELD_MAX_RTOL[k], (k, mx)
+    # the divergence a converged solve answers for, relative to the
+    # divergence the projection removed, is at the solver tolerance
+    assert dev64 < 10 * TOL * du64
+    assert dev32 < 10 * TOL * du32

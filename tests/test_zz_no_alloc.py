@@ -8,7 +8,8 @@ Its only scratch is a file-scope device array shared by every call, so this
 test checks two calls in a row (the second must not see the first's partial
 sums) against the context-based cfd_cdcl, which allocates its scratch in
 cfd_create.  The input arrays here come from PyTorch's allocator: the caller
-owns its memory, the entry point adds none.
+owns its memory, the entry point adds none, which the free device memory
+before and after a call shows.
 
 This file is collected last so that a run stopping at the first failure has
 run every other test already; it does not depend on them.
@@ -36,29 +37,62 @@ def _uniform_widths(w):
     return [np.full(n + 4, L / (n + 4 - 4.0)) for n, L in ((w.nxc, w.lx), (w.nyc, w.ly), (w.nzc, w.lz))]
 
 
-@pytest.mark.parametrize("name", ["g1", "c1"])
-def test_noalloc_cdcl_matches_cfd_cdcl_twice(name):
+def _random_widths(w, seed):
+    """Positive, different widths on every axis (a swapped axis would show)."""
+    return [0.5 + seeded_field(n + 4, seed + a, 0.0, 1.0) for a, n in enumerate((w.nxc, w.nyc, w.nzc))]
+
+
+def _metrics(widths):
+    """cfd_set_metrics arrays for ghosted cell widths: nodes as cumulative
+    sums, staggered widths as the mean of neighbouring cells."""
+    out = {}
+    for name, d in zip("xyz", widths):
+        out[name.upper()] = np.concatenate([[0.0], np.cumsum(d)])
+        out["D" + name] = d
+        out["D" + name + "s"] = np.concatenate([0.5 * (d[:-1] + d[1:]), d[-1:]])
+    return out
+
+
+def _noalloc(w, widths_dev, f_dev, stream):
+    cd, cl = C.c_double(), C.c_double()
+    check(lib().cfd_cdcl_noalloc(w.nxc, w.nyc, w.nzc, w.lz, widths_dev[0].data_ptr(), widths_dev[1].data_ptr(),
+                                 widths_dev[2].data_ptr(), f_dev.data_ptr(), C.byref(cd), C.byref(cl),
+                                 C.c_void_p(stream.cuda_stream)))
+    return cd.value, cl.value
+
+
+@pytest.mark.parametrize("name,widths", [("g1", "uniform"), ("c1", "uniform"), ("g1", "random"),
+                                         ("c1", "random")])
+def test_noalloc_cdcl_matches_cfd_cdcl_twice(name, widths):
     import torch
 
     w = WORKLOADS[name]
     n = w.n_cells
     dev = torch.device("cuda", 0)
-    widths = [torch.from_numpy(a).to(dev) for a in _uniform_widths(w)]
+    host_widths = _uniform_widths(w) if widths == "uniform" else _random_widths(w, 700)
+    widths_dev = [torch.from_numpy(a).to(dev) for a in host_widths]
     stream = torch.cuda.current_stream(dev)
     with Simulation(w) as S:
-        S.grid_uniform()
+        if widths == "uniform":
+            S.grid_uniform()
+        else:
+            S.set_metrics(_metrics(host_widths))
+        fs = [seeded_field(3 * n, 500 + call, -10.0, 10.0) for call in range(2)]
+        f_devs = [torch.from_numpy(f).to(dev) for f in fs]
+        torch.cuda.synchronize()
         for call in range(2):
-            f = seeded_field(3 * n, 500 + call, -10.0, 10.0)
-            S.upload("F", f)
+            S.upload("F", fs[call])
             cd_ref, cl_ref = S.Delay_IO_CD_CL()
-            f_dev = torch.from_numpy(f).to(dev)
-            stream.synchronize()
-            cd, cl = C.c_double(), C.c_double()
-            check(lib().cfd_cdcl_noalloc(w.nxc, w.nyc, w.nzc, w.lz, widths[0].data_ptr(),
-                                         widths[1].data_ptr(), widths[2].data_ptr(), f_dev.data_ptr(),
-                                         C.byref(cd), C.byref(cl), C.c_void_p(stream.cuda_stream)))
-            assert cd.value == pytest.approx(cd_ref, rel=CDCL_RTOL, abs=1e-12), call
-            assert cl.value == pytest.approx(cl_ref, rel=CDCL_RTOL, abs=1e-12), call
+            free0 = torch.cuda.mem_get_info(dev)[0]
+            cd, cl = _noalloc(w, widths_dev, f_devs[call], stream)
+            free1 = torch.cuda.mem_get_info(dev)[0]
+            assert cd == pytest.approx(cd_ref, rel=CDCL_RTOL, abs=1e-12), call
+            assert cl == pytest.approx(cl_ref, rel=CDCL_RTOL, abs=1e-12), call
+            if call == 1:
+                # the first call may load the library's device code on this
+                # device (and with it the scratch array); later calls take
+                # no device memory at all
+                assert free1 == free0
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():
