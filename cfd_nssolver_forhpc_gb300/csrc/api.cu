@@ -415,38 +415,50 @@ int poisson_solve(cfd_ctx *c, int *iters, double *relres, int *outer)
     return solve64(c, spe64(c), iters, relres);
 }
 
+// SorPipeLine_seq (SorPipeLine.seq.hpp:48-117) in red-black order: the
+// right-hand side from velocity slot si, then sweeps until the max change
+// is at most the tolerance or p_sor_iter_max sweeps ran, all on the device
+// (graph 5: a WHILE node over check_every sweeps; host-polled batches when
+// device loops are off).  iters = sweeps - 1 and err = the last max change,
+// as the reference reports them.
 template <class T>
 int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
 {
     const Geo &g = c->g;
     const Metrics<double> m = metrics_of<double>(c);
-    launch_sor_rhs<T>(c->s, g, m, 1.0 / c->cfg.dt, dv<T>(c, si, 0), dv<T>(c, si, 1), dv<T>(c, si, 2),
-                      c->cf6);
-    c->launches += 1;
     const int itmax = c->cfg.p_sor_iter_max;
-    CK(cudaMemsetAsync(c->sor_res, 0, (size_t)(itmax + 1) * sizeof(unsigned long long), c->s));
-    CK(cudaMemsetAsync(c->sor_state, 0, 2 * sizeof(int), c->s));
     const int batch = c->cfg.check_every;
-    int sweep = 0;
-    for (;;) {
-        for (int q = 0; q < batch && sweep <= itmax; ++q, ++sweep) {
-            launch_sor_sweep(c->s, g, m, c->cf6, c->cf7, c->p, c->cfg.p_sor_omega, c->cfg.p_criteria,
-                             itmax, sweep, c->sor_res, c->sor_state);
-            c->launches += 2;
+    const int cap = trip_cap(c, (long long)itmax / batch + 3);
+    auto head = [&] {
+        launch_sor_rhs_rb<T>(c->s, g, m, 1.0 / c->cfg.dt, dv<T>(c, si, 0), dv<T>(c, si, 1), dv<T>(c, si, 2),
+                             c->sor_rhs, c->sc, c->sor_acc);
+    };
+    auto body = [&] {
+        for (int q = 0; q < batch; ++q)
+            launch_sor_rb_sweep(c->s, g, c->sor_cf, c->sor_rhs, c->p, c->cfg.p_sor_omega, c->cfg.p_criteria, itmax,
+                                c->sc, c->sor_acc);
+    };
+    const long long key = ((long long)cap << 20) | ((long long)batch << 4) | si;
+    if (c->use_graphs && c->device_loops) {
+        CKS(while_graph(c, 5, key, c->sc, cap, head, body));
+        CKS(run_while_graph(c, 5, c->sc, 1, 2LL * batch, "SOR"));
+    } else {
+        if (c->use_graphs) CKS(batch_graph(c, 5, -key, body));
+        head();
+        c->launches += 1;
+        for (long long nb = 0;; ++nb) {
+            if (nb >= cap) return fail(CFD_ERR_TIMEOUT, "SOR did not report completion");
+            if (c->use_graphs) CK(cudaGraphLaunch(c->graph[5], c->s));
+            else body();
+            c->launches += 2LL * batch;
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(c->h_sc, c->sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
+            CK(cudaStreamSynchronize(c->s));
+            if (c->h_sc->done != BICG_RUNNING) break;
         }
-        CK(cudaGetLastError());
-        CK(cudaMemcpyAsync(c->h_sor_state, c->sor_state, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->s));
-        CK(cudaStreamSynchronize(c->s));
-        if (c->h_sor_state[0] || sweep > itmax) break;
     }
-    const int run = c->h_sor_state[1];
-    unsigned long long last = 0;
-    if (run > 0)
-        CK(cudaMemcpy(&last, c->sor_res + (run - 1), sizeof(last), cudaMemcpyDeviceToHost));
-    double e;
-    std::memcpy(&e, &last, sizeof(e));
-    if (iters) *iters = run - 1;
-    if (err) *err = e;
+    if (iters) *iters = c->h_sc->iter - 1;
+    if (err) *err = c->h_sc->relres;
     return CFD_OK;
 }
 
@@ -699,21 +711,22 @@ int build_tables(cfd_ctx *c)
     if (c->cfg.solver == CFD_SOLVER_BICG_ELL)
         launch_ell_assemble(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7],
                             c->rawp[8], c->ell_cols, c->ell_vals, c->jp);
-    if (c->cfg.solver == CFD_SOLVER_SOR_RB)
-        launch_sor_setup(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7], c->rawp[8],
-                         c->cf7);
-    if (c->fp32) {
-        for (int a = 0; a < 3; ++a) {
-            const int na = a == 0 ? g.nxc : a == 1 ? g.nyc : g.nzc;
-            launch_convert<double, float>(c->lc, 2LL * na, c->spe_c[a], c->spe_c32[a]);
-            if (c->fv_sum[a]) launch_fv_axes(c->s, na, c->spe_c32[a], fv_width_src(c, a), c->fv_sum[a]);
-        }
-        launch_convert<double, float>(c->lc, g.n, c->jp, c->jp32);
-        if (c->jp32lo) launch_split_lo(c->lc, g.n, c->jp, c->jp32lo);
-        if (c->cg_ip) launch_cg_ip(c->lc, fv32(c), c->cg_ip);
-        if (c->cfg.solver == CFD_SOLVER_BICG_ELL)
-            launch_convert<double, float>(c->lc, 7 * g.n, c->ell_vals, c->ell_vals32);
+    if (c->sor_cf)
+        launch_sor_coef_rb(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7], c->rawp[8],
+                           c->sor_cf);
+    // FP32 copies of the operator, each only where the context holds one (a
+    // mixed-precision SOR context has none; FP64 contexts get them when a
+    // defect-correction solve first needs them)
+    for (int a = 0; a < 3; ++a) {
+        const int na = a == 0 ? g.nxc : a == 1 ? g.nyc : g.nzc;
+        if (!c->spe_c32[a]) continue;
+        launch_convert<double, float>(c->lc, 2LL * na, c->spe_c[a], c->spe_c32[a]);
+        if (c->fv_sum[a]) launch_fv_axes(c->s, na, c->spe_c32[a], fv_width_src(c, a), c->fv_sum[a]);
     }
+    if (c->jp32) launch_convert<double, float>(c->lc, g.n, c->jp, c->jp32);
+    if (c->jp32lo) launch_split_lo(c->lc, g.n, c->jp, c->jp32lo);
+    if (c->cg_ip) launch_cg_ip(c->lc, fv32(c), c->cg_ip);
+    if (c->ell_vals32) launch_convert<double, float>(c->lc, 7 * g.n, c->ell_vals, c->ell_vals32);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->s));
     c->metrics = true;
@@ -729,7 +742,6 @@ void free_ctx(cfd_ctx *c)
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_sc) cudaFreeHost(c->h_sc);
     if (c->h_scal) cudaFreeHost(c->h_scal);
-    if (c->h_sor_state) cudaFreeHost(c->h_sor_state);
     if (c->h_max) cudaFreeHost(c->h_max);
     adj_free(c->adj);
     if (c->s) cudaStreamDestroy(c->s);
@@ -808,6 +820,8 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (k.periodic_z != 0 && k.periodic_z != 1) return fail(CFD_ERR_ARG, "periodic_z must be 0 or 1");
     if (k.periodic_z && k.solver == CFD_SOLVER_SOR_RB)
         return fail(CFD_ERR_ARG, "periodic z needs a Krylov solver (SPE or ELL), not SOR");
+    if (k.solver == CFD_SOLVER_SOR_RB && k.nx_cal > 65535)
+        return fail(CFD_ERR_ARG, "the SOR sweeps take at most 65535 cells in x");
 
     cfd_ctx *c = new cfd_ctx();
     c->cfg = k;
@@ -888,10 +902,9 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
     }
     if (!bicg) {
-        AL(c->cf6, n * 8);
-        AL(c->cf7, n * 8);
-        AL(c->sor_res, (size_t)(k.p_sor_iter_max + 2) * sizeof(unsigned long long));
-        AL(c->sor_state, 4 * sizeof(int));
+        AL(c->sor_cf, (size_t)(14 * sor_slots(g)) * sizeof(double));
+        AL(c->sor_rhs, (size_t)(2 * sor_slots(g)) * sizeof(double));
+        AL(c->sor_acc, sizeof(SorAcc));
     }
     AL(c->sc, sizeof(BicgScal));
     AL(c->sc_in, sizeof(BicgScal));
@@ -908,7 +921,6 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
 #undef AL
     if (cudaMallocHost(reinterpret_cast<void **>(&c->h_sc), sizeof(BicgScal)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_scal), 8 * sizeof(double)) != cudaSuccess ||
-        cudaMallocHost(reinterpret_cast<void **>(&c->h_sor_state), 4 * sizeof(int)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_max), 3 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(CFD_ERR_NOMEM, "pinned host allocation failed"));
@@ -1532,7 +1544,7 @@ int cfd_set_test_limits(cfd_ctx *c, int loop_trip_cap, long long tma_wait_limit)
     c->test_trip_cap = loop_trip_cap > 0 ? loop_trip_cap : 0;
     c->cgtma.wait_limit = tma_wait_limit >= 0 ? tma_wait_limit : (1LL << 24);
     // the cached solve graphs hold the old cap and limit as launch arguments
-    for (int q = 0; q < 5; ++q) {
+    for (int q = 0; q < cfd_ctx::kGraphs; ++q) {
         if (c->graph[q]) cudaGraphExecDestroy(c->graph[q]);
         c->graph[q] = nullptr;
         c->graph_batch[q] = 0;
@@ -1645,6 +1657,17 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                 }
             }
         }
+    }
+    if (c->cfg.solver == CFD_SOLVER_SOR_RB) {
+        // sweeps of a copy of p (in T3, or in the FP64 staging buffer of a
+        // mixed context) with a tolerance that never stops them
+        double *ps = c->fp32 ? c->staging : dv<double>(c, 2, 0);
+        CK(cudaMemcpyAsync(ps, c->p, (size_t)g.ng * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+        if ((st = timed(CFD_KERNEL_SOR_SWEEP, [&] {
+                 launch_sor_rb_sweep(c->s, g, c->sor_cf, c->sor_rhs, ps, c->cfg.p_sor_omega, -1.0, 0x7fffffff,
+                                     c->sc_t, c->sor_acc);
+             })) != CFD_OK)
+            return st;
     }
     st = dispatch(c, [&](auto tag) -> int {
         using T = typename decltype(tag)::type;

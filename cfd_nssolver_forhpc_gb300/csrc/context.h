@@ -112,14 +112,14 @@ struct cfd_ctx {
     cfd::BicgScal sc_init{}, sc_in_init{};  // scalars of a fresh solver (cfd_start restores them)
     cfd::BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
     // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
-    // [4] multigrid-preconditioned CG
-    cudaGraphExec_t graph[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    long long graph_batch[5] = {0, 0, 0, 0, 0};  // shape key of each cached graph
+    // [4] multigrid-preconditioned CG, [5] red-black SOR
+    static constexpr int kGraphs = 6;
+    cudaGraphExec_t graph[kGraphs] = {};
+    long long graph_batch[kGraphs] = {};  // shape key of each cached graph
 
     // SOR
-    double *cf6 = nullptr, *cf7 = nullptr;
-    unsigned long long *sor_res = nullptr;
-    int *sor_state = nullptr, *h_sor_state = nullptr;
+    double *sor_cf = nullptr, *sor_rhs = nullptr;  // colour-split SOR coefficients and right-hand side
+    cfd::SorAcc *sor_acc = nullptr;
 
     // scalars: [0] rhs mean, [1..2] cd/cl, [3] residual norm^2, [4] dot
     double *dscal = nullptr, *h_scal = nullptr;

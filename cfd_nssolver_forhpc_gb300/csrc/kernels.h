@@ -250,16 +250,39 @@ template <class V>
 void launch_bicg_nan_reset(cfd_launch_ctx &c, long long n, V *x, const V *px1, const V *px2,
                            BicgScal *sc);
 
-// SorPipeLine (SorPipeLine.seq.hpp), red-black ordered
-void launch_sor_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
-                      const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
-                      double *cf7);
+// SorPipeLine (SorPipeLine.seq.hpp:30-117) in red-black order, colour-split.
+// Colour c holds the cells with i + j + k + c even; in the row (i, j) they
+// sit at k = GC + ((i + j + GC + c) & 1) + 2 m, m < sor_pairs(g) (the last
+// slot of a row is unused when its colour has one cell fewer).  Slot
+// h = ((i - GC) nyc + (j - GC)) sor_pairs + m of colour c holds
+//   cf[(c * 7 + q) * nh + h], q = 0..5: face area / staggered distance
+//     towards +x, -x, +y, -y, +z, -z; q = 6: -1 / (their sum);
+//   rhs[c * nh + h]: mass change / dt,
+// with nh = nxc nyc sor_pairs: every access of a sweep to them is coalesced.
+inline long long sor_pairs(const Geo &g) { return (g.nzc + 1) / 2; }
+inline long long sor_slots(const Geo &g) { return (long long)g.nxc * g.nyc * sor_pairs(g); }
+// running maxima of |change| of the two colours and the last-block ticket
+struct SorAcc {
+    unsigned long long mx[2];
+    unsigned int ticket, pad;
+};
+void launch_sor_coef_rb(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy, const double *Dz,
+                        const double *Dxs, const double *Dys, const double *Dzs, double *cf);
+// the right-hand side from (u1, v1, w1); its first thread also starts a solve:
+// sc->done = running, sc->iter = 0 sweeps, acc cleared
 template <class T>
-void launch_sor_rhs(cudaStream_t s, const Geo &g, const Metrics<double> &m, double rdt, const T *u1,
-                    const T *v1, const T *w1, double *cf6);
-void launch_sor_sweep(cudaStream_t s, const Geo &g, const Metrics<double> &m, const double *cf6,
-                      const double *cf7, double *p, double omega, double tol, int itmax, int sweep,
-                      unsigned long long *res, int *state);
+void launch_sor_rhs_rb(cudaStream_t s, const Geo &g, const Metrics<double> &m, double rdt, const T *u1,
+                       const T *v1, const T *w1, double *rhs, BicgScal *sc, SorAcc *acc);
+// one sweep (both colours) of p += omega (p_new - p); after the sweep the
+// do-while test of SorPipeLine.seq.hpp:112 (max |change| > tol and
+// sweeps < itmax) runs on the device: sc->iter = sweeps so far, and when the
+// test fails sc->relres = the last max change and sc->done is set.  Sweeps
+// issued after that return at once.
+void launch_sor_rb_sweep(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, double *p,
+                         double omega, double tol, int itmax, BicgScal *sc, SorAcc *acc);
+// one colour alone, for timing
+void launch_sor_rb_colour(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, double *p,
+                          double omega, double tol, int itmax, int colour, BicgScal *sc, SorAcc *acc);
 
 // mixed precision pieces
 template <class V>

@@ -85,8 +85,10 @@ using Ix = std::conditional_t<SM, int, long long>;
 // symmetric operator
 __device__ __forceinline__ float smooth_rcp(float d) { return __fdividef(1.0f, d); }
 
-// the neighbour sum of L at (i, j, k), cell t
-template <bool SM = false>
+// the neighbour sum of L at (i, j, k), cell t.  PZ: the level is periodic in
+// z (its end cells couple across the period).  A compile-time switch: the
+// wrap costs the non-periodic smoother registers and occupancy.
+template <bool SM = false, bool PZ = false>
 __device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict__ x, int i, int j, int k, Ix<SM> t)
 {
     const Ix<SM> sx = (Ix<SM>)L.ny * L.nz, sy = L.nz;
@@ -96,9 +98,9 @@ __device__ __forceinline__ float mg_nb(const MgLevel &L, const float *__restrict
     if (j > 0) s = fmaf(tl<SM>(L.cm[1] + j), x[t - sy], s);
     if (j < L.ny - 1) s = fmaf(tl<SM>(L.cp[1] + j), x[t + sy], s);
     if (k > 0) s = fmaf(tl<SM>(L.cm[2] + k), x[t - 1], s);
-    else if (L.pz) s = fmaf(tl<SM>(L.cm[2] + k), x[t + (L.nz - 1)], s);
+    else if (PZ) s = fmaf(tl<SM>(L.cm[2] + k), x[t + (L.nz - 1)], s);
     if (k < L.nz - 1) s = fmaf(tl<SM>(L.cp[2] + k), x[t + 1], s);
-    else if (L.pz) s = fmaf(tl<SM>(L.cp[2] + k), x[t - (L.nz - 1)], s);
+    else if (PZ) s = fmaf(tl<SM>(L.cp[2] + k), x[t - (L.nz - 1)], s);
     return s;
 }
 
@@ -117,18 +119,18 @@ __device__ __forceinline__ float mg_rdv(const MgLevel &L, int i, int j, int k)
 // Gauss-Seidel update of one cell: x = (b / dV + neighbours) / diag; the
 // small-level kernel reads 1 / dV and 1 / diag from its per-cell tables
 // (the same values, computed once by k_mg_cell_tables)
-template <bool SM = false>
+template <bool SM = false, bool PZ = false>
 __device__ __forceinline__ void gs_cell(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x, int i,
                                         int j, int k, Ix<SM> t, bool zero_init)
 {
-    const float nb = zero_init ? 0.f : mg_nb<SM>(L, x, i, j, k, t);
+    const float nb = zero_init ? 0.f : mg_nb<SM, PZ>(L, x, i, j, k, t);
     if constexpr (SM) x[t] = fmaf(b[t], L.rv[t], nb) * L.rg[t];
     else x[t] = fmaf(b[t], mg_rdv<SM>(L, i, j, k), nb) * smooth_rcp(mg_diag<SM>(L, i, j, k));
 }
 
 // one colour over a level with nz % 4 == 0: one thread per quad of cells
 // k = 4m..4m+3 (float4 rows), updating the two cells of that colour
-template <bool SM = false, class I = Ix<SM>>
+template <bool SM = false, class I = Ix<SM>, bool PZ = false>
 __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
                                              int color, bool zero_init, I t0, I stride)
 {
@@ -174,8 +176,8 @@ __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__re
             if ((int)i < L.nx - 1) xp = *reinterpret_cast<const float4 *>(x + t + sx);
             if (j > 0) ym = *reinterpret_cast<const float4 *>(x + t - sy);
             if ((int)j < L.ny - 1) yp = *reinterpret_cast<const float4 *>(x + t + sy);
-            const float zlo = k0 > 0 ? x[t - 1] : (L.pz ? x[t + (L.nz - 1)] : 0.f);
-            const float zhi = k0 + 4 < L.nz ? x[t + 4] : (L.pz ? x[t + 4 - L.nz] : 0.f);
+            const float zlo = k0 > 0 ? x[t - 1] : (PZ ? x[t + (L.nz - 1)] : 0.f);
+            const float zhi = k0 + 4 < L.nz ? x[t + 4] : (PZ ? x[t + 4 - L.nz] : 0.f);
             const float cxm = tl<SM>(L.cm[0] + i), cxp = tl<SM>(L.cp[0] + i);
             const float cym = tl<SM>(L.cm[1] + j), cyp = tl<SM>(L.cp[1] + j);
             const float4 czm = tl4<SM>(L.cm[2] + k0);
@@ -373,7 +375,7 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong_first4(MgLevel L, MgLevel
 // one colour over the level: pairs (k = 2m, 2m + 1) when nz is even (one
 // thread per pair updates the cell of that colour), single cells otherwise;
 // zero_init starts from x = 0 (the other colour written as 0)
-template <bool SM = false>
+template <bool SM = false, bool PZ = false>
 __device__ __forceinline__ void smooth_level(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
                                              int color, bool zero_init, Ix<SM> t0, Ix<SM> stride)
 {
@@ -386,7 +388,7 @@ __device__ __forceinline__ void smooth_level(const MgLevel &L, const float *__re
             const int m = (int)(r - j * (unsigned)nh);
             const int k = 2 * m + (int)((color + i + j) & 1u);
             const Ix<SM> t = ((Ix<SM>)i * L.ny + j) * L.nz + k;
-            gs_cell<SM>(L, b, x, (int)i, (int)j, k, t, zero_init);
+            gs_cell<SM, PZ>(L, b, x, (int)i, (int)j, k, t, zero_init);
             if (zero_init) x[t + ((k & 1) ? -1 : 1)] = 0.f;
         }
         return;
@@ -398,7 +400,7 @@ __device__ __forceinline__ void smooth_level(const MgLevel &L, const float *__re
             if (zero_init) x[t] = 0.f;
             continue;
         }
-        gs_cell<SM>(L, b, x, i, j, k, t, zero_init);
+        gs_cell<SM, PZ>(L, b, x, i, j, k, t, zero_init);
     }
 }
 
@@ -407,7 +409,7 @@ __device__ __forceinline__ void smooth_level(const MgLevel &L, const float *__re
 // the residual of every colour-1 cell is zero (its Gauss-Seidel equation
 // holds exactly for the colour-0 values around it, none of which changed
 // since), so only the colour-0 children are summed.
-template <bool SM = false>
+template <bool SM = false, bool PZ = false>
 __device__ __forceinline__ void restrict_level(const MgLevel &F, const MgLevel &C, const float *__restrict__ bf,
                                                const float *__restrict__ xf, float *__restrict__ bc, Ix<SM> t0,
                                                Ix<SM> stride)
@@ -424,7 +426,7 @@ __device__ __forceinline__ void restrict_level(const MgLevel &F, const MgLevel &
                     if ((i + j + k) & 1) continue;
                     const Ix<SM> t = ((Ix<SM>)i * F.ny + j) * F.nz + k;
                     const float dv = tl<SM>(F.w[0] + i) * tl<SM>(F.w[1] + j) * tl<SM>(F.w[2] + k);
-                    s += bf[t] - dv * (mg_diag<SM>(F, i, j, k) * xf[t] - mg_nb<SM>(F, xf, i, j, k, t));
+                    s += bf[t] - dv * (mg_diag<SM>(F, i, j, k) * xf[t] - mg_nb<SM, PZ>(F, xf, i, j, k, t));
                 }
         bc[T] = s;
     }
@@ -459,36 +461,38 @@ __global__ void k_mg_cell_tables(MgLevel L, float *__restrict__ rv, float *__res
     }
 }
 
+template <bool PZ>
 __global__ void __launch_bounds__(kBlock) k_mg_smooth(MgLevel L, const float *b, float *x, int color, int zero_init,
                                                       const int *done)
 {
     pdl_wait();
     pdl_allow();
     if (*done) return;
-    smooth_level(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+    smooth_level<false, PZ>(L, b, x, color, zero_init != 0, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                  (long long)gridDim.x * blockDim.x);
 }
 
 // the float4 form (nz % 4 == 0) as its own kernel; I = int where every
 // index of the level fits (fewer instructions per quad)
-template <class I>
+template <class I, bool PZ>
 __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, const float *b, float *x, int color,
                                                           int zero_init, const int *done)
 {
     pdl_wait();
     pdl_allow();
     if (*done) return;
-    smooth_quads<false, I>(L, b, x, color, zero_init != 0, (I)blockIdx.x * blockDim.x + threadIdx.x,
+    smooth_quads<false, I, PZ>(L, b, x, color, zero_init != 0, (I)blockIdx.x * blockDim.x + threadIdx.x,
                            (I)gridDim.x * blockDim.x);
 }
 
+template <bool PZ>
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, const float *bf, const float *xf,
                                                         float *bc, const int *done)
 {
     pdl_wait();
     pdl_allow();
     if (*done) return;
-    restrict_level(F, C, bf, xf, bc, (long long)blockIdx.x * blockDim.x + threadIdx.x,
+    restrict_level<false, PZ>(F, C, bf, xf, bc, (long long)blockIdx.x * blockDim.x + threadIdx.x,
                    (long long)gridDim.x * blockDim.x);
 }
 
@@ -724,6 +728,7 @@ __device__ __forceinline__ MgLevel small_view(const MgSmall &S, float *sm, int l
 // b; pre-smooth and restrict down, solve the coarsest, prolong and
 // post-smooth up; store the first small level's x.  Block barriers separate
 // the phases.
+template <bool PZ>
 __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
 {
     pdl_wait();
@@ -751,15 +756,15 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
     for (int l = first; l < last - 1; ++l) {
         const MgLevel L = small_view(S, sm, l);
         for (int s = 0; s < S.pre; ++s) {
-            if (L.quads) smooth_quads<true>(L, L.b, L.x, 0, s == 0, t0, st);
-            else smooth_level<true>(L, L.b, L.x, 0, s == 0, t0, st);
+            if (L.quads) smooth_quads<true, int, PZ>(L, L.b, L.x, 0, s == 0, t0, st);
+            else smooth_level<true, PZ>(L, L.b, L.x, 0, s == 0, t0, st);
             __syncthreads();
-            if (L.quads) smooth_quads<true>(L, L.b, L.x, 1, false, t0, st);
-            else smooth_level<true>(L, L.b, L.x, 1, false, t0, st);
+            if (L.quads) smooth_quads<true, int, PZ>(L, L.b, L.x, 1, false, t0, st);
+            else smooth_level<true, PZ>(L, L.b, L.x, 1, false, t0, st);
             __syncthreads();
         }
         const MgLevel C = small_view(S, sm, l + 1);
-        restrict_level<true>(L, C, L.b, L.x, C.b, t0, st);
+        restrict_level<true, PZ>(L, C, L.b, L.x, C.b, t0, st);
         __syncthreads();
     }
     {
@@ -796,11 +801,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
         prolong_level<true>(L, S.lev[l + 1], small_view(S, sm, l + 1).x, L.x, t0, st);
         __syncthreads();
         for (int s = 0; s < S.post; ++s) {
-            if (L.quads) smooth_quads<true>(L, L.b, L.x, 1, false, t0, st);
-            else smooth_level<true>(L, L.b, L.x, 1, false, t0, st);
+            if (L.quads) smooth_quads<true, int, PZ>(L, L.b, L.x, 1, false, t0, st);
+            else smooth_level<true, PZ>(L, L.b, L.x, 1, false, t0, st);
             __syncthreads();
-            if (L.quads) smooth_quads<true>(L, L.b, L.x, 0, false, t0, st);
-            else smooth_level<true>(L, L.b, L.x, 0, false, t0, st);
+            if (L.quads) smooth_quads<true, int, PZ>(L, L.b, L.x, 0, false, t0, st);
+            else smooth_level<true, PZ>(L, L.b, L.x, 0, false, t0, st);
             __syncthreads();
         }
     }
@@ -1220,7 +1225,8 @@ int mg_setup(cfd_ctx *c)
     G.cinv_smem = small_layout(G, G.first_small, true, nullptr) <= kMgSmallSmem;
     G.small_smem = (int)small_layout(G, G.first_small, G.cinv_smem, nullptr);
     if (G.small_smem > kMgSmallSmem) return fail(CFD_ERR_STATE, "multigrid: coarsest level too large for shared memory");
-    CK(cudaFuncSetAttribute(k_mg_small, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
+    CK(cudaFuncSetAttribute(k_mg_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
+    CK(cudaFuncSetAttribute(k_mg_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
     CKS(small_image(c, G));
     // fused sweeps on the grid-wide levels with float4 rows: about 128
     // threads a block (TJ rows x nz/4 quads), chunks of CI planes sized for
@@ -1322,17 +1328,38 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
 }
 
 // one colour of the smoother over a grid-wide level
-static void smooth_launch(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
+template <bool PZ>
+static void smooth_launch_t(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
 {
     if (L.quads && L.n + (long long)L.ny * L.nz < (1LL << 31))
-        launch_pdl(k_mg_smooth4<int>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
+        launch_pdl(k_mg_smooth4<int, PZ>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
                    zero_init, done);
     else if (L.quads)
-        launch_pdl(k_mg_smooth4<long long>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x,
+        launch_pdl(k_mg_smooth4<long long, PZ>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x,
                    color, zero_init, done);
     else
-        launch_pdl(k_mg_smooth, dim3(nblk((L.nz % 2 == 0) ? L.n / 2 : L.n)), dim3(kBlock), 0, s, L,
+        launch_pdl(k_mg_smooth<PZ>, dim3(nblk((L.nz % 2 == 0) ? L.n / 2 : L.n)), dim3(kBlock), 0, s, L,
                    (const float *)L.b, L.x, color, zero_init, done);
+}
+
+static void smooth_launch(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
+{
+    if (L.pz) smooth_launch_t<true>(L, color, zero_init, done, s);
+    else smooth_launch_t<false>(L, color, zero_init, done, s);
+}
+
+static void restrict_launch(const MgLevel &F, const MgLevel &C, const int *done, cudaStream_t s, bool pdl = true)
+{
+    auto k = F.pz ? k_mg_restrict<true> : k_mg_restrict<false>;
+    if (pdl) launch_pdl(k, dim3(nblk(C.n)), dim3(kBlock), 0, s, F, C, (const float *)F.b, (const float *)F.x, C.b, done);
+    else k<<<nblk(C.n), kBlock, 0, s>>>(F, C, F.b, F.x, C.b, done);
+}
+
+static void small_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl = true)
+{
+    auto k = G.lev[0].pz ? k_mg_small<true> : k_mg_small<false>;
+    if (pdl) launch_pdl(k, dim3(1), dim3(kSmallThreads), G.small_smem, s, small_desc(G, done));
+    else k<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
 }
 
 // z = V(h): one V-cycle; every kernel returns at once when *done
@@ -1344,10 +1371,9 @@ void mg_vcycle(cfd_ctx *c, const int *done)
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
         smooth_phase(G, l, true, done, s);
-        launch_pdl(k_mg_restrict, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1], (const float *)L.b,
-                   (const float *)L.x, G.lev[l + 1].b, done);
+        restrict_launch(L, G.lev[l + 1], done, s);
     }
-    launch_pdl(k_mg_small, dim3(1), dim3(kSmallThreads), G.small_smem, s, small_desc(G, done));
+    small_launch(G, done, s);
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
         if (fused_ends(G, L)) {
@@ -1376,9 +1402,9 @@ void mg_time_part(cfd_ctx *c, int part)
     const MgLevel &L = G.lev[0];
     const int *done = G.never;
     if (part == 0) smooth_launch(L, 0, 0, done, s);
-    else if (part == 1) k_mg_restrict<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], L.b, L.x, G.lev[1].b, done);
+    else if (part == 1) restrict_launch(L, G.lev[1], done, s, false);
     else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
-    else if (part == 3) k_mg_small<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
+    else if (part == 3) small_launch(G, done, s, false);
     else if (part == 5) {
         if (L.sweep_tj > 0) sweep_launch(L, L.x, L.xalt, 0, 0, done, s);
     }

@@ -1445,126 +1445,181 @@ template void launch_bicg_nan_reset<double>(cfd_launch_ctx &, long long, double 
                                             const double *, BicgScal *);
 
 // ---------------------------------------------------------------------------
-// SOR (SorPipeLine.seq.hpp:30-117) in red-black order.
-// cf7 = -1/coef with the reference's operation order (bitwise equal).
-__global__ void k_sor_setup(Geo g, const double *__restrict__ Dx, const double *__restrict__ Dy,
-                            const double *__restrict__ Dz, const double *__restrict__ Dxs,
-                            const double *__restrict__ Dys, const double *__restrict__ Dzs,
-                            double *__restrict__ cf7)
+// SOR (SorPipeLine.seq.hpp:30-117) in red-black order with colour-split
+// coefficients (the layout is described with launch_sor_coef_rb in
+// kernels.h).  Every value is formed with the reference's operations in its
+// order, each rounded on its own (no contraction into FMAs), so the sweeps
+// are bit-for-bit those of a sequential red-black loop: the cells of one
+// colour do not read each other.
+
+// slot -> cell of colour c; false for the unused last slot of a short row
+__device__ __forceinline__ bool sor_cell_of(const Geo &g, FastDiv fpairs, int colour, int i0, unsigned t, int &i,
+                                            int &j, int &k)
 {
-    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < g.n;
-         row += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(row / g.sxc) + GC;
-        const long long rem = row - (long long)(i - GC) * g.sxc;
-        const int j = (int)(rem / g.nzc) + GC, k = (int)(rem % g.nzc) + GC;
-        const double yz = __dmul_rn(Dy[j], Dz[k]), xz = __dmul_rn(Dx[i], Dz[k]), xy = __dmul_rn(Dx[i], Dy[j]);
-        double c = __ddiv_rn(yz, Dxs[i]);
-        c = __dadd_rn(c, __ddiv_rn(yz, Dxs[i - 1]));
-        c = __dadd_rn(c, __ddiv_rn(xz, Dys[j]));
-        c = __dadd_rn(c, __ddiv_rn(xz, Dys[j - 1]));
-        c = __dadd_rn(c, __ddiv_rn(xy, Dzs[k]));
-        c = __dadd_rn(c, __ddiv_rn(xy, Dzs[k - 1]));
-        cf7[row] = __ddiv_rn(-1.0, c);
+    const unsigned jj = fpairs.div(t);
+    const int m = (int)(t - jj * fpairs.d);
+    i = i0 + GC;
+    j = (int)jj + GC;
+    k = GC + ((i + j + GC + colour) & 1) + 2 * m;
+    return k < g.nz - GC;
+}
+
+__global__ void k_sor_coef_rb(Geo g, FastDiv fpairs, const double *__restrict__ Dx, const double *__restrict__ Dy,
+                              const double *__restrict__ Dz, const double *__restrict__ Dxs,
+                              const double *__restrict__ Dys, const double *__restrict__ Dzs, double *__restrict__ cf)
+{
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int colour = blockIdx.z;
+    if (t >= (unsigned)g.nyc * fpairs.d) return;
+    const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
+    const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
+    double *o = cf + (long long)colour * 7 * nh + h;
+    int i, j, k;
+    if (!sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) {
+        // unused slot: a zero row that changes nothing
+        for (int q = 0; q < 7; ++q) o[q * nh] = 0.0;
+        return;
     }
+    // grid::coef products and SorPipeLine.seq.hpp:30-43 quotients, in order
+    const double yz = __dmul_rn(Dy[j], Dz[k]), xz = __dmul_rn(Dx[i], Dz[k]), xy = __dmul_rn(Dx[i], Dy[j]);
+    const double c0 = __ddiv_rn(yz, Dxs[i]), c1 = __ddiv_rn(yz, Dxs[i - 1]);
+    const double c2 = __ddiv_rn(xz, Dys[j]), c3 = __ddiv_rn(xz, Dys[j - 1]);
+    const double c4 = __ddiv_rn(xy, Dzs[k]), c5 = __ddiv_rn(xy, Dzs[k - 1]);
+    double sum = __dadd_rn(c0, c1);
+    sum = __dadd_rn(sum, c2);
+    sum = __dadd_rn(sum, c3);
+    sum = __dadd_rn(sum, c4);
+    sum = __dadd_rn(sum, c5);
+    o[0] = c0;
+    o[nh] = c1;
+    o[2 * nh] = c2;
+    o[3 * nh] = c3;
+    o[4 * nh] = c4;
+    o[5 * nh] = c5;
+    o[6 * nh] = __ddiv_rn(-1.0, sum);
 }
 
-void launch_sor_setup(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy,
-                      const double *Dz, const double *Dxs, const double *Dys, const double *Dzs,
-                      double *cf7)
+void launch_sor_coef_rb(cudaStream_t s, const Geo &g, const double *Dx, const double *Dy, const double *Dz,
+                        const double *Dxs, const double *Dys, const double *Dzs, double *cf)
 {
-    k_sor_setup<<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, Dx, Dy, Dz, Dxs, Dys, Dzs, cf7);
+    const FastDiv fp((unsigned)sor_pairs(g));
+    const dim3 grid((unsigned)((g.nyc * sor_pairs(g) + kBlock - 1) / kBlock), (unsigned)g.nxc, 2);
+    k_sor_coef_rb<<<grid, kBlock, 0, s>>>(g, fp, Dx, Dy, Dz, Dxs, Dys, Dzs, cf);
 }
 
-// cf6 = mass change / dt (SorPipeLine.seq.hpp:48-60)
+// mass change / dt (SorPipeLine.seq.hpp:48-60), the reference's operation order
 template <class T>
-__global__ void k_sor_rhs(Geo g, Metrics<double> m, double rdt, const T *__restrict__ u1,
-                          const T *__restrict__ v1, const T *__restrict__ w1, double *__restrict__ cf6)
+__global__ void k_sor_rhs_rb(Geo g, FastDiv fpairs, Metrics<double> m, double rdt, const T *__restrict__ u1,
+                             const T *__restrict__ v1, const T *__restrict__ w1, double *__restrict__ rhs,
+                             BicgScal *sc, SorAcc *acc)
 {
-    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < g.n;
-         row += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(row / g.sxc) + GC;
-        const long long rem = row - (long long)(i - GC) * g.sxc;
-        const int j = (int)(rem / g.nzc) + GC, k = (int)(rem % g.nzc) + GC;
-        const long long ic = icel(g, i, j, k);
-        const double Dx = m.x(AX_D, i), Dy = m.y(AX_D, j), Dz = m.z(AX_D, k);
-        const double mc = ((double)u1[ic] - (double)u1[ic - g.sx]) * Dy * Dz
-                        + ((double)v1[ic] - (double)v1[ic - g.sy]) * Dx * Dz
-                        + ((double)w1[ic] - (double)w1[ic - 1]) * Dx * Dy;
-        cf6[row] = mc * rdt;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int colour = blockIdx.z;
+    if (t == 0 && blockIdx.y == 0 && colour == 0) {
+        sc->done = BICG_RUNNING;
+        sc->iter = 0;
+        sc->relres = 0.0;
+        acc->mx[0] = acc->mx[1] = 0ull;
+        acc->ticket = 0u;
     }
+    if (t >= (unsigned)g.nyc * fpairs.d) return;
+    const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
+    const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
+    int i, j, k;
+    if (!sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) {
+        rhs[colour * nh + h] = 0.0;
+        return;
+    }
+    const long long ic = icel(g, i, j, k);
+    const double Dx = m.x(AX_D, i), Dy = m.y(AX_D, j), Dz = m.z(AX_D, k);
+    const double du = __dsub_rn((double)u1[ic], (double)u1[ic - g.sx]);
+    const double dv = __dsub_rn((double)v1[ic], (double)v1[ic - g.sy]);
+    const double dw = __dsub_rn((double)w1[ic], (double)w1[ic - 1]);
+    double mc = __dmul_rn(__dmul_rn(du, Dy), Dz);
+    mc = __dadd_rn(mc, __dmul_rn(__dmul_rn(dv, Dx), Dz));
+    mc = __dadd_rn(mc, __dmul_rn(__dmul_rn(dw, Dx), Dy));
+    rhs[colour * nh + h] = __dmul_rn(mc, rdt);
 }
 
 template <class T>
-void launch_sor_rhs(cudaStream_t s, const Geo &g, const Metrics<double> &m, double rdt, const T *u1,
-                    const T *v1, const T *w1, double *cf6)
+void launch_sor_rhs_rb(cudaStream_t s, const Geo &g, const Metrics<double> &m, double rdt, const T *u1,
+                       const T *v1, const T *w1, double *rhs, BicgScal *sc, SorAcc *acc)
 {
-    k_sor_rhs<T><<<blocks_for(g.n, 65536), kBlock, 0, s>>>(g, m, rdt, u1, v1, w1, cf6);
+    const FastDiv fp((unsigned)sor_pairs(g));
+    const dim3 grid((unsigned)((g.nyc * sor_pairs(g) + kBlock - 1) / kBlock), (unsigned)g.nxc, 2);
+    k_sor_rhs_rb<T><<<grid, kBlock, 0, s>>>(g, fp, m, rdt, u1, v1, w1, rhs, sc, acc);
 }
-template void launch_sor_rhs<double>(cudaStream_t, const Geo &, const Metrics<double> &, double,
-                                     const double *, const double *, const double *, double *);
-template void launch_sor_rhs<float>(cudaStream_t, const Geo &, const Metrics<double> &, double,
-                                    const float *, const float *, const float *, double *);
+template void launch_sor_rhs_rb<double>(cudaStream_t, const Geo &, const Metrics<double> &, double, const double *,
+                                        const double *, const double *, double *, BicgScal *, SorAcc *);
+template void launch_sor_rhs_rb<float>(cudaStream_t, const Geo &, const Metrics<double> &, double, const float *,
+                                       const float *, const float *, double *, BicgScal *, SorAcc *);
 
-// One colour of one sweep.  state[0] = done flag, state[1] = sweeps run.
-// The do-while test of the reference (residual > tol && iters < itmax,
-// SorPipeLine.seq.hpp:112) is evaluated at the start of the next sweep's
-// first colour from the previous sweep's max change, so sweeps queued past
-// convergence do nothing.
+// One colour of a sweep.  The second colour's last block (by ticket) closes
+// the sweep: the do-while test of SorPipeLine.seq.hpp:112 on the larger of
+// the two colours' maxima.
 __global__ void __launch_bounds__(kBlock)
-k_sor_sweep(Geo g, Metrics<double> m, const double *__restrict__ cf6, const double *__restrict__ cf7,
-            double *__restrict__ p, double omega, double tol, int itmax, int sweep, int color,
-            unsigned long long *__restrict__ res, int *state)
+k_sor_rb(Geo g, FastDiv fpairs, const double *__restrict__ cf, const double *__restrict__ rhs, double *p,
+         double omega, double tol, int itmax, int colour, BicgScal *sc, SorAcc *acc)
 {
-    if (state[0]) return;
-    if (color == 0 && sweep > 0) {
-        const double prev = __longlong_as_double((long long)res[sweep - 1]);
-        if (!(prev > tol && sweep < itmax)) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                state[0] = 1;
-                state[1] = sweep;
-            }
-            return;
-        }
-    }
-    const int nzh = (g.nzc + 1) >> 1;
-    const long long total = (long long)g.nxc * g.nyc * nzh;
+    if (*(volatile int *)&sc->done != BICG_RUNNING) return;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
     double mx = 0.0;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long ij = t / nzh;
-        const int kk = (int)(t - ij * nzh);
-        const int i = (int)(ij / g.nyc) + GC, j = (int)(ij % g.nyc) + GC;
-        const int k = GC + ((i + j + GC + color) & 1) + 2 * kk;
-        if (k >= g.nz - GC) continue;
+    int i, j, k;
+    if (t < (unsigned)g.nyc * fpairs.d && sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) {
+        const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
+        const double *c = cf + (long long)colour * 7 * nh + h;
         const long long ic = icel(g, i, j, k);
-        const long long row = icelcal(g, i, j, k);
-        const double yz = m.y(AX_D, j) * m.z(AX_D, k), xz = m.x(AX_D, i) * m.z(AX_D, k),
-                     xy = m.x(AX_D, i) * m.y(AX_D, j);
-        double s = -p[ic + g.sx] * (yz * m.x(AX_RDS, i));
-        s = fma(-p[ic - g.sx], yz * m.x(AX_RDS, i - 1), s);
-        s = fma(-p[ic + g.sy], xz * m.y(AX_RDS, j), s);
-        s = fma(-p[ic - g.sy], xz * m.y(AX_RDS, j - 1), s);
-        s = fma(-p[ic + 1], xy * m.z(AX_RDS, k), s);
-        s = fma(-p[ic - 1], xy * m.z(AX_RDS, k - 1), s);
-        const double pnew = (s + cf6[row]) * cf7[row];
+        // (-p[+x] c0 - p[-x] c1 - p[+y] c2 - p[-y] c3 - p[+z] c4 - p[-z] c5 + rhs) c6
+        double s = __dmul_rn(-p[ic + g.sx], __ldg(c));
+        s = __dsub_rn(s, __dmul_rn(p[ic - g.sx], __ldg(c + nh)));
+        s = __dsub_rn(s, __dmul_rn(p[ic + g.sy], __ldg(c + 2 * nh)));
+        s = __dsub_rn(s, __dmul_rn(p[ic - g.sy], __ldg(c + 3 * nh)));
+        s = __dsub_rn(s, __dmul_rn(p[ic + 1], __ldg(c + 4 * nh)));
+        s = __dsub_rn(s, __dmul_rn(p[ic - 1], __ldg(c + 5 * nh)));
+        s = __dadd_rn(s, __ldg(rhs + colour * nh + h));
+        const double pnew = __dmul_rn(s, __ldg(c + 6 * nh));
         const double pc = p[ic];
-        const double d = pnew - pc;
-        p[ic] = fma(omega, d, pc);
-        const double a = fabs(d);
-        mx = (a > mx || a != a) ? a : mx;
+        const double d = __dsub_rn(pnew, pc);
+        p[ic] = __dadd_rn(pc, __dmul_rn(omega, d));
+        mx = fabs(d);  // a NaN wins the maximum and ends the solve
     }
-    grid_max_nonneg(mx, res + sweep);
-    if (color == 1 && blockIdx.x == 0 && threadIdx.x == 0) state[1] = sweep + 1;
+    grid_max_nonneg(mx, &acc->mx[colour]);
+    if (colour == 0) return;
+    __shared__ bool last;
+    __threadfence();
+    if (threadIdx.x == 0) {
+        const unsigned nb = gridDim.x * gridDim.y;
+        last = atomicAdd(&acc->ticket, 1u) == nb - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    const unsigned long long b0 = atomicAdd(&acc->mx[0], 0ull), b1 = atomicAdd(&acc->mx[1], 0ull);
+    const double res = __longlong_as_double((long long)(b0 > b1 ? b0 : b1));
+    const int it = sc->iter + 1;
+    sc->iter = it;
+    if (!(res > tol && it < itmax)) {
+        sc->relres = res;
+        sc->done = res > tol ? BICG_CAPPED : BICG_CONVERGED;
+    }
+    acc->mx[0] = acc->mx[1] = 0ull;
+    acc->ticket = 0u;
 }
 
-void launch_sor_sweep(cudaStream_t s, const Geo &g, const Metrics<double> &m, const double *cf6,
-                      const double *cf7, double *p, double omega, double tol, int itmax, int sweep,
-                      unsigned long long *res, int *state)
+void launch_sor_rb_colour(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, double *p,
+                          double omega, double tol, int itmax, int colour, BicgScal *sc, SorAcc *acc)
 {
-    const long long total = (long long)g.nxc * g.nyc * ((g.nzc + 1) / 2);
-    const int G = blocks_for(total, 4096);
-    k_sor_sweep<<<G, kBlock, 0, s>>>(g, m, cf6, cf7, p, omega, tol, itmax, sweep, 0, res, state);
-    k_sor_sweep<<<G, kBlock, 0, s>>>(g, m, cf6, cf7, p, omega, tol, itmax, sweep, 1, res, state);
+    const FastDiv fp((unsigned)sor_pairs(g));
+    const dim3 grid((unsigned)((g.nyc * sor_pairs(g) + kBlock - 1) / kBlock), (unsigned)g.nxc);
+    k_sor_rb<<<grid, kBlock, 0, s>>>(g, fp, cf, rhs, p, omega, tol, itmax, colour, sc, acc);
+}
+
+void launch_sor_rb_sweep(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, double *p,
+                         double omega, double tol, int itmax, BicgScal *sc, SorAcc *acc)
+{
+    launch_sor_rb_colour(s, g, cf, rhs, p, omega, tol, itmax, 0, sc, acc);
+    launch_sor_rb_colour(s, g, cf, rhs, p, omega, tol, itmax, 1, sc, acc);
 }
 
 // ---------------------------------------------------------------------------

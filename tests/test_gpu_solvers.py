@@ -137,9 +137,23 @@ def test_mixed_precision_defect_correction(oracle, solver, inner):
     assert it > 0
 
 
-@pytest.mark.parametrize("name", ["g1", "c1"])
-def test_sor_redblack_matches_oracle(oracle, name):
-    w = WORKLOADS[name]
+def _sor_workload(name):
+    if name == "g2_odd":  # nz odd: one colour has one cell fewer in every row
+        return WORKLOADS["g2"].with_(nzc=7, lz=0.875)
+    return WORKLOADS[name]
+
+
+@pytest.mark.parametrize("name,loop", [("g1", "device"), ("c1", "device"), ("c1", "host"), ("g2_odd", "device"),
+                                       ("g2_odd", "host")])
+def test_sor_redblack_matches_oracle_bitwise(monkeypatch, oracle, name, loop):
+    """The sweeps form every value with the reference's operations in its
+    order, one rounding each, and the cells of one colour do not read each
+    other, so p, the sweep count and the last max change are those of the
+    oracle's sequential red-black loop, bit for bit (device WHILE loop or
+    host-polled batches; an odd nz leaves the last slot of every other row
+    unused)."""
+    monkeypatch.setenv("CFDGPU_SOLVE_LOOP", loop)
+    w = _sor_workload(name)
     g = Grid.of(w, oracle)
     I = kernel_inputs(g.ng, g.n)
     u1, v1, w1 = (0.01 * I[k] for k in ("u1", "v1", "w1"))
@@ -156,12 +170,33 @@ def test_sor_redblack_matches_oracle(oracle, name):
             S.upload(k, a)
         it, err = S.SorPipeLine(S.T1)
         p = S.download("P")
-    assert abs(it - it_ref) <= 1
-    assert rel_err(g.interior(p), g.interior(p_ref)) < 1e-10
-    # ghost pressures are not touched by the sweeps (SorPipeLine.seq.hpp:74-104)
-    ghost = np.ones(g.ng, dtype=bool)
-    g.interior(ghost.view())[...] = False
-    np.testing.assert_array_equal(p[ghost], p0[ghost])
+        # a second solve from the converged p stops after one sweep
+        it2, err2 = S.SorPipeLine(S.T1)
+    assert it == it_ref and err == err_ref
+    np.testing.assert_array_equal(p, p_ref)  # ghost pressures untouched (SorPipeLine.seq.hpp:74-104)
+    assert it2 == 0 and err2 <= 1e-9
+
+
+def test_sor_sweep_cap(oracle):
+    """p_sor_iter_max sweeps, then the solve stops above tolerance and
+    reports iters = cap - 1 with the last max change, as the reference."""
+    w = WORKLOADS["g1"]
+    g = Grid.of(w, oracle)
+    I = kernel_inputs(g.ng, g.n)
+    u1, v1, w1 = (0.01 * I[k] for k in ("u1", "v1", "w1"))
+    cf = oracle.sor_coef(g)
+    oracle.sor_rhs(g, w.dt, u1, v1, w1, cf)
+    p_ref = I["sor_p"].copy()
+    it_ref, err_ref = oracle.sor(g, 1.7, 1e-14, 37, cf, p_ref, redblack=True)
+    with Simulation(w, solver=capi.SOLVER_SOR_RB, tol=1e-14, omega=1.7, sor_maxit=37, check_every=5) as S:
+        S.grid_uniform()
+        S.upload("P", I["sor_p"])
+        for k, a in (("U1", u1), ("V1", v1), ("W1", w1)):
+            S.upload(k, a)
+        it, err = S.SorPipeLine(S.T1)
+        p = S.download("P")
+    assert it == it_ref == 36 and err == err_ref and err > 1e-14
+    np.testing.assert_array_equal(p, p_ref)
 
 
 @pytest.mark.parametrize("dims", [(64, 48, 32), (24, 40, 64), (32, 20, 8), (16, 24, 12)])

@@ -114,6 +114,21 @@ def test_sor_steps_match_oracle(oracle):
     S.close()
 
 
+def test_mixed_sor_steps_close_to_fp64_sor():
+    """FP32 fields with the FP64 red-black SOR on p (a mixed context holds no
+    FP32 Krylov tables: the metric set-up must convert only what exists)."""
+    w = WORKLOADS["c1"]
+    S64, h64 = gpu_run(w, 4, solver=capi.SOLVER_SOR_RB, tol=1e-9, omega=w.omega)
+    S32, h32 = gpu_run(w, 4, solver=capi.SOLVER_SOR_RB, tol=1e-9, omega=w.omega, precision=capi.PREC_MIXED)
+    try:
+        np.testing.assert_allclose([h["cd"] for h in h32], [h["cd"] for h in h64], rtol=1e-5)
+        assert rel_err(S32.download("U0"), S64.download("U0")) < 1e-5
+        assert all(h["iters"][0] > 0 for h in h32[1:])
+    finally:
+        S64.close()
+        S32.close()
+
+
 def test_steps_are_bitwise_reproducible():
     w = WORKLOADS["g1"]
     a, ha = gpu_run(w, 4, tol=1e-10)
