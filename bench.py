@@ -69,6 +69,19 @@ KERNEL_BYTES_PER_CELL_FLOW = {
     "update_uf": 13,  # read u*, v*, w*, p, eta; write u, v, w, f (3)
     "rhs": 6,        # read u*, v*, w*, jp; write b (+ mean pass reads jp, b, writes b)
 }
+# the fused predictor-corrector pass kernels: (field words, extra FP64 bytes)
+# per cell; a word is the field type (FP32 in the mixed path)
+KERNEL_BYTES_PASS = {
+    "pass": (9, 16),         # read C (3), src (3); write T1 (3); read jp, write b (FP64 or a float pair)
+    "update_pass": (13, 8),  # read T1 (3), eta; write T3 (3); src += dt f (read, write 3 each); read p
+}
+# one red-black SOR sweep (both colours) per cell: seven FP64 coefficients
+# and the right-hand side read, p read and written once
+SOR_BYTES_PER_CELL = 80
+# FP64 operations per cell of a sweep: six products and six sums of the
+# neighbour term, the right-hand side, the scale, the change, its product
+# with omega and the update
+SOR_FP64_OPS_PER_CELL = 16
 
 
 def parse():
@@ -319,9 +332,20 @@ def roofline(S, w, infos, precision, ms_step):
     else:
         counts = {k: iters for k in KERNEL_BYTES_PER_ROW}
         per_row = {k: v * 8 for k, v in KERNEL_BYTES_PER_ROW.items()}
-    counts.update({"convdiff": npass, "update_uf": npass, "rhs": npass})
     word = 4 if precision == "mixed" else 8
     per_row.update({k: v * word for k, v in KERNEL_BYTES_PER_CELL_FLOW.items()})
+    if "pass" in ms:
+        # fused predictor-corrector step: one convection-diffusion, then per
+        # pass the pass kernel and the fused projection
+        counts.update({"convdiff": 1, "pass": npass, "update_pass": npass})
+        per_row.update({k: a * word + b for k, (a, b) in KERNEL_BYTES_PASS.items()})
+    else:
+        counts.update({"convdiff": npass, "update_uf": npass, "rhs": npass})
+    if "sor_sweep" in ms:
+        counts = {k: v for k, v in counts.items() if k in ("convdiff", "pass", "update_pass", "update_uf")}
+        # sweeps per step: iterations + 1 per solve (the timed steps all solve)
+        counts["sor_sweep"] = sum(sum(n + 1 for n in i["iters"]) for i in infos) / len(infos)
+        per_row["sor_sweep"] = SOR_BYTES_PER_CELL
     shares = {k: ms[k] * counts[k] for k in ms if k in counts}
     total = ms_step if ms_step > 0 else (sum(shares.values()) or 1.0)
     top = max((k for k in shares if k in per_row), key=shares.get)
@@ -345,7 +369,14 @@ def roofline(S, w, infos, precision, ms_step):
         out["note"] = ("launch time from back-to-back launches on the finest level, whose x and b "
                        "(8 B/cell) stay in L2 between passes as they do inside the V-cycle; an ncu "
                        "capture with caches flushed gives the cold figure")
-    if precision != "mixed":
+    if top == "sor_sweep":
+        # the sweeps are bound by the FP64 pipe (one rounding per operation)
+        rate = SOR_FP64_OPS_PER_CELL * w.n_cells / (ms[top] * 1e-3) / 1e12
+        out["bound"] = "fp64"
+        out["fp64_pipe"] = {"achieved_tops": round(rate, 4), "peak_tops": FP64_PEAK_TOPS,
+                            "frac": round(rate / FP64_PEAK_TOPS, 3),
+                            "peak_source": "register-resident DFMA loop on GB300 (0.599 T FMA/s)"}
+    if precision != "mixed" and top != "sor_sweep":
         # the FP64 Krylov kernels are bound by the FP64 pipe: FP64 operations
         # per row (SpMV 7, each dot 1, updates as written) / measured DFMA rate
         fp64_ops = {"bicg_ap": 8, "bicg_s": 1, "bicg_as": 9, "bicg_xr": 6, "bicg_p": 2}
@@ -451,7 +482,12 @@ def adjoint_leg(args, dist):
            "objective": f"mean Cd over steps {first}..{n} (bounded sample of the {wa.steps}-step run)",
            "parameters": f"inflow profile ({wa.nyc}) + eta ({wa.n_ghosted})",
            "checkpoint_interval": interval}
-    for prec_name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+    out["legs"] = {"fp64": "FP64 fields, FP64 BiCGSTAB forward; the adjoint solves run the FP64 defect "
+                           "correction around the FP32 multigrid-CG (not the same solver family)",
+                   "fp64_dc": "FP64 fields, the FP64 defect correction around the FP32 multigrid-CG in "
+                              "both directions (like for like)",
+                   "mixed": "FP32 fields, the same defect-correction solver in both directions"}
+    for prec_name, prec in (("fp64", capi.PREC_FP64), ("fp64_dc", capi.PREC_FP64_DC), ("mixed", capi.PREC_MIXED)):
         m = MeanDrag(wa, first, n, interval, precision=prec, tol=wa.tol)
         try:
             eta = m.default_eta().numpy()

@@ -274,6 +274,11 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
 {
     const int v = (int)mg_vcycle_launches(c->mg);
     float *z = c->w32.r0, *q = c->w32.ap;
+    // V-cycle, then rho' = h . z (fused into the V-cycle's last launch where it can be)
+    const int fr = mg_fuses_rho(c->mg) ? 1 : 0;
+    auto vcycle_rho = [&] {
+        if (!mg_vcycle(c, &sc->done, sc)) mg_rho(c, h, z, nullptr, sc);
+    };
     return run_pairs(
         c, 4, sc,
         [&] {
@@ -282,17 +287,15 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
             mg_rho(c, h, z, c->w32.p1, sc);
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
             mg_upd(c, e, c->w32.p1, h, q, sc);
-            mg_vcycle(c, &sc->done);
-            mg_rho(c, h, z, nullptr, sc);
+            vcycle_rho();
         },
         [&](int from) {
             float *P[2] = {c->w32.p1, c->p_alt};
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, from, false);
             mg_upd(c, e, P[1 - from], h, q, sc);
-            mg_vcycle(c, &sc->done);
-            mg_rho(c, h, z, nullptr, sc);
+            vcycle_rho();
         },
-        2 * v + 5, v + 3, c->mg.pairs);
+        2 * v + 5 - fr, v + 3 - fr, c->mg.pairs);
 }
 
 // The graphs bake in the buffers and operator of the context; they are
@@ -365,6 +368,11 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
         if (rel < c->cfg.p_criteria || !std::isfinite(rel)) break;
         if (sweeps >= c->cfg.max_outer) { st = fail(CFD_ERR_NOCONV, "defect correction reached its sweep cap"); break; }
         CK(cudaMemsetAsync(c->e32, 0, (size_t)n * sizeof(float), c->s));
+        if (c->inner_adapt > 0.0) {
+            const double want = std::min(0.5, c->inner_adapt * c->cfg.p_criteria / rel);
+            launch_set_tol(c->s, c->sc_in, std::max(c->cfg.inner_tol, want));
+            c->launches += 1;
+        }
         if constexpr (std::is_same<Op32, SpeOp<float>>::value) {
             SpeOp<float> Afly = A32;
             Afly.jp = nullptr;
@@ -421,36 +429,55 @@ int poisson_solve(cfd_ctx *c, int *iters, double *relres, int *outer)
 // (graph 5: a WHILE node over check_every sweeps; host-polled batches when
 // device loops are off).  iters = sweeps - 1 and err = the last max change,
 // as the reference reports them.
+//
+// Mixed-precision contexts sweep in FP32 inside an FP64 defect correction:
+// each loop body is one FP64 sweep (whose max change is the reference's stop
+// test, unchanged), the FP64 change of a Jacobi step at every cell, 4 x
+// check_every FP32 sweeps on the correction, and p += correction.  The FP32
+// sweeps count towards p_sor_iter_max, which is tested at the FP64 sweeps
+// (a capped solve can run up to one body's FP32 sweeps past it).
 template <class T>
 int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
 {
     const Geo &g = c->g;
     const Metrics<double> m = metrics_of<double>(c);
     const int itmax = c->cfg.p_sor_iter_max;
-    const int batch = c->cfg.check_every;
-    const int cap = trip_cap(c, (long long)itmax / batch + 3);
-    auto head = [&] {
+    const bool mixed = c->sor_e != nullptr;
+    const int batch = c->cfg.check_every, inner = 4 * batch;
+    const int cap = trip_cap(c, mixed ? (long long)itmax / (inner + 1) + 3 : (long long)itmax / batch + 3);
+    const double omega = c->cfg.p_sor_omega, tol = c->cfg.p_criteria;
+    auto head = [&]() -> int {
+        if (mixed) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.ng * sizeof(float), c->s));
         launch_sor_rhs_rb<T>(c->s, g, m, 1.0 / c->cfg.dt, dv<T>(c, si, 0), dv<T>(c, si, 1), dv<T>(c, si, 2),
                              c->sor_rhs, c->sc, c->sor_acc);
+        return CFD_OK;
     };
     auto body = [&] {
+        if (mixed) {
+            launch_sor_rb_sweep(c->s, g, c->sor_cf, c->sor_rhs, c->p, omega, tol, itmax, c->sc, c->sor_acc);
+            launch_sor_delta(c->s, g, c->sor_cf, c->sor_rhs, c->p, c->sor_d, c->sc);
+            const Metrics<float> m32 = metrics_of<float>(c);
+            for (int q = 0; q < inner; ++q) launch_sor32_sweep(c->s, g, m32, c->sor_d, c->sor_e, (float)omega, c->sc);
+            launch_sor_correct(c->s, g, c->p, c->sor_e, inner, c->sc);
+            return;
+        }
         for (int q = 0; q < batch; ++q)
-            launch_sor_rb_sweep(c->s, g, c->sor_cf, c->sor_rhs, c->p, c->cfg.p_sor_omega, c->cfg.p_criteria, itmax,
-                                c->sc, c->sor_acc);
+            launch_sor_rb_sweep(c->s, g, c->sor_cf, c->sor_rhs, c->p, omega, tol, itmax, c->sc, c->sor_acc);
     };
-    const long long key = ((long long)cap << 20) | ((long long)batch << 4) | si;
+    const long long body_launches = mixed ? 4LL + 2LL * inner : 2LL * batch;
+    const long long key = ((long long)cap << 20) | ((long long)batch << 4) | (mixed ? 8 : 0) | si;
     if (c->use_graphs && c->device_loops) {
         CKS(while_graph(c, 5, key, c->sc, cap, head, body));
-        CKS(run_while_graph(c, 5, c->sc, 1, 2LL * batch, "SOR"));
+        CKS(run_while_graph(c, 5, c->sc, mixed ? 2 : 1, body_launches, "SOR"));
     } else {
         if (c->use_graphs) CKS(batch_graph(c, 5, -key, body));
-        head();
+        CKS(head());
         c->launches += 1;
         for (long long nb = 0;; ++nb) {
             if (nb >= cap) return fail(CFD_ERR_TIMEOUT, "SOR did not report completion");
             if (c->use_graphs) CK(cudaGraphLaunch(c->graph[5], c->s));
             else body();
-            c->launches += 2LL * batch;
+            c->launches += body_launches;
             CK(cudaGetLastError());
             CK(cudaMemcpyAsync(c->h_sc, c->sc, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
             CK(cudaStreamSynchronize(c->s));
@@ -535,6 +562,7 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
             A.partials = rhs_done && c->cfg.compat_rhs ? c->lc.partials : nullptr;
             A.counter = c->lc.counter;
             A.mean = c->dscal + 0;
+            A.vol = c->vol_total;
             const bool ghosts = !aligned && pass > 0;
             launch_pass<T>(c->lc, g, metrics_of<double>(c), metrics_of<float>(c), A, ghosts);
             c->launches += 1 + (ghosts ? 1 : 0) + (A.partials ? 1 : 0);
@@ -700,11 +728,17 @@ int build_tables(cfd_ctx *c)
         std::vector<float> t32(t.begin(), t.end());
         CK(cudaMemcpyAsync(c->tab32[a], t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, c->s));
         CK(cudaStreamSynchronize(c->s));
-        (void)n;
     }
     for (int q = 0; q < 9; ++q)
         CK(cudaMemcpyAsync(c->rawp[q], c->hraw[q].data(), c->hraw[q].size() * sizeof(double),
                            cudaMemcpyHostToDevice, c->s));
+    {
+        // the interior volume: the product of the interior lengths
+        double len[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < 3; ++a)
+            for (int i = GC; i < n[a] - GC; ++i) len[a] += c->hraw[3 + a][i];
+        c->vol_total = len[0] * len[1] * len[2];
+    }
     // operators
     launch_spe_setup(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7], c->rawp[8],
                      c->spe_c[0], c->spe_c[1], c->spe_c[2], c->jp);
@@ -842,6 +876,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (const char *e = std::getenv("CFDGPU_SOLVE_LOOP")) c->device_loops = std::strcmp(e, "host") != 0;
     if (const char *e = std::getenv("CFDGPU_DEBUG")) c->debug = std::atoi(e);
     if (const char *e = std::getenv("CFDGPU_NO_FUSED")) c->fused = !(e[0] == '1');
+    if (const char *e = std::getenv("CFDGPU_INNER_ADAPT")) c->inner_adapt = std::max(0.0, std::atof(e));
 
     int st = CFD_OK;
     auto bail = [&](int code) { free_ctx(c); return code; };
@@ -905,6 +940,12 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         AL(c->sor_cf, (size_t)(14 * sor_slots(g)) * sizeof(double));
         AL(c->sor_rhs, (size_t)(2 * sor_slots(g)) * sizeof(double));
         AL(c->sor_acc, sizeof(SorAcc));
+        bool sweeps32 = c->fp32;
+        if (const char *e = std::getenv("CFDGPU_SOR_FP32")) sweeps32 = sweeps32 && e[0] != '0';
+        if (sweeps32) {
+            AL(c->sor_e, (size_t)g.ng * sizeof(float));
+            AL(c->sor_d, (size_t)(2 * sor_slots(g)) * sizeof(float));
+        }
     }
     AL(c->sc, sizeof(BicgScal));
     AL(c->sc_in, sizeof(BicgScal));
@@ -1668,6 +1709,12 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                                      c->sc_t, c->sor_acc);
              })) != CFD_OK)
             return st;
+        if (c->sor_e && (st = timed(CFD_KERNEL_SOR32_SWEEP, [&] {
+                             launch_sor32_sweep(c->s, g, metrics_of<float>(c), c->sor_d, c->sor_e,
+                                                (float)c->cfg.p_sor_omega, c->sc_t);
+                         })) != CFD_OK)
+            return st;
+        if (c->sor_e) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.ng * sizeof(float), c->s));
     }
     st = dispatch(c, [&](auto tag) -> int {
         using T = typename decltype(tag)::type;
@@ -1686,6 +1733,40 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                                      dv<T>(c, 2, 1), dv<T>(c, 2, 2), static_cast<T *>(c->f));
              })) != CFD_OK)
             return s2;
+        if (c->cfg.method == CFD_METHOD_PC) {
+            // a middle pass of the fused step (source in the reference's
+            // index convention, right-hand side with the compatibility sums),
+            // T1 and T3 both scratch: the pass writes T3 from the stored
+            // convection-diffusion, the update reads T3 and writes T1
+            PassArgs<T> A{};
+            for (int q = 0; q < 3; ++q) {
+                A.C[q] = static_cast<const T *>(c->cdbuf[q]);
+                A.T1[q] = dv<T>(c, 2, q);
+            }
+            A.src = static_cast<const T *>(c->src);
+            A.src_mode = c->cfg.aligned_source ? 2 : 1;
+            A.jp = c->jp;
+            A.jph = c->jp32;
+            A.jpl = c->jp32lo;
+            A.ddt = 1.0 / c->cfg.dt;
+            const bool krylov = c->cfg.solver != CFD_SOLVER_SOR_RB;
+            A.b = krylov ? c->b : nullptr;
+            A.partials = krylov && c->cfg.compat_rhs ? c->lc.partials : nullptr;
+            A.counter = c->lc.counter;
+            A.mean = c->dscal + 7;
+            A.vol = c->vol_total;
+            if ((s2 = timed(CFD_KERNEL_PASS, [&] {
+                     launch_pass<T>(c->lc, g, metrics_of<double>(c), metrics_of<float>(c), A, false);
+                 })) != CFD_OK)
+                return s2;
+            if ((s2 = timed(CFD_KERNEL_UPDATE_PASS, [&] {
+                     launch_update_pass<T>(c->lc, g, m, metrics_of<double>(c), c->cfg.dt, c->p,
+                                           static_cast<T *>(c->eta), dv<T>(c, 2, 0), dv<T>(c, 2, 1), dv<T>(c, 2, 2),
+                                           dv<T>(c, 1, 0), dv<T>(c, 1, 1), dv<T>(c, 1, 2), static_cast<T *>(c->f),
+                                           false, static_cast<T *>(c->src), c->cfg.lz, nullptr);
+                 })) != CFD_OK)
+                return s2;
+        }
         if (c->cfg.solver != CFD_SOLVER_SOR_RB) {
             if ((s2 = timed(CFD_KERNEL_RHS, [&] {
                      launch_rhs<T>(c->lc, g, metrics_of<double>(c), 1.0 / c->cfg.dt, c->jp, dv<T>(c, 1, 0),

@@ -56,7 +56,8 @@ int linear_solve_cg(cfd_ctx *c, const double *b, double *x, const double *zero, 
 int ensure_fp32_solver(cfd_ctx *c);
 // multigrid.cu: level set-up, V-cycle z = V(h), and the CG pieces around it
 int mg_setup(cfd_ctx *c);
-void mg_vcycle(cfd_ctx *c, const int *done);
+bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc = nullptr);
+bool mg_fuses_rho(const Mg &G);
 void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc);
 void mg_time_part(cfd_ctx *c, int part);
 long long mg_vcycle_launches(const Mg &G);
@@ -120,6 +121,9 @@ struct cfd_ctx {
     // SOR
     double *sor_cf = nullptr, *sor_rhs = nullptr;  // colour-split SOR coefficients and right-hand side
     cfd::SorAcc *sor_acc = nullptr;
+    // mixed-precision SOR: the FP32 correction (ghosted, zero ghosts) and the
+    // FP32 per-slot change of a Jacobi step; null where the sweeps stay FP64
+    float *sor_e = nullptr, *sor_d = nullptr;
 
     // scalars: [0] rhs mean, [1..2] cd/cl, [3] residual norm^2, [4] dot
     double *dscal = nullptr, *h_scal = nullptr;
@@ -133,6 +137,12 @@ struct cfd_ctx {
     bool fused = true;  // fused FP32 inner iterations (SPE operator)
     long long launches = 0;  // kernels issued by the step and solver paths
     int test_trip_cap = 0;   // > 0: cap on the body runs of every solve loop (cfd_set_test_limits)
+    double vol_total = 0.0;  // interior volume of the grid (set with the metrics)
+    // > 0: the inner tolerance of a defect-correction sweep is loosened to
+    // inner_adapt * tol / (the relative residual before it) when that is
+    // larger than inner_tol (at most 0.5): the last sweep stops once it has
+    // the digits the outer test needs
+    double inner_adapt = 0.2;
     bool div_check = false;  // cfd_set_step_divergence_check
     double last_div[3] = {-1.0, -1.0, -1.0};  // its result for the last step
 

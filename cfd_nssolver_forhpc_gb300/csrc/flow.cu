@@ -319,35 +319,71 @@ __device__ __forceinline__ T pass_value(const Geo &g, const PassArgs<T> &A, int 
     return v;
 }
 
+// The face value of pass_value away from the boundary, where every face the
+// pass reads is written by the convection-diffusion: q the ghosted index of
+// the face, r the compact index of its cell.
 template <class T>
-__global__ void __launch_bounds__(kBlock)
+__device__ __forceinline__ T pass_inner(const Geo &g, const PassArgs<T> &A, int c, long long q, long long r)
+{
+    T v = A.C[c][q];
+    if (A.src_mode == 1) {
+        if (q < g.n) v += A.src[c * g.n + q];
+    } else if (A.src_mode == 2) {
+        v += A.src[c * g.n + r];
+    }
+    return v;
+}
+
+// RHS: form b; PART: also the volume-weighted sum of the unscaled right-hand
+// side, whose mean (over the total volume A.vol) the last block stores.
+template <class T, bool RHS, bool PART>
+__global__ void __launch_bounds__(kBlock, 5)
 k_pass(Geo g, Metrics<double> m, Metrics<float> m32, PassArgs<T> A)
 {
-    double acc[2] = {0.0, 0.0};
-    ff accf[2] = {{0.f, 0.f}, {0.f, 0.f}};
+    double acc = 0.0;
+    ff accf = {0.f, 0.f};
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_of(g, t, i, j, k);
         const long long ic = icel(g, i, j, k);
-        const T ue = pass_value(g, A, 0, i, j, k), vn = pass_value(g, A, 1, i, j, k),
-                wt = pass_value(g, A, 2, i, j, k);
-        if (cd_writes(g, 0, i, j, k)) A.T1[0][ic] = ue;
-        if (cd_writes(g, 1, i, j, k)) A.T1[1][ic] = vn;
-        if (cd_writes(g, 2, i, j, k)) A.T1[2][ic] = wt;
-        if (!A.b) continue;
-        const T uw = pass_value(g, A, 0, i - 1, j, k), vs = pass_value(g, A, 1, i, j - 1, k),
+        // every face of the cell and the three faces below it are written by
+        // the convection-diffusion
+        const bool inner = i > GC && j > GC && k > GC && i < g.nx - GC - 1 && j < g.ny - GC - 1 &&
+                           k < g.nz - GC - 1;
+        T ue, vn, wt, uw = T(0), vs = T(0), wb = T(0);
+        if (inner) {
+            ue = pass_inner(g, A, 0, ic, t);
+            vn = pass_inner(g, A, 1, ic, t);
+            wt = pass_inner(g, A, 2, ic, t);
+            A.T1[0][ic] = ue;
+            A.T1[1][ic] = vn;
+            A.T1[2][ic] = wt;
+            if (RHS) {
+                uw = pass_inner(g, A, 0, ic - g.sx, t - g.sxc);
+                vs = pass_inner(g, A, 1, ic - g.sy, t - g.syc);
+                wb = pass_inner(g, A, 2, ic - 1, t - 1);
+            }
+        } else {
+            ue = pass_value(g, A, 0, i, j, k);
+            vn = pass_value(g, A, 1, i, j, k);
+            wt = pass_value(g, A, 2, i, j, k);
+            if (cd_writes(g, 0, i, j, k)) A.T1[0][ic] = ue;
+            if (cd_writes(g, 1, i, j, k)) A.T1[1][ic] = vn;
+            if (cd_writes(g, 2, i, j, k)) A.T1[2][ic] = wt;
+            if (RHS) {
+                uw = pass_value(g, A, 0, i - 1, j, k);
+                vs = pass_value(g, A, 1, i, j - 1, k);
                 wb = pass_value(g, A, 2, i, j, k - 1);
+            }
+        }
+        if constexpr (!RHS) continue;
         if constexpr (sizeof(T) == sizeof(double)) {
             // createBMatrix_omp in FP64, the arithmetic of k_rhs
             const double div = ((double)ue - (double)uw) * m.x(AX_RD, i) + ((double)vn - (double)vs) * m.y(AX_RD, j)
                              + ((double)wt - (double)wb) * m.z(AX_RD, k);
             A.b[t] = -A.jp[t] * A.ddt * div;
-            if (A.partials) {
-                const double vol = m.x(AX_D, i) * m.y(AX_D, j) * m.z(AX_D, k);
-                acc[0] += vol * (-A.ddt * div);
-                acc[1] += vol;
-            }
+            if (PART) acc += m.x(AX_D, i) * m.y(AX_D, j) * m.z(AX_D, k) * (-A.ddt * div);
         } else {
             // FP32 velocities: their differences are exact as float pairs and the
             // rest runs in float-float, so b keeps the digits FP64 would
@@ -355,23 +391,19 @@ k_pass(Geo g, Metrics<double> m, Metrics<float> m32, PassArgs<T> A)
             const ff div = ff_add(ff_add(ff_mul(ff_two_diff((float)ue, (float)uw), rd(m32.x, i)),
                                          ff_mul(ff_two_diff((float)vn, (float)vs), rd(m32.y, j))),
                                   ff_mul(ff_two_diff((float)wt, (float)wb), rd(m32.z, k)));
-            const ff d = ff_mul(div, ff_of(-A.ddt));  // the unscaled right-hand side
+            const ff d = ff_mul(div, A.mddt);  // the unscaled right-hand side
             A.b[t] = ff_to_double(ff_mul(ff{__ldg(A.jph + t), __ldg(A.jpl + t)}, d));
-            if (A.partials) {
+            if (PART) {
                 auto wd = [](const Axis<float> &a, int x) { return ff{a(AX_D, x), a(AX_DL, x)}; };
                 const ff vol = ff_mul(ff_mul(wd(m32.x, i), wd(m32.y, j)), wd(m32.z, k));
-                accf[0] = ff_add(accf[0], ff_mul(vol, d));
-                accf[1] = ff_add(accf[1], vol);
+                accf = ff_add(accf, ff_mul(vol, d));
             }
         }
     }
-    if (!A.partials) return;
-    if constexpr (sizeof(T) != sizeof(double)) {
-        acc[0] = ff_to_double(accf[0]);
-        acc[1] = ff_to_double(accf[1]);
-    }
-    double tot[2];
-    if (grid_reduce<2>(acc, A.partials, A.counter, tot) && threadIdx.x == 0) *A.mean = tot[0] / tot[1];
+    if constexpr (!PART) return;
+    if constexpr (sizeof(T) != sizeof(double)) acc = ff_to_double(accf);
+    double v[1] = {acc}, tot[1];
+    if (grid_reduce<1>(v, A.partials, A.counter, tot) && threadIdx.x == 0) *A.mean = tot[0] / A.vol;
 }
 
 // update_UandF_omp (updateUandF.hpp:95-190) of one pass with the step's
@@ -382,7 +414,7 @@ k_pass(Geo g, Metrics<double> m, Metrics<float> m32, PassArgs<T> A)
 // shape and summation order).  The faces update_UandF skips keep the f they
 // had (it never writes them), which is what the source and the sums read.
 template <class T>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 6)
 k_update_pass(Geo g, Metrics<T> m, Metrics<double> m64, double dt, T rdt, const double *__restrict__ p,
               const T *__restrict__ eta, const T *__restrict__ u1, const T *__restrict__ v1,
               const T *__restrict__ w1, T *__restrict__ u3, T *__restrict__ v3, T *__restrict__ w3,
@@ -390,6 +422,7 @@ k_update_pass(Geo g, Metrics<T> m, Metrics<double> m64, double dt, T rdt, const 
               unsigned int *counter, double *cdcl)
 {
     double acc[2] = {0.0, 0.0};
+    const float dtf = (float)dt;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < g.n;
          t += (long long)gridDim.x * blockDim.x) {
         int i, j, k;
@@ -397,23 +430,30 @@ k_update_pass(Geo g, Metrics<T> m, Metrics<double> m64, double dt, T rdt, const 
         const long long ic = icel(g, i, j, k);
         const double pc = p[ic];
         const T ec = eta[ic];
+        // dt (p_nb - p_c): FP64 fields keep update_uf's arithmetic; FP32
+        // fields take the FP64 difference to FP32 and scale it there (the FP64
+        // pipe is the scarce one, and the product is rounded to FP32 anyway)
+        auto grad = [&](double pn) -> T {
+            if constexpr (sizeof(T) == sizeof(double)) return (T)(dt * (pn - pc));
+            else return (T)(pn - pc) * dtf;
+        };
         T fv[3] = {T(0), T(0), T(0)};
         if (i < g.nx - GC - 1) {
-            const T T2 = u1[ic] - (T)(dt * (p[ic + g.sx] - pc)) * m.x(AX_RDS, i);
+            const T T2 = u1[ic] - grad(p[ic + g.sx]) * m.x(AX_RDS, i);
             const T ef = ec + (eta[ic + g.sx] - ec) * m.x(AX_IT, i);
             const T un = (T(1) - ef) * T2;
             u3[ic] = un;
             fv[0] = (un - T2) * rdt;
         }
         if (j < g.ny - GC - 1) {
-            const T T2 = v1[ic] - (T)(dt * (p[ic + g.sy] - pc)) * m.y(AX_RDS, j);
+            const T T2 = v1[ic] - grad(p[ic + g.sy]) * m.y(AX_RDS, j);
             const T ef = ec + (eta[ic + g.sy] - ec) * m.y(AX_IT, j);
             const T vn = (T(1) - ef) * T2;
             v3[ic] = vn;
             fv[1] = (vn - T2) * rdt;
         }
         if (k < g.nz - GC - 1 + g.pz) {
-            const T T2 = w1[ic] - (T)(dt * (p[ic + 1] - pc)) * m.z(AX_RDS, k);
+            const T T2 = w1[ic] - grad(p[ic + 1]) * m.z(AX_RDS, k);
             const T ef = ec + (eta[ic + 1] - ec) * m.z(AX_IT, k);
             const T wn = (T(1) - ef) * T2;
             w3[ic] = wn;
@@ -1045,9 +1085,18 @@ void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, cons
                  const PassArgs<T> &A, bool ghosts)
 {
     if (ghosts) k_pass_ghosts<T><<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g, A.T1[0], A.T1[1], A.T1[2], A.src);
-    // the compatibility sums need the reduction's fixed launch shape
-    const int grid = A.partials ? c.red_blocks : blocks_for(g.n, c.grid_cap);
-    k_pass<T><<<grid, kBlock, 0, c.s>>>(g, m, m32, A);
+    PassArgs<T> B = A;
+    B.mddt = ff_of(-A.ddt);
+    if (!A.b) {
+        k_pass<T, false, false><<<nblk(g.n), kBlock, 0, c.s>>>(g, m, m32, B);
+    } else if (!A.partials) {
+        k_pass<T, true, false><<<nblk(g.n), kBlock, 0, c.s>>>(g, m, m32, B);
+    } else {
+        // one sum per block: the partials buffer holds kMaxReduce per block
+        // of the reduction grid
+        const int grid = (int)std::min<long long>(nblk(g.n), (long long)kMaxReduce * c.red_blocks);
+        k_pass<T, true, true><<<grid, kBlock, 0, c.s>>>(g, m, m32, B);
+    }
     if (A.partials) {
         const double *jp = A.jp;
         if (jp) k_rhs_compat<<<blocks_for(g.n, c.grid_cap), kBlock, 0, c.s>>>(g.n, jp, A.mean, A.b);

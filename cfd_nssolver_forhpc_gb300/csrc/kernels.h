@@ -60,6 +60,8 @@ struct PassArgs {
     double *partials;
     unsigned int *counter;
     double *mean;
+    double vol;  // total interior volume (the compatibility mean's denominator)
+    ff mddt;     // -ddt as a float pair (set by launch_pass)
 };
 template <class T>
 void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const Metrics<float> &m32,
@@ -182,6 +184,8 @@ void launch_bc_convective(cfd_launch_ctx &c, const Geo &g, const Metrics<double>
 // fewer than cap times; first != 0 is the check after the head (resets the
 // trip count)
 void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc, int cap, int first);
+// sc->tol = tol, in stream order
+void launch_set_tol(cudaStream_t s, BicgScal *sc, double tol);
 
 // periodic z: the z ghost planes of up to three fields (null fields skipped)
 template <class T>
@@ -283,6 +287,17 @@ void launch_sor_rb_sweep(cudaStream_t s, const Geo &g, const double *cf, const d
 // one colour alone, for timing
 void launch_sor_rb_colour(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, double *p,
                           double omega, double tol, int itmax, int colour, BicgScal *sc, SorAcc *acc);
+// Mixed-precision SOR: FP32 sweeps on the correction inside an FP64 defect
+// correction.  delta = p_new - p at every cell (the change one Jacobi step
+// would make, FP64, stored in FP32 colour-split slots); then SOR sweeps in
+// FP32 on e (ghosted, zero ghosts) for  e = delta + (sum c_q e_q) / sum c,
+// the same equations shifted by p; then p += e, e = 0, and sc->iter +=
+// the FP32 sweeps run.  All return at once when sc->done.
+void launch_sor_delta(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, const double *p,
+                      float *delta, const BicgScal *sc);
+void launch_sor32_sweep(cudaStream_t s, const Geo &g, const Metrics<float> &m, const float *delta, float *e,
+                        float omega, const BicgScal *sc);
+void launch_sor_correct(cudaStream_t s, const Geo &g, double *p, float *e, int sweeps, BicgScal *sc);
 
 // mixed precision pieces
 template <class V>
@@ -359,6 +374,7 @@ struct MgLevel {
     int sweep_tj, sweep_ci;  // fused sweep tiling: j rows and i planes per block (0: not fused)
     bool quads;           // the float4 smoother applies (nz % 4 == 0, aligned arrays)
     int pz;               // 1: periodic in z (nz even: red-black stays a two-colouring)
+    float om;             // smoother relaxation: x += om (x_gs - x); 1 is Gauss-Seidel
 };
 constexpr int kMgSmallSmem = 200 * 1024;  // shared-memory bytes for the small levels' x and b
 struct MgSmall {
@@ -377,8 +393,8 @@ struct Mg {
     int nlev = 0, first_small = 0;
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
     int sweeps0 = 2; // ... on the finest level
-    bool fuse_ends = true;  // the first pre-sweep from zero and the prolongation + first
-                            // post-colour each in one pass (float4 levels)
+    bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
+                             // post-colour each in one pass (float4 levels); measured slower
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve
     float *cinv = nullptr;
     bool usable = false;

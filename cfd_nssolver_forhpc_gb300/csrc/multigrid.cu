@@ -124,15 +124,19 @@ __device__ __forceinline__ void gs_cell(const MgLevel &L, const float *__restric
                                         int j, int k, Ix<SM> t, bool zero_init)
 {
     const float nb = zero_init ? 0.f : mg_nb<SM, PZ>(L, x, i, j, k, t);
-    if constexpr (SM) x[t] = fmaf(b[t], L.rv[t], nb) * L.rg[t];
-    else x[t] = fmaf(b[t], mg_rdv<SM>(L, i, j, k), nb) * smooth_rcp(mg_diag<SM>(L, i, j, k));
+    float v;
+    if constexpr (SM) v = fmaf(b[t], L.rv[t], nb) * L.rg[t];
+    else v = fmaf(b[t], mg_rdv<SM>(L, i, j, k), nb) * smooth_rcp(mg_diag<SM>(L, i, j, k));
+    if (L.om != 1.f) v = zero_init ? L.om * v : fmaf(L.om, v - x[t], x[t]);
+    x[t] = v;
 }
 
 // one colour over a level with nz % 4 == 0: one thread per quad of cells
 // k = 4m..4m+3 (float4 rows), updating the two cells of that colour
-template <bool SM = false, class I = Ix<SM>, bool PZ = false>
+// RHO: also accumulate b . x of the quads after the update into *rho
+template <bool SM = false, class I = Ix<SM>, bool PZ = false, bool RHO = false>
 __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__restrict__ b, float *__restrict__ x,
-                                             int color, bool zero_init, I t0, I stride)
+                                             int color, bool zero_init, I t0, I stride, float *rho = nullptr)
 {
     const I nq = (I)(L.n >> 2);
     const int n4 = L.nz >> 2;
@@ -196,13 +200,19 @@ __device__ __forceinline__ void smooth_quads(const MgLevel &L, const float *__re
             nB = fmaf(pick(czm.z, czm.w), pick(xc.y, xc.z), nB);
             nB = fmaf(pick(czp.z, czp.w), pick(xc.w, zhi), nB);
         }
-        const float vA = fmaf(bA, rA, nA) * dA, vB = fmaf(bB, rB, nB) * dB;
+        float vA = fmaf(bA, rA, nA) * dA, vB = fmaf(bB, rB, nB) * dB;
+        if (L.om != 1.f) {  // over-relaxation (xc is 0 from a zero start)
+            const float oA = pick(xc.x, xc.y), oB = pick(xc.z, xc.w);
+            vA = fmaf(L.om, vA - oA, oA);
+            vB = fmaf(L.om, vB - oB, oB);
+        }
         float xo[4];
         xo[0] = odd ? xc.x : vA;
         xo[1] = odd ? vA : xc.y;
         xo[2] = odd ? xc.z : vB;
         xo[3] = odd ? vB : xc.w;
         *reinterpret_cast<float4 *>(x + t) = make_float4(xo[0], xo[1], xo[2], xo[3]);
+        if constexpr (RHO) *rho = fmaf(bv.x, xo[0], fmaf(bv.y, xo[1], fmaf(bv.z, xo[2], fmaf(bv.w, xo[3], *rho))));
     }
 }
 
@@ -874,6 +884,24 @@ k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, do
         sc->r0n2 = fmax(tot[0] - tot[1] * tot[1] / (double)F.A.n, 0.0);
 }
 
+// the CG scalars after rho' = h . z (not the first): the iteration cap, else
+// the flexible beta and the iteration count
+__device__ __forceinline__ void mg_rho_update(BicgScal *sc, double tot)
+{
+    if (sc->iter + 1 >= sc->maxit) {
+        sc->done = BICG_CAPPED;
+    } else {
+        // flexible (Polak-Ribiere) beta = h.(z - z_old) / rho_old, with
+        // h.z_old = rho_old - alpha q.z_old (q.z from the stencil launch):
+        // keeps the recurrences sound with an FP32 V-cycle, symmetric only
+        // to rounding
+        sc->beta = (tot - (sc->rho - sc->alpha * sc->qz)) / sc->rho;
+        sc->rho = tot;
+        sc->iter += 1;
+        sc->total_iters += 1;
+    }
+}
+
 // rho = h . z; with p0 != null also p0 = z and the solve's initial scalars
 // (sc->r0n2 was set by k_mg_h), else beta and the iteration count (the
 // stopping test is in k_mg_upd, before the V-cycle)
@@ -911,18 +939,27 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
         sc->relres = sc->done == BICG_RUNNING ? 1.0 : 0.0;
         return;
     }
-    if (sc->iter + 1 >= sc->maxit) {
-        sc->done = BICG_CAPPED;
-    } else {
-        // flexible (Polak-Ribiere) beta = h.(z - z_old) / rho_old, with
-        // h.z_old = rho_old - alpha q.z_old (q.z from the stencil launch):
-        // keeps the recurrences sound with an FP32 V-cycle, symmetric only
-        // to rounding
-        sc->beta = (tot[0] - (sc->rho - sc->alpha * sc->qz)) / sc->rho;
-        sc->rho = tot[0];
-        sc->iter += 1;
-        sc->total_iters += 1;
-    }
+    mg_rho_update(sc, tot[0]);
+}
+
+// The V-cycle's last launch, the colour-0 pass of the finest level's
+// post-smoothing, with rho' = h . z of the CG reduced from the quads it
+// writes (h = b and z = x of the finest level): k_mg_rho without its own
+// pass over h and z.  A grid-stride launch of at most kMaxReduce x the
+// reduction grid, one partial per block.
+template <class I, bool PZ>
+__global__ void __launch_bounds__(kBlock)
+k_mg_smooth4_rho(MgLevel L, const float *b, float *x, BicgScal *sc, double *partials, unsigned int *counter)
+{
+    pdl_wait();
+    pdl_allow();
+    if (sc->done) return;
+    float pa = 0.f;
+    smooth_quads<false, I, PZ, true>(L, b, x, 0, false, (I)blockIdx.x * blockDim.x + threadIdx.x,
+                                     (I)gridDim.x * blockDim.x, &pa);
+    double acc[1] = {(double)pa}, tot[1];
+    if (!grid_reduce<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    mg_rho_update(sc, tot[0]);
 }
 
 // e += alpha p, h -= alpha q and the stopping test on |h - mean h| /
@@ -1152,6 +1189,8 @@ int mg_setup(cfd_ctx *c)
     if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS")) G.fuse_ends = std::atoi(e) != 0;
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
+    float om = 1.f;  // smoother relaxation (1: Gauss-Seidel)
+    if (const char *e = std::getenv("CFDGPU_MG_OMEGA")) om = std::max(0.5f, std::min(1.5f, (float)std::atof(e)));
     const FvOp<float> F = fv32(c);
     std::vector<double> W[3];
     const int n0[3] = {g.nxc, g.nyc, g.nzc};
@@ -1175,6 +1214,7 @@ int mg_setup(cfd_ctx *c)
     L0.x = c->w32.r0;  // z
     L0.b = c->r32;     // h
     L0.pz = g.pz;
+    L0.om = om;
     set_divs(L0);
     G.lev[0] = L0;
     int nl = 1;
@@ -1201,6 +1241,7 @@ int mg_setup(cfd_ctx *c)
             CKS(upload_axis(c, W[a], L, a, a == 2 && g.pz));
         }
         L.pz = g.pz;
+        L.om = om;
         L.nx = n[0]; L.ny = n[1]; L.nz = n[2];
         L.n = (long long)n[0] * n[1] * n[2];
         CKS(dalloc_t(c, &L.x, (size_t)L.n));
@@ -1241,7 +1282,7 @@ int mg_setup(cfd_ctx *c)
     for (int l = 0; l < G.first_small; ++l) {
         MgLevel &L = G.lev[l];
         L.sweep_tj = L.sweep_ci = 0;
-        if (!fused || !L.quads || L.pz || level_sweeps(G, l) % 2 != 0) continue;
+        if (!fused || !L.quads || L.pz || L.om != 1.f || level_sweeps(G, l) % 2 != 0) continue;
         const int n4 = L.nz / 4;
         const int tj = std::max(1, std::min({128 / std::max(n4, 1), L.ny, 1024 / n4}));
         if (tj * n4 > 1024 || (long long)sweep_smem(tj, L.nz) > kSweepSmemMax) continue;
@@ -1287,15 +1328,45 @@ static void sweep_launch(const MgLevel &L, const float *xo, float *xn, int c0, i
 // a grid-wide level: fused sweeps alternate between x and xalt and end in x
 // (an even number of sweeps), else colour launches in place
 // a level whose sweep ends run fused (k_mg_first4, k_mg_prolong_first4)
-static bool fused_ends(const Mg &G, const MgLevel &L) { return G.fuse_ends && L.quads && L.sweep_tj == 0; }
+static bool fused_ends(const Mg &G, const MgLevel &L) { return G.fuse_ends && L.quads && L.sweep_tj == 0 && L.om == 1.f; }
 static bool int_index(const MgLevel &L) { return L.n + (long long)L.ny * L.nz < (1LL << 31); }
 
+// the CG's rho' fused into the V-cycle's last launch (k_mg_smooth4_rho)
+struct RhoFuse {
+    BicgScal *sc;
+    double *partials;
+    unsigned int *counter;
+    long long grid_cap;  // kMaxReduce x the reduction grid: one partial per block
+};
+
+template <bool PZ>
+static void rho_launch_t(const MgLevel &L, const RhoFuse &r, cudaStream_t s)
+{
+    const int grid = (int)std::min<long long>(nblk(L.n / 4), r.grid_cap);
+    if (int_index(L))
+        launch_pdl(k_mg_smooth4_rho<int, PZ>, dim3(grid), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, r.sc,
+                   r.partials, r.counter);
+    else
+        launch_pdl(k_mg_smooth4_rho<long long, PZ>, dim3(grid), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, r.sc,
+                   r.partials, r.counter);
+}
+
 // pre: the sweeps before the coarse correction; post_fused: the caller ran
-// the first colour of the post-smoothing with the prolongation
-static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStream_t s, bool post_fused = false)
+// the first colour of the post-smoothing with the prolongation; rf: the
+// last colour launch (colour 0 of the post-smoothing) also reduces rho'
+static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStream_t s, bool post_fused = false,
+                         const RhoFuse *rf = nullptr)
 {
     const MgLevel &L = G.lev[l];
     const int sweeps = level_sweeps(G, l);
+    auto last = [&](int q) {
+        if (rf && q == sweeps - 1) {
+            if (L.pz) rho_launch_t<true>(L, *rf, s);
+            else rho_launch_t<false>(L, *rf, s);
+        } else {
+            smooth_launch(L, pre ? 1 : 0, 0, done, s);
+        }
+    };
     if (fused_ends(G, L)) {
         for (int q = 0; q < sweeps; ++q) {
             if (pre && q == 0) {
@@ -1308,7 +1379,7 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
                 continue;
             }
             if (!(post_fused && q == 0)) smooth_launch(L, pre ? 0 : 1, 0, done, s);
-            smooth_launch(L, pre ? 1 : 0, 0, done, s);
+            last(q);
         }
         return;
     }
@@ -1323,7 +1394,7 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
     }
     for (int q = 0; q < sweeps; ++q) {
         smooth_launch(L, pre ? 0 : 1, pre && q == 0, done, s);
-        smooth_launch(L, pre ? 1 : 0, 0, done, s);
+        last(q);
     }
 }
 
@@ -1362,12 +1433,24 @@ static void small_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl 
     else k<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
 }
 
-// z = V(h): one V-cycle; every kernel returns at once when *done
-void mg_vcycle(cfd_ctx *c, const int *done)
+// the CG's rho' can run inside the V-cycle's last launch: the finest level
+// is a grid-wide float4 level smoothed by colour launches
+bool mg_fuses_rho(const Mg &G)
+{
+    return G.first_small > 0 && G.lev[0].quads && G.lev[0].sweep_tj == 0;
+}
+
+// z = V(h): one V-cycle; every kernel returns at once when *done.  With
+// rho_sc (done == &rho_sc->done) the CG's rho' = h . z and its scalar update
+// run inside the last launch where the finest level is a grid-wide float4
+// level; returns whether they did (else the caller runs k_mg_rho).
+bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc)
 {
     Mg &G = c->mg;
     const cudaStream_t s = c->s;
     const int fs = G.first_small;
+    const bool fuse_rho = rho_sc && mg_fuses_rho(G);
+    const RhoFuse rf{rho_sc, c->lc.partials, c->lc.counter, (long long)kMaxReduce * c->lc.red_blocks};
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
         smooth_phase(G, l, true, done, s);
@@ -1383,14 +1466,15 @@ void mg_vcycle(cfd_ctx *c, const int *done)
             else
                 launch_pdl(k_mg_prolong_first4<long long>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
                            (const float *)L.b, L.x, (const float *)G.lev[l + 1].x, done);
-            smooth_phase(G, l, false, done, s, true);
+            smooth_phase(G, l, false, done, s, true, l == 0 && fuse_rho ? &rf : nullptr);
             continue;
         }
         launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1],
                    (const float *)G.lev[l + 1].x, L.x, done);
-        smooth_phase(G, l, false, done, s);
+        smooth_phase(G, l, false, done, s, false, l == 0 && fuse_rho ? &rf : nullptr);
     }
     c->launches += mg_vcycle_launches(G);
+    return fuse_rho;
 }
 
 // one piece of the V-cycle for timing: 0 finest smoothing colour, 1 finest

@@ -317,14 +317,19 @@ typedef enum {
     CFD_KERNEL_MG_UPD,       /* multigrid CG: e, h update */
     CFD_KERNEL_MG_RHO,       /* multigrid CG: h.z and the scalar update */
     CFD_KERNEL_MG_SWEEP,     /* multigrid: one fused red-black sweep on the finest level */
+    CFD_KERNEL_PASS,         /* predictor-corrector pass: T1 = C + source and the right-hand side */
+    CFD_KERNEL_UPDATE_PASS,  /* predictor-corrector pass: update_UandF with src += dt f */
+    CFD_KERNEL_SOR32_SWEEP,  /* mixed precision: one red + one black FP32 sweep on the SOR correction */
     CFD_KERNEL_COUNT
 } cfd_kernel_id;
 
 /* Mean device time (ms) of one launch of each hot kernel, measured with CUDA
    events around `reps` back-to-back launches on the context stream.  The
    Krylov kernels run on the solver's scratch vectors and a scratch copy of
-   x, so the simulation state is left as it was; ms[k] < 0 marks a kernel the
-   context does not use.  nms is the length of ms (at most CFD_KERNEL_COUNT
+   x, the SOR sweep on a copy of p; the flow kernels write T3 and the
+   predictor-corrector source, both rewritten by the next step before they
+   are read.  Call it between steps.  ms[k] < 0 marks a kernel the context
+   does not use.  nms is the length of ms (at most CFD_KERNEL_COUNT
    entries are written). */
 int cfd_time_kernels(cfd_ctx *ctx, int reps, double *ms, int nms);
 

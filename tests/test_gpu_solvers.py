@@ -199,6 +199,34 @@ def test_sor_sweep_cap(oracle):
     np.testing.assert_array_equal(p, p_ref)
 
 
+@pytest.mark.parametrize("name", ["g1", "c1", "g2_odd"])
+def test_sor_fp32_sweeps_reach_the_fp64_fixed_point(oracle, name):
+    """Mixed-precision contexts sweep in FP32 on the correction between FP64
+    sweeps, whose max change is the reference's stop test.  At a tight
+    tolerance both runs reach the same fixed point, and the FP32 sweeps take
+    about as many sweeps as FP64 ones (the count includes them; the stop test
+    runs once per loop body of 4 x check_every FP32 sweeps)."""
+    w = _sor_workload(name)
+    g = Grid.of(w, oracle)
+    I = kernel_inputs(g.ng, g.n)
+    u1, v1, w1 = (0.01 * I[k] for k in ("u1", "v1", "w1"))
+    out = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        with Simulation(w, solver=capi.SOLVER_SOR_RB, precision=prec, tol=1e-12, omega=1.7, sor_maxit=20000,
+                        check_every=4) as S:
+            S.grid_uniform()
+            S.upload("P", I["sor_p"])
+            for k, a in (("U1", u1), ("V1", v1), ("W1", w1)):
+                S.upload(k, a)
+            it, err = S.SorPipeLine(S.T1)
+            out[prec] = (it, err, S.download("P"))
+    (it64, err64, p64), (it32, err32, p32) = out[capi.PREC_FP64], out[capi.PREC_MIXED]
+    assert err64 <= 1e-12 and err32 <= 1e-12
+    assert it64 < 20000 and it32 < 20000
+    assert abs(it32 - it64) <= 17 + 0.1 * it64, (it32, it64)
+    assert rel_err(g.interior(p32), g.interior(p64)) < 1e-9
+
+
 @pytest.mark.parametrize("dims", [(64, 48, 32), (24, 40, 64), (32, 20, 8), (16, 24, 12)])
 def test_cg_stencil_tma_matches_plain_kernel(monkeypatch, dims):
     """The TMA-fed CG stencil (z and p planes streamed into shared memory,
