@@ -82,6 +82,10 @@ SOR_BYTES_PER_CELL = 80
 # neighbour term, the right-hand side, the scale, the change, its product
 # with omega and the update
 SOR_FP64_OPS_PER_CELL = 16
+# the FP32 sweeps of the mixed path: the correction read and written, the
+# change of a Jacobi step read (coefficients from the axis tables)
+SOR32_BYTES_PER_CELL = 12
+SOR32_PER_BODY = 4 * 16  # FP32 sweeps per loop body (4 x check_every)
 
 
 def parse():
@@ -344,7 +348,15 @@ def roofline(S, w, infos, precision, ms_step):
     if "sor_sweep" in ms:
         counts = {k: v for k, v in counts.items() if k in ("convdiff", "pass", "update_pass", "update_uf")}
         # sweeps per step: iterations + 1 per solve (the timed steps all solve)
-        counts["sor_sweep"] = sum(sum(n + 1 for n in i["iters"]) for i in infos) / len(infos)
+        sweeps = [n + 1 for i in infos for n in i["iters"]]
+        if "sor32_sweep" in ms:
+            # mixed precision: one FP64 sweep per loop body of 4 x 16 FP32 sweeps
+            fp64 = [-(-n // (SOR32_PER_BODY + 1)) for n in sweeps]
+            counts["sor_sweep"] = sum(fp64) / len(infos)
+            counts["sor32_sweep"] = (sum(sweeps) - sum(fp64)) / len(infos)
+            per_row["sor32_sweep"] = SOR32_BYTES_PER_CELL
+        else:
+            counts["sor_sweep"] = sum(sweeps) / len(infos)
         per_row["sor_sweep"] = SOR_BYTES_PER_CELL
     shares = {k: ms[k] * counts[k] for k in ms if k in counts}
     total = ms_step if ms_step > 0 else (sum(shares.values()) or 1.0)
@@ -767,6 +779,7 @@ def main():
                        "tol": w.tol, "precision": args.precision, "parallelism": f"replicas x{dist.world}",
                        "l2": "working set larger than L2 (no flush needed)"},
             "iters_per_step": [sum(i["iters"]) for i in infos],
+            "outer_per_step": [sum(i["outer"]) for i in infos],
             "max_relres": max(r for i in infos[1:] or infos for r in i["relres"]),
             "solves_above_tol": cap_hits(infos, w.tol),
             "cd_last": infos[-1]["cd"], "divergence": div,

@@ -201,23 +201,30 @@ int bicg_run(cfd_ctx *c, const Op &A, const V *b, V *x, const BicgVecs<V> &w, V 
 // back): prologue(), then pair(0), pair(1) while the solve runs -- inside
 // one graph (a WHILE node over `pairs` pairs) or, without graphs, polled
 // from the host after every `pairs` pairs.
+// single: the body is one iteration, pair(0) (its kernels alternate their
+// buffers at run time).
 template <class Pro, class Pair>
 int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int launches_prologue,
-              int launches_pair, int pairs_req = 0)
+              int launches_pair, int pairs_req = 0, bool single = false)
 {
     const int pairs = pairs_req > 0 ? pairs_req : (c->cfg.check_every + 1) / 2;
-    const int cap = trip_cap(c, (long long)c->cfg.p_iter_max / (2 * pairs) + 3);
+    const int per_body = single ? 1 : 2 * pairs;
+    const int cap = trip_cap(c, (long long)c->cfg.p_iter_max / per_body + 3);
     auto body = [&] {
+        if (single) {
+            pair(0);
+            return;
+        }
         for (int q = 0; q < pairs; ++q) {
             pair(0);
             pair(1);
         }
     };
     if (c->use_graphs && c->device_loops) {
-        CKS(while_graph(c, gi, ((long long)cap << 20) | pairs, sc, cap, prologue, body));
-        return run_while_graph(c, gi, sc, launches_prologue, (long long)launches_pair * 2 * pairs, "inner solve");
+        CKS(while_graph(c, gi, ((long long)cap << 20) | (single ? 0 : pairs), sc, cap, prologue, body));
+        return run_while_graph(c, gi, sc, launches_prologue, (long long)launches_pair * per_body, "inner solve");
     }
-    if (c->use_graphs) CKS(batch_graph(c, gi, -pairs, body));
+    if (c->use_graphs) CKS(batch_graph(c, gi, -(single ? 0 : pairs) - 1, body));
     prologue();
     c->launches += launches_prologue;
     CK(cudaGetLastError());
@@ -227,7 +234,7 @@ int run_pairs(cfd_ctx *c, int gi, BicgScal *sc, Pro &&prologue, Pair &&pair, int
         if (c->h_sc->wait_timeout) return fail(CFD_ERR_TIMEOUT, "a bounded wait of the TMA pipeline gave up");
         if (c->h_sc->done != BICG_RUNNING) break;
         if (nb >= cap) return fail(CFD_ERR_TIMEOUT, "inner solve did not report completion");
-        c->launches += (long long)launches_pair * 2 * pairs;
+        c->launches += (long long)launches_pair * per_body;
         if (c->use_graphs) CK(cudaGraphLaunch(c->graph[gi], c->s));
         else body();
         CK(cudaGetLastError());
@@ -267,9 +274,13 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 }
 
 // FP32 CG on M e = P r preconditioned by one multigrid V-cycle per iteration
-// (multigrid.cu): z = V(h), rho = h.z, p0 = z, then per iteration the
-// stencil launch (pn, q, alpha), the update (e, h), a V-cycle and rho'.  Few
-// iterations per solve, so the loop body holds one pair.
+// (multigrid.cu): z = V(h), rho = h.z, p0 = z, the first stencil launch
+// (pn, q, alpha) and update (e, h, the stopping test); then per iteration a
+// V-cycle and rho', the stencil launch and the update.  The loop body is one
+// iteration ending with its stopping test, so the loop condition after it
+// sees the test at once and no launches run dead after convergence (a dead
+// V-cycle is some thirty launches); the stencil launch and the update
+// alternate the two p buffers at run time (sc->pp) to make that possible.
 int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 {
     const int v = (int)mg_vcycle_launches(c->mg);
@@ -287,15 +298,13 @@ int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc
             mg_rho(c, h, z, c->w32.p1, sc);
             launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
             mg_upd(c, e, c->w32.p1, h, q, sc);
-            vcycle_rho();
         },
-        [&](int from) {
-            float *P[2] = {c->w32.p1, c->p_alt};
-            launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, from, false);
-            mg_upd(c, e, P[1 - from], h, q, sc);
+        [&](int) {
             vcycle_rho();
+            launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, false, true);
+            mg_upd(c, e, c->w32.p1, h, q, sc, c->p_alt);
         },
-        2 * v + 5 - fr, v + 3 - fr, c->mg.pairs);
+        v + 4, v + 3 - fr, 1, true);
 }
 
 // The graphs bake in the buffers and operator of the context; they are

@@ -196,36 +196,16 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV])
         for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
 }
 
+// the last block's part of a grid reduction, after every block has written
+// its partials and taken its ticket (last: this block's ticket was the last)
 template <int NV>
-__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials,
-                                            unsigned int *counter, double (&tot)[NV])
+__device__ __forceinline__ bool grid_reduce_tail(bool last, double *partials, unsigned int *counter,
+                                                 double (&sm)[32][NV], double (&tot)[NV])
 {
-    static_assert(NV <= kMaxReduce, "wider than the partials buffer");
-    __shared__ double sm[32][NV];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nwarps = (blockDim.x + 31) >> 5;
-    warp_sum<NV>(v);
-    if (lane == 0)
-#pragma unroll
-        for (int q = 0; q < NV; ++q) sm[warp][q] = v[q];
-    __syncthreads();
-    if (warp == 0) {
-        double w[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? sm[lane][q] : 0.0;
-        warp_sum<NV>(w);
-        if (lane == 0) {
-#pragma unroll
-            for (int q = 0; q < NV; ++q) partials[q * gridDim.x + blockIdx.x] = w[q];
-            __threadfence();
-            unsigned int t = atomicAdd(counter, 1u);
-            last = (t == gridDim.x - 1);
-        }
-    }
-    __syncthreads();
     if (!last) return false;
     __threadfence();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
     double s[NV];
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
@@ -254,6 +234,80 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials,
 #pragma unroll
     for (int q = 0; q < NV; ++q) tot[q] = sm[0][q];
     return true;
+}
+
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double *partials,
+                                            unsigned int *counter, double (&tot)[NV])
+{
+    static_assert(NV <= kMaxReduce, "wider than the partials buffer");
+    __shared__ double sm[32][NV];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    warp_sum<NV>(v);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sm[warp][q] = v[q];
+    __syncthreads();
+    if (warp == 0) {
+        double w[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? sm[lane][q] : 0.0;
+        warp_sum<NV>(w);
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) partials[q * gridDim.x + blockIdx.x] = w[q];
+            __threadfence();
+            unsigned int t = atomicAdd(counter, 1u);
+            last = (t == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    return grid_reduce_tail<NV>(last, partials, counter, sm, tot);
+}
+
+// The same reduction for FP32 per-thread values: the block's tree runs in
+// FP32 (warp shuffles, then the warps in index order; relative error of
+// about log2(blockDim) roundings), and only the block totals, the partials,
+// are FP64.  GB300 issues FP64 at 1/64 of the FP32 rate, so a double tree
+// in every block is a measurable part of a short kernel.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce_f(float (&v)[NV], double *partials, unsigned int *counter,
+                                              double (&tot)[NV])
+{
+    static_assert(NV <= kMaxReduce, "wider than the partials buffer");
+    __shared__ float smf[32][NV];
+    __shared__ double sm[32][NV];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], off);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) smf[warp][q] = v[q];
+    __syncthreads();
+    if (warp == 0) {
+        float w[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) w[q] = lane < nwarps ? smf[lane][q] : 0.f;
+#pragma unroll
+        for (int q = 0; q < NV; ++q)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) w[q] += __shfl_down_sync(0xffffffffu, w[q], off);
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) partials[q * gridDim.x + blockIdx.x] = (double)w[q];
+            __threadfence();
+            unsigned int t = atomicAdd(counter, 1u);
+            last = (t == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    return grid_reduce_tail<NV>(last, partials, counter, sm, tot);
 }
 
 // The same last-block scheme for maxima (order-independent, so any launch

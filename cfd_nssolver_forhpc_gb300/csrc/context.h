@@ -62,7 +62,8 @@ void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc);
 void mg_time_part(cfd_ctx *c, int part);
 long long mg_vcycle_launches(const Mg &G);
 void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc);
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc);
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc,
+            const float *p2 = nullptr);
 // adjoint_api.cu: releases the host side of the adjoint state
 void adj_free(AdjState *a);
 

@@ -347,22 +347,27 @@ k_pass(Geo g, Metrics<double> m, Metrics<float> m32, PassArgs<T> A)
         int i, j, k;
         cell_of(g, t, i, j, k);
         const long long ic = icel(g, i, j, k);
-        // every face of the cell and the three faces below it are written by
-        // the convection-diffusion
-        const bool inner = i > GC && j > GC && k > GC && i < g.nx - GC - 1 && j < g.ny - GC - 1 &&
-                           k < g.nz - GC - 1;
+        // away from the x and y boundaries the u and v faces of the cell and
+        // below it are convection-diffusion faces; the w faces are too except
+        // the top one of the column and the ghost one below it (selected per
+        // cell: a warp holds a whole k row, so a k-boundary test here keeps
+        // the warp on this path); periodic z leaves the k ends to the
+        // general path
+        const bool inner = i > GC && j > GC && i < g.nx - GC - 1 && j < g.ny - GC - 1 &&
+                           (!g.pz || (k > GC && k < g.nz - GC - 1));
         T ue, vn, wt, uw = T(0), vs = T(0), wb = T(0);
         if (inner) {
+            const bool wt_cd = k < g.nz - GC - 1 + g.pz, wb_cd = k > GC;
             ue = pass_inner(g, A, 0, ic, t);
             vn = pass_inner(g, A, 1, ic, t);
-            wt = pass_inner(g, A, 2, ic, t);
+            wt = wt_cd ? pass_inner(g, A, 2, ic, t) : A.T1[2][ic];
             A.T1[0][ic] = ue;
             A.T1[1][ic] = vn;
-            A.T1[2][ic] = wt;
+            if (wt_cd) A.T1[2][ic] = wt;
             if (RHS) {
                 uw = pass_inner(g, A, 0, ic - g.sx, t - g.sxc);
                 vs = pass_inner(g, A, 1, ic - g.sy, t - g.syc);
-                wb = pass_inner(g, A, 2, ic - 1, t - 1);
+                wb = wb_cd ? pass_inner(g, A, 2, ic - 1, t - 1) : A.T1[2][ic - 1];
             }
         } else {
             ue = pass_value(g, A, 0, i, j, k);

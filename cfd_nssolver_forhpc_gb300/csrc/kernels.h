@@ -161,6 +161,7 @@ struct BicgScal {
     int loop_trips;    // body runs of the solve's device-side loop (graph WHILE node)
     double rhs_scale;  // the multigrid-CG solves for rhs / rhs_scale; the correction multiplies back
     double qz;         // q . z of the CG stencil launch (flexible beta: h_new . z_old = rho - alpha q . z)
+    int pp;            // multigrid CG with one iteration per loop body: which of its two p buffers holds p
 };
 enum { BICG_RUNNING = 0, BICG_CONVERGED = 1, BICG_CAPPED = 2, BICG_ZERO_RHS = 3 };
 
@@ -237,9 +238,11 @@ void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *i
 // one full wave of the CG inner kernels on this device, capped at red_blocks
 int cg_resident_grid(int sms, int red_blocks);
 // one stencil launch of the multigrid-preconditioned CG: pn = z + beta p
-// (first: pn = p0), q = M pn, alpha; z is a vector (the V-cycle's output)
+// (first: pn = p0), q = M pn, alpha; z is a vector (the V-cycle's output).
+// p is read from P[from] and pn written to the other buffer, or, with dyn
+// (not first), from buffer sc->pp of (p, p_alt) at run time
 void launch_cg_pq_mg(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma *tma, float *z, float *p, float *p_alt,
-                     float *q, BicgScal *sc, int from, bool first);
+                     float *q, BicgScal *sc, int from, bool first, bool dyn = false);
 // iP = 1 / diag(M), once per context
 void launch_cg_ip(cfd_launch_ctx &c, const FvOp<float> &F, float *iP);
 void launch_fv_axes(cudaStream_t s, int n, const float *c, const float *width, float *out);

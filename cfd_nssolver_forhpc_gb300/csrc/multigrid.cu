@@ -879,8 +879,9 @@ k_mg_h(FvOp<float> F, float *__restrict__ h, const double *rn2, BicgScal *sc, do
             ps += v;
         }
     }
-    double acc[2] = {(double)pa, (double)ps}, tot[2];
-    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0)
+    float acc[2] = {pa, ps};
+    double tot[2];
+    if (grid_reduce_f<2>(acc, partials, counter, tot) && threadIdx.x == 0)
         sc->r0n2 = fmax(tot[0] - tot[1] * tot[1] / (double)F.A.n, 0.0);
 }
 
@@ -927,9 +928,11 @@ k_mg_rho(long long n, const float *__restrict__ h, const float *__restrict__ z, 
         if (p0) p0[r] = zv;
         pa = fmaf(h[r], zv, pa);
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (!grid_reduce<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    float acc[1] = {pa};
+    double tot[1];
+    if (!grid_reduce_f<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
     if (p0) {
+        sc->pp = 0;
         sc->rho = tot[0];
         sc->norm0 = sqrt(sc->r0n2);
         sc->iter = 0;
@@ -957,21 +960,25 @@ k_mg_smooth4_rho(MgLevel L, const float *b, float *x, BicgScal *sc, double *part
     float pa = 0.f;
     smooth_quads<false, I, PZ, true>(L, b, x, 0, false, (I)blockIdx.x * blockDim.x + threadIdx.x,
                                      (I)gridDim.x * blockDim.x, &pa);
-    double acc[1] = {(double)pa}, tot[1];
-    if (!grid_reduce<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    float acc[1] = {pa};
+    double tot[1];
+    if (!grid_reduce_f<1>(acc, partials, counter, tot) || threadIdx.x != 0) return;
     mg_rho_update(sc, tot[0]);
 }
 
 // e += alpha p, h -= alpha q and the stopping test on |h - mean h| /
 // |h0 - mean h0| (the unpreconditioned residual without its null-space part):
 // a converged solve skips the V-cycle after it
+// p2 != null: p and p2 are the two buffers of the run-time alternation; pn
+// is the one sc->pp does not name, and the last block flips sc->pp
 __global__ void __launch_bounds__(kBlock)
-k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float *__restrict__ h,
-         const float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter)
+k_mg_upd(long long n, float *__restrict__ e, const float *p_, float *__restrict__ h,
+         const float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter, const float *p2)
 {
     pdl_wait();
     pdl_allow();
     if (sc->done) return;
+    const float *__restrict__ p = p2 ? (sc->pp ? p_ : p2) : p_;
     const float alpha = (float)sc->alpha;
     float pa = 0.f, ps = 0.f;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
@@ -998,8 +1005,10 @@ k_mg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float 
         pa = fmaf(hv, hv, pa);
         ps += hv;
     }
-    double acc[2] = {(double)pa, (double)ps}, tot[2];
-    if (!grid_reduce<2>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    float acc[2] = {pa, ps};
+    double tot[2];
+    if (!grid_reduce_f<2>(acc, partials, counter, tot) || threadIdx.x != 0) return;
+    if (p2) sc->pp = 1 - sc->pp;
     const double rel = sqrt(fmax(tot[0] - tot[1] * tot[1] / (double)n, 0.0) / sc->r0n2);
     sc->relres = rel;
     if (rel < sc->tol) sc->done = BICG_CONVERGED;
@@ -1521,10 +1530,10 @@ void mg_rho(cfd_ctx *c, const float *h, const float *z, float *p0, BicgScal *sc)
                c->lc.counter);
 }
 
-void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc)
+void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, BicgScal *sc, const float *p2)
 {
     launch_pdl(k_mg_upd, dim3(c->lc.red_blocks), dim3(kBlock), 0, c->s, c->g.n, e, p, h, q, sc, c->lc.partials,
-               c->lc.counter);
+               c->lc.counter, p2);
 }
 
 }  // namespace cfd

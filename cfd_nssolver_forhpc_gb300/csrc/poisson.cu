@@ -537,8 +537,9 @@ k_cg_init(FvOp<float> F, float *__restrict__ h, float *__restrict__ p, BicgScal 
         p[row] = r;
         pa = fmaf(hv, r, pa);
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    float acc[1] = {pa};
+    double tot[1];
+    if (grid_reduce_f<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
         sc->rho = tot[0];
         sc->r0n2 = tot[0];
         sc->norm0 = sqrt(tot[0]);
@@ -566,14 +567,19 @@ constexpr int kCgTileSmem = (kBlock / 8 + 2) * (8 + 2);
 // outside the domain are 0; their coefficients are 0 as well.
 // first: the solve's first iteration, pn = z (beta = 0, p not read, pn not
 // written: the caller passes pn = z).
+// dyn: p and pn are the two buffers of the run-time alternation (p is read
+// from buffer sc->pp, pn written to the other; see k_cg_pq_tma)
 template <bool first>
 __global__ void __launch_bounds__(kBlock, 5)
-k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p, float *__restrict__ pn,
-        float *__restrict__ q, BicgScal *sc, double *partials, unsigned int *counter, int TK, int ichunk)
+k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *p_, float *pn_, float *__restrict__ q,
+        BicgScal *sc, double *partials, unsigned int *counter, int TK, int ichunk, int dyn = 0)
 {
     pdl_wait();
     pdl_allow();
     if (sc->done) return;
+    const int sel = dyn ? sc->pp : 0;
+    const float *__restrict__ p = dyn ? (sel ? pn_ : p_) : p_;
+    float *__restrict__ pn = dyn ? (sel ? const_cast<float *>(p_) : pn_) : pn_;
     const SpeOp<float> &A = F.A;
     const int TJ = kBlock / TK, SW = TK + 2;
     const int t = threadIdx.x, tk = t % TK, tj = t / TK;
@@ -663,8 +669,9 @@ k_cg_pq(FvOp<float> F, const float *__restrict__ z, const float *__restrict__ p,
         }
         __syncthreads();  // the next item rewrites both planes
     }
-    double acc[2] = {(double)pa, (double)pz}, tot[2];
-    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    float acc[2] = {pa, pz};
+    double tot[2];
+    if (grid_reduce_f<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
         sc->alpha = sc->rho / tot[0];
         sc->qz = tot[1];
     }
@@ -748,11 +755,14 @@ struct CgTile {
     static constexpr size_t smem(int nv) { return 128 + (size_t)(kCgStages * nv + 3) * STRIDE + 128; }
 };
 
+// dyn: the two p buffers alternate at run time (sc->pp holds p; mp / pn_out
+// are buffer 0, mp2 / pn_out2 buffer 1): p is read from buffer pp and pn
+// written to the other, so a loop body of one iteration replays correctly
 template <bool first, int TK, bool FZ>
 __global__ void __launch_bounds__(kBlock)
 k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_constant__ CUtensorMap mp,
-            float *__restrict__ pn_out, float *__restrict__ q, BicgScal *sc, double *partials,
-            unsigned int *counter, int ichunk, long long wait_limit)
+            const __grid_constant__ CUtensorMap mp2, float *pn_out0, float *pn_out2, int dyn, float *__restrict__ q,
+            BicgScal *sc, double *partials, unsigned int *counter, int ichunk, long long wait_limit)
 {
     using G = CgTile<TK>;
     constexpr int NV = first ? 1 : 2;
@@ -760,6 +770,9 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
     pdl_wait();
     pdl_allow();
     if (sc->done) return;
+    const int sel = dyn ? sc->pp : 0;
+    const CUtensorMap *mpp = sel ? &mp2 : &mp;
+    float *__restrict__ pn_out = dyn ? (sel ? pn_out0 : pn_out2) : pn_out0;
     extern __shared__ unsigned char dsm[];
     const unsigned base = (smem_u32(dsm) + 127u) & ~127u;
     unsigned char *gbase = dsm + (base - smem_u32(dsm));
@@ -792,7 +805,7 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
         const unsigned bar = bars + 8 * st;
         mbar_expect_tx(bar, NV * G::BOXB);
         tma_load_3d(stage0 + (unsigned)(st * NV) * G::STRIDE, &mh, k0 - 4, j0 - 1, ip, bar);
-        if (!first) tma_load_3d(stage0 + (unsigned)(st * NV + 1) * G::STRIDE, &mp, k0 - 4, j0 - 1, ip, bar);
+        if (!first) tma_load_3d(stage0 + (unsigned)(st * NV + 1) * G::STRIDE, mpp, k0 - 4, j0 - 1, ip, bar);
     };
     // box position (row, float4 column) of halo item h
     auto halo_pos = [&](int h, int &row, int &col) {
@@ -960,8 +973,9 @@ k_cg_pq_tma(FvOp<float> F, const __grid_constant__ CUtensorMap mh, const __grid_
     if (t == 0 && bad) sc->wait_timeout = 1;
     // pn . q gives alpha; q . z (z as loaded) serves the flexible beta of
     // the multigrid-CG
-    double acc[2] = {(double)pa, (double)pz}, tot[2];
-    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    float acc[2] = {pa, pz};
+    double tot[2];
+    if (grid_reduce_f<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
         sc->alpha = sc->rho / tot[0];
         sc->qz = tot[1];
     }
@@ -1003,8 +1017,9 @@ k_cg_upd_fv(FvOp<float> F, float *__restrict__ e, const float *__restrict__ p, f
         pa = fmaf(hv.z, hv.z * __frcp_rn(cg_P(wx, sx, wy * wz.z, sy + sz.z)), pa);
         pa = fmaf(hv.w, hv.w * __frcp_rn(cg_P(wx, sx, wy * wz.w, sy + sz.w)), pa);
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    float acc[1] = {pa};
+    double tot[1];
+    if (grid_reduce_f<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
         const double rel = sqrt(fabs(tot[0]) / sc->r0n2);
         sc->relres = rel;
         if (rel < sc->tol) {
@@ -1057,8 +1072,9 @@ k_cg_upd(long long n, float *__restrict__ e, const float *__restrict__ p, float 
         z[r] = zv;
         pa = fmaf(hv, zv, pa);
     }
-    double acc[1] = {(double)pa}, tot[1];
-    if (grid_reduce<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
+    float acc[1] = {pa};
+    double tot[1];
+    if (grid_reduce_f<1>(acc, partials, counter, tot) && threadIdx.x == 0) {
         const double rel = sqrt(fabs(tot[0]) / sc->r0n2);
         sc->relres = rel;
         if (rel < sc->tol) {
@@ -1128,42 +1144,53 @@ static void cg_tma_launch_shape(const CgTma &t, const FvOp<float> &F, int &ichun
 
 template <bool first, int TK>
 static void launch_tma_t(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t, const CUtensorMap *mz,
-                         const CUtensorMap *mp, float *pn, float *q, BicgScal *sc, bool form_z)
+                         const CUtensorMap *mp, float *pn, float *q, BicgScal *sc, bool form_z,
+                         const CUtensorMap *mp2, float *pn2, int dyn)
 {
     int ichunk, grid;
     cg_tma_launch_shape(t, F, ichunk, grid);
     const size_t sm = CgTile<TK>::smem(first ? 1 : 2);
     if (form_z)
-        launch_pdl(k_cg_pq_tma<first, TK, true>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, pn, q, sc, c.partials,
-                   c.counter, ichunk, t.wait_limit);
+        launch_pdl(k_cg_pq_tma<first, TK, true>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, *mp2, pn, pn2, dyn, q,
+                   sc, c.partials, c.counter, ichunk, t.wait_limit);
     else
-        launch_pdl(k_cg_pq_tma<first, TK, false>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, pn, q, sc,
-                   c.partials, c.counter, ichunk, t.wait_limit);
+        launch_pdl(k_cg_pq_tma<first, TK, false>, dim3(grid), dim3(kBlock), sm, c.s, F, *mz, *mp, *mp2, pn, pn2, dyn, q,
+                   sc, c.partials, c.counter, ichunk, t.wait_limit);
 }
 
 // z_map: the z vector (or p itself on the first iteration), p_map: p
+// dyn: p_map / pn are buffer 0 and p_map2 / pn2 buffer 1 of the run-time
+// alternation (k_cg_pq_tma)
 static void launch_cg_pq_tma(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma &t, bool first,
                              const CUtensorMap *z_map, const CUtensorMap *p_map, float *pn, float *q, BicgScal *sc,
-                             bool form_z)
+                             bool form_z, const CUtensorMap *p_map2 = nullptr, float *pn2 = nullptr, int dyn = 0)
 {
+    if (!p_map2) {
+        p_map2 = p_map;
+        pn2 = pn;
+    }
     if (t.TK == 32) {
-        if (first) launch_tma_t<true, 32>(c, F, t, z_map, p_map, pn, q, sc, form_z);
-        else launch_tma_t<false, 32>(c, F, t, z_map, p_map, pn, q, sc, form_z);
+        if (first) launch_tma_t<true, 32>(c, F, t, z_map, p_map, pn, q, sc, form_z, p_map2, pn2, dyn);
+        else launch_tma_t<false, 32>(c, F, t, z_map, p_map, pn, q, sc, form_z, p_map2, pn2, dyn);
     } else if (t.TK == 16) {
-        if (first) launch_tma_t<true, 16>(c, F, t, z_map, p_map, pn, q, sc, form_z);
-        else launch_tma_t<false, 16>(c, F, t, z_map, p_map, pn, q, sc, form_z);
+        if (first) launch_tma_t<true, 16>(c, F, t, z_map, p_map, pn, q, sc, form_z, p_map2, pn2, dyn);
+        else launch_tma_t<false, 16>(c, F, t, z_map, p_map, pn, q, sc, form_z, p_map2, pn2, dyn);
     } else {
-        if (first) launch_tma_t<true, 8>(c, F, t, z_map, p_map, pn, q, sc, form_z);
-        else launch_tma_t<false, 8>(c, F, t, z_map, p_map, pn, q, sc, form_z);
+        if (first) launch_tma_t<true, 8>(c, F, t, z_map, p_map, pn, q, sc, form_z, p_map2, pn2, dyn);
+        else launch_tma_t<false, 8>(c, F, t, z_map, p_map, pn, q, sc, form_z, p_map2, pn2, dyn);
     }
 }
 
 void launch_cg_pq_mg(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma *tma, float *z, float *p, float *p_alt,
-                     float *q, BicgScal *sc, int from, bool first)
+                     float *q, BicgScal *sc, int from, bool first, bool dyn)
 {
     float *P[2] = {p, p_alt};
     const int to = first ? from : 1 - from;
     if (tma && tma->ok) {
+        if (dyn && !first) {
+            launch_cg_pq_tma(c, F, *tma, false, &tma->zv, &tma->p, p, q, sc, false, &tma->palt, p_alt, 1);
+            return;
+        }
         const CUtensorMap *pmap = from == 0 ? &tma->p : &tma->palt;
         launch_cg_pq_tma(c, F, *tma, first, first ? pmap : &tma->zv, pmap, P[to], q, sc, false);
         return;
@@ -1171,10 +1198,13 @@ void launch_cg_pq_mg(cfd_launch_ctx &c, const FvOp<float> &F, const CgTma *tma, 
     const CgShape cs = cg_shape(c, F);
     if (first)
         launch_pdl(k_cg_pq<true>, dim3(cs.grid), dim3(kBlock), 0, c.s, F, (const float *)P[from],
-                   (const float *)P[from], P[from], q, sc, c.partials, c.counter, cs.TK, cs.ichunk);
+                   (const float *)P[from], P[from], q, sc, c.partials, c.counter, cs.TK, cs.ichunk, 0);
+    else if (dyn)
+        launch_pdl(k_cg_pq<false>, dim3(cs.grid), dim3(kBlock), 0, c.s, F, (const float *)z, (const float *)p, p_alt,
+                   q, sc, c.partials, c.counter, cs.TK, cs.ichunk, 1);
     else
         launch_pdl(k_cg_pq<false>, dim3(cs.grid), dim3(kBlock), 0, c.s, F, (const float *)z, (const float *)P[from],
-                   P[to], q, sc, c.partials, c.counter, cs.TK, cs.ichunk);
+                   P[to], q, sc, c.partials, c.counter, cs.TK, cs.ichunk, 0);
 }
 
 void launch_cg_iteration(cfd_launch_ctx &c, const FvOp<float> &F, const float *iP, float *e, float *h, float *z,
@@ -1689,11 +1719,60 @@ k_sor32(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta
     e[ic] = fmaf(omega, gs - eo, eo);
 }
 
+// The same colour update with one thread per k pair (k0 = GC + 2m, k0 + 1)
+// for even nz, where every pair starts on an 8-byte boundary: the thread
+// loads the pair and its four x / y neighbour pairs as float2 (whole sectors
+// for a warp) plus the one z neighbour outside the pair, and updates the cell
+// of the colour.  Same arithmetic as k_sor32.
+__global__ void __launch_bounds__(kBlock)
+k_sor32_pairs(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta, float *e, float omega,
+              int colour, const BicgScal *sc)
+{
+    if (*(volatile const int *)&sc->done != BICG_RUNNING) return;
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (unsigned)g.nyc * fpairs.d) return;
+    const unsigned jj = fpairs.div(t);
+    const int mm = (int)(t - jj * fpairs.d);
+    const int i = (int)blockIdx.y + GC, j = (int)jj + GC, k0 = GC + 2 * mm;
+    const int hi = (i + j + GC + colour) & 1;  // the colour's cell is k0 + hi
+    const int k = k0 + hi;
+    const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
+    const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
+    const long long i0 = icel(g, i, j, k0);
+    const float2 c = *reinterpret_cast<const float2 *>(e + i0);
+    const float2 xp = *reinterpret_cast<const float2 *>(e + i0 + g.sx);
+    const float2 xm = *reinterpret_cast<const float2 *>(e + i0 - g.sx);
+    const float2 yp = *reinterpret_cast<const float2 *>(e + i0 + g.sy);
+    const float2 ym = *reinterpret_cast<const float2 *>(e + i0 - g.sy);
+    const float zo = hi ? e[i0 + 2] : e[i0 - 1];  // the z neighbour outside the pair
+    const float eo = hi ? c.y : c.x;
+    const float zm = hi ? c.x : zo, zp = hi ? zo : c.y;
+    const float dx = m.x(AX_D, i), dy = m.y(AX_D, j), dz = m.z(AX_D, k);
+    const float yz = dy * dz, xz = dx * dz, xy = dx * dy;
+    const float c0 = yz * m.x(AX_RDS, i), c1 = yz * m.x(AX_RDS, i - 1);
+    const float c2 = xz * m.y(AX_RDS, j), c3 = xz * m.y(AX_RDS, j - 1);
+    const float c4 = xy * m.z(AX_RDS, k), c5 = xy * m.z(AX_RDS, k - 1);
+    float nb = c0 * (hi ? xp.y : xp.x);
+    nb = fmaf(c1, hi ? xm.y : xm.x, nb);
+    nb = fmaf(c2, hi ? yp.y : yp.x, nb);
+    nb = fmaf(c3, hi ? ym.y : ym.x, nb);
+    nb = fmaf(c4, zp, nb);
+    nb = fmaf(c5, zm, nb);
+    const float sum = ((c0 + c1) + (c2 + c3)) + (c4 + c5);
+    const float gs = fmaf(nb, __frcp_rn(sum), __ldg(delta + colour * nh + h));
+    e[i0 + hi] = fmaf(omega, gs - eo, eo);
+}
+
 void launch_sor32_sweep(cudaStream_t s, const Geo &g, const Metrics<float> &m, const float *delta, float *e,
                         float omega, const BicgScal *sc)
 {
     const FastDiv fp((unsigned)sor_pairs(g));
     const dim3 grid((unsigned)((g.nyc * sor_pairs(g) + kBlock - 1) / kBlock), (unsigned)g.nxc);
+    if (g.nzc % 2 == 0) {
+        k_sor32_pairs<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 0, sc);
+        k_sor32_pairs<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 1, sc);
+        return;
+    }
     k_sor32<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 0, sc);
     k_sor32<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 1, sc);
 }
@@ -1759,10 +1838,16 @@ k_residual64(Op A, const double *__restrict__ b, const double *__restrict__ x, V
         ra = fmaf((float)r, (float)r, ra);
         if constexpr (BN) bb = fma(bv, bv, bb);
     }
-    double acc[2] = {(double)ra, bb}, tot[2];
-    if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
-        *out = tot[0];
-        if (BN) *bout = tot[1];
+    if constexpr (BN) {
+        double acc[2] = {(double)ra, bb}, tot[2];
+        if (grid_reduce<2>(acc, partials, counter, tot) && threadIdx.x == 0) {
+            *out = tot[0];
+            *bout = tot[1];
+        }
+    } else {
+        float acc[1] = {ra};
+        double tot[1];
+        if (grid_reduce_f<1>(acc, partials, counter, tot) && threadIdx.x == 0) *out = tot[0];
     }
 }
 

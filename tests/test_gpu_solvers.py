@@ -205,11 +205,12 @@ def test_sor_fp32_sweeps_reach_the_fp64_fixed_point(oracle, name):
     sweeps, whose max change is the reference's stop test.  At a tight
     tolerance both runs reach the same fixed point, and the FP32 sweeps take
     about as many sweeps as FP64 ones (the count includes them; the stop test
-    runs once per loop body of 4 x check_every FP32 sweeps)."""
+    runs once per loop body of 4 x check_every FP32 sweeps).  The velocities
+    are FP32 values, so both contexts hold the same right-hand side."""
     w = _sor_workload(name)
     g = Grid.of(w, oracle)
     I = kernel_inputs(g.ng, g.n)
-    u1, v1, w1 = (0.01 * I[k] for k in ("u1", "v1", "w1"))
+    u1, v1, w1 = ((0.01 * I[k]).astype(np.float32).astype(np.float64) for k in ("u1", "v1", "w1"))
     out = {}
     for prec in (capi.PREC_FP64, capi.PREC_MIXED):
         with Simulation(w, solver=capi.SOLVER_SOR_RB, precision=prec, tol=1e-12, omega=1.7, sor_maxit=20000,
