@@ -456,7 +456,7 @@ int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
     const int cap = trip_cap(c, mixed ? (long long)itmax / (inner + 1) + 3 : (long long)itmax / batch + 3);
     const double omega = c->cfg.p_sor_omega, tol = c->cfg.p_criteria;
     auto head = [&]() -> int {
-        if (mixed) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.ng * sizeof(float), c->s));
+        if (mixed) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.n * sizeof(float), c->s));
         launch_sor_rhs_rb<T>(c->s, g, m, 1.0 / c->cfg.dt, dv<T>(c, si, 0), dv<T>(c, si, 1), dv<T>(c, si, 2),
                              c->sor_rhs, c->sc, c->sor_acc);
         return CFD_OK;
@@ -515,7 +515,8 @@ int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer, bo
     CK(cudaGetLastError());
     int st = poisson_solve(c, iters, relres, outer);
     if (st != CFD_OK && st != CFD_ERR_NOCONV) return st;
-    launch_transform(c->s, g, c->x, c->p);
+    if (c->ppair) launch_transform_pair(c->s, g, c->x, c->p, c->ppair);
+    else launch_transform(c->s, g, c->x, c->p);
     c->launches += 1;
     CK(cudaGetLastError());
     return st;
@@ -610,9 +611,12 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
             // the predictor passes feed f into the source; the final pass
             // stores f and reduces the drag and lift
             const bool last = pass == npass - 1;
+            // the float-pair pressure only where this pass's transform wrote
+            // it (a solve ran) and no ghost sync of p is needed (periodic z)
+            const float2 *pp = (c->ppair && c->loop > 1 && !g.pz) ? c->ppair : nullptr;
             launch_update_pass<T>(c->lc, g, m, metrics_of<double>(c), c->cfg.dt, c->p, static_cast<T *>(c->eta),
                                   u1, v1, w1, u3, v3, w3, f, last, last ? nullptr : src, c->cfg.lz,
-                                  last ? c->dscal + 1 : nullptr);
+                                  last ? c->dscal + 1 : nullptr, pp);
             c->launches += 1;
         } else {
             launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
@@ -944,6 +948,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         AL(c->jp32, n * 4);
         AL(c->jp32lo, n * 4);
         if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
+        AL(c->ppair, (size_t)g.ng * sizeof(float2));
     }
     if (!bicg) {
         AL(c->sor_cf, (size_t)(14 * sor_slots(g)) * sizeof(double));
@@ -952,7 +957,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         bool sweeps32 = c->fp32;
         if (const char *e = std::getenv("CFDGPU_SOR_FP32")) sweeps32 = sweeps32 && e[0] != '0';
         if (sweeps32) {
-            AL(c->sor_e, (size_t)g.ng * sizeof(float));
+            AL(c->sor_e, (size_t)g.n * sizeof(float));
             AL(c->sor_d, (size_t)(2 * sor_slots(g)) * sizeof(float));
         }
     }
@@ -1723,7 +1728,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                                                 (float)c->cfg.p_sor_omega, c->sc_t);
                          })) != CFD_OK)
             return st;
-        if (c->sor_e) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.ng * sizeof(float), c->s));
+        if (c->sor_e) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.n * sizeof(float), c->s));
     }
     st = dispatch(c, [&](auto tag) -> int {
         using T = typename decltype(tag)::type;
@@ -1772,7 +1777,8 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                      launch_update_pass<T>(c->lc, g, m, metrics_of<double>(c), c->cfg.dt, c->p,
                                            static_cast<T *>(c->eta), dv<T>(c, 2, 0), dv<T>(c, 2, 1), dv<T>(c, 2, 2),
                                            dv<T>(c, 1, 0), dv<T>(c, 1, 1), dv<T>(c, 1, 2), static_cast<T *>(c->f),
-                                           false, static_cast<T *>(c->src), c->cfg.lz, nullptr);
+                                           false, static_cast<T *>(c->src), c->cfg.lz, nullptr,
+                                           g.pz ? nullptr : c->ppair);
                  })) != CFD_OK)
                 return s2;
         }

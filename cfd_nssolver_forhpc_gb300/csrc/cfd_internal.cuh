@@ -206,12 +206,23 @@ __device__ __forceinline__ bool grid_reduce_tail(bool last, double *partials, un
     __threadfence();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps = (blockDim.x + 31) >> 5;
+    // four independent chains per thread, so the loads of a large grid's
+    // partials are in flight together rather than one after another
     double s[NV];
+    const int nb = (int)gridDim.x, bd = (int)blockDim.x;
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
-        s[q] = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-            s[q] += __ldcg(partials + q * gridDim.x + b);
+        const double *pq = partials + q * gridDim.x;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int b = threadIdx.x;
+        for (; b + 3 * bd < nb; b += 4 * bd) {
+            s0 += __ldcg(pq + b);
+            s1 += __ldcg(pq + b + bd);
+            s2 += __ldcg(pq + b + 2 * bd);
+            s3 += __ldcg(pq + b + 3 * bd);
+        }
+        for (; b < nb; b += bd) s0 += __ldcg(pq + b);
+        s[q] = (s0 + s1) + (s2 + s3);
     }
     warp_sum<NV>(s);
     __syncthreads();

@@ -122,7 +122,11 @@ struct cfd_ctx {
     // SOR
     double *sor_cf = nullptr, *sor_rhs = nullptr;  // colour-split SOR coefficients and right-hand side
     cfd::SorAcc *sor_acc = nullptr;
-    // mixed-precision SOR: the FP32 correction (ghosted, zero ghosts) and the
+    // mixed Krylov contexts: p as float pairs (ghosted layout, interior
+    // written by the transform after each solve), read by the projection of
+    // the same pass
+    float2 *ppair = nullptr;
+    // mixed-precision SOR: the FP32 correction (compact) and the
     // FP32 per-slot change of a Jacobi step; null where the sweeps stay FP64
     float *sor_e = nullptr, *sor_d = nullptr;
 

@@ -67,11 +67,13 @@ template <class T>
 void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const Metrics<float> &m32,
                  const PassArgs<T> &A, bool ghosts);
 // update_UandF of one pass with src += dt f (src != nullptr), f stored
-// (store_f) and Cd/Cl reduced into cdcl[0..1] (cdcl != nullptr)
+// (store_f) and Cd/Cl reduced into cdcl[0..1] (cdcl != nullptr).  pp: the
+// interior pressure as float pairs, valid for this pass (FP32 fields only;
+// null: the FP64 p)
 template <class T>
 void launch_update_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<T> &m, const Metrics<double> &m64, double dt,
                         const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3, T *v3, T *w3,
-                        T *f, bool store_f, T *src, double lz, double *cdcl);
+                        T *f, bool store_f, T *src, double lz, double *cdcl, const float2 *pp = nullptr);
 // lo[t] = the low float of a[t] as a float pair
 void launch_split_lo(cfd_launch_ctx &c, long long n, const double *a, float *lo);
 template <class T>
@@ -79,6 +81,8 @@ void launch_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, doubl
                 const double *jp, const T *u1, const T *v1, const T *w1, double *b, bool compat,
                 double *mean);
 void launch_transform(cudaStream_t s, const Geo &g, const double *x, double *p);
+// the transform, also writing p as float pairs pp[icel] (hi, lo)
+void launch_transform_pair(cudaStream_t s, const Geo &g, const double *x, double *p, float2 *pp);
 template <class T>
 void launch_update_uf(cudaStream_t s, const Geo &g, const Metrics<T> &m, double dt, T rdt,
                       const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3,
@@ -293,7 +297,7 @@ void launch_sor_rb_colour(cudaStream_t s, const Geo &g, const double *cf, const 
 // Mixed-precision SOR: FP32 sweeps on the correction inside an FP64 defect
 // correction.  delta = p_new - p at every cell (the change one Jacobi step
 // would make, FP64, stored in FP32 colour-split slots); then SOR sweeps in
-// FP32 on e (ghosted, zero ghosts) for  e = delta + (sum c_q e_q) / sum c,
+// FP32 on e (compact, 0 beyond the interior) for  e = delta + (sum c_q e_q) / sum c,
 // the same equations shifted by p; then p += e, e = 0, and sc->iter +=
 // the FP32 sweeps run.  All return at once when sc->done.
 void launch_sor_delta(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, const double *p,
@@ -396,6 +400,7 @@ struct Mg {
     int nlev = 0, first_small = 0;
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
     int sweeps0 = 2; // ... on the finest level
+    int small_sweeps = 2;  // ... on the levels inside the single-block kernel
     bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
                              // post-colour each in one pass (float4 levels); measured slower
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve

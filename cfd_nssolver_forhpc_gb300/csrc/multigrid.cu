@@ -1196,6 +1196,8 @@ int mg_setup(cfd_ctx *c)
     if (const char *e = std::getenv("CFDGPU_MG_SWEEPS0")) G.sweeps0 = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_PAIRS")) G.pairs = std::atoi(e) > 0 ? std::atoi(e) : 1;
     if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS")) G.fuse_ends = std::atoi(e) != 0;
+    G.small_sweeps = G.sweeps;
+    if (const char *e = std::getenv("CFDGPU_MG_SMALL_SWEEPS")) G.small_sweeps = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
     float om = 1.f;  // smoother relaxation (1: Gauss-Seidel)
@@ -1313,8 +1315,8 @@ static MgSmall small_desc(const Mg &G, const int *done)
     S.done = done;
     S.first = G.first_small;
     S.nlev = G.nlev;
-    S.pre = G.sweeps;
-    S.post = G.sweeps;
+    S.pre = G.small_sweeps;
+    S.post = G.small_sweeps;
     S.cinv = G.cinv;
     S.image = G.image;
     for (int l = 0; l < G.nlev; ++l) S.lev[l] = G.lev[l];

@@ -1688,8 +1688,10 @@ void launch_sor_delta(cudaStream_t s, const Geo &g, const double *cf, const doub
     k_sor_delta<<<grid, kBlock, 0, s>>>(g, fp, cf, rhs, p, delta, sc);
 }
 
-// one colour of an FP32 sweep on e; the coefficients are formed from the
-// FP32 axis tables (area / staggered distance), so only e and delta move
+// one colour of an FP32 sweep on e (compact, icelCal order: 4 B a cell, so
+// e and the per-slot change stay in L2 between sweeps); the coefficients are
+// formed from the FP32 axis tables (area / staggered distance), and e is 0
+// beyond the interior (the ghost pressures are fixed during a solve)
 __global__ void __launch_bounds__(kBlock)
 k_sor32(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta, float *e, float omega, int colour,
         const BicgScal *sc)
@@ -1701,29 +1703,29 @@ k_sor32(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta
     if (!sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) return;
     const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
     const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
-    const long long ic = icel(g, i, j, k);
+    const long long r = icelcal(g, i, j, k);
     const float dx = m.x(AX_D, i), dy = m.y(AX_D, j), dz = m.z(AX_D, k);
     const float yz = dy * dz, xz = dx * dz, xy = dx * dy;
     const float c0 = yz * m.x(AX_RDS, i), c1 = yz * m.x(AX_RDS, i - 1);
     const float c2 = xz * m.y(AX_RDS, j), c3 = xz * m.y(AX_RDS, j - 1);
     const float c4 = xy * m.z(AX_RDS, k), c5 = xy * m.z(AX_RDS, k - 1);
-    float nb = c0 * e[ic + g.sx];
-    nb = fmaf(c1, e[ic - g.sx], nb);
-    nb = fmaf(c2, e[ic + g.sy], nb);
-    nb = fmaf(c3, e[ic - g.sy], nb);
-    nb = fmaf(c4, e[ic + 1], nb);
-    nb = fmaf(c5, e[ic - 1], nb);
+    float nb = i < g.nx - GC - 1 ? c0 * e[r + g.sxc] : 0.f;
+    if (i > GC) nb = fmaf(c1, e[r - g.sxc], nb);
+    if (j < g.ny - GC - 1) nb = fmaf(c2, e[r + g.syc], nb);
+    if (j > GC) nb = fmaf(c3, e[r - g.syc], nb);
+    if (k < g.nz - GC - 1) nb = fmaf(c4, e[r + 1], nb);
+    if (k > GC) nb = fmaf(c5, e[r - 1], nb);
     const float sum = ((c0 + c1) + (c2 + c3)) + (c4 + c5);
     const float gs = fmaf(nb, __frcp_rn(sum), __ldg(delta + colour * nh + h));
-    const float eo = e[ic];
-    e[ic] = fmaf(omega, gs - eo, eo);
+    const float eo = e[r];
+    e[r] = fmaf(omega, gs - eo, eo);
 }
 
-// The same colour update with one thread per k pair (k0 = GC + 2m, k0 + 1)
-// for even nz, where every pair starts on an 8-byte boundary: the thread
-// loads the pair and its four x / y neighbour pairs as float2 (whole sectors
-// for a warp) plus the one z neighbour outside the pair, and updates the cell
-// of the colour.  Same arithmetic as k_sor32.
+// The same colour update with one thread per k pair (k0 = 2m, 2m + 1 of the
+// interior row) for even nzc, where every pair starts on an 8-byte
+// boundary: the thread loads the pair and its four x / y neighbour pairs as
+// float2 (whole sectors for a warp) plus the one z neighbour outside the
+// pair, and updates the cell of the colour.  Same arithmetic as k_sor32.
 __global__ void __launch_bounds__(kBlock)
 k_sor32_pairs(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta, float *e, float omega,
               int colour, const BicgScal *sc)
@@ -1738,13 +1740,15 @@ k_sor32_pairs(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__
     const int k = k0 + hi;
     const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
     const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
-    const long long i0 = icel(g, i, j, k0);
-    const float2 c = *reinterpret_cast<const float2 *>(e + i0);
-    const float2 xp = *reinterpret_cast<const float2 *>(e + i0 + g.sx);
-    const float2 xm = *reinterpret_cast<const float2 *>(e + i0 - g.sx);
-    const float2 yp = *reinterpret_cast<const float2 *>(e + i0 + g.sy);
-    const float2 ym = *reinterpret_cast<const float2 *>(e + i0 - g.sy);
-    const float zo = hi ? e[i0 + 2] : e[i0 - 1];  // the z neighbour outside the pair
+    const long long r0 = icelcal(g, i, j, k0);
+    const float2 zero = make_float2(0.f, 0.f);
+    const float2 c = *reinterpret_cast<const float2 *>(e + r0);
+    const float2 xp = i < g.nx - GC - 1 ? *reinterpret_cast<const float2 *>(e + r0 + g.sxc) : zero;
+    const float2 xm = i > GC ? *reinterpret_cast<const float2 *>(e + r0 - g.sxc) : zero;
+    const float2 yp = j < g.ny - GC - 1 ? *reinterpret_cast<const float2 *>(e + r0 + g.syc) : zero;
+    const float2 ym = j > GC ? *reinterpret_cast<const float2 *>(e + r0 - g.syc) : zero;
+    // the z neighbour outside the pair (0 beyond the interior)
+    const float zo = hi ? (k0 + 2 < g.nz - GC ? e[r0 + 2] : 0.f) : (k0 > GC ? e[r0 - 1] : 0.f);
     const float eo = hi ? c.y : c.x;
     const float zm = hi ? c.x : zo, zp = hi ? zo : c.y;
     const float dx = m.x(AX_D, i), dy = m.y(AX_D, j), dz = m.z(AX_D, k);
@@ -1760,7 +1764,7 @@ k_sor32_pairs(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__
     nb = fmaf(c5, zm, nb);
     const float sum = ((c0 + c1) + (c2 + c3)) + (c4 + c5);
     const float gs = fmaf(nb, __frcp_rn(sum), __ldg(delta + colour * nh + h));
-    e[i0 + hi] = fmaf(omega, gs - eo, eo);
+    e[r0 + hi] = fmaf(omega, gs - eo, eo);
 }
 
 void launch_sor32_sweep(cudaStream_t s, const Geo &g, const Metrics<float> &m, const float *delta, float *e,
@@ -1787,8 +1791,8 @@ __global__ void k_sor_correct(Geo g, double *__restrict__ p, float *__restrict__
     const unsigned t32 = (unsigned)t;
     const unsigned ii = g.fsxc.div(t32), rem = t32 - ii * (unsigned)g.sxc, jj = g.fsyc.div(rem);
     const long long ic = icel(g, (int)ii + GC, (int)jj + GC, (int)(rem - jj * (unsigned)g.syc) + GC);
-    p[ic] += (double)e[ic];
-    e[ic] = 0.f;
+    p[ic] += (double)e[t];
+    e[t] = 0.f;
 }
 
 void launch_sor_correct(cudaStream_t s, const Geo &g, double *p, float *e, int sweeps, BicgScal *sc)
