@@ -82,9 +82,10 @@ SOR_BYTES_PER_CELL = 80
 # neighbour term, the right-hand side, the scale, the change, its product
 # with omega and the update
 SOR_FP64_OPS_PER_CELL = 16
-# the FP32 sweeps of the mixed path: the correction read and written, the
-# change of a Jacobi step read (coefficients from the axis tables)
-SOR32_BYTES_PER_CELL = 12
+# the FP32 sweeps of the mixed path (two colour passes of the level-0
+# smoother): per pass the correction read, half of it and half of the
+# right-hand side written / read
+SOR32_BYTES_PER_CELL = 16
 SOR32_PER_BODY = 4 * 16  # FP32 sweeps per loop body (4 x check_every)
 
 
@@ -636,18 +637,23 @@ def leg_c5(args):
     nck = run.get("checkpoints") or -(-n // interval)
     ck_bytes = (free1 - free2) / max(1, nck) if free2 < free1 else None
     base = (free0 - free1) - interval * tape_step
-    full_steps = 400
+    # the full run: 400 steps, J over the last 200; only the reversed window
+    # needs checkpoints (one at its start, then one per interval) and a tape
+    # of one interval
+    full_steps, reversed_steps = 400, 200
     plan = None
     if ck_bytes:
         budget = 0.92 * total
         best = None
-        for I in range(1, full_steps + 1):
-            tot = base + I * tape_step + -(-full_steps // I) * ck_bytes
+        for I in range(1, reversed_steps + 1):
+            nck_full = -(-reversed_steps // I)
+            tot = base + I * tape_step + nck_full * ck_bytes
+            # fewest recomputed steps (one forward of the window) first, then memory
             if tot <= budget and (best is None or tot < best[1]):
-                best = (I, tot)
+                best = (I, tot, nck_full)
         if best:
-            plan = {"interval": best[0], "checkpoints": -(-full_steps // best[0]),
-                    "device_bytes": int(best[1]), "of_total": round(best[1] / total, 3)}
+            plan = {"steps": full_steps, "reversed_steps": reversed_steps, "interval": best[0],
+                    "checkpoints": best[2], "device_bytes": int(best[1]), "of_total": round(best[1] / total, 3)}
     return {"leg": "c5",
             "workload": f"{w.name}: cylinder wake {w.nxc}x{w.nyc}x{w.nzc} ({w.n_cells} cells), Re {w.re:g}, "
                         f"dt {w.dt:g}, tol {w.tol:g}, mixed forward",

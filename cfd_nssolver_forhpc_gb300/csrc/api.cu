@@ -464,9 +464,8 @@ int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
     auto body = [&] {
         if (mixed) {
             launch_sor_rb_sweep(c->s, g, c->sor_cf, c->sor_rhs, c->p, omega, tol, itmax, c->sc, c->sor_acc);
-            launch_sor_delta(c->s, g, c->sor_cf, c->sor_rhs, c->p, c->sor_d, c->sc);
-            const Metrics<float> m32 = metrics_of<float>(c);
-            for (int q = 0; q < inner; ++q) launch_sor32_sweep(c->s, g, m32, c->sor_d, c->sor_e, (float)omega, c->sc);
+            launch_sor_residual(c->s, g, c->sor_cf, c->sor_rhs, c->p, c->sor_rho, c->sc);
+            for (int q = 0; q < inner; ++q) sor_smooth_sweep(c, &c->sc->done);
             launch_sor_correct(c->s, g, c->p, c->sor_e, inner, c->sc);
             return;
         }
@@ -761,6 +760,7 @@ int build_tables(cfd_ctx *c)
     if (c->sor_cf)
         launch_sor_coef_rb(c->s, g, c->rawp[3], c->rawp[4], c->rawp[5], c->rawp[6], c->rawp[7], c->rawp[8],
                            c->sor_cf);
+    if (c->sor_e) CKS(sor_level_setup(c, (float)c->cfg.p_sor_omega));
     // FP32 copies of the operator, each only where the context holds one (a
     // mixed-precision SOR context has none; FP64 contexts get them when a
     // defect-correction solve first needs them)
@@ -958,7 +958,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         if (const char *e = std::getenv("CFDGPU_SOR_FP32")) sweeps32 = sweeps32 && e[0] != '0';
         if (sweeps32) {
             AL(c->sor_e, (size_t)g.n * sizeof(float));
-            AL(c->sor_d, (size_t)(2 * sor_slots(g)) * sizeof(float));
+            AL(c->sor_rho, (size_t)g.n * sizeof(float));
         }
     }
     AL(c->sc, sizeof(BicgScal));
@@ -1723,10 +1723,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                                      c->sc_t, c->sor_acc);
              })) != CFD_OK)
             return st;
-        if (c->sor_e && (st = timed(CFD_KERNEL_SOR32_SWEEP, [&] {
-                             launch_sor32_sweep(c->s, g, metrics_of<float>(c), c->sor_d, c->sor_e,
-                                                (float)c->cfg.p_sor_omega, c->sc_t);
-                         })) != CFD_OK)
+        if (c->sor_e && (st = timed(CFD_KERNEL_SOR32_SWEEP, [&] { sor_smooth_sweep(c, &c->sc_t->done); })) != CFD_OK)
             return st;
         if (c->sor_e) CK(cudaMemsetAsync(c->sor_e, 0, (size_t)g.n * sizeof(float), c->s));
     }

@@ -58,6 +58,8 @@ int ensure_fp32_solver(cfd_ctx *c);
 int mg_setup(cfd_ctx *c);
 bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc = nullptr);
 bool mg_fuses_rho(const Mg &G);
+int sor_level_setup(cfd_ctx *c, float omega);
+void sor_smooth_sweep(cfd_ctx *c, const int *done);
 void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc);
 void mg_time_part(cfd_ctx *c, int part);
 long long mg_vcycle_launches(const Mg &G);
@@ -126,9 +128,10 @@ struct cfd_ctx {
     // written by the transform after each solve), read by the projection of
     // the same pass
     float2 *ppair = nullptr;
-    // mixed-precision SOR: the FP32 correction (compact) and the
-    // FP32 per-slot change of a Jacobi step; null where the sweeps stay FP64
-    float *sor_e = nullptr, *sor_d = nullptr;
+    // mixed-precision SOR: the FP32 correction and its right-hand side (the
+    // FP64 residual, both compact); null where the sweeps stay FP64
+    float *sor_e = nullptr, *sor_rho = nullptr;
+    cfd::MgLevel sor_lev{};  // the FP32 sweeps as the level-0 smoother (sor_level_setup)
 
     // scalars: [0] rhs mean, [1..2] cd/cl, [3] residual norm^2, [4] dot
     double *dscal = nullptr, *h_scal = nullptr;

@@ -295,15 +295,14 @@ void launch_sor_rb_sweep(cudaStream_t s, const Geo &g, const double *cf, const d
 void launch_sor_rb_colour(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, double *p,
                           double omega, double tol, int itmax, int colour, BicgScal *sc, SorAcc *acc);
 // Mixed-precision SOR: FP32 sweeps on the correction inside an FP64 defect
-// correction.  delta = p_new - p at every cell (the change one Jacobi step
-// would make, FP64, stored in FP32 colour-split slots); then SOR sweeps in
-// FP32 on e (compact, 0 beyond the interior) for  e = delta + (sum c_q e_q) / sum c,
-// the same equations shifted by p; then p += e, e = 0, and sc->iter +=
-// the FP32 sweeps run.  All return at once when sc->done.
-void launch_sor_delta(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, const double *p,
-                      float *delta, const BicgScal *sc);
-void launch_sor32_sweep(cudaStream_t s, const Geo &g, const Metrics<float> &m, const float *delta, float *e,
-                        float omega, const BicgScal *sc);
+// correction.  rho = sum_q c_q p_q - rhs - (sum c) p at every cell (FP64,
+// stored FP32, icelCal order), the right-hand side of the correction
+// equation (sum c) e - sum_q c_q e_q = rho (e = 0 beyond the interior), which
+// the level-0 smoother sweeps in FP32 (sor_smooth_sweep, multigrid.cu); then
+// p += e, e = 0, and sc->iter += the FP32 sweeps run.  All return at once
+// when sc->done.
+void launch_sor_residual(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, const double *p,
+                         float *rho, const BicgScal *sc);
 void launch_sor_correct(cudaStream_t s, const Geo &g, double *p, float *e, int sweeps, BicgScal *sc);
 
 // mixed precision pieces
@@ -373,6 +372,7 @@ struct MgLevel {
     FastDiv fyz, fz;      // division by ny*nz and nz
     FastDiv fyh, fh;      // division by ny*(nz/2) and nz/2 (cell pairs along k, nz even)
     FastDiv fyq, fq;      // division by ny*(nz/4) and nz/4 (cell quads along k, nz % 4 == 0)
+    FastDiv fy2q;         // division by (ny/2)*(nz/4) (pairs of quads in j, ny even)
     const float *cm[3], *cp[3], *sum[3], *w[3];  // per axis: -face, +face, cm + cp, width
     const float *rw[3];   // per axis: 1 / width
     float *x, *b;
@@ -382,6 +382,7 @@ struct MgLevel {
     bool quads;           // the float4 smoother applies (nz % 4 == 0, aligned arrays)
     int pz;               // 1: periodic in z (nz even: red-black stays a two-colouring)
     float om;             // smoother relaxation: x += om (x_gs - x); 1 is Gauss-Seidel
+    bool rows2;           // colour launches run k_mg_smooth4x2 (two j rows a thread)
 };
 constexpr int kMgSmallSmem = 200 * 1024;  // shared-memory bytes for the small levels' x and b
 struct MgSmall {
@@ -401,6 +402,8 @@ struct Mg {
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
     int sweeps0 = 2; // ... on the finest level
     int small_sweeps = 2;  // ... on the levels inside the single-block kernel
+    bool transfer4 = true; // float4-row restriction / prolongation where the levels allow
+    bool rows2 = false;    // colour launches of float4 levels with even ny: two j rows a thread
     bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
                              // post-colour each in one pass (float4 levels); measured slower
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve

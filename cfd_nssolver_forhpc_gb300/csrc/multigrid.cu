@@ -495,6 +495,68 @@ __global__ void __launch_bounds__(kBlock) k_mg_smooth4(MgLevel L, const float *b
                            (I)gridDim.x * blockDim.x);
 }
 
+// One colour over a float4 level with even ny, two j rows (j0, j0 + 1) of one
+// quad each per thread: the two rows are each other's y neighbours (whose
+// cells of the other colour this pass does not change), so a thread loads
+// four x rows, two y rows and the two b rows instead of two quads' worth of
+// six.  quad_update is smooth_quads' arithmetic term for term, so the pass
+// equals k_mg_smooth4 bit for bit.  Gauss-Seidel only (om == 1).
+template <class I, bool PZ>
+__global__ void __launch_bounds__(kBlock, 4) k_mg_smooth4x2(MgLevel L, const float *b, float *x, int color,
+                                                            int zero_init, const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    const int n4 = L.nz >> 2;
+    const I nq2 = (I)(L.n >> 3);
+    const I sx = (I)L.ny * L.nz, sy = L.nz;
+    for (I q = (I)blockIdx.x * blockDim.x + threadIdx.x; q < nq2; q += (I)gridDim.x * blockDim.x) {
+        const unsigned u = (unsigned)q;
+        const unsigned i = L.fy2q.div(u), r = u - i * (unsigned)((L.ny >> 1) * n4), jp = L.fq.div(r);
+        const int k0 = 4 * (int)(r - jp * (unsigned)n4);
+        const unsigned j0 = 2 * jp;
+        const I t0 = ((I)i * L.ny + j0) * L.nz + k0, t1 = t0 + sy;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 b0 = *reinterpret_cast<const float4 *>(b + t0), b1 = *reinterpret_cast<const float4 *>(b + t1);
+        float4 c0 = zero, c1 = zero, xm0 = zero, xm1 = zero, xp0 = zero, xp1 = zero, ym = zero, yp = zero;
+        float zl0 = 0.f, zh0 = 0.f, zl1 = 0.f, zh1 = 0.f;
+        if (!zero_init) {
+            c0 = *reinterpret_cast<const float4 *>(x + t0);
+            c1 = *reinterpret_cast<const float4 *>(x + t1);
+            if (i > 0) {
+                xm0 = *reinterpret_cast<const float4 *>(x + t0 - sx);
+                xm1 = *reinterpret_cast<const float4 *>(x + t1 - sx);
+            }
+            if ((int)i < L.nx - 1) {
+                xp0 = *reinterpret_cast<const float4 *>(x + t0 + sx);
+                xp1 = *reinterpret_cast<const float4 *>(x + t1 + sx);
+            }
+            if (j0 > 0) ym = *reinterpret_cast<const float4 *>(x + t0 - sy);
+            if ((int)j0 + 2 < L.ny) yp = *reinterpret_cast<const float4 *>(x + t1 + sy);
+            if (k0 > 0) {
+                zl0 = x[t0 - 1];
+                zl1 = x[t1 - 1];
+            } else if (PZ) {
+                zl0 = x[t0 + (L.nz - 1)];
+                zl1 = x[t1 + (L.nz - 1)];
+            }
+            if (k0 + 4 < L.nz) {
+                zh0 = x[t0 + 4];
+                zh1 = x[t1 + 4];
+            } else if (PZ) {
+                zh0 = x[t0 + 4 - L.nz];
+                zh1 = x[t1 + 4 - L.nz];
+            }
+        }
+        float4 o0, o1;
+        quad_update(L, i, j0, k0, b0, c0, xm0, xp0, ym, c1, zl0, zh0, color, o0);
+        quad_update(L, i, j0 + 1, k0, b1, c1, xm1, xp1, c0, yp, zl1, zh1, color, o1);
+        *reinterpret_cast<float4 *>(x + t0) = o0;
+        *reinterpret_cast<float4 *>(x + t1) = o1;
+    }
+}
+
 template <bool PZ>
 __global__ void __launch_bounds__(kBlock) k_mg_restrict(MgLevel F, MgLevel C, const float *bf, const float *xf,
                                                         float *bc, const int *done)
@@ -513,6 +575,104 @@ __global__ void __launch_bounds__(kBlock) k_mg_prolong(MgLevel F, MgLevel C, con
     pdl_allow();
     if (*done) return;
     prolong_level(F, C, xc, xf, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
+}
+
+// ---- transfers on float4 rows (2x2x2 coarsening, nz % 4 == 0) -------------
+// The restriction with one thread per pair of coarse cells along k: their
+// colour-0 children are one cell in each quad k0 = 4 kp .. 4 kp + 3 of the
+// four fine rows (2I + a, 2J + b), so the thread reads those four quads and
+// their neighbour quads as float4 (the smoother's pattern) instead of one
+// scalar per neighbour per child.  The sum runs over the rows in the order
+// of restrict_level and each term is formed with its operations, so the
+// result is the same bit for bit.
+template <bool PZ>
+__global__ void __launch_bounds__(kBlock)
+k_mg_restrict4(MgLevel F, MgLevel C, const float *__restrict__ bf, const float *__restrict__ xf, float *__restrict__ bc,
+               const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    const int ncp = C.nz >> 1;
+    const long long total = C.n >> 1;
+    const long long sx = (long long)F.ny * F.nz, sy = F.nz;
+    for (long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x; u < total;
+         u += (long long)gridDim.x * blockDim.x) {
+        const long long line = u / ncp;
+        const int kp = (int)(u - line * ncp);
+        const int I = (int)(line / C.ny), J = (int)(line - (long long)I * C.ny);
+        const int k0 = 4 * kp;
+        const float4 czm = __ldg(reinterpret_cast<const float4 *>(F.cm[2] + k0));
+        const float4 czp = __ldg(reinterpret_cast<const float4 *>(F.cp[2] + k0));
+        const float4 sz = __ldg(reinterpret_cast<const float4 *>(F.sum[2] + k0));
+        const float4 wz = __ldg(reinterpret_cast<const float4 *>(F.w[2] + k0));
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b2 = 0; b2 < 2; ++b2) {
+                const int i = 2 * I + a, j = 2 * J + b2;
+                const long long t = ((long long)i * F.ny + j) * F.nz + k0;
+                const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 xc = *reinterpret_cast<const float4 *>(xf + t);
+                const float4 xm = i > 0 ? *reinterpret_cast<const float4 *>(xf + t - sx) : zero;
+                const float4 xp = i < F.nx - 1 ? *reinterpret_cast<const float4 *>(xf + t + sx) : zero;
+                const float4 ym = j > 0 ? *reinterpret_cast<const float4 *>(xf + t - sy) : zero;
+                const float4 yp = j < F.ny - 1 ? *reinterpret_cast<const float4 *>(xf + t + sy) : zero;
+                const float zlo = k0 > 0 ? xf[t - 1] : (PZ ? xf[t + (F.nz - 1)] : 0.f);
+                const float zhi = k0 + 4 < F.nz ? xf[t + 4] : (PZ ? xf[t + 4 - F.nz] : 0.f);
+                const float4 bv = *reinterpret_cast<const float4 *>(bf + t);
+                const bool odd = ((i + j) & 1) != 0;  // the colour-0 cells: k0 + odd, k0 + odd + 2
+                auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+                const float cxm = __ldg(F.cm[0] + i), cxp = __ldg(F.cp[0] + i);
+                const float cym = __ldg(F.cm[1] + j), cyp = __ldg(F.cp[1] + j);
+                const float sxy = __ldg(F.sum[0] + i) + __ldg(F.sum[1] + j);
+                const float wxy = __ldg(F.w[0] + i) * __ldg(F.w[1] + j);
+                // mg_nb's terms in its order: x-, x+, y-, y+, z-, z+ (fmaf from 0)
+                float nA = fmaf(cxm, pick(xm.x, xm.y), 0.f);
+                nA = fmaf(cxp, pick(xp.x, xp.y), nA);
+                nA = fmaf(cym, pick(ym.x, ym.y), nA);
+                nA = fmaf(cyp, pick(yp.x, yp.y), nA);
+                nA = fmaf(pick(czm.x, czm.y), pick(zlo, xc.x), nA);
+                nA = fmaf(pick(czp.x, czp.y), pick(xc.y, xc.z), nA);
+                float nB = fmaf(cxm, pick(xm.z, xm.w), 0.f);
+                nB = fmaf(cxp, pick(xp.z, xp.w), nB);
+                nB = fmaf(cym, pick(ym.z, ym.w), nB);
+                nB = fmaf(cyp, pick(yp.z, yp.w), nB);
+                nB = fmaf(pick(czm.z, czm.w), pick(xc.y, xc.z), nB);
+                nB = fmaf(pick(czp.z, czp.w), pick(xc.w, zhi), nB);
+                const float dA = wxy * pick(wz.x, wz.y), dB = wxy * pick(wz.z, wz.w);
+                s0 += pick(bv.x, bv.y) - dA * ((sxy + pick(sz.x, sz.y)) * pick(xc.x, xc.y) - nA);
+                s1 += pick(bv.z, bv.w) - dB * ((sxy + pick(sz.z, sz.w)) * pick(xc.z, xc.w) - nB);
+            }
+        *reinterpret_cast<float2 *>(bc + ((long long)I * C.ny + J) * C.nz + 2 * kp) = make_float2(s0, s1);
+    }
+}
+
+// The prolongation with one thread per fine quad: its four cells take the
+// values of their two parents along k, one float4 read-add-write.
+__global__ void __launch_bounds__(kBlock)
+k_mg_prolong4(MgLevel F, MgLevel C, const float *__restrict__ xc, float *__restrict__ xf, const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    const int n4 = F.nz >> 2;
+    const long long nq = F.n >> 2;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nq;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long line = q / n4;
+        const int k0 = 4 * (int)(q - line * n4);
+        const int i = (int)(line / F.ny), j = (int)(line - (long long)i * F.ny);
+        const float2 v = __ldg(reinterpret_cast<const float2 *>(xc + ((long long)(i >> 1) * C.ny + (j >> 1)) * C.nz +
+                                                                (k0 >> 1)));
+        float4 x = reinterpret_cast<float4 *>(xf)[q];
+        x.x += v.x;
+        x.y += v.x;
+        x.z += v.y;
+        x.w += v.y;
+        reinterpret_cast<float4 *>(xf)[q] = x;
+    }
 }
 
 // ---- fused red-black sweep (grid-wide levels, nz % 4 == 0) ------------------
@@ -1053,6 +1213,7 @@ void set_divs(MgLevel &L)
     L.fh = FastDiv((unsigned)nh);
     const int nq = L.nz / 4 > 0 ? L.nz / 4 : 1;
     L.fyq = FastDiv((unsigned)(L.ny * nq));
+    L.fy2q = FastDiv((unsigned)((L.ny / 2 > 0 ? L.ny / 2 : 1) * nq));
     L.fq = FastDiv((unsigned)nq);
     // float4 rows need nz % 4 == 0 and 16-byte aligned z-axis tables
     auto al = [](const void *p) { return (reinterpret_cast<unsigned long long>(p) & 15ull) == 0; };
@@ -1197,6 +1358,8 @@ int mg_setup(cfd_ctx *c)
     if (const char *e = std::getenv("CFDGPU_MG_PAIRS")) G.pairs = std::atoi(e) > 0 ? std::atoi(e) : 1;
     if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS")) G.fuse_ends = std::atoi(e) != 0;
     G.small_sweeps = G.sweeps;
+    if (const char *e = std::getenv("CFDGPU_MG_TRANSFER4")) G.transfer4 = e[0] != '0';
+    if (const char *e = std::getenv("CFDGPU_MG_ROWS2")) G.rows2 = e[0] != '0';
     if (const char *e = std::getenv("CFDGPU_MG_SMALL_SWEEPS")) G.small_sweeps = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
@@ -1261,6 +1424,10 @@ int mg_setup(cfd_ctx *c)
         G.lev[nl++] = L;
     }
     G.nlev = nl;
+    for (int l = 0; l < nl; ++l) {
+        MgLevel &L = G.lev[l];
+        L.rows2 = G.rows2 && L.quads && L.ny % 2 == 0 && L.om == 1.f;
+    }
     const long long ncoarse = G.lev[nl - 1].n;
     G.usable = nl > 1 && ncoarse <= kMgCoarsest;
     if (!G.usable) return CFD_OK;
@@ -1287,13 +1454,18 @@ int mg_setup(cfd_ctx *c)
     // for the two colour launches (the plane march is latency-bound)
     bool fused = false;
     if (const char *e = std::getenv("CFDGPU_MG_FUSED")) fused = std::atoi(e) != 0;
+    int fused_from = 0;  // the first level that runs fused sweeps
+    if (const char *e = std::getenv("CFDGPU_MG_FUSED_FROM")) {
+        fused = true;
+        fused_from = std::max(0, std::atoi(e));
+    }
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     for (int l = 0; l < G.first_small; ++l) {
         MgLevel &L = G.lev[l];
         L.sweep_tj = L.sweep_ci = 0;
-        if (!fused || !L.quads || L.pz || L.om != 1.f || level_sweeps(G, l) % 2 != 0) continue;
+        if (!fused || l < fused_from || !L.quads || L.pz || L.om != 1.f || level_sweeps(G, l) % 2 != 0) continue;
         const int n4 = L.nz / 4;
         const int tj = std::max(1, std::min({128 / std::max(n4, 1), L.ny, 1024 / n4}));
         if (tj * n4 > 1024 || (long long)sweep_smem(tj, L.nz) > kSweepSmemMax) continue;
@@ -1413,6 +1585,16 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
 template <bool PZ>
 static void smooth_launch_t(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
 {
+    if (L.rows2 && L.n + (long long)L.ny * L.nz < (1LL << 31)) {
+        launch_pdl(k_mg_smooth4x2<int, PZ>, dim3(nblk(L.n / 8)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
+                   zero_init, done);
+        return;
+    }
+    if (L.rows2) {
+        launch_pdl(k_mg_smooth4x2<long long, PZ>, dim3(nblk(L.n / 8)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x,
+                   color, zero_init, done);
+        return;
+    }
     if (L.quads && L.n + (long long)L.ny * L.nz < (1LL << 31))
         launch_pdl(k_mg_smooth4<int, PZ>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
                    zero_init, done);
@@ -1430,8 +1612,23 @@ static void smooth_launch(const MgLevel &L, int color, int zero_init, const int 
     else smooth_launch_t<false>(L, color, zero_init, done, s);
 }
 
-static void restrict_launch(const MgLevel &F, const MgLevel &C, const int *done, cudaStream_t s, bool pdl = true)
+// the float4-row transfers apply: 2x2x2 coarsening of a float4 level whose
+// coarse level has an even nz (aligned float2 pairs), and the switch is on
+static bool transfers4(const Mg &G, const MgLevel &F, const MgLevel &C)
 {
+    return G.transfer4 && F.quads && F.nx == 2 * C.nx && F.ny == 2 * C.ny && F.nz == 2 * C.nz && C.nz % 2 == 0 &&
+           (reinterpret_cast<unsigned long long>(C.b) & 7ull) == 0 && (reinterpret_cast<unsigned long long>(C.x) & 7ull) == 0;
+}
+
+static void restrict_launch(const Mg &G, const MgLevel &F, const MgLevel &C, const int *done, cudaStream_t s,
+                            bool pdl = true)
+{
+    if (transfers4(G, F, C)) {
+        auto k4 = F.pz ? k_mg_restrict4<true> : k_mg_restrict4<false>;
+        if (pdl) launch_pdl(k4, dim3(nblk(C.n / 2)), dim3(kBlock), 0, s, F, C, (const float *)F.b, (const float *)F.x, C.b, done);
+        else k4<<<nblk(C.n / 2), kBlock, 0, s>>>(F, C, F.b, F.x, C.b, done);
+        return;
+    }
     auto k = F.pz ? k_mg_restrict<true> : k_mg_restrict<false>;
     if (pdl) launch_pdl(k, dim3(nblk(C.n)), dim3(kBlock), 0, s, F, C, (const float *)F.b, (const float *)F.x, C.b, done);
     else k<<<nblk(C.n), kBlock, 0, s>>>(F, C, F.b, F.x, C.b, done);
@@ -1465,7 +1662,7 @@ bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc)
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
         smooth_phase(G, l, true, done, s);
-        restrict_launch(L, G.lev[l + 1], done, s);
+        restrict_launch(G, L, G.lev[l + 1], done, s);
     }
     small_launch(G, done, s);
     for (int l = fs - 1; l >= 0; --l) {
@@ -1480,8 +1677,12 @@ bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc)
             smooth_phase(G, l, false, done, s, true, l == 0 && fuse_rho ? &rf : nullptr);
             continue;
         }
-        launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1],
-                   (const float *)G.lev[l + 1].x, L.x, done);
+        if (transfers4(G, L, G.lev[l + 1]))
+            launch_pdl(k_mg_prolong4, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
+                       (const float *)G.lev[l + 1].x, L.x, done);
+        else
+            launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1],
+                       (const float *)G.lev[l + 1].x, L.x, done);
         smooth_phase(G, l, false, done, s, false, l == 0 && fuse_rho ? &rf : nullptr);
     }
     c->launches += mg_vcycle_launches(G);
@@ -1497,7 +1698,9 @@ void mg_time_part(cfd_ctx *c, int part)
     const MgLevel &L = G.lev[0];
     const int *done = G.never;
     if (part == 0) smooth_launch(L, 0, 0, done, s);
-    else if (part == 1) restrict_launch(L, G.lev[1], done, s, false);
+    else if (part == 1) restrict_launch(G, L, G.lev[1], done, s, false);
+    else if (part == 2 && transfers4(G, L, G.lev[1]))
+        k_mg_prolong4<<<nblk(L.n / 4), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
     else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
     else if (part == 3) small_launch(G, done, s, false);
     else if (part == 5) {
@@ -1536,6 +1739,64 @@ void mg_upd(cfd_ctx *c, float *e, const float *p, float *h, const float *q, Bicg
 {
     launch_pdl(k_mg_upd, dim3(c->lc.red_blocks), dim3(kBlock), 0, c->s, c->g.n, e, p, h, q, sc, c->lc.partials,
                c->lc.counter, p2);
+}
+
+// ---- the FP32 sweeps of the mixed-precision SOR ---------------------------
+// The correction equation of the FP64 defect correction around SOR is
+// sum_c e - sum_q c_q e_q = rho with the SOR coefficients c_q = area /
+// staggered distance (SorPipeLine.seq.hpp:30-43) and e = 0 beyond the
+// interior (the ghost pressures are fixed during a solve).  Divided by the
+// cell volume it is the smoother's form e = (rho / dV + sum cm_q e_q) /
+// sum cm_q with per-axis cm = 1 / (D_i Ds_{i-1}), cp = 1 / (D_i Ds_i): the
+// boundary cells keep their coupling to the ghost in the diagonal, and the
+// smoother reads no neighbour beyond the level.  So one SOR sweep in FP32 is
+// the two colour passes of the level-0 smoother with relaxation omega.
+int sor_level_setup(cfd_ctx *c, float omega)
+{
+    const Geo &g = c->g;
+    MgLevel &L = c->sor_lev;
+    const int n[3] = {g.nxc, g.nyc, g.nzc};
+    const MgLevel old = L;
+    L = MgLevel{};
+    for (int a = 0; a < 3; ++a) L.cm[a] = old.cm[a];
+    for (int a = 0; a < 3; ++a) {
+        const std::vector<double> &D = c->hraw[3 + a], &Ds = c->hraw[6 + a];
+        const int m = n[a];
+        std::vector<float> all((size_t)5 * m);
+        for (int i = 0; i < m; ++i) {
+            const int gi = i + GC;
+            const double cm = 1.0 / (D[gi] * Ds[gi - 1]), cp = 1.0 / (D[gi] * Ds[gi]);
+            all[i] = (float)cm;
+            all[m + i] = (float)cp;
+            all[2 * m + i] = (float)(cm + cp);
+            all[3 * m + i] = (float)D[gi];
+            all[4 * m + i] = (float)(1.0 / D[gi]);
+        }
+        float *d = const_cast<float *>(L.cm[a]);  // new metrics reuse the tables
+        if (!d) CKS(dalloc_t(c, &d, all.size()));
+        CK(cudaMemcpy(d, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice));
+        L.cm[a] = d;
+        L.cp[a] = d + m;
+        L.sum[a] = d + 2 * m;
+        L.w[a] = d + 3 * m;
+        L.rw[a] = d + 4 * m;
+    }
+    L.nx = g.nxc; L.ny = g.nyc; L.nz = g.nzc; L.n = g.n;
+    L.x = c->sor_e;
+    L.b = c->sor_rho;
+    L.om = omega;
+    L.pz = 0;
+    set_divs(L);
+    L.rows2 = false;
+    return CFD_OK;
+}
+
+// one FP32 SOR sweep (colour 0, then 1) of the correction; returns at once
+// when *done
+void sor_smooth_sweep(cfd_ctx *c, const int *done)
+{
+    smooth_launch(c->sor_lev, 0, 0, done, c->s);
+    smooth_launch(c->sor_lev, 1, 0, done, c->s);
 }
 
 }  // namespace cfd

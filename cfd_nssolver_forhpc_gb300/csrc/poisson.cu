@@ -1653,9 +1653,13 @@ void launch_sor_rb_sweep(cudaStream_t s, const Geo &g, const double *cf, const d
 }
 
 // ---- mixed-precision SOR (the FP32 sweeps of an FP64 defect correction) ----
+// rho = sum_q c_q p_q - rhs - (sum c) p at every cell, FP64, stored in FP32
+// in icelCal order: the right-hand side of the correction equation
+// (sum c) e - sum_q c_q e_q = rho, whose solution added to p satisfies the
+// SOR equations (a Jacobi step would change p by rho / sum c)
 __global__ void __launch_bounds__(kBlock)
-k_sor_delta(Geo g, FastDiv fpairs, const double *__restrict__ cf, const double *__restrict__ rhs,
-            const double *__restrict__ p, float *__restrict__ delta, const BicgScal *sc)
+k_sor_residual(Geo g, FastDiv fpairs, const double *__restrict__ cf, const double *__restrict__ rhs,
+               const double *__restrict__ p, float *__restrict__ rho, const BicgScal *sc)
 {
     if (*(volatile const int *)&sc->done != BICG_RUNNING) return;
     const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1664,121 +1668,28 @@ k_sor_delta(Geo g, FastDiv fpairs, const double *__restrict__ cf, const double *
     const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
     const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
     int i, j, k;
-    if (!sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) {
-        delta[colour * nh + h] = 0.f;
-        return;
-    }
+    if (!sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) return;
     const double *c = cf + (long long)colour * 7 * nh + h;
     const long long ic = icel(g, i, j, k);
-    double s = __ldg(rhs + colour * nh + h);
-    s = fma(-p[ic + g.sx], __ldg(c), s);
-    s = fma(-p[ic - g.sx], __ldg(c + nh), s);
-    s = fma(-p[ic + g.sy], __ldg(c + 2 * nh), s);
-    s = fma(-p[ic - g.sy], __ldg(c + 3 * nh), s);
-    s = fma(-p[ic + 1], __ldg(c + 4 * nh), s);
-    s = fma(-p[ic - 1], __ldg(c + 5 * nh), s);
-    delta[colour * nh + h] = (float)fma(s, __ldg(c + 6 * nh), -p[ic]);
+    const double c0 = __ldg(c), c1 = __ldg(c + nh), c2 = __ldg(c + 2 * nh), c3 = __ldg(c + 3 * nh);
+    const double c4 = __ldg(c + 4 * nh), c5 = __ldg(c + 5 * nh);
+    double s = -__ldg(rhs + colour * nh + h);
+    s = fma(p[ic + g.sx], c0, s);
+    s = fma(p[ic - g.sx], c1, s);
+    s = fma(p[ic + g.sy], c2, s);
+    s = fma(p[ic - g.sy], c3, s);
+    s = fma(p[ic + 1], c4, s);
+    s = fma(p[ic - 1], c5, s);
+    const double sum = ((c0 + c1) + (c2 + c3)) + (c4 + c5);
+    rho[icelcal(g, i, j, k)] = (float)fma(-sum, p[ic], s);
 }
 
-void launch_sor_delta(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, const double *p,
-                      float *delta, const BicgScal *sc)
+void launch_sor_residual(cudaStream_t s, const Geo &g, const double *cf, const double *rhs, const double *p,
+                         float *rho, const BicgScal *sc)
 {
     const FastDiv fp((unsigned)sor_pairs(g));
     const dim3 grid((unsigned)((g.nyc * sor_pairs(g) + kBlock - 1) / kBlock), (unsigned)g.nxc, 2);
-    k_sor_delta<<<grid, kBlock, 0, s>>>(g, fp, cf, rhs, p, delta, sc);
-}
-
-// one colour of an FP32 sweep on e (compact, icelCal order: 4 B a cell, so
-// e and the per-slot change stay in L2 between sweeps); the coefficients are
-// formed from the FP32 axis tables (area / staggered distance), and e is 0
-// beyond the interior (the ghost pressures are fixed during a solve)
-__global__ void __launch_bounds__(kBlock)
-k_sor32(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta, float *e, float omega, int colour,
-        const BicgScal *sc)
-{
-    if (*(volatile const int *)&sc->done != BICG_RUNNING) return;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (unsigned)g.nyc * fpairs.d) return;
-    int i, j, k;
-    if (!sor_cell_of(g, fpairs, colour, blockIdx.y, t, i, j, k)) return;
-    const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
-    const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
-    const long long r = icelcal(g, i, j, k);
-    const float dx = m.x(AX_D, i), dy = m.y(AX_D, j), dz = m.z(AX_D, k);
-    const float yz = dy * dz, xz = dx * dz, xy = dx * dy;
-    const float c0 = yz * m.x(AX_RDS, i), c1 = yz * m.x(AX_RDS, i - 1);
-    const float c2 = xz * m.y(AX_RDS, j), c3 = xz * m.y(AX_RDS, j - 1);
-    const float c4 = xy * m.z(AX_RDS, k), c5 = xy * m.z(AX_RDS, k - 1);
-    float nb = i < g.nx - GC - 1 ? c0 * e[r + g.sxc] : 0.f;
-    if (i > GC) nb = fmaf(c1, e[r - g.sxc], nb);
-    if (j < g.ny - GC - 1) nb = fmaf(c2, e[r + g.syc], nb);
-    if (j > GC) nb = fmaf(c3, e[r - g.syc], nb);
-    if (k < g.nz - GC - 1) nb = fmaf(c4, e[r + 1], nb);
-    if (k > GC) nb = fmaf(c5, e[r - 1], nb);
-    const float sum = ((c0 + c1) + (c2 + c3)) + (c4 + c5);
-    const float gs = fmaf(nb, __frcp_rn(sum), __ldg(delta + colour * nh + h));
-    const float eo = e[r];
-    e[r] = fmaf(omega, gs - eo, eo);
-}
-
-// The same colour update with one thread per k pair (k0 = 2m, 2m + 1 of the
-// interior row) for even nzc, where every pair starts on an 8-byte
-// boundary: the thread loads the pair and its four x / y neighbour pairs as
-// float2 (whole sectors for a warp) plus the one z neighbour outside the
-// pair, and updates the cell of the colour.  Same arithmetic as k_sor32.
-__global__ void __launch_bounds__(kBlock)
-k_sor32_pairs(Geo g, FastDiv fpairs, Metrics<float> m, const float *__restrict__ delta, float *e, float omega,
-              int colour, const BicgScal *sc)
-{
-    if (*(volatile const int *)&sc->done != BICG_RUNNING) return;
-    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (unsigned)g.nyc * fpairs.d) return;
-    const unsigned jj = fpairs.div(t);
-    const int mm = (int)(t - jj * fpairs.d);
-    const int i = (int)blockIdx.y + GC, j = (int)jj + GC, k0 = GC + 2 * mm;
-    const int hi = (i + j + GC + colour) & 1;  // the colour's cell is k0 + hi
-    const int k = k0 + hi;
-    const long long nh = (long long)g.nxc * g.nyc * fpairs.d;
-    const long long h = (long long)blockIdx.y * g.nyc * fpairs.d + t;
-    const long long r0 = icelcal(g, i, j, k0);
-    const float2 zero = make_float2(0.f, 0.f);
-    const float2 c = *reinterpret_cast<const float2 *>(e + r0);
-    const float2 xp = i < g.nx - GC - 1 ? *reinterpret_cast<const float2 *>(e + r0 + g.sxc) : zero;
-    const float2 xm = i > GC ? *reinterpret_cast<const float2 *>(e + r0 - g.sxc) : zero;
-    const float2 yp = j < g.ny - GC - 1 ? *reinterpret_cast<const float2 *>(e + r0 + g.syc) : zero;
-    const float2 ym = j > GC ? *reinterpret_cast<const float2 *>(e + r0 - g.syc) : zero;
-    // the z neighbour outside the pair (0 beyond the interior)
-    const float zo = hi ? (k0 + 2 < g.nz - GC ? e[r0 + 2] : 0.f) : (k0 > GC ? e[r0 - 1] : 0.f);
-    const float eo = hi ? c.y : c.x;
-    const float zm = hi ? c.x : zo, zp = hi ? zo : c.y;
-    const float dx = m.x(AX_D, i), dy = m.y(AX_D, j), dz = m.z(AX_D, k);
-    const float yz = dy * dz, xz = dx * dz, xy = dx * dy;
-    const float c0 = yz * m.x(AX_RDS, i), c1 = yz * m.x(AX_RDS, i - 1);
-    const float c2 = xz * m.y(AX_RDS, j), c3 = xz * m.y(AX_RDS, j - 1);
-    const float c4 = xy * m.z(AX_RDS, k), c5 = xy * m.z(AX_RDS, k - 1);
-    float nb = c0 * (hi ? xp.y : xp.x);
-    nb = fmaf(c1, hi ? xm.y : xm.x, nb);
-    nb = fmaf(c2, hi ? yp.y : yp.x, nb);
-    nb = fmaf(c3, hi ? ym.y : ym.x, nb);
-    nb = fmaf(c4, zp, nb);
-    nb = fmaf(c5, zm, nb);
-    const float sum = ((c0 + c1) + (c2 + c3)) + (c4 + c5);
-    const float gs = fmaf(nb, __frcp_rn(sum), __ldg(delta + colour * nh + h));
-    e[r0 + hi] = fmaf(omega, gs - eo, eo);
-}
-
-void launch_sor32_sweep(cudaStream_t s, const Geo &g, const Metrics<float> &m, const float *delta, float *e,
-                        float omega, const BicgScal *sc)
-{
-    const FastDiv fp((unsigned)sor_pairs(g));
-    const dim3 grid((unsigned)((g.nyc * sor_pairs(g) + kBlock - 1) / kBlock), (unsigned)g.nxc);
-    if (g.nzc % 2 == 0) {
-        k_sor32_pairs<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 0, sc);
-        k_sor32_pairs<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 1, sc);
-        return;
-    }
-    k_sor32<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 0, sc);
-    k_sor32<<<grid, kBlock, 0, s>>>(g, fp, m, delta, e, omega, 1, sc);
+    k_sor_residual<<<grid, kBlock, 0, s>>>(g, fp, cf, rhs, p, rho, sc);
 }
 
 // p += e and e = 0 over the interior; the FP32 sweeps join the sweep count

@@ -1,12 +1,18 @@
-"""The V-cycle's fused sweep ends against the separate launches (GPU).
+"""Alternative forms of V-cycle kernels against the plain ones (GPU).
 
-On float4 levels the first pre-smoothing sweep (both colours from x = 0)
-and the prolongation with the first post-smoothing colour each run as one
-kernel.  The arithmetic is that of the separate launches term for term, so
-steps with and without the fusion (CFDGPU_MG_FUSE_ENDS=0) agree bit for bit,
-with the multigrid-preconditioned inner solve of the mixed path and with the
-FP64 defect-correction variant, on grids whose levels are all float4 rows
-and on one (periodic z) whose z axis stops coarsening early."""
+* Fused sweep ends (CFDGPU_MG_FUSE_ENDS=1, off by default): on float4 levels
+  the first pre-smoothing sweep (both colours from x = 0) and the
+  prolongation with the first post-smoothing colour each run as one kernel.
+* Float4-row transfers (default; CFDGPU_MG_TRANSFER4=0 gives the scalar
+  kernels): the restriction reads the children's rows as float4 quads, the
+  prolongation adds to one quad per thread.
+* Two-row colour launches (CFDGPU_MG_ROWS2=1): a thread updates one quad in
+  each of two neighbouring j rows.
+
+Both keep the arithmetic of the plain launches term for term, so steps agree
+bit for bit, with the multigrid-preconditioned inner solve of the mixed path
+and with the FP64 defect-correction variant, on grids whose levels are all
+float4 rows and on one (periodic z) whose z axis stops coarsening early."""
 from __future__ import annotations
 
 import os
@@ -22,9 +28,9 @@ from cfd_nssolver_forhpc_gb300.simulation import Simulation
 pytestmark = pytest.mark.gpu
 
 
-def _run(w, fuse, **kw):
-    old = os.environ.get("CFDGPU_MG_FUSE_ENDS")
-    os.environ["CFDGPU_MG_FUSE_ENDS"] = "1" if fuse else "0"
+def _run(w, fuse, var="CFDGPU_MG_FUSE_ENDS", **kw):
+    old = os.environ.get(var)
+    os.environ[var] = "1" if fuse else "0"
     try:
         with Simulation(w, tol=1e-10, **kw) as S:
             S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
@@ -32,9 +38,9 @@ def _run(w, fuse, **kw):
             return hist, {k: S.download(k) for k in ("U0", "V0", "W0", "P")}
     finally:
         if old is None:
-            del os.environ["CFDGPU_MG_FUSE_ENDS"]
+            del os.environ[var]
         else:
-            os.environ["CFDGPU_MG_FUSE_ENDS"] = old
+            os.environ[var] = old
 
 
 @pytest.mark.parametrize("precision,periodic", [(capi.PREC_MIXED, False), (capi.PREC_FP64_DC, False),
@@ -43,6 +49,29 @@ def test_fused_sweep_ends_bitwise(precision, periodic):
     w = WORKLOADS["c1"]
     h1, f1 = _run(w, True, precision=precision, periodic_z=periodic)
     h0, f0 = _run(w, False, precision=precision, periodic_z=periodic)
+    assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
+    assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
+    for k in f1:
+        np.testing.assert_array_equal(f1[k], f0[k], err_msg=k)
+
+
+@pytest.mark.parametrize("precision,periodic", [(capi.PREC_MIXED, False), (capi.PREC_FP64_DC, False),
+                                                (capi.PREC_MIXED, True)])
+def test_float4_transfers_bitwise(precision, periodic):
+    w = WORKLOADS["c1"]
+    h1, f1 = _run(w, True, "CFDGPU_MG_TRANSFER4", precision=precision, periodic_z=periodic)
+    h0, f0 = _run(w, False, "CFDGPU_MG_TRANSFER4", precision=precision, periodic_z=periodic)
+    assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
+    assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
+    for k in f1:
+        np.testing.assert_array_equal(f1[k], f0[k], err_msg=k)
+
+
+@pytest.mark.parametrize("precision,periodic", [(capi.PREC_MIXED, False), (capi.PREC_MIXED, True)])
+def test_two_row_smoother_bitwise(precision, periodic):
+    w = WORKLOADS["c1"]
+    h1, f1 = _run(w, True, "CFDGPU_MG_ROWS2", precision=precision, periodic_z=periodic)
+    h0, f0 = _run(w, False, "CFDGPU_MG_ROWS2", precision=precision, periodic_z=periodic)
     assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
     assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
     for k in f1:
