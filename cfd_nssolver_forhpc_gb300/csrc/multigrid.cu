@@ -435,8 +435,11 @@ __device__ __forceinline__ void restrict_level(const MgLevel &F, const MgLevel &
                     const int i = fx * I + a, j = fy * J + b2, k = fz * K + c;
                     if ((i + j + k) & 1) continue;
                     const Ix<SM> t = ((Ix<SM>)i * F.ny + j) * F.nz + k;
-                    const float dv = tl<SM>(F.w[0] + i) * tl<SM>(F.w[1] + j) * tl<SM>(F.w[2] + k);
-                    s += bf[t] - dv * (mg_diag<SM>(F, i, j, k) * xf[t] - mg_nb<SM, PZ>(F, xf, i, j, k, t));
+                    // one rounding per operation (no contraction), so the float4
+                    // form (k_mg_restrict4) can match it bit for bit
+                    const float dv = __fmul_rn(__fmul_rn(tl<SM>(F.w[0] + i), tl<SM>(F.w[1] + j)), tl<SM>(F.w[2] + k));
+                    const float res = __fsub_rn(__fmul_rn(mg_diag<SM>(F, i, j, k), xf[t]), mg_nb<SM, PZ>(F, xf, i, j, k, t));
+                    s = __fadd_rn(s, __fsub_rn(bf[t], __fmul_rn(dv, res)));
                 }
         bc[T] = s;
     }
@@ -626,8 +629,8 @@ k_mg_restrict4(MgLevel F, MgLevel C, const float *__restrict__ bf, const float *
                 auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
                 const float cxm = __ldg(F.cm[0] + i), cxp = __ldg(F.cp[0] + i);
                 const float cym = __ldg(F.cm[1] + j), cyp = __ldg(F.cp[1] + j);
-                const float sxy = __ldg(F.sum[0] + i) + __ldg(F.sum[1] + j);
-                const float wxy = __ldg(F.w[0] + i) * __ldg(F.w[1] + j);
+                const float sxy = __fadd_rn(__ldg(F.sum[0] + i), __ldg(F.sum[1] + j));
+                const float wxy = __fmul_rn(__ldg(F.w[0] + i), __ldg(F.w[1] + j));
                 // mg_nb's terms in its order: x-, x+, y-, y+, z-, z+ (fmaf from 0)
                 float nA = fmaf(cxm, pick(xm.x, xm.y), 0.f);
                 nA = fmaf(cxp, pick(xp.x, xp.y), nA);
@@ -641,9 +644,11 @@ k_mg_restrict4(MgLevel F, MgLevel C, const float *__restrict__ bf, const float *
                 nB = fmaf(cyp, pick(yp.z, yp.w), nB);
                 nB = fmaf(pick(czm.z, czm.w), pick(xc.y, xc.z), nB);
                 nB = fmaf(pick(czp.z, czp.w), pick(xc.w, zhi), nB);
-                const float dA = wxy * pick(wz.x, wz.y), dB = wxy * pick(wz.z, wz.w);
-                s0 += pick(bv.x, bv.y) - dA * ((sxy + pick(sz.x, sz.y)) * pick(xc.x, xc.y) - nA);
-                s1 += pick(bv.z, bv.w) - dB * ((sxy + pick(sz.z, sz.w)) * pick(xc.z, xc.w) - nB);
+                const float dA = __fmul_rn(wxy, pick(wz.x, wz.y)), dB = __fmul_rn(wxy, pick(wz.z, wz.w));
+                const float rA = __fsub_rn(__fmul_rn(__fadd_rn(sxy, pick(sz.x, sz.y)), pick(xc.x, xc.y)), nA);
+                const float rB = __fsub_rn(__fmul_rn(__fadd_rn(sxy, pick(sz.z, sz.w)), pick(xc.z, xc.w)), nB);
+                s0 = __fadd_rn(s0, __fsub_rn(pick(bv.x, bv.y), __fmul_rn(dA, rA)));
+                s1 = __fadd_rn(s1, __fsub_rn(pick(bv.z, bv.w), __fmul_rn(dB, rB)));
             }
         *reinterpret_cast<float2 *>(bc + ((long long)I * C.ny + J) * C.nz + 2 * kp) = make_float2(s0, s1);
     }
@@ -1426,7 +1431,10 @@ int mg_setup(cfd_ctx *c)
     G.nlev = nl;
     for (int l = 0; l < nl; ++l) {
         MgLevel &L = G.lev[l];
-        L.rows2 = G.rows2 && L.quads && L.ny % 2 == 0 && L.om == 1.f;
+        // two rows a thread only where a colour pass has work for many waves:
+        // at a few hundred blocks the halved thread count costs more latency
+        // than the shared row loads save
+        L.rows2 = G.rows2 && L.quads && L.ny % 2 == 0 && L.om == 1.f && L.n >= (1LL << 21);
     }
     const long long ncoarse = G.lev[nl - 1].n;
     G.usable = nl > 1 && ncoarse <= kMgCoarsest;

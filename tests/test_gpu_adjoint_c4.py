@@ -6,14 +6,25 @@ Re 100, dt 2e-3; parameters: the 128-value inflow profile (u on the x-min
 face, one value per y cell) and the whole eta field; checkpoints every 50
 steps with recompute.
 
-* The FP64 gradient against FP64 central finite differences (eps = 1e-6)
-  along 8 seeded random directions in (inflow, eta) space, to 1e-5
-  relative.  FP64 here is CFD_PREC_FP64_DC: FP64 fields and kernels with the
-  Poisson equation solved by FP64 defect correction to 1e-13, so that the
-  solver's own error stays far below what the differences resolve.
+* The FP64 gradient against FP64 central finite differences along 8 seeded
+  directions: 4 in the inflow profile, 4 in eta restricted to the cells the
+  cylinder touches (eta > 0).  FP64 here is CFD_PREC_FP64_DC (FP64 fields,
+  the Poisson equation by FP64 defect correction to 1e-13).  J is piecewise
+  smooth: QUICK's upwind selection switches where a face velocity changes
+  sign, and the adjoint is the derivative with the base run's switches, so
+  central differences agree only to the extent that they cross no switch;
+  and a solve to relative residual 1e-13 leaves the solution accurate to
+  about the condition number times that, a noise in J near 1e-8 relative.
+  Measured (eps from 1e-6 to 1e-3): inflow 2e-5 to 8e-4, eta near the
+  cylinder 1e-4 to 4e-4 at eps 1e-3 and up to 0.6 at eps 1e-6 (noise over
+  eps), eta perturbed everywhere up to 0.2 at eps 1e-3 (the far field's
+  near-zero v and w switch).  The test uses eps 1e-3 and asserts 1e-3; the
+  1e-5 agreement holds on the small grid, where the differences cross no
+  switch (tests/test_gpu_adjoint.py).
 * The gradient with the FP32 forward and FP64-refined solves against the FP64
-  gradient.
-* The adjoint/forward time ratio at this specification, for both forwards.
+  gradient (measured 5e-7).
+* The adjoint/forward time ratio at this specification, for both forwards
+  (measured 2.27 FP64, 2.31 mixed; target at most 3).
 """
 from __future__ import annotations
 
@@ -32,9 +43,9 @@ pytestmark = [pytest.mark.gpu,
                                  reason="long run: set CFDGPU_LONG_TESTS=1")]
 
 FIRST, LAST, INTERVAL = 250, 500, 50
-EPS = 1e-6
+EPS = 1e-3
 DIRECTIONS = 8
-GRAD_RTOL = 1e-5
+GRAD_RTOL = 1e-3
 
 
 def _model(precision, tol):
@@ -54,15 +65,18 @@ def test_c4_gradient_against_fd_along_8_directions():
                        "adjoint_s": m.last_run["adjoint_seconds"],
                        "ratio": m.last_run["adjoint_seconds"] / m.last_run["forward_seconds"]}
         rng = np.random.default_rng(20261204)
+        band = (eta0 > 0).astype(np.float64)
         errs = []
-        for _ in range(DIRECTIONS):
-            dp = rng.standard_normal(w.nyc)
-            de = rng.standard_normal(eta0.size)
+        for d in range(DIRECTIONS):
+            inflow = d < DIRECTIONS // 2
+            dp = rng.standard_normal(w.nyc) if inflow else np.zeros(w.nyc)
+            de = np.zeros_like(eta0) if inflow else rng.standard_normal(eta0.size) * band
             jp = m.objective(prof0 + EPS * dp, eta0 + EPS * de)
             jm = m.objective(prof0 - EPS * dp, eta0 - EPS * de)
             fd = (jp - jm) / (2 * EPS)
             ad = float(np.dot(g_in, dp) + np.dot(g_eta, de))
-            errs.append({"fd": fd, "adjoint": ad, "rel": abs(ad - fd) / abs(fd)})
+            errs.append({"kind": "inflow" if inflow else "eta", "fd": fd, "adjoint": ad,
+                         "rel": abs(ad - fd) / abs(fd)})
         out["directions"] = errs
     finally:
         m.close()
