@@ -514,8 +514,7 @@ int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer, bo
     CK(cudaGetLastError());
     int st = poisson_solve(c, iters, relres, outer);
     if (st != CFD_OK && st != CFD_ERR_NOCONV) return st;
-    if (c->ppair) launch_transform_pair(c->s, g, c->x, c->p, c->ppair);
-    else launch_transform(c->s, g, c->x, c->p);
+    launch_transform(c->s, g, c->x, c->p);
     c->launches += 1;
     CK(cudaGetLastError());
     return st;
@@ -610,12 +609,9 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
             // the predictor passes feed f into the source; the final pass
             // stores f and reduces the drag and lift
             const bool last = pass == npass - 1;
-            // the float-pair pressure only where this pass's transform wrote
-            // it (a solve ran) and no ghost sync of p is needed (periodic z)
-            const float2 *pp = (c->ppair && c->loop > 1 && !g.pz) ? c->ppair : nullptr;
             launch_update_pass<T>(c->lc, g, m, metrics_of<double>(c), c->cfg.dt, c->p, static_cast<T *>(c->eta),
                                   u1, v1, w1, u3, v3, w3, f, last, last ? nullptr : src, c->cfg.lz,
-                                  last ? c->dscal + 1 : nullptr, pp);
+                                  last ? c->dscal + 1 : nullptr);
             c->launches += 1;
         } else {
             launch_update_uf<T>(c->s, g, m, c->cfg.dt, (T)(1.0 / c->cfg.dt), c->p, static_cast<T *>(c->eta),
@@ -948,7 +944,6 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
         AL(c->jp32, n * 4);
         AL(c->jp32lo, n * 4);
         if (k.solver == CFD_SOLVER_BICG_ELL) AL(c->ell_vals32, (size_t)(7 * n) * sizeof(float));
-        AL(c->ppair, (size_t)g.ng * sizeof(float2));
     }
     if (!bicg) {
         AL(c->sor_cf, (size_t)(14 * sor_slots(g)) * sizeof(double));
@@ -1774,8 +1769,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                      launch_update_pass<T>(c->lc, g, m, metrics_of<double>(c), c->cfg.dt, c->p,
                                            static_cast<T *>(c->eta), dv<T>(c, 2, 0), dv<T>(c, 2, 1), dv<T>(c, 2, 2),
                                            dv<T>(c, 1, 0), dv<T>(c, 1, 1), dv<T>(c, 1, 2), static_cast<T *>(c->f),
-                                           false, static_cast<T *>(c->src), c->cfg.lz, nullptr,
-                                           g.pz ? nullptr : c->ppair);
+                                           false, static_cast<T *>(c->src), c->cfg.lz, nullptr);
                  })) != CFD_OK)
                 return s2;
         }

@@ -124,10 +124,6 @@ struct cfd_ctx {
     // SOR
     double *sor_cf = nullptr, *sor_rhs = nullptr;  // colour-split SOR coefficients and right-hand side
     cfd::SorAcc *sor_acc = nullptr;
-    // mixed Krylov contexts: p as float pairs (ghosted layout, interior
-    // written by the transform after each solve), read by the projection of
-    // the same pass
-    float2 *ppair = nullptr;
     // mixed-precision SOR: the FP32 correction and its right-hand side (the
     // FP64 residual, both compact); null where the sweeps stay FP64
     float *sor_e = nullptr, *sor_rho = nullptr;

@@ -424,7 +424,7 @@ k_update_pass(Geo g, Metrics<T> m, Metrics<double> m64, double dt, T rdt, const 
               const T *__restrict__ eta, const T *__restrict__ u1, const T *__restrict__ v1,
               const T *__restrict__ w1, T *__restrict__ u3, T *__restrict__ v3, T *__restrict__ w3,
               T *__restrict__ f, int store_f, T *__restrict__ src, T srcdt, double lz, double *partials,
-              unsigned int *counter, double *cdcl, const float2 *__restrict__ pp)
+              unsigned int *counter, double *cdcl)
 {
     double acc[2] = {0.0, 0.0};
     const float dtf = (float)dt;
@@ -433,43 +433,32 @@ k_update_pass(Geo g, Metrics<T> m, Metrics<double> m64, double dt, T rdt, const 
         int i, j, k;
         cell_of(g, t, i, j, k);
         const long long ic = icel(g, i, j, k);
-        const double pc = pp ? 0.0 : p[ic];
+        const double pc = p[ic];
         const T ec = eta[ic];
         // dt (p_nb - p_c): FP64 fields keep update_uf's arithmetic; FP32
         // fields take the FP64 difference to FP32 and scale it there (the FP64
         // pipe is the scarce one, and the product is rounded to FP32 anyway)
-        // with pp (p as float pairs, written by this pass's transform) the
-        // difference is formed in FP32: hi - hi is exact for neighbouring
-        // values within a factor 2, and rounded once otherwise, as the FP64
-        // difference taken to FP32 would be
-        auto grad = [&](double pn, long long qn) -> T {
-            if constexpr (sizeof(T) == sizeof(double)) {
-                return (T)(dt * (pn - pc));
-            } else {
-                if (pp) {
-                    const float2 a = __ldg(pp + qn), b = __ldg(pp + ic);
-                    return ((a.x - b.x) + (a.y - b.y)) * dtf;
-                }
-                return (T)(pn - pc) * dtf;
-            }
+        auto grad = [&](double pn) -> T {
+            if constexpr (sizeof(T) == sizeof(double)) return (T)(dt * (pn - pc));
+            else return (T)(pn - pc) * dtf;
         };
         T fv[3] = {T(0), T(0), T(0)};
         if (i < g.nx - GC - 1) {
-            const T T2 = u1[ic] - grad(pp ? 0.0 : p[ic + g.sx], ic + g.sx) * m.x(AX_RDS, i);
+            const T T2 = u1[ic] - grad(p[ic + g.sx]) * m.x(AX_RDS, i);
             const T ef = ec + (eta[ic + g.sx] - ec) * m.x(AX_IT, i);
             const T un = (T(1) - ef) * T2;
             u3[ic] = un;
             fv[0] = (un - T2) * rdt;
         }
         if (j < g.ny - GC - 1) {
-            const T T2 = v1[ic] - grad(pp ? 0.0 : p[ic + g.sy], ic + g.sy) * m.y(AX_RDS, j);
+            const T T2 = v1[ic] - grad(p[ic + g.sy]) * m.y(AX_RDS, j);
             const T ef = ec + (eta[ic + g.sy] - ec) * m.y(AX_IT, j);
             const T vn = (T(1) - ef) * T2;
             v3[ic] = vn;
             fv[1] = (vn - T2) * rdt;
         }
         if (k < g.nz - GC - 1 + g.pz) {
-            const T T2 = w1[ic] - grad(pp ? 0.0 : p[ic + 1], ic + 1) * m.z(AX_RDS, k);
+            const T T2 = w1[ic] - grad(p[ic + 1]) * m.z(AX_RDS, k);
             const T ef = ec + (eta[ic + 1] - ec) * m.z(AX_IT, k);
             const T wn = (T(1) - ef) * T2;
             w3[ic] = wn;
@@ -1122,38 +1111,17 @@ void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, cons
 template <class T>
 void launch_update_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<T> &m, const Metrics<double> &m64, double dt,
                         const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3, T *v3, T *w3,
-                        T *f, bool store_f, T *src, double lz, double *cdcl, const float2 *pp)
+                        T *f, bool store_f, T *src, double lz, double *cdcl)
 {
     // the drag/lift sums need k_cdcl's launch shape (the same sums, bit for bit)
     const int grid = cdcl ? c.red_blocks : (int)((g.n + kBlock - 1) / kBlock);
     k_update_pass<T><<<grid, kBlock, 0, c.s>>>(g, m, m64, dt, (T)(1.0 / dt), p, eta, u1, v1, w1, u3, v3, w3, f,
-                                               store_f ? 1 : 0, src, (T)dt, lz, c.partials, c.counter, cdcl,
-                                               sizeof(T) == sizeof(double) ? nullptr : pp);
+                                               store_f ? 1 : 0, src, (T)dt, lz, c.partials, c.counter, cdcl);
 }
 
 void launch_split_lo(cfd_launch_ctx &c, long long n, const double *a, float *lo)
 {
     k_split_lo<<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, a, lo);
-}
-
-// the same, also writing p as a float pair (hi, lo) for the FP32-field
-// projection of the same pass
-__global__ void k_transform_pair(Geo g, const double *__restrict__ x, double *__restrict__ p, float2 *__restrict__ pp)
-{
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.n) return;
-    int i, j, k;
-    cell_of(g, t, i, j, k);
-    const long long ic = icel(g, i, j, k);
-    const double v = x[t];
-    p[ic] = v;
-    const ff f = ff_of(v);
-    pp[ic] = make_float2(f.hi, f.lo);
-}
-
-void launch_transform_pair(cudaStream_t s, const Geo &g, const double *x, double *p, float2 *pp)
-{
-    k_transform_pair<<<nblk(g.n), kBlock, 0, s>>>(g, x, p, pp);
 }
 
 void launch_transform(cudaStream_t s, const Geo &g, const double *x, double *p)
@@ -1326,7 +1294,7 @@ void launch_link_copy(cfd_launch_ctx &c, long long n, const A *a, B *b)
     template void launch_update_pass<T>(cfd_launch_ctx &, const Geo &, const Metrics<T> &,        \
                                         const Metrics<double> &, double, const double *, const T *, \
                                         const T *, const T *, const T *, T *, T *, T *, T *, bool, \
-                                        T *, double, double *, const float2 *);                   \
+                                        T *, double, double *);                                   \
     template void launch_bc_main<T>(cudaStream_t, const Geo &, const BcTab &, T *, T *, T *,     \
                                     double *);                                                   \
     template void launch_bc_convective<T>(cfd_launch_ctx &, const Geo &, const Metrics<double> &, double,  \

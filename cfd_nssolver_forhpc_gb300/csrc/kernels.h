@@ -67,13 +67,11 @@ template <class T>
 void launch_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, const Metrics<float> &m32,
                  const PassArgs<T> &A, bool ghosts);
 // update_UandF of one pass with src += dt f (src != nullptr), f stored
-// (store_f) and Cd/Cl reduced into cdcl[0..1] (cdcl != nullptr).  pp: the
-// interior pressure as float pairs, valid for this pass (FP32 fields only;
-// null: the FP64 p)
+// (store_f) and Cd/Cl reduced into cdcl[0..1] (cdcl != nullptr)
 template <class T>
 void launch_update_pass(cfd_launch_ctx &c, const Geo &g, const Metrics<T> &m, const Metrics<double> &m64, double dt,
                         const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3, T *v3, T *w3,
-                        T *f, bool store_f, T *src, double lz, double *cdcl, const float2 *pp = nullptr);
+                        T *f, bool store_f, T *src, double lz, double *cdcl);
 // lo[t] = the low float of a[t] as a float pair
 void launch_split_lo(cfd_launch_ctx &c, long long n, const double *a, float *lo);
 template <class T>
@@ -81,8 +79,6 @@ void launch_rhs(cfd_launch_ctx &c, const Geo &g, const Metrics<double> &m, doubl
                 const double *jp, const T *u1, const T *v1, const T *w1, double *b, bool compat,
                 double *mean);
 void launch_transform(cudaStream_t s, const Geo &g, const double *x, double *p);
-// the transform, also writing p as float pairs pp[icel] (hi, lo)
-void launch_transform_pair(cudaStream_t s, const Geo &g, const double *x, double *p, float2 *pp);
 template <class T>
 void launch_update_uf(cudaStream_t s, const Geo &g, const Metrics<T> &m, double dt, T rdt,
                       const double *p, const T *eta, const T *u1, const T *v1, const T *w1, T *u3,
@@ -403,7 +399,7 @@ struct Mg {
     int sweeps0 = 2; // ... on the finest level
     int small_sweeps = 2;  // ... on the levels inside the single-block kernel
     bool transfer4 = true; // float4-row restriction / prolongation where the levels allow
-    bool rows2 = false;    // colour launches of float4 levels with even ny: two j rows a thread
+    bool rows2 = true;     // colour launches of large float4 levels with even ny: two j rows a thread
     bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
                              // post-colour each in one pass (float4 levels); measured slower
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve

@@ -6,8 +6,10 @@
 * Float4-row transfers (default; CFDGPU_MG_TRANSFER4=0 gives the scalar
   kernels): the restriction reads the children's rows as float4 quads, the
   prolongation adds to one quad per thread.
-* Two-row colour launches (CFDGPU_MG_ROWS2=1): a thread updates one quad in
-  each of two neighbouring j rows.
+* Two-row colour launches (default on levels of at least 2^21 cells;
+  CFDGPU_MG_ROWS2=0 turns them off): a thread updates one quad in each of two
+  neighbouring j rows.  c1's levels are below the size, so the test runs a
+  512x256x32 grid for one step.
 
 Both keep the arithmetic of the plain launches term for term, so steps agree
 bit for bit, with the multigrid-preconditioned inner solve of the mixed path
@@ -28,13 +30,13 @@ from cfd_nssolver_forhpc_gb300.simulation import Simulation
 pytestmark = pytest.mark.gpu
 
 
-def _run(w, fuse, var="CFDGPU_MG_FUSE_ENDS", **kw):
+def _run(w, fuse, var="CFDGPU_MG_FUSE_ENDS", steps=3, **kw):
     old = os.environ.get(var)
     os.environ[var] = "1" if fuse else "0"
     try:
         with Simulation(w, tol=1e-10, **kw) as S:
             S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
-            hist = [S.step() for _ in range(3)]
+            hist = [S.step() for _ in range(steps)]
             return hist, {k: S.download(k) for k in ("U0", "V0", "W0", "P")}
     finally:
         if old is None:
@@ -69,9 +71,9 @@ def test_float4_transfers_bitwise(precision, periodic):
 
 @pytest.mark.parametrize("precision,periodic", [(capi.PREC_MIXED, False), (capi.PREC_MIXED, True)])
 def test_two_row_smoother_bitwise(precision, periodic):
-    w = WORKLOADS["c1"]
-    h1, f1 = _run(w, True, "CFDGPU_MG_ROWS2", precision=precision, periodic_z=periodic)
-    h0, f0 = _run(w, False, "CFDGPU_MG_ROWS2", precision=precision, periodic_z=periodic)
+    w = WORKLOADS["c2"]
+    h1, f1 = _run(w, True, "CFDGPU_MG_ROWS2", precision=precision, periodic_z=periodic, steps=2)
+    h0, f0 = _run(w, False, "CFDGPU_MG_ROWS2", precision=precision, periodic_z=periodic, steps=2)
     assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
     assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
     for k in f1:
