@@ -1694,7 +1694,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                     const int ids[6] = {CFD_KERNEL_MG_SMOOTH, CFD_KERNEL_MG_RESTRICT, CFD_KERNEL_MG_PROLONG,
                                         CFD_KERNEL_MG_SMALL, CFD_KERNEL_MG_VCYCLE, CFD_KERNEL_MG_SWEEP};
                     for (int part = 0; part < 6; ++part)
-                        if (!((part < 3 || part == 5) && c->mg.first_small == 0) &&
+                        if (!((part < 3 || part == 5) && mg_grid_levels(c->mg) == 0) &&
                             !(part == 5 && c->mg.lev[0].sweep_tj == 0))
                             if ((st = timed(ids[part], [&] { mg_time_part(c, part); })) != CFD_OK) return st;
                     if ((st = timed(CFD_KERNEL_MG_UPD, [&] {

@@ -58,6 +58,7 @@ int ensure_fp32_solver(cfd_ctx *c);
 int mg_setup(cfd_ctx *c);
 bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc = nullptr);
 bool mg_fuses_rho(const Mg &G);
+int mg_grid_levels(const Mg &G);
 int sor_level_setup(cfd_ctx *c, float omega);
 void sor_smooth_sweep(cfd_ctx *c, const int *done);
 void mg_h(cfd_ctx *c, float *h, const double *rn2, BicgScal *sc);

@@ -393,13 +393,32 @@ struct MgSmall {
     int off[kMgMaxLevels];      // ... its x, then b (not part of the image)
     MgLevel lev[kMgMaxLevels];
 };
+// The coarse levels first..nlev-1 of a V-cycle in one thread-block cluster
+// of kClusterCtas CTAs (multigrid.cu, k_mg_cluster): CTA r owns the x planes
+// [r nx / C, (r + 1) nx / C) of every level in its shared memory, reads its
+// neighbours' boundary planes through distributed shared memory, and the
+// phases are separated by cluster barriers.
+constexpr int kClusterCtas = 8;
+constexpr int kClusterThreads = 1024;
+constexpr int kMgClusterSmem = 200 * 1024;  // shared memory a CTA may use for its slabs
+struct MgCluster {
+    int first, nlev, pre, post;
+    const int *done;
+    const float *cinv;           // dense inverse of the coarsest level (global), nc x nc
+    int off[kMgMaxLevels];       // per level: shared-memory float offset of the slab's x, then its b
+    int part_off;                // CTA partial sums (the coarsest level's mean)
+    MgLevel lev[kMgMaxLevels];
+};
 struct Mg {
     int nlev = 0, first_small = 0;
+    int first_cluster = 0;   // > 0: levels from it on run in k_mg_cluster (else the small kernel)
+    int cluster_smem = 0;    // its dynamic shared memory per CTA (bytes)
     int sweeps = 2;  // smoothing sweeps per level, before and after the coarse correction
     int sweeps0 = 2; // ... on the finest level
     int small_sweeps = 2;  // ... on the levels inside the single-block kernel
     bool transfer4 = true; // float4-row restriction / prolongation where the levels allow
     bool rows2 = true;     // colour launches of large float4 levels with even ny: two j rows a thread
+    bool cluster = true;   // the coarse levels in one thread-block cluster where they partition
     bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
                              // post-colour each in one pass (float4 levels); measured slower
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve

@@ -33,6 +33,8 @@
 
 #include "context.h"
 
+#include <cooperative_groups.h>
+
 using namespace cfd;
 
 namespace {
@@ -991,6 +993,201 @@ __global__ void __launch_bounds__(kSmallThreads) k_mg_small(MgSmall S)
     }
 }
 
+// ---- the coarse levels in one thread-block cluster ---------------------------
+namespace cgx = cooperative_groups;
+
+// The slab of level L that CTA `rank` of the cluster owns: planes
+// [rank P, (rank + 1) P) with P = nx / kClusterCtas, x then b in shared
+// memory at `base`; x of a plane outside the slab is read from the CTA that
+// owns it (distributed shared memory).
+struct ClusterSlab {
+    MgLevel L;
+    int P, i0;
+    float *x, *b;
+    __device__ __forceinline__ long long loc(int i, int j, int k) const
+    {
+        return ((long long)(i - i0) * L.ny + j) * L.nz + k;
+    }
+    __device__ __forceinline__ float xat(cgx::cluster_group &cl, int i, int j, int k) const
+    {
+        if (i >= i0 && i < i0 + P) return x[loc(i, j, k)];
+        const int r = i / P;
+        const float *rx = cl.map_shared_rank(x, r);
+        return rx[((long long)(i - r * P) * L.ny + j) * L.nz + k];
+    }
+};
+
+__device__ __forceinline__ ClusterSlab cluster_slab(const MgCluster &S, float *sm, int l, int rank)
+{
+    ClusterSlab c;
+    c.L = S.lev[l];
+    c.P = c.L.nx / kClusterCtas;
+    c.i0 = rank * c.P;
+    c.x = sm + S.off[l];
+    c.b = c.x + (long long)c.P * c.L.ny * c.L.nz;
+    return c;
+}
+
+// mg_nb with the slab accessor (the same terms in the same order)
+template <bool PZ>
+__device__ __forceinline__ float cluster_nb(const ClusterSlab &c, cgx::cluster_group &cl, int i, int j, int k)
+{
+    const MgLevel &L = c.L;
+    float s = 0.f;
+    if (i > 0) s = fmaf(__ldg(L.cm[0] + i), c.xat(cl, i - 1, j, k), s);
+    if (i < L.nx - 1) s = fmaf(__ldg(L.cp[0] + i), c.xat(cl, i + 1, j, k), s);
+    if (j > 0) s = fmaf(__ldg(L.cm[1] + j), c.x[c.loc(i, j - 1, k)], s);
+    if (j < L.ny - 1) s = fmaf(__ldg(L.cp[1] + j), c.x[c.loc(i, j + 1, k)], s);
+    if (k > 0) s = fmaf(__ldg(L.cm[2] + k), c.x[c.loc(i, j, k - 1)], s);
+    else if (PZ) s = fmaf(__ldg(L.cm[2] + k), c.x[c.loc(i, j, L.nz - 1)], s);
+    if (k < L.nz - 1) s = fmaf(__ldg(L.cp[2] + k), c.x[c.loc(i, j, k + 1)], s);
+    else if (PZ) s = fmaf(__ldg(L.cp[2] + k), c.x[c.loc(i, j, 0)], s);
+    return s;
+}
+
+// one colour over the slab (gs_cell's arithmetic); zero_init: from x = 0, the
+// other colour written as 0
+template <bool PZ>
+__device__ __forceinline__ void cluster_smooth(const ClusterSlab &c, cgx::cluster_group &cl, int color, bool zero_init)
+{
+    const MgLevel &L = c.L;
+    const int ny = L.ny, nz = L.nz;
+    const int cells = c.P * ny * nz;
+    for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+        const int li = t / (ny * nz), r = t - li * ny * nz, j = r / nz, k = r - j * nz;
+        const int i = c.i0 + li;
+        if (((i + j + k) & 1) != color) {
+            if (zero_init) c.x[t] = 0.f;
+            continue;
+        }
+        const float nb = zero_init ? 0.f : cluster_nb<PZ>(c, cl, i, j, k);
+        const float rv = __ldg(L.rw[0] + i) * __ldg(L.rw[1] + j) * __ldg(L.rw[2] + k);
+        const float dg = __ldg(L.sum[0] + i) + __ldg(L.sum[1] + j) + __ldg(L.sum[2] + k);
+        c.x[t] = fmaf(c.b[t], rv, nb) * smooth_rcp(dg);
+    }
+}
+
+// coarse b = sum over the colour-0 children of (b - M x) (restrict_level's
+// arithmetic, one rounding per operation), coarse slab from the fine one
+template <bool PZ>
+__device__ __forceinline__ void cluster_restrict(const ClusterSlab &f, const ClusterSlab &c, cgx::cluster_group &cl)
+{
+    const MgLevel &F = f.L, &C = c.L;
+    const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
+    const int cells = c.P * C.ny * C.nz;
+    for (int T = threadIdx.x; T < cells; T += blockDim.x) {
+        const int lI = T / (C.ny * C.nz), r = T - lI * C.ny * C.nz, J = r / C.nz, K = r - J * C.nz;
+        const int I = c.i0 + lI;
+        float s = 0.f;
+        for (int a = 0; a < fx; ++a)
+            for (int b2 = 0; b2 < fy; ++b2)
+                for (int cc = 0; cc < fz; ++cc) {
+                    const int i = fx * I + a, j = fy * J + b2, k = fz * K + cc;
+                    if ((i + j + k) & 1) continue;
+                    const long long t = f.loc(i, j, k);
+                    const float dv = __fmul_rn(__fmul_rn(__ldg(F.w[0] + i), __ldg(F.w[1] + j)), __ldg(F.w[2] + k));
+                    const float dg = __ldg(F.sum[0] + i) + __ldg(F.sum[1] + j) + __ldg(F.sum[2] + k);
+                    const float res = __fsub_rn(__fmul_rn(dg, f.x[t]), cluster_nb<PZ>(f, cl, i, j, k));
+                    s = __fadd_rn(s, __fsub_rn(f.b[t], __fmul_rn(dv, res)));
+                }
+        c.b[T] = s;
+    }
+}
+
+// fine x += coarse x (the parent is in the same CTA: the slabs nest)
+__device__ __forceinline__ void cluster_prolong(const ClusterSlab &f, const ClusterSlab &c)
+{
+    const MgLevel &F = f.L, &C = c.L;
+    const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
+    const int cells = f.P * F.ny * F.nz;
+    for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+        const int li = t / (F.ny * F.nz), r = t - li * F.ny * F.nz, j = r / F.nz, k = r - j * F.nz;
+        const int i = f.i0 + li;
+        f.x[t] += c.x[c.loc(i / fx, j / fy, k / fz)];
+    }
+}
+
+template <bool PZ>
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kClusterThreads, 1) k_mg_cluster(MgCluster S)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*S.done) return;  // the same decision in every CTA of the cluster
+    cgx::cluster_group cl = cgx::this_cluster();
+    const int rank = (int)cl.block_rank();
+    extern __shared__ float4 cluster_sm4[];
+    float *sm = reinterpret_cast<float *>(cluster_sm4);
+    const int first = S.first, last = S.nlev;
+    {
+        const ClusterSlab c = cluster_slab(S, sm, first, rank);
+        const int cells = c.P * c.L.ny * c.L.nz;
+        const float *gb = c.L.b + (long long)c.i0 * c.L.ny * c.L.nz;
+        for (int t = threadIdx.x; t < cells; t += blockDim.x) c.b[t] = gb[t];
+    }
+    __syncthreads();
+    for (int l = first; l < last - 1; ++l) {
+        const ClusterSlab c = cluster_slab(S, sm, l, rank);
+        for (int s = 0; s < S.pre; ++s) {
+            cluster_smooth<PZ>(c, cl, 0, s == 0);
+            cl.sync();
+            cluster_smooth<PZ>(c, cl, 1, false);
+            cl.sync();
+        }
+        cluster_restrict<PZ>(c, cluster_slab(S, sm, l + 1, rank), cl);
+        cl.sync();
+    }
+    {
+        // coarsest: x = C (b - mean b), C the regularised dense inverse; the
+        // mean from the CTAs' partial sums in rank order
+        const ClusterSlab c = cluster_slab(S, sm, last - 1, rank);
+        const int cells = c.P * c.L.ny * c.L.nz;
+        const int nc = (int)c.L.n;
+        __shared__ float red[kClusterThreads / 32];
+        float s = 0.f;
+        for (int t = threadIdx.x; t < cells; t += blockDim.x) s += c.b[t];
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float tot = 0.f;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += red[q];
+            sm[S.part_off] = tot;
+        }
+        cl.sync();
+        float tot = 0.f;
+        for (int r = 0; r < kClusterCtas; ++r) tot += *cl.map_shared_rank(sm + S.part_off, r);
+        const float mean = tot / (float)nc;
+        const int row0 = c.i0 * c.L.ny * c.L.nz;
+        for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+            const float *crow = S.cinv + (long long)(row0 + t) * nc;
+            float acc = 0.f;
+            for (int r = 0; r < kClusterCtas; ++r) {
+                const float *rb = cl.map_shared_rank(c.b, r);
+                for (int q = 0; q < cells; ++q) acc = fmaf(__ldg(crow + r * cells + q), rb[q] - mean, acc);
+            }
+            c.x[t] = acc;
+        }
+        cl.sync();
+    }
+    for (int l = last - 2; l >= first; --l) {
+        const ClusterSlab c = cluster_slab(S, sm, l, rank);
+        cluster_prolong(c, cluster_slab(S, sm, l + 1, rank));
+        cl.sync();
+        for (int s = 0; s < S.post; ++s) {
+            cluster_smooth<PZ>(c, cl, 1, false);
+            cl.sync();
+            cluster_smooth<PZ>(c, cl, 0, false);
+            cl.sync();
+        }
+    }
+    {
+        const ClusterSlab c = cluster_slab(S, sm, first, rank);
+        const int cells = c.P * c.L.ny * c.L.nz;
+        float *gx = c.L.x + (long long)c.i0 * c.L.ny * c.L.nz;
+        for (int t = threadIdx.x; t < cells; t += blockDim.x) gx[t] = c.x[t];
+    }
+}
+
 // ---- CG with the V-cycle preconditioner -------------------------------------
 // h = P r / |r| (in place): the Jacobi-scaled residual in the finite-volume
 // form, normalised by the FP64 residual norm (rn2 = |r|^2) so the FP32 solve
@@ -1455,6 +1652,42 @@ int mg_setup(cfd_ctx *c)
     CK(cudaFuncSetAttribute(k_mg_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
     CK(cudaFuncSetAttribute(k_mg_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMgSmallSmem));
     CKS(small_image(c, G));
+    // the coarse levels in one thread-block cluster, from the largest level
+    // whose own and coarser levels all split into kClusterCtas nesting x slabs
+    // that fit a CTA's shared memory (at most the small kernel's levels plus
+    // the grid-wide ones above them that fit)
+    G.first_cluster = 0;
+    if (const char *e = std::getenv("CFDGPU_MG_CLUSTER")) G.cluster = e[0] != '0';
+    if (G.cluster) {
+        for (int l = 1; l <= G.first_small && l < nl; ++l) {
+            long long floats = 0;
+            bool ok = true;
+            for (int q = l; q < nl && ok; ++q) {
+                const MgLevel &L = G.lev[q];
+                ok = L.nx % kClusterCtas == 0 && (q == l || G.lev[q - 1].nx % L.nx == 0);
+                floats += (2LL * (L.nx / kClusterCtas) * L.ny * L.nz + 3) & ~3LL;
+            }
+            floats += 4;
+            if (ok && floats * 4 <= kMgClusterSmem) {
+                G.first_cluster = l;
+                G.cluster_smem = (int)(floats * 4);
+                break;
+            }
+        }
+        if (G.first_cluster > 0) {
+            auto k = g.pz ? k_mg_cluster<true> : k_mg_cluster<false>;
+            CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, G.cluster_smem));
+            cudaLaunchConfig_t cfg{};
+            cfg.gridDim = dim3(kClusterCtas);
+            cfg.blockDim = dim3(kClusterThreads);
+            cfg.dynamicSmemBytes = (size_t)G.cluster_smem;
+            int nclusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&nclusters, k, &cfg) != cudaSuccess || nclusters < 1) {
+                cudaGetLastError();
+                G.first_cluster = 0;  // not co-schedulable here: the small kernel instead
+            }
+        }
+    }
     // fused sweeps on the grid-wide levels with float4 rows: about 128
     // threads a block (TJ rows x nz/4 quads), chunks of CI planes sized for
     // about six blocks per SM, a second x buffer each
@@ -1470,7 +1703,7 @@ int mg_setup(cfd_ctx *c)
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    for (int l = 0; l < G.first_small; ++l) {
+    for (int l = 0; l < mg_grid_levels(G); ++l) {
         MgLevel &L = G.lev[l];
         L.sweep_tj = L.sweep_ci = 0;
         if (!fused || l < fused_from || !L.quads || L.pz || L.om != 1.f || level_sweeps(G, l) % 2 != 0) continue;
@@ -1487,6 +1720,27 @@ int mg_setup(cfd_ctx *c)
     CKS(dalloc_t(c, &G.never, 1));
     CK(cudaMemset(G.never, 0, sizeof(int)));
     return CFD_OK;
+}
+
+static MgCluster cluster_desc(const Mg &G, const int *done)
+{
+    MgCluster S{};
+    S.first = G.first_cluster;
+    S.nlev = G.nlev;
+    S.pre = G.sweeps;
+    S.post = G.sweeps;
+    S.done = done;
+    S.cinv = G.cinv;
+    int acc = 0;
+    for (int l = 0; l < G.nlev; ++l) {
+        S.lev[l] = G.lev[l];
+        if (l < G.first_cluster) continue;
+        const MgLevel &L = G.lev[l];
+        S.off[l] = acc;
+        acc += (int)((2LL * (L.nx / kClusterCtas) * L.ny * L.nz + 3) & ~3LL);
+    }
+    S.part_off = acc;
+    return S;
 }
 
 static MgSmall small_desc(const Mg &G, const int *done)
@@ -1642,6 +1896,10 @@ static void restrict_launch(const Mg &G, const MgLevel &F, const MgLevel &C, con
     else k<<<nblk(C.n), kBlock, 0, s>>>(F, C, F.b, F.x, C.b, done);
 }
 
+// the coarse levels: the cluster kernel where the hierarchy allows, else the
+// single-block kernel of the small levels
+static void coarse_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl = true);
+
 static void small_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl = true)
 {
     auto k = G.lev[0].pz ? k_mg_small<true> : k_mg_small<false>;
@@ -1649,12 +1907,26 @@ static void small_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl 
     else k<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
 }
 
+static void coarse_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl)
+{
+    if (G.first_cluster == 0) {
+        small_launch(G, done, s, pdl);
+        return;
+    }
+    auto k = G.lev[0].pz ? k_mg_cluster<true> : k_mg_cluster<false>;
+    if (pdl) launch_pdl(k, dim3(kClusterCtas), dim3(kClusterThreads), G.cluster_smem, s, cluster_desc(G, done));
+    else k<<<kClusterCtas, kClusterThreads, G.cluster_smem, s>>>(cluster_desc(G, done));
+}
+
 // the CG's rho' can run inside the V-cycle's last launch: the finest level
 // is a grid-wide float4 level smoothed by colour launches
 bool mg_fuses_rho(const Mg &G)
 {
-    return G.first_small > 0 && G.lev[0].quads && G.lev[0].sweep_tj == 0;
+    return mg_grid_levels(G) > 0 && G.lev[0].quads && G.lev[0].sweep_tj == 0;
 }
+
+// the levels that run grid-wide launches (before the cluster or small kernel)
+int mg_grid_levels(const Mg &G) { return G.first_cluster > 0 ? G.first_cluster : G.first_small; }
 
 // z = V(h): one V-cycle; every kernel returns at once when *done.  With
 // rho_sc (done == &rho_sc->done) the CG's rho' = h . z and its scalar update
@@ -1664,7 +1936,7 @@ bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc)
 {
     Mg &G = c->mg;
     const cudaStream_t s = c->s;
-    const int fs = G.first_small;
+    const int fs = mg_grid_levels(G);
     const bool fuse_rho = rho_sc && mg_fuses_rho(G);
     const RhoFuse rf{rho_sc, c->lc.partials, c->lc.counter, (long long)kMaxReduce * c->lc.red_blocks};
     for (int l = 0; l < fs; ++l) {
@@ -1672,7 +1944,7 @@ bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc)
         smooth_phase(G, l, true, done, s);
         restrict_launch(G, L, G.lev[l + 1], done, s);
     }
-    small_launch(G, done, s);
+    coarse_launch(G, done, s);
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
         if (fused_ends(G, L)) {
@@ -1710,7 +1982,7 @@ void mg_time_part(cfd_ctx *c, int part)
     else if (part == 2 && transfers4(G, L, G.lev[1]))
         k_mg_prolong4<<<nblk(L.n / 4), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
     else if (part == 2) k_mg_prolong<<<nblk(G.lev[1].n), kBlock, 0, s>>>(L, G.lev[1], G.lev[1].x, L.x, done);
-    else if (part == 3) small_launch(G, done, s, false);
+    else if (part == 3) coarse_launch(G, done, s, false);
     else if (part == 5) {
         if (L.sweep_tj > 0) sweep_launch(L, L.x, L.xalt, 0, 0, done, s);
     }
@@ -1721,7 +1993,7 @@ void mg_time_part(cfd_ctx *c, int part)
 long long mg_vcycle_launches(const Mg &G)
 {
     long long n = 1;
-    for (int l = 0; l < G.first_small; ++l) {
+    for (int l = 0; l < mg_grid_levels(G); ++l) {
         const MgLevel &L = G.lev[l];
         // pre 2s - 1 (the first sweep in one launch), restriction, the
         // prolongation with the first post colour, then 2s - 1 colours

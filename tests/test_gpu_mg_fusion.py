@@ -6,6 +6,10 @@
 * Float4-row transfers (default; CFDGPU_MG_TRANSFER4=0 gives the scalar
   kernels): the restriction reads the children's rows as float4 quads, the
   prolongation adds to one quad per thread.
+* The coarse levels in one thread-block cluster (default where the hierarchy
+  splits into nesting x slabs; CFDGPU_MG_CLUSTER=0 gives the single-block
+  kernel of the small levels): a different summation in the coarsest solve,
+  so the runs agree to the solver tolerance rather than bit for bit.
 * Two-row colour launches (default on levels of at least 2^21 cells;
   CFDGPU_MG_ROWS2=0 turns them off): a thread updates one quad in each of two
   neighbouring j rows.  c1's levels are below the size, so the test runs a
@@ -78,3 +82,18 @@ def test_two_row_smoother_bitwise(precision, periodic):
     assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
     for k in f1:
         np.testing.assert_array_equal(f1[k], f0[k], err_msg=k)
+
+
+@pytest.mark.parametrize("name,precision,periodic", [("c1", capi.PREC_MIXED, False), ("c1", capi.PREC_FP64_DC, False),
+                                                     ("c1", capi.PREC_MIXED, True)])
+def test_cluster_coarse_levels_match_single_block(name, precision, periodic):
+    w = WORKLOADS[name]
+    h1, f1 = _run(w, True, "CFDGPU_MG_CLUSTER", precision=precision, periodic_z=periodic)
+    h0, f0 = _run(w, False, "CFDGPU_MG_CLUSTER", precision=precision, periodic_z=periodic)
+    np.testing.assert_allclose([h["cd"] for h in h1], [h["cd"] for h in h0], rtol=1e-8)
+    for a, b in zip(h1, h0):
+        assert all(abs(x - y) <= 2 for x, y in zip(a["iters"], b["iters"])), (a["iters"], b["iters"])
+        assert all(r < 1e-10 for r in a["relres"][1:] if r > 0)
+    for k in ("U0", "V0", "W0"):
+        d = np.abs(f1[k] - f0[k]).max() / np.abs(f0[k]).max()
+        assert d < 1e-6, (k, d)
