@@ -418,7 +418,8 @@ struct Mg {
     int small_sweeps = 2;  // ... on the levels inside the single-block kernel
     bool transfer4 = true; // float4-row restriction / prolongation where the levels allow
     bool rows2 = true;     // colour launches of large float4 levels with even ny: two j rows a thread
-    bool cluster = true;   // the coarse levels in one thread-block cluster where they partition
+    bool cluster = false;  // the coarse levels in one thread-block cluster where they partition;
+                           // measured slower than the launches and the small kernel it replaces
     bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
                              // post-colour each in one pass (float4 levels); measured slower
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve

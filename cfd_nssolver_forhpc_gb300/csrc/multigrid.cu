@@ -1045,17 +1045,57 @@ __device__ __forceinline__ float cluster_nb(const ClusterSlab &c, cgx::cluster_g
     return s;
 }
 
-// one colour over the slab (gs_cell's arithmetic); zero_init: from x = 0, the
-// other colour written as 0
+// x of the slab's neighbour plane i (i0 - 1 or i0 + P) as float4 rows
+__device__ __forceinline__ const float *cluster_plane(const ClusterSlab &c, cgx::cluster_group &cl, int i)
+{
+    if (i >= c.i0 && i < c.i0 + c.P) return c.x + (long long)(i - c.i0) * c.L.ny * c.L.nz;
+    const int r = i / c.P;
+    return cl.map_shared_rank(c.x, r) + (long long)(i - r * c.P) * c.L.ny * c.L.nz;
+}
+
+// one colour over the slab; zero_init: from x = 0, the other colour written
+// as 0.  Float4 levels: one thread a quad, quad_update's arithmetic (that of
+// smooth_quads); others: gs_cell's arithmetic cell by cell.
 template <bool PZ>
 __device__ __forceinline__ void cluster_smooth(const ClusterSlab &c, cgx::cluster_group &cl, int color, bool zero_init)
 {
     const MgLevel &L = c.L;
     const int ny = L.ny, nz = L.nz;
+    if (L.quads) {
+        const int n4 = nz >> 2;
+        const int quads = c.P * ny * n4;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int q = threadIdx.x; q < quads; q += blockDim.x) {
+            const unsigned u = (unsigned)q;
+            const unsigned li = L.fyq.div(u), r = u - li * (unsigned)(ny * n4), j = L.fq.div(r);
+            const int k0 = 4 * (int)(r - j * (unsigned)n4);
+            const int i = c.i0 + (int)li;
+            const int t = ((int)li * ny + (int)j) * nz + k0;
+            const float4 bv = *reinterpret_cast<const float4 *>(c.b + t);
+            float4 xc = zero, xm = zero, xp = zero, ym = zero, yp = zero;
+            float zlo = 0.f, zhi = 0.f;
+            if (!zero_init) {
+                xc = *reinterpret_cast<const float4 *>(c.x + t);
+                const int rowoff = (int)j * nz + k0;
+                if (i > 0) xm = *reinterpret_cast<const float4 *>(cluster_plane(c, cl, i - 1) + rowoff);
+                if (i < L.nx - 1) xp = *reinterpret_cast<const float4 *>(cluster_plane(c, cl, i + 1) + rowoff);
+                if (j > 0) ym = *reinterpret_cast<const float4 *>(c.x + t - nz);
+                if ((int)j < ny - 1) yp = *reinterpret_cast<const float4 *>(c.x + t + nz);
+                zlo = k0 > 0 ? c.x[t - 1] : (PZ ? c.x[t + nz - 1] : 0.f);
+                zhi = k0 + 4 < nz ? c.x[t + 4] : (PZ ? c.x[t + 4 - nz] : 0.f);
+            }
+            float4 out;
+            quad_update(L, (unsigned)i, j, k0, bv, xc, xm, xp, ym, yp, zlo, zhi, color, out);
+            *reinterpret_cast<float4 *>(c.x + t) = out;
+        }
+        return;
+    }
     const int cells = c.P * ny * nz;
     for (int t = threadIdx.x; t < cells; t += blockDim.x) {
-        const int li = t / (ny * nz), r = t - li * ny * nz, j = r / nz, k = r - j * nz;
-        const int i = c.i0 + li;
+        const unsigned u = (unsigned)t;
+        const unsigned li = L.fyz.div(u), r = u - li * (unsigned)(ny * nz), jj = L.fz.div(r);
+        const int j = (int)jj, k = (int)(r - jj * (unsigned)nz);
+        const int i = c.i0 + (int)li;
         if (((i + j + k) & 1) != color) {
             if (zero_init) c.x[t] = 0.f;
             continue;
@@ -1076,8 +1116,10 @@ __device__ __forceinline__ void cluster_restrict(const ClusterSlab &f, const Clu
     const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
     const int cells = c.P * C.ny * C.nz;
     for (int T = threadIdx.x; T < cells; T += blockDim.x) {
-        const int lI = T / (C.ny * C.nz), r = T - lI * C.ny * C.nz, J = r / C.nz, K = r - J * C.nz;
-        const int I = c.i0 + lI;
+        const unsigned u = (unsigned)T;
+        const unsigned lI = C.fyz.div(u), r = u - lI * (unsigned)(C.ny * C.nz), JJ = C.fz.div(r);
+        const int J = (int)JJ, K = (int)(r - JJ * (unsigned)C.nz);
+        const int I = c.i0 + (int)lI;
         float s = 0.f;
         for (int a = 0; a < fx; ++a)
             for (int b2 = 0; b2 < fy; ++b2)
@@ -1101,8 +1143,10 @@ __device__ __forceinline__ void cluster_prolong(const ClusterSlab &f, const Clus
     const int fx = F.nx / C.nx, fy = F.ny / C.ny, fz = F.nz / C.nz;
     const int cells = f.P * F.ny * F.nz;
     for (int t = threadIdx.x; t < cells; t += blockDim.x) {
-        const int li = t / (F.ny * F.nz), r = t - li * F.ny * F.nz, j = r / F.nz, k = r - j * F.nz;
-        const int i = f.i0 + li;
+        const unsigned u = (unsigned)t;
+        const unsigned li = F.fyz.div(u), r = u - li * (unsigned)(F.ny * F.nz), jj = F.fz.div(r);
+        const int j = (int)jj, k = (int)(r - jj * (unsigned)F.nz);
+        const int i = f.i0 + (int)li;
         f.x[t] += c.x[c.loc(i / fx, j / fy, k / fz)];
     }
 }

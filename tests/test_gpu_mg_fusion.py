@@ -6,10 +6,10 @@
 * Float4-row transfers (default; CFDGPU_MG_TRANSFER4=0 gives the scalar
   kernels): the restriction reads the children's rows as float4 quads, the
   prolongation adds to one quad per thread.
-* The coarse levels in one thread-block cluster (default where the hierarchy
-  splits into nesting x slabs; CFDGPU_MG_CLUSTER=0 gives the single-block
-  kernel of the small levels): a different summation in the coarsest solve,
-  so the runs agree to the solver tolerance rather than bit for bit.
+* The coarse levels in one thread-block cluster (CFDGPU_MG_CLUSTER=1, off by
+  default: measured slower; the single-block kernel of the small levels
+  otherwise): a different summation in the coarsest solve, so the runs agree
+  to the solver tolerance rather than bit for bit.
 * Two-row colour launches (default on levels of at least 2^21 cells;
   CFDGPU_MG_ROWS2=0 turns them off): a thread updates one quad in each of two
   neighbouring j rows.  c1's levels are below the size, so the test runs a
