@@ -99,6 +99,8 @@ def parse():
     ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="precision of the headline step (the other one is timed beside it)")
+    ap.add_argument("--inner-tol", type=float, default=1e-3,
+                    help="relative tolerance of each FP32 inner solve of the mixed defect correction")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip the other-precision comparison leg")
@@ -240,7 +242,8 @@ def build_sim(args, w, precision):
     solver = {"spe": capi.SOLVER_BICG_SPE, "ell": capi.SOLVER_BICG_ELL, "sor": capi.SOLVER_SOR_RB}[args.solver]
     prec = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
     maxit = args.fp64_maxit if precision == "fp64" else 5000
-    S = Simulation(w, solver=solver, precision=prec, tol=w.tol, check_every=16, maxit=maxit)
+    S = Simulation(w, solver=solver, precision=prec, tol=w.tol, check_every=16, maxit=maxit,
+                   inner_tol=args.inner_tol)
     S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
     return S
 
@@ -792,6 +795,8 @@ def main():
             "roofline": rl, "cpu_baseline": cpu, "clocks": clocks, "e2e": e2e,
             "gpu_launches": launches,
         }
+        if mixed:
+            line["config"]["inner_tol"] = args.inner_tol
         if other:
             line[other_prec] = other
             line["ratio_mixed_vs_fp64"] = other["ratio_mixed_vs_fp64"]

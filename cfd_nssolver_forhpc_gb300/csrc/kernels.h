@@ -361,7 +361,7 @@ void launch_adj_add(cfd_launch_ctx &c, long long n, double *a, const double *b);
 
 // ---- multigrid.cu: V-cycle preconditioner of the FP32 inner CG ----
 constexpr int kMgMaxLevels = 10;
-constexpr long long kMgSmall = 16384;  // levels at or below this size run in one block
+constexpr long long kMgSmall = 4096;  // levels at or below this size run in one block (larger ones as tiles)
 struct MgLevel {
     int nx, ny, nz;
     long long n;
@@ -379,6 +379,14 @@ struct MgLevel {
     int pz;               // 1: periodic in z (nz even: red-black stays a two-colouring)
     float om;             // smoother relaxation: x += om (x_gs - x); 1 is Gauss-Seidel
     bool rows2;           // colour launches run k_mg_smooth4x2 (two j rows a thread)
+};
+// A grid-wide level whose smoothing phases run as tiles with a recomputed
+// halo (multigrid.cu, k_mg_tile): tx == 0 where the level runs colour launches
+struct MgTile {
+    int tx, ty, h, sweeps;  // interior tile, halo (2 sweeps), sweeps of a phase
+    int wx, wy, n4;         // tile extent with halo, quads along k
+    int tiles_y;            // tiles along y
+    FastDiv fn4, fwy;       // division by n4 and wy
 };
 constexpr int kMgSmallSmem = 200 * 1024;  // shared-memory bytes for the small levels' x and b
 struct MgSmall {
@@ -420,8 +428,10 @@ struct Mg {
     bool rows2 = true;     // colour launches of large float4 levels with even ny: two j rows a thread
     bool cluster = false;  // the coarse levels in one thread-block cluster where they partition;
                            // measured slower than the launches and the small kernel it replaces
-    bool fuse_ends = false;  // the first pre-sweep from zero and the prolongation + first
-                             // post-colour each in one pass (float4 levels); measured slower
+    MgTile tile[kMgMaxLevels] = {};  // per grid-wide level: its phases as tiles (tx > 0)
+    int fuse_from = kMgMaxLevels;  // from this level down, the first pre-sweep from zero and the
+                                   // prolongation + first post-colour each in one pass (float4
+                                   // levels); off by default
     int pairs = 1;   // CG iteration pairs per loop body (graph replay) of the inner solve
     float *cinv = nullptr;
     bool usable = false;

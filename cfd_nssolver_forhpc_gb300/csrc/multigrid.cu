@@ -231,9 +231,47 @@ __device__ __forceinline__ void quad_of(const MgLevel &L, I q, unsigned &i, unsi
     t = ((I)i * L.ny + j) * L.nz + k0;
 }
 
+// the axis-table values a quad update reads: x- and x-faces, 1 / width and
+// the coefficient sum of its column (i, j) and of its k quad
+struct QuadTab {
+    float cxm, cxp, cym, cyp, rwx, rwy, sx, sy;
+    float4 czm, czp, rz, sz;
+};
+
 // the colour-`color` update of the two cells of a quad (offsets e0, e0 + 2)
-// from the quad's and its neighbours' values: smooth_quads' arithmetic, term
-// for term
+// from the quad's and its neighbours' values and its table values:
+// smooth_quads' arithmetic, term for term
+__device__ __forceinline__ void quad_update_t(const QuadTab &T, unsigned i, unsigned j, const float4 &bv,
+                                              const float4 &xc, const float4 &xm, const float4 &xp, const float4 &ym,
+                                              const float4 &yp, float zlo, float zhi, int color, float4 &out)
+{
+    const int e0 = (int)((color + i + j) & 1u);
+    const bool odd = e0 != 0;
+    auto pick = [odd](float a0, float a1) { return odd ? a1 : a0; };
+    const float bA = pick(bv.x, bv.y), bB = pick(bv.z, bv.w);
+    const float rxy = T.rwx * T.rwy;
+    const float sxy = T.sx + T.sy;
+    const float rA = rxy * pick(T.rz.x, T.rz.y), rB = rxy * pick(T.rz.z, T.rz.w);
+    const float dA = smooth_rcp(sxy + pick(T.sz.x, T.sz.y)), dB = smooth_rcp(sxy + pick(T.sz.z, T.sz.w));
+    float nA = T.cxm * pick(xm.x, xm.y);
+    nA = fmaf(T.cxp, pick(xp.x, xp.y), nA);
+    nA = fmaf(T.cym, pick(ym.x, ym.y), nA);
+    nA = fmaf(T.cyp, pick(yp.x, yp.y), nA);
+    nA = fmaf(pick(T.czm.x, T.czm.y), pick(zlo, xc.x), nA);
+    nA = fmaf(pick(T.czp.x, T.czp.y), pick(xc.y, xc.z), nA);
+    float nB = T.cxm * pick(xm.z, xm.w);
+    nB = fmaf(T.cxp, pick(xp.z, xp.w), nB);
+    nB = fmaf(T.cym, pick(ym.z, ym.w), nB);
+    nB = fmaf(T.cyp, pick(yp.z, yp.w), nB);
+    nB = fmaf(pick(T.czm.z, T.czm.w), pick(xc.y, xc.z), nB);
+    nB = fmaf(pick(T.czp.z, T.czp.w), pick(xc.w, zhi), nB);
+    const float vA = fmaf(bA, rA, nA) * dA, vB = fmaf(bB, rB, nB) * dB;
+    out = make_float4(odd ? xc.x : vA, odd ? vA : xc.y, odd ? xc.z : vB, odd ? vB : xc.w);
+}
+
+// the same with the tables read from the level as they are needed (the
+// grid-wide kernels: loading them all first costs the two-row kernel
+// registers)
 __device__ __forceinline__ void quad_update(const MgLevel &L, unsigned i, unsigned j, int k0, const float4 &bv,
                                             const float4 &xc, const float4 &xm, const float4 &xp, const float4 &ym,
                                             const float4 &yp, float zlo, float zhi, int color, float4 &out)
@@ -682,6 +720,208 @@ k_mg_prolong4(MgLevel F, MgLevel C, const float *__restrict__ xc, float *__restr
     }
 }
 
+// ---- tiled smoothing phases (grid-wide float4 levels) -----------------------
+// One block owns an interior tile of tx x ty columns (all of k) and holds it
+// with a halo of h = 2 s columns on each side (s sweeps) in shared memory, x
+// and b as float4 quads.  All 2 s colour passes of the phase run inside the
+// block over the tile: a pass needs the other colour at the four column
+// neighbours, so a value stays exact only one column further in from the
+// tile edge per pass, and after 2 s passes the interior holds what the
+// grid-wide colour launches produce.  The arithmetic is quad_update's (that
+// of k_mg_smooth4), and the transfers are those of k_mg_restrict4 and
+// k_mg_prolong4, term for term, so the level ends bit for bit as with the
+// separate launches.  Columns outside the level hold 0 and are never updated,
+// which is how the grid-wide launches read them.
+//   PRE: from x = 0 (the first colour-0 pass reads no neighbours), the
+//   pre-smoothing, then the restriction of the interior's children into the
+//   coarse b; the interior's x is stored.
+//   POST: x of the tile plus the coarse correction (the prolongation), the
+//   post-smoothing (colour 1 first); the interior's x is stored to a second
+//   buffer (xout = L.xalt), since other blocks still read the halo columns
+//   of this one from L.x; the prolongation into the finer level reads it.
+// One launch replaces the 2 s + 1 launches of the phase, each of which waits
+// for the whole level; the price is the halo recomputation.
+constexpr int kTileThreads = 512;
+constexpr long long kTileCells = 1 << 17;  // levels up to this size run their phases as tiles
+constexpr int kTileSmemMax = 160 * 1024;  // shared memory of a tile block at most
+
+// x and b of the tile, then its k tables (cm, cp, 1 / w, sum, w as float4
+// quads) and its column tables (the same five along x, then along y)
+__host__ inline size_t tile_smem(const MgTile &T)
+{
+    return (2ull * T.wx * T.wy * T.n4 + 5ull * T.n4) * sizeof(float4) + 5ull * (T.wx + T.wy) * sizeof(float);
+}
+
+template <bool PZ, bool PRE>
+__global__ void __launch_bounds__(kTileThreads, 2)
+k_mg_tile(MgLevel L, MgLevel C, MgTile T, float *__restrict__ xout, const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    extern __shared__ float4 tile_sm4[];
+    const int nq = T.wx * T.wy * T.n4;
+    float4 *xs = tile_sm4, *bs = tile_sm4 + nq;
+    const int ti = blockIdx.x / T.tiles_y, tj = blockIdx.x - ti * T.tiles_y;
+    const int i0 = ti * T.tx - T.h, j0 = tj * T.ty - T.h;  // global column of tile column 0
+    const int sq = T.wy * T.n4;                             // quad stride of a tile column along x
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    // the tables of the tile (0 outside the level, where nothing is updated)
+    float4 *tz = bs + nq;                                  // czm, czp, rz, sz, wz: n4 quads each
+    float *tx = reinterpret_cast<float *>(tz + 5 * T.n4);  // cm, cp, rw, sum, w: wx columns each
+    float *ty = tx + 5 * T.wx;                             // the same along y: wy each
+    for (int u = threadIdx.x; u < 5 * T.n4; u += blockDim.x) {
+        const int f = u / T.n4, kq = u - f * T.n4;
+        const float *src = f == 0 ? L.cm[2] : f == 1 ? L.cp[2] : f == 2 ? L.rw[2] : f == 3 ? L.sum[2] : L.w[2];
+        tz[u] = __ldg(reinterpret_cast<const float4 *>(src) + kq);
+    }
+    for (int u = threadIdx.x; u < 5 * (T.wx + T.wy); u += blockDim.x) {
+        const bool ax = u < 5 * T.wx;
+        const int v = ax ? u : u - 5 * T.wx, w = ax ? T.wx : T.wy;
+        const int f = v / w, c = v - f * w, g = (ax ? i0 : j0) + c, a = ax ? 0 : 1;
+        const float *src = f == 0 ? L.cm[a] : f == 1 ? L.cp[a] : f == 2 ? L.rw[a] : f == 3 ? L.sum[a] : L.w[a];
+        const bool in = g >= 0 && g < (ax ? L.nx : L.ny);
+        (ax ? tx : ty)[v] = in ? __ldg(src + g) : 0.f;
+    }
+    auto tab = [&](int a, int bb, int kq) {
+        QuadTab Q;
+        Q.cxm = tx[a];
+        Q.cxp = tx[T.wx + a];
+        Q.rwx = tx[2 * T.wx + a];
+        Q.sx = tx[3 * T.wx + a];
+        Q.cym = ty[bb];
+        Q.cyp = ty[T.wy + bb];
+        Q.rwy = ty[2 * T.wy + bb];
+        Q.sy = ty[3 * T.wy + bb];
+        Q.czm = tz[kq];
+        Q.czp = tz[T.n4 + kq];
+        Q.rz = tz[2 * T.n4 + kq];
+        Q.sz = tz[3 * T.n4 + kq];
+        return Q;
+    };
+    // tile quad q -> tile column (a, bb), quad kq along k
+    auto split = [&](int q, int &a, int &bb, int &kq) {
+        const unsigned c = T.fn4.div((unsigned)q);
+        kq = q - (int)c * T.n4;
+        a = (int)T.fwy.div(c);
+        bb = (int)c - a * T.wy;
+    };
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        int a, bb, kq;
+        split(q, a, bb, kq);
+        const int i = i0 + a, j = j0 + bb;
+        float4 xv = zero, bv = zero;
+        if (i >= 0 && i < L.nx && j >= 0 && j < L.ny) {
+            const long long t = ((long long)i * L.ny + j) * L.nz + 4 * kq;
+            bv = __ldg(reinterpret_cast<const float4 *>(L.b + t));
+            if (!PRE) {
+                xv = *reinterpret_cast<const float4 *>(L.x + t);
+                const float2 v = __ldg(reinterpret_cast<const float2 *>(
+                    C.x + ((long long)(i >> 1) * C.ny + (j >> 1)) * C.nz + 2 * kq));
+                xv.x += v.x;
+                xv.y += v.x;
+                xv.z += v.y;
+                xv.w += v.y;
+            }
+        }
+        xs[q] = xv;
+        bs[q] = bv;
+    }
+    __syncthreads();
+    const int passes = 2 * T.sweeps;
+    for (int p = 0; p < passes; ++p) {
+        // PRE: colours 0, 1, 0, 1 ...; pass p updates the columns at least p
+        // from the tile edge (pass 0, from zero, reads no neighbour), so after
+        // the last pass columns from h - 1 in are exact, as the restriction
+        // of the interior needs.  POST: colours 1, 0, 1, 0 ...; pass p
+        // updates the columns at least p + 1 from the edge.  Every updated
+        // column has its four neighbours inside the tile.
+        const int color = PRE ? (p & 1) : 1 - (p & 1);
+        const int dmin = PRE ? p : p + 1;
+        const bool zero_pass = PRE && p == 0;
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            int a, bb, kq;
+            split(q, a, bb, kq);
+            const int d = min(min(a, T.wx - 1 - a), min(bb, T.wy - 1 - bb));
+            const int i = i0 + a, j = j0 + bb;
+            if (d < dmin || i < 0 || i >= L.nx || j < 0 || j >= L.ny) continue;
+            float4 out;
+            const QuadTab Q = tab(a, bb, kq);
+            if (zero_pass) {
+                quad_update_t(Q, (unsigned)i, (unsigned)j, bs[q], zero, zero, zero, zero, zero, 0.f, 0.f, color, out);
+            } else {
+                const float zlo = kq > 0 ? xs[q - 1].w : (PZ ? xs[q + T.n4 - 1].w : 0.f);
+                const float zhi = kq < T.n4 - 1 ? xs[q + 1].x : (PZ ? xs[q - (T.n4 - 1)].x : 0.f);
+                quad_update_t(Q, (unsigned)i, (unsigned)j, bs[q], xs[q], xs[q - sq], xs[q + sq], xs[q - T.n4],
+                              xs[q + T.n4], zlo, zhi, color, out);
+            }
+            xs[q] = out;
+        }
+        __syncthreads();
+    }
+    if (PRE) {
+        // k_mg_restrict4 over the interior's coarse cells: one thread per
+        // pair of coarse cells along k (the children's quad kq of the four
+        // fine columns)
+        const int cx = T.tx >> 1, cy = T.ty >> 1, nr = cx * cy * T.n4;
+        for (int u = threadIdx.x; u < nr; u += blockDim.x) {
+            const int col = u / T.n4, kq = u - col * T.n4;
+            const int ca = col / cy, cb = col - ca * cy;
+            const int I = (ti * T.tx >> 1) + ca, J = (tj * T.ty >> 1) + cb;
+            if (I >= C.nx || J >= C.ny) continue;
+            const float4 czm = tz[kq], czp = tz[T.n4 + kq], sz = tz[3 * T.n4 + kq], wz = tz[4 * T.n4 + kq];
+            float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+            for (int a2 = 0; a2 < 2; ++a2)
+#pragma unroll
+                for (int b2 = 0; b2 < 2; ++b2) {
+                    const int i = 2 * I + a2, j = 2 * J + b2;
+                    const int q = ((i - i0) * T.wy + (j - j0)) * T.n4 + kq;
+                    const float4 xc = xs[q];
+                    const float4 xm = xs[q - sq], xp = xs[q + sq], ym = xs[q - T.n4], yp = xs[q + T.n4];
+                    const float zlo = kq > 0 ? xs[q - 1].w : (PZ ? xs[q + T.n4 - 1].w : 0.f);
+                    const float zhi = kq < T.n4 - 1 ? xs[q + 1].x : (PZ ? xs[q - (T.n4 - 1)].x : 0.f);
+                    const float4 bv = bs[q];
+                    const bool odd = ((i + j) & 1) != 0;
+                    auto pick = [odd](float v0, float v1) { return odd ? v1 : v0; };
+                    const int a = i - i0, bb = j - j0;
+                    const float cxm = tx[a], cxp = tx[T.wx + a];
+                    const float cym = ty[bb], cyp = ty[T.wy + bb];
+                    const float sxy = __fadd_rn(tx[3 * T.wx + a], ty[3 * T.wy + bb]);
+                    const float wxy = __fmul_rn(tx[4 * T.wx + a], ty[4 * T.wy + bb]);
+                    float nA = fmaf(cxm, pick(xm.x, xm.y), 0.f);
+                    nA = fmaf(cxp, pick(xp.x, xp.y), nA);
+                    nA = fmaf(cym, pick(ym.x, ym.y), nA);
+                    nA = fmaf(cyp, pick(yp.x, yp.y), nA);
+                    nA = fmaf(pick(czm.x, czm.y), pick(zlo, xc.x), nA);
+                    nA = fmaf(pick(czp.x, czp.y), pick(xc.y, xc.z), nA);
+                    float nB = fmaf(cxm, pick(xm.z, xm.w), 0.f);
+                    nB = fmaf(cxp, pick(xp.z, xp.w), nB);
+                    nB = fmaf(cym, pick(ym.z, ym.w), nB);
+                    nB = fmaf(cyp, pick(yp.z, yp.w), nB);
+                    nB = fmaf(pick(czm.z, czm.w), pick(xc.y, xc.z), nB);
+                    nB = fmaf(pick(czp.z, czp.w), pick(xc.w, zhi), nB);
+                    const float dA = __fmul_rn(wxy, pick(wz.x, wz.y)), dB = __fmul_rn(wxy, pick(wz.z, wz.w));
+                    const float rA = __fsub_rn(__fmul_rn(__fadd_rn(sxy, pick(sz.x, sz.y)), pick(xc.x, xc.y)), nA);
+                    const float rB = __fsub_rn(__fmul_rn(__fadd_rn(sxy, pick(sz.z, sz.w)), pick(xc.z, xc.w)), nB);
+                    s0 = __fadd_rn(s0, __fsub_rn(pick(bv.x, bv.y), __fmul_rn(dA, rA)));
+                    s1 = __fadd_rn(s1, __fsub_rn(pick(bv.z, bv.w), __fmul_rn(dB, rB)));
+                }
+            *reinterpret_cast<float2 *>(C.b + ((long long)I * C.ny + J) * C.nz + 2 * kq) = make_float2(s0, s1);
+        }
+    }
+    // the interior's x
+    const int nin = T.tx * T.ty * T.n4;
+    for (int u = threadIdx.x; u < nin; u += blockDim.x) {
+        const int col = u / T.n4, kq = u - col * T.n4;
+        const int a = col / T.ty, bb = col - a * T.ty;
+        const int i = ti * T.tx + a, j = tj * T.ty + bb;
+        if (i >= L.nx || j >= L.ny) continue;
+        const int q = ((a + T.h) * T.wy + (bb + T.h)) * T.n4 + kq;
+        *reinterpret_cast<float4 *>(xout + ((long long)i * L.ny + j) * L.nz + 4 * kq) = xs[q];
+    }
+}
+
 // ---- fused red-black sweep (grid-wide levels, nz % 4 == 0) ------------------
 // One symmetric-order sweep in one pass: xn = colour c1 applied after colour
 // c0 to xo (c1 = 1 - c0), written to a second buffer so that no block reads a
@@ -702,11 +942,6 @@ __device__ __forceinline__ void cp16(unsigned dst, const void *src, bool valid)
     // 16-byte asynchronous copy; an invalid source fills zeros and reads nothing
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(valid ? 16 : 0)
                  : "memory");
-}
-
-__device__ __forceinline__ float comp4(const float4 &v, int e)
-{
-    return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
 }
 
 __global__ void __launch_bounds__(1024)
@@ -1592,6 +1827,8 @@ int small_image(cfd_ctx *c, Mg &G)
 
 namespace cfd {
 
+static bool transfers4(const Mg &G, const MgLevel &F, const MgLevel &C);
+
 // host set-up of the level hierarchy (level 0 is the CG's own operator)
 int mg_setup(cfd_ctx *c)
 {
@@ -1602,7 +1839,8 @@ int mg_setup(cfd_ctx *c)
     G.sweeps0 = G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_SWEEPS0")) G.sweeps0 = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_PAIRS")) G.pairs = std::atoi(e) > 0 ? std::atoi(e) : 1;
-    if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS")) G.fuse_ends = std::atoi(e) != 0;
+    if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS")) G.fuse_from = std::atoi(e) != 0 ? 0 : kMgMaxLevels;
+    if (const char *e = std::getenv("CFDGPU_MG_FUSE_ENDS_FROM")) G.fuse_from = std::max(0, std::atoi(e));
     G.small_sweeps = G.sweeps;
     if (const char *e = std::getenv("CFDGPU_MG_TRANSFER4")) G.transfer4 = e[0] != '0';
     if (const char *e = std::getenv("CFDGPU_MG_ROWS2")) G.rows2 = e[0] != '0';
@@ -1761,6 +1999,49 @@ int mg_setup(cfd_ctx *c)
         L.sweep_ci = ci;
     }
     CK(cudaFuncSetAttribute(k_mg_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSweepSmemMax));
+    // tiled smoothing phases on the grid-wide levels of at most kTileCells
+    // cells, whose colour launches are latency-bound (at 512x256x32 the
+    // 65 536-cell level gains 11 us a V-cycle, the 524 288-cell level loses
+    // 6: its tiles, 2.25 times the cells, are bound by the shared-memory and
+    // L1 bandwidth of 128 SMs).  The finest level's post-smoothing always
+    // stays launches: the CG's rho' is fused into its last colour and the
+    // V-cycle's result is its x.  Tiles of 16 x 16 columns where they give a
+    // wave of blocks, else 8 x 8; a second x buffer for the post-smoothing.
+    long long tile_cells = kTileCells;
+    int tile_from = kMgMaxLevels, tile_xy = 0;
+    if (const char *e = std::getenv("CFDGPU_MG_TILE")) tile_cells = e[0] != '0' ? tile_cells : 0;
+    if (const char *e = std::getenv("CFDGPU_MG_TILE_FROM")) tile_from = std::max(0, std::atoi(e));
+    if (const char *e = std::getenv("CFDGPU_MG_TILE_XY")) tile_xy = std::max(0, std::atoi(e)) & ~1;
+    for (int l = 0; l < mg_grid_levels(G); ++l) {
+        MgLevel &L = G.lev[l];
+        G.tile[l] = MgTile{};
+        if (l < tile_from && (l == 0 || L.n > tile_cells)) continue;
+        if (!L.quads || L.om != 1.f || L.sweep_tj > 0 || !transfers4(G, L, G.lev[l + 1])) continue;
+        const int sw = level_sweeps(G, l), h = 2 * sw, n4 = L.nz / 4;
+        auto make = [&](int t) {
+            MgTile T{};
+            T.tx = T.ty = t;
+            T.h = h;
+            T.sweeps = sw;
+            T.wx = t + 2 * h;
+            T.wy = t + 2 * h;
+            T.n4 = n4;
+            T.tiles_y = (L.ny + t - 1) / t;
+            T.fn4 = FastDiv((unsigned)n4);
+            T.fwy = FastDiv((unsigned)T.wy);
+            return T;
+        };
+        auto fits = [&](int t) { return tile_smem(make(t)) <= (size_t)kTileSmemMax; };
+        auto blocks = [&](int t) { return (long long)((L.nx + t - 1) / t) * ((L.ny + t - 1) / t); };
+        int t = tile_xy;
+        if (t == 0) t = fits(16) && blocks(16) >= sms ? 16 : 8;
+        if (t < 2 || !fits(t)) continue;
+        const MgTile T = make(t);
+        if (l > 0 && !L.xalt) CKS(dalloc_t(c, &L.xalt, (size_t)L.n));
+        G.tile[l] = T;
+    }
+    for (auto k : {k_mg_tile<false, true>, k_mg_tile<false, false>, k_mg_tile<true, true>, k_mg_tile<true, false>})
+        CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmemMax));
     CKS(dalloc_t(c, &G.never, 1));
     CK(cudaMemset(G.never, 0, sizeof(int)));
     return CFD_OK;
@@ -1817,7 +2098,11 @@ static void sweep_launch(const MgLevel &L, const float *xo, float *xn, int c0, i
 // a grid-wide level: fused sweeps alternate between x and xalt and end in x
 // (an even number of sweeps), else colour launches in place
 // a level whose sweep ends run fused (k_mg_first4, k_mg_prolong_first4)
-static bool fused_ends(const Mg &G, const MgLevel &L) { return G.fuse_ends && L.quads && L.sweep_tj == 0 && L.om == 1.f; }
+static bool fused_ends(const Mg &G, int l)
+{
+    const MgLevel &L = G.lev[l];
+    return l >= G.fuse_from && L.quads && L.sweep_tj == 0 && L.om == 1.f;
+}
 static bool int_index(const MgLevel &L) { return L.n + (long long)L.ny * L.nz < (1LL << 31); }
 
 // the CG's rho' fused into the V-cycle's last launch (k_mg_smooth4_rho)
@@ -1856,7 +2141,7 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
             smooth_launch(L, pre ? 1 : 0, 0, done, s);
         }
     };
-    if (fused_ends(G, L)) {
+    if (fused_ends(G, l)) {
         for (int q = 0; q < sweeps; ++q) {
             if (pre && q == 0) {
                 if (int_index(L))
@@ -1972,6 +2257,29 @@ bool mg_fuses_rho(const Mg &G)
 // the levels that run grid-wide launches (before the cluster or small kernel)
 int mg_grid_levels(const Mg &G) { return G.first_cluster > 0 ? G.first_cluster : G.first_small; }
 
+// the post-smoothing of level l runs as tiles (never on the finest level)
+static bool tiled_post(const Mg &G, int l) { return l > 0 && G.tile[l].tx > 0; }
+
+// where level l's x ends after its post-smoothing (what the prolongation
+// into level l - 1 reads)
+static const float *level_out(const Mg &G, int l) { return tiled_post(G, l) ? G.lev[l].xalt : G.lev[l].x; }
+
+// one smoothing phase of level l as tiles (k_mg_tile): PRE with the
+// restriction, or POST with the prolongation
+static void tile_launch(const Mg &G, int l, bool pre, const int *done, cudaStream_t s)
+{
+    const MgLevel &L = G.lev[l];
+    const MgTile &T = G.tile[l];
+    MgLevel C = G.lev[l + 1];
+    if (!pre) C.x = const_cast<float *>(level_out(G, l + 1));
+    float *xout = pre ? L.x : L.xalt;
+    const dim3 grid((unsigned)((L.nx + T.tx - 1) / T.tx * T.tiles_y));
+    const size_t sm = tile_smem(T);
+    auto k = L.pz ? (pre ? k_mg_tile<true, true> : k_mg_tile<true, false>)
+                  : (pre ? k_mg_tile<false, true> : k_mg_tile<false, false>);
+    launch_pdl(k, grid, dim3(kTileThreads), sm, s, L, C, T, xout, done);
+}
+
 // z = V(h): one V-cycle; every kernel returns at once when *done.  With
 // rho_sc (done == &rho_sc->done) the CG's rho' = h . z and its scalar update
 // run inside the last launch where the finest level is a grid-wide float4
@@ -1985,28 +2293,35 @@ bool mg_vcycle(cfd_ctx *c, const int *done, BicgScal *rho_sc)
     const RhoFuse rf{rho_sc, c->lc.partials, c->lc.counter, (long long)kMaxReduce * c->lc.red_blocks};
     for (int l = 0; l < fs; ++l) {
         const MgLevel &L = G.lev[l];
+        if (G.tile[l].tx > 0) {
+            tile_launch(G, l, true, done, s);
+            continue;
+        }
         smooth_phase(G, l, true, done, s);
         restrict_launch(G, L, G.lev[l + 1], done, s);
     }
     coarse_launch(G, done, s);
     for (int l = fs - 1; l >= 0; --l) {
         const MgLevel &L = G.lev[l];
-        if (fused_ends(G, L)) {
+        const float *xc = level_out(G, l + 1);
+        if (tiled_post(G, l)) {
+            tile_launch(G, l, false, done, s);
+            continue;
+        }
+        if (fused_ends(G, l)) {
             if (int_index(L))
                 launch_pdl(k_mg_prolong_first4<int>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
-                           (const float *)L.b, L.x, (const float *)G.lev[l + 1].x, done);
+                           (const float *)L.b, L.x, xc, done);
             else
                 launch_pdl(k_mg_prolong_first4<long long>, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
-                           (const float *)L.b, L.x, (const float *)G.lev[l + 1].x, done);
+                           (const float *)L.b, L.x, xc, done);
             smooth_phase(G, l, false, done, s, true, l == 0 && fuse_rho ? &rf : nullptr);
             continue;
         }
         if (transfers4(G, L, G.lev[l + 1]))
-            launch_pdl(k_mg_prolong4, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1],
-                       (const float *)G.lev[l + 1].x, L.x, done);
+            launch_pdl(k_mg_prolong4, dim3(nblk(L.n / 4)), dim3(kBlock), 0, s, L, G.lev[l + 1], xc, L.x, done);
         else
-            launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1],
-                       (const float *)G.lev[l + 1].x, L.x, done);
+            launch_pdl(k_mg_prolong, dim3(nblk(G.lev[l + 1].n)), dim3(kBlock), 0, s, L, G.lev[l + 1], xc, L.x, done);
         smooth_phase(G, l, false, done, s, false, l == 0 && fuse_rho ? &rf : nullptr);
     }
     c->launches += mg_vcycle_launches(G);
@@ -2039,10 +2354,19 @@ long long mg_vcycle_launches(const Mg &G)
     long long n = 1;
     for (int l = 0; l < mg_grid_levels(G); ++l) {
         const MgLevel &L = G.lev[l];
-        // pre 2s - 1 (the first sweep in one launch), restriction, the
-        // prolongation with the first post colour, then 2s - 1 colours
-        if (fused_ends(G, L)) n += 4LL * level_sweeps(G, l);
-        else n += 2 + (L.sweep_tj > 0 ? 1LL : 2LL) * 2 * level_sweeps(G, l);
+        const long long sw = level_sweeps(G, l), per_sweep = L.sweep_tj > 0 ? 1 : 2;
+        // pre-smoothing and restriction: one tile launch; or 2s - 1 colour
+        // launches (the first sweep in one) and the restriction; or s fused
+        // sweeps or 2s colours and the restriction
+        if (G.tile[l].tx > 0) n += 1;
+        else if (fused_ends(G, l)) n += 2 * sw;
+        else n += per_sweep * sw + 1;
+        // prolongation and post-smoothing: one tile launch; or the
+        // prolongation with the first colour and 2s - 1 colours; or the
+        // prolongation and the sweeps
+        if (tiled_post(G, l)) n += 1;
+        else if (fused_ends(G, l)) n += 2 * sw;
+        else n += 1 + per_sweep * sw;
     }
     return n;
 }

@@ -14,6 +14,13 @@
   CFDGPU_MG_ROWS2=0 turns them off): a thread updates one quad in each of two
   neighbouring j rows.  c1's levels are below the size, so the test runs a
   512x256x32 grid for one step.
+* Tiled smoothing phases (default on the grid-wide levels below the finest
+  of at most 2^17 cells; CFDGPU_MG_TILE=0 gives the colour launches,
+  CFDGPU_MG_TILE_FROM=l tiles every level from l on, l = 0 the finest
+  level's pre-smoothing too): one launch per phase over tiles with a
+  recomputed halo.  The 512x256x32 grid runs with both of its levels below
+  the finest tiled, the 128x64x8 grid (none below the finest) with the
+  finest level's pre-smoothing tiled.
 
 Both keep the arithmetic of the plain launches term for term, so steps agree
 bit for bit, with the multigrid-preconditioned inner solve of the mixed path
@@ -34,19 +41,24 @@ from cfd_nssolver_forhpc_gb300.simulation import Simulation
 pytestmark = pytest.mark.gpu
 
 
-def _run(w, fuse, var="CFDGPU_MG_FUSE_ENDS", steps=3, **kw):
-    old = os.environ.get(var)
-    os.environ[var] = "1" if fuse else "0"
+def _run_env(w, env, steps=3, **kw):
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update(env)
     try:
         with Simulation(w, tol=1e-10, **kw) as S:
             S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
             hist = [S.step() for _ in range(steps)]
             return hist, {k: S.download(k) for k in ("U0", "V0", "W0", "P")}
     finally:
-        if old is None:
-            del os.environ[var]
-        else:
-            os.environ[var] = old
+        for k, v in old.items():
+            if v is None:
+                del os.environ[k]
+            else:
+                os.environ[k] = v
+
+
+def _run(w, fuse, var="CFDGPU_MG_FUSE_ENDS", steps=3, **kw):
+    return _run_env(w, {var: "1" if fuse else "0"}, steps, **kw)
 
 
 @pytest.mark.parametrize("precision,periodic", [(capi.PREC_MIXED, False), (capi.PREC_FP64_DC, False),
@@ -97,3 +109,17 @@ def test_cluster_coarse_levels_match_single_block(name, precision, periodic):
     for k in ("U0", "V0", "W0"):
         d = np.abs(f1[k] - f0[k]).max() / np.abs(f0[k]).max()
         assert d < 1e-6, (k, d)
+
+
+@pytest.mark.parametrize("name,precision,periodic,tile_from",
+                         [("c2", capi.PREC_MIXED, False, "1"), ("c2", capi.PREC_MIXED, True, "1"),
+                          ("c1", capi.PREC_MIXED, False, "0"), ("c1", capi.PREC_FP64_DC, True, "0")])
+def test_tiled_phases_bitwise(name, precision, periodic, tile_from):
+    w = WORKLOADS[name]
+    steps = 2 if name == "c2" else 3
+    h1, f1 = _run_env(w, {"CFDGPU_MG_TILE_FROM": tile_from}, steps, precision=precision, periodic_z=periodic)
+    h0, f0 = _run_env(w, {"CFDGPU_MG_TILE": "0"}, steps, precision=precision, periodic_z=periodic)
+    assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
+    assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
+    for k in f1:
+        np.testing.assert_array_equal(f1[k], f0[k], err_msg=k)
