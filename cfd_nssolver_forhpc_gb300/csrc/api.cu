@@ -281,30 +281,37 @@ int cg_run(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 // sees the test at once and no launches run dead after convergence (a dead
 // V-cycle is some thirty launches); the stencil launch and the update
 // alternate the two p buffers at run time (sc->pp) to make that possible.
-int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
+static void cg_mg_prologue(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
 {
-    const int v = (int)mg_vcycle_launches(c->mg);
+    float *z = c->w32.r0, *q = c->w32.ap;
+    mg_h(c, h, c->dscal + 3, sc);
+    mg_vcycle(c, c->mg.never);
+    mg_rho(c, h, z, c->w32.p1, sc);
+    launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
+    mg_upd(c, e, c->w32.p1, h, q, sc);
+}
+
+static void cg_mg_iteration(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
+{
     float *z = c->w32.r0, *q = c->w32.ap;
     // V-cycle, then rho' = h . z (fused into the V-cycle's last launch where it can be)
-    const int fr = mg_fuses_rho(c->mg) ? 1 : 0;
-    auto vcycle_rho = [&] {
-        if (!mg_vcycle(c, &sc->done, sc)) mg_rho(c, h, z, nullptr, sc);
-    };
+    if (!mg_vcycle(c, &sc->done, sc)) mg_rho(c, h, z, nullptr, sc);
+    launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, false, true);
+    mg_upd(c, e, c->w32.p1, h, q, sc, c->p_alt);
+}
+
+// launches of the prologue and of one iteration
+static int cg_mg_launches(const cfd_ctx *c, bool prologue)
+{
+    const int v = (int)mg_vcycle_launches(c->mg), fr = mg_fuses_rho(c->mg) ? 1 : 0;
+    return prologue ? v + 4 : v + 3 - fr;
+}
+
+int cg_run_mg(cfd_ctx *c, const FvOp<float> &F, float *h, float *e, BicgScal *sc)
+{
     return run_pairs(
-        c, 4, sc,
-        [&] {
-            mg_h(c, h, c->dscal + 3, sc);
-            mg_vcycle(c, c->mg.never);
-            mg_rho(c, h, z, c->w32.p1, sc);
-            launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, true);
-            mg_upd(c, e, c->w32.p1, h, q, sc);
-        },
-        [&](int) {
-            vcycle_rho();
-            launch_cg_pq_mg(c->lc, F, &c->cgtma, z, c->w32.p1, c->p_alt, q, sc, 0, false, true);
-            mg_upd(c, e, c->w32.p1, h, q, sc, c->p_alt);
-        },
-        v + 4, v + 3 - fr, 1, true);
+        c, 4, sc, [&] { cg_mg_prologue(c, F, h, e, sc); }, [&](int) { cg_mg_iteration(c, F, h, e, sc); },
+        cg_mg_launches(c, true), cg_mg_launches(c, false), 1, true);
 }
 
 // The graphs bake in the buffers and operator of the context; they are
@@ -338,6 +345,153 @@ void residual64(cfd_ctx *c, const EllOp<double> &A, const double *b, const doubl
     launch_residual64_ell<float>(c->lc, A, b, x, r32, out, bout);
 }
 
+// The defect correction of solve_mixed as one CUDA graph (SPE operator,
+// multigrid-CG inner solve): the first residual and the outer state
+// (k_outer_start), then a WHILE node whose body is one sweep -- e = 0, the
+// inner solve (its prologue and its own WHILE node, nested), the outer
+// bookkeeping (k_outer_inner_done), the correction, the new residual and the
+// outer condition (k_outer_next).  A Poisson solve is then one graph launch
+// and one wait, where the host loop waits twice a sweep.  Graph slot 6 for
+// the context's b and x, 7 for caller buffers; rebuilt when the buffers, the
+// trip caps or the sweep parameters change.
+static bool same_cfg(const OuterCfg &a, const OuterCfg &b)
+{
+    return a.tol == b.tol && a.inner_tol == b.inner_tol && a.adapt == b.adapt && a.max_outer == b.max_outer &&
+           a.cap == b.cap;
+}
+
+int mixed_graph(cfd_ctx *c, int gi, const SpeOp<double> &A64, const double *b, double *x, const OuterCfg &cfg,
+                int cap_in)
+{
+    cudaGraphExec_t &ge = c->graph[gi];
+    const int slot = gi - 6;
+    const long long key = ((long long)cap_in << 20) | 1;
+    if (ge && c->graph_batch[gi] == key && same_cfg(c->outer_cfg[slot], cfg) && c->outer_b[slot] == b &&
+        c->outer_x[slot] == x)
+        return CFD_OK;
+    if (ge) { cudaGraphExecDestroy(ge); ge = nullptr; }
+    const FvOp<float> F = fv32(c);
+    const long long n = c->g.n;
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    std::string what;
+    cudaError_t e = cudaSuccess;
+    bool capturing = false;
+    // end the capture into a graph, returning its last nodes
+    auto end = [&](std::vector<cudaGraphNode_t> &last) {
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        cudaError_t e1 = cudaStreamGetCaptureInfo(c->s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        last.assign(deps, deps + (e1 == cudaSuccess ? nd : 0));
+        cudaGraph_t cg = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(c->s, &cg);
+        capturing = false;
+        return e1 != cudaSuccess ? e1 : e2;
+    };
+    auto begin = [&](cudaGraph_t into, const cudaGraphNode_t *deps, size_t nd) {
+        const cudaError_t e1 = cudaStreamBeginCaptureToGraph(c->s, into, deps, nullptr, nd,
+                                                             cudaStreamCaptureModeThreadLocal);
+        capturing = e1 == cudaSuccess;
+        return e1;
+    };
+    auto add_while = [&](cudaGraph_t into, cudaGraphConditionalHandle h, const std::vector<cudaGraphNode_t> &deps,
+                         cudaGraphNode_t *node, cudaGraph_t *body) {
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        const cudaError_t e1 = cudaGraphAddNode(node, into, deps.data(), nullptr, deps.size(), &p);
+        if (e1 == cudaSuccess) *body = p.conditional.phGraph_out[0];
+        return e1;
+    };
+    do {
+        std::vector<cudaGraphNode_t> last;
+        cudaGraphConditionalHandle ho, hi;
+        if ((e = cudaGraphConditionalHandleCreate(&ho, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) { what = "handle"; break; }
+        if ((e = begin(g, nullptr, 0)) != cudaSuccess) { what = "capture"; break; }
+        residual64(c, A64, b, x, c->r32, c->dscal + 3, c->dscal + 4);
+        launch_outer_start(c->s, ho, c->os, c->dscal + 3, c->sc_in, cfg);
+        if ((e = end(last)) != cudaSuccess) { what = "capture"; break; }
+        cudaGraphNode_t wo, wi;
+        cudaGraph_t gb = nullptr, gib = nullptr;
+        if ((e = add_while(g, ho, last, &wo, &gb)) != cudaSuccess) { what = "outer while node"; break; }
+        if ((e = cudaGraphConditionalHandleCreate(&hi, gb, 0, cudaGraphCondAssignDefault)) != cudaSuccess) { what = "inner handle"; break; }
+        if ((e = begin(gb, nullptr, 0)) != cudaSuccess) { what = "sweep capture"; break; }
+        cudaMemsetAsync(c->e32, 0, (size_t)n * sizeof(float), c->s);
+        cg_mg_prologue(c, F, c->r32, c->e32, c->sc_in);
+        launch_loop_cond(c->s, hi, c->sc_in, cap_in, 1);
+        if ((e = end(last)) != cudaSuccess) { what = "sweep capture"; break; }
+        if ((e = add_while(gb, hi, last, &wi, &gib)) != cudaSuccess) { what = "inner while node"; break; }
+        if ((e = begin(gib, nullptr, 0)) != cudaSuccess) { what = "inner capture"; break; }
+        cg_mg_iteration(c, F, c->r32, c->e32, c->sc_in);
+        launch_loop_cond(c->s, hi, c->sc_in, cap_in, 0);
+        if ((e = end(last)) != cudaSuccess) { what = "inner capture"; break; }
+        if ((e = begin(gb, &wi, 1)) != cudaSuccess) { what = "sweep capture"; break; }
+        launch_outer_inner_done(c->s, c->os, c->sc_in);
+        launch_correct_gated(c->lc, n, x, c->e32, &c->sc_in->rhs_scale, c->os);
+        residual64(c, A64, b, x, c->r32, c->dscal + 3);
+        launch_outer_next(c->s, ho, c->os, c->dscal + 3, c->sc_in, cfg);
+        if ((e = end(last)) != cudaSuccess) { what = "sweep capture"; break; }
+        if ((e = cudaGraphInstantiate(&ge, g, 0)) != cudaSuccess) { ge = nullptr; what = "instantiate"; break; }
+    } while (false);
+    if (capturing) {
+        cudaGraph_t cg = nullptr;
+        cudaStreamEndCapture(c->s, &cg);
+    }
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(CFD_ERR_CUDA, "defect-correction graph (" + what + "): " + cudaGetErrorString(e));
+    }
+    c->graph_batch[gi] = key;
+    c->outer_cfg[slot] = cfg;
+    c->outer_b[slot] = b;
+    c->outer_x[slot] = x;
+    return CFD_OK;
+}
+
+int solve_mixed_graph(cfd_ctx *c, const SpeOp<double> &A64, const double *b, double *x, int *iters, double *relres,
+                      int *outer, bool zero_x_if_zero_rhs)
+{
+    OuterCfg cfg{};
+    cfg.tol = c->cfg.p_criteria;
+    cfg.inner_tol = c->cfg.inner_tol;
+    cfg.adapt = c->inner_adapt;
+    cfg.max_outer = c->cfg.max_outer;
+    cfg.cap = trip_cap(c, (long long)c->cfg.max_outer + 2);
+    const int cap_in = trip_cap(c, (long long)c->cfg.p_iter_max + 3);
+    const int gi = (b == c->b && x == c->x) ? 6 : 7;
+    CKS(mixed_graph(c, gi, A64, b, x, cfg, cap_in));
+    CK(cudaGraphLaunch(c->graph[gi], c->s));
+    CK(cudaMemcpyAsync(c->h_os, c->os, sizeof(OuterScal), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaMemcpyAsync(c->h_sc, c->sc_in, sizeof(BicgScal), cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    const OuterScal o = *c->h_os;
+    c->launches += 2 + (long long)o.loop_trips * (cg_mg_launches(c, true) + 5) +
+                   (long long)o.inner_trips * (cg_mg_launches(c, false) + 1);
+    if (o.state == OUTER_ZERO_RHS) {
+        if (zero_x_if_zero_rhs) CK(cudaMemsetAsync(x, 0, (size_t)c->g.n * sizeof(double), c->s));
+        if (iters) *iters = 0;
+        if (relres) *relres = 0.0;
+        if (outer) *outer = 0;
+        return CFD_OK;
+    }
+    if (o.state == OUTER_INNER_WAIT) return fail(CFD_ERR_TIMEOUT, "a bounded wait of the TMA pipeline gave up");
+    if (o.state == OUTER_INNER_CAP) return fail(CFD_ERR_TIMEOUT, "inner solve did not report completion");
+    if (iters) *iters = o.iters;
+    if (relres) *relres = o.rel;
+    if (outer) *outer = o.sweeps;
+    switch (o.state) {
+    case OUTER_CONVERGED: return CFD_OK;
+    case OUTER_CAPPED: return fail(CFD_ERR_NOCONV, "defect correction reached its sweep cap");
+    case OUTER_DIVERGED: return fail(CFD_ERR_NOCONV, "FP32 inner solve diverged");
+    case OUTER_NONFINITE: return fail(CFD_ERR_NAN, "non-finite Poisson residual");
+    default: return fail(CFD_ERR_TIMEOUT, "defect correction did not report completion");
+    }
+}
+
 // Mixed precision: FP64 defect correction around FP32 BiCGSTAB solves.
 //   r = b - A x (FP64, written as FP32);  stop when |r|/|b| < tol
 //   solve A e = r in FP32 to inner_tol (e from 0);  x += e (FP64)
@@ -346,6 +500,16 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
                 int inner, int *iters, double *relres, int *outer, bool zero_x_if_zero_rhs = false)
 {
     const long long n = c->g.n;
+    if constexpr (std::is_same<Op64, SpeOp<double>>::value && std::is_same<Op32, SpeOp<float>>::value) {
+        if (inner == CFD_INNER_MG && c->mg.usable && c->use_graphs && c->device_loops && c->outer_graph &&
+            !c->debug) {
+            const int st = solve_mixed_graph(c, A64, b, x, iters, relres, outer, zero_x_if_zero_rhs);
+            // a graph the driver cannot build (nested conditional nodes):
+            // the host loop from here on
+            if (st != CFD_ERR_CUDA || c->graph[(b == c->b && x == c->x) ? 6 : 7]) return st;
+            c->outer_graph = false;
+        }
+    }
     // the first residual (from the warm start) also gives |b|^2, the
     // reference norm of the stopping test
     (void)zero;
@@ -784,6 +948,7 @@ void free_ctx(cfd_ctx *c)
     if (c->s) cudaStreamSynchronize(c->s);
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_sc) cudaFreeHost(c->h_sc);
+    if (c->h_os) cudaFreeHost(c->h_os);
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->h_max) cudaFreeHost(c->h_max);
     adj_free(c->adj);
@@ -886,6 +1051,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (const char *e = std::getenv("CFDGPU_DEBUG")) c->debug = std::atoi(e);
     if (const char *e = std::getenv("CFDGPU_NO_FUSED")) c->fused = !(e[0] == '1');
     if (const char *e = std::getenv("CFDGPU_INNER_ADAPT")) c->inner_adapt = std::max(0.0, std::atof(e));
+    if (const char *e = std::getenv("CFDGPU_OUTER_LOOP")) c->outer_graph = std::strcmp(e, "host") != 0;
 
     int st = CFD_OK;
     auto bail = [&](int code) { free_ctx(c); return code; };
@@ -959,6 +1125,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     AL(c->sc, sizeof(BicgScal));
     AL(c->sc_in, sizeof(BicgScal));
     AL(c->sc_t, sizeof(BicgScal));
+    AL(c->os, sizeof(OuterScal));
     AL(c->dscal, 8 * sizeof(double));
     AL(c->mon, 8 * sizeof(double));
     if (k.les_smagorinsky) AL(c->vis, (size_t)n * ts);
@@ -970,6 +1137,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (c->fp32) AL(c->staging, (size_t)std::max<long long>(g.ng, 3 * g.n) * sizeof(double));
 #undef AL
     if (cudaMallocHost(reinterpret_cast<void **>(&c->h_sc), sizeof(BicgScal)) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void **>(&c->h_os), sizeof(OuterScal)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_scal), 8 * sizeof(double)) != cudaSuccess ||
         cudaMallocHost(reinterpret_cast<void **>(&c->h_max), 3 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();

@@ -116,9 +116,16 @@ struct cfd_ctx {
     cfd::Mg mg{};                               // multigrid levels of the MG-preconditioned CG
     cfd::BicgScal sc_init{}, sc_in_init{};  // scalars of a fresh solver (cfd_start restores them)
     cfd::BicgScal *sc = nullptr, *sc_in = nullptr, *sc_t = nullptr, *h_sc = nullptr;
+    cfd::OuterScal *os = nullptr, *h_os = nullptr;  // the defect correction's state (graph 6)
+    cfd::OuterCfg outer_cfg[2] = {};                // ... the sweep parameters graphs 6 and 7 were built with
+    const double *outer_b[2] = {};                  // ... and their right-hand side and solution buffers
+    double *outer_x[2] = {};
+    bool outer_graph = true;  // the mixed defect correction as one graph where it applies
     // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
-    // [4] multigrid-preconditioned CG, [5] red-black SOR
-    static constexpr int kGraphs = 6;
+    // [4] multigrid-preconditioned CG, [5] red-black SOR, [6] the mixed defect
+    // correction around the multigrid CG (outer loop and inner solves) for the
+    // context's own b and x, [7] the same for caller buffers (adjoint solves)
+    static constexpr int kGraphs = 8;
     cudaGraphExec_t graph[kGraphs] = {};
     long long graph_batch[kGraphs] = {};  // shape key of each cached graph
 

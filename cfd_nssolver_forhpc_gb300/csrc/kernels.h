@@ -188,6 +188,35 @@ void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc
 // sc->tol = tol, in stream order
 void launch_set_tol(cudaStream_t s, BicgScal *sc, double tol);
 
+// The mixed defect correction as one CUDA graph (api.cu, solve_mixed_graph):
+// the outer loop's state on the device.  `state` ends as one of OUTER_*.
+struct OuterScal {
+    double norm0, rel;  // |b| and the last |r| / |b|
+    int sweeps, iters, inner_trips, loop_trips, state;
+};
+enum {
+    OUTER_RUNNING = 0, OUTER_CONVERGED = 1, OUTER_CAPPED = 2, OUTER_DIVERGED = 3, OUTER_NONFINITE = 4,
+    OUTER_INNER_WAIT = 5, OUTER_INNER_CAP = 6, OUTER_ZERO_RHS = 7
+};
+// the sweep parameters the graph bakes in
+struct OuterCfg {
+    double tol, inner_tol, adapt;  // outer tolerance, inner tolerance floor, adaptive factor (0: off)
+    int max_outer, cap;            // sweep cap, trip cap of the outer loop
+};
+// after the first residual (norm2[0] = |r|^2, norm2[1] = |b|^2): the state,
+// the first inner tolerance and the WHILE condition
+void launch_outer_start(cudaStream_t s, cudaGraphConditionalHandle h, OuterScal *os, const double *norm2,
+                        BicgScal *sc_in, OuterCfg cfg);
+// after an inner solve: its iterations and trips, and whether it failed
+void launch_outer_inner_done(cudaStream_t s, OuterScal *os, const BicgScal *sc_in);
+// after the correction and the new residual (norm2[0] = |r|^2): the next
+// sweep's inner tolerance and the WHILE condition
+void launch_outer_next(cudaStream_t s, cudaGraphConditionalHandle h, OuterScal *os, const double *norm2,
+                       BicgScal *sc_in, OuterCfg cfg);
+// x += scale e unless the defect correction has stopped (os->state)
+void launch_correct_gated(cfd_launch_ctx &c, long long n, double *x, const float *e, const double *scale,
+                          const OuterScal *os);
+
 // periodic z: the z ghost planes of up to three fields (null fields skipped)
 template <class T>
 void launch_sync_z(cudaStream_t s, const Geo &g, T *a0, T *a1, T *a2);

@@ -1731,6 +1731,71 @@ void launch_loop_cond(cudaStream_t s, cudaGraphConditionalHandle h, BicgScal *sc
     k_loop_cond<<<1, 32, 0, s>>>(h, sc, cap, first);
 }
 
+// ---- the defect correction's outer loop on the device ------------------------
+// The host loop of solve_mixed, step for step: stop when |r| / |b| < tol or
+// the ratio is not finite, fail at the sweep cap; before each sweep the inner
+// tolerance max(inner_tol, min(0.5, adapt tol / rel)).
+__device__ void outer_decide(cudaGraphConditionalHandle h, OuterScal *os, BicgScal *sc_in, const OuterCfg &cfg)
+{
+    if (os->state == OUTER_RUNNING) {
+        if (os->rel < cfg.tol) os->state = OUTER_CONVERGED;
+        else if (!isfinite(os->rel)) os->state = OUTER_NONFINITE;
+        else if (os->sweeps >= cfg.max_outer) os->state = OUTER_CAPPED;
+    }
+    const bool go = os->state == OUTER_RUNNING && os->loop_trips < cfg.cap;
+    if (go) sc_in->tol = cfg.adapt > 0.0 ? fmax(cfg.inner_tol, fmin(0.5, cfg.adapt * cfg.tol / os->rel)) : cfg.inner_tol;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+__global__ void k_outer_start(cudaGraphConditionalHandle h, OuterScal *os, const double *norm2, BicgScal *sc_in,
+                              OuterCfg cfg)
+{
+    if (threadIdx.x != 0) return;
+    os->norm0 = sqrt(norm2[1]);
+    os->rel = os->norm0 == 0.0 ? 0.0 : sqrt(norm2[0]) / os->norm0;  // NaN stays NaN
+    os->sweeps = os->iters = os->inner_trips = os->loop_trips = 0;
+    os->state = os->norm0 == 0.0 ? OUTER_ZERO_RHS : OUTER_RUNNING;
+    outer_decide(h, os, sc_in, cfg);
+}
+
+__global__ void k_outer_inner_done(OuterScal *os, const BicgScal *sc_in)
+{
+    if (threadIdx.x != 0) return;
+    os->iters += sc_in->iter;
+    os->inner_trips += sc_in->loop_trips;
+    if (sc_in->wait_timeout) os->state = OUTER_INNER_WAIT;
+    else if (sc_in->done == BICG_RUNNING) os->state = OUTER_INNER_CAP;
+    else if (!(sc_in->relres < 1.0)) os->state = OUTER_DIVERGED;  // the host loop counts this sweep too
+    if (os->state != OUTER_RUNNING && os->state != OUTER_INNER_WAIT && os->state != OUTER_INNER_CAP) os->sweeps += 1;
+}
+
+__global__ void k_outer_next(cudaGraphConditionalHandle h, OuterScal *os, const double *norm2, BicgScal *sc_in,
+                             OuterCfg cfg)
+{
+    if (threadIdx.x != 0) return;
+    os->loop_trips += 1;
+    if (os->state == OUTER_RUNNING) {
+        os->sweeps += 1;
+        os->rel = sqrt(norm2[0]) / os->norm0;
+    }
+    outer_decide(h, os, sc_in, cfg);
+}
+
+void launch_outer_start(cudaStream_t s, cudaGraphConditionalHandle h, OuterScal *os, const double *norm2,
+                        BicgScal *sc_in, OuterCfg cfg)
+{
+    k_outer_start<<<1, 32, 0, s>>>(h, os, norm2, sc_in, cfg);
+}
+void launch_outer_inner_done(cudaStream_t s, OuterScal *os, const BicgScal *sc_in)
+{
+    k_outer_inner_done<<<1, 32, 0, s>>>(os, sc_in);
+}
+void launch_outer_next(cudaStream_t s, cudaGraphConditionalHandle h, OuterScal *os, const double *norm2,
+                       BicgScal *sc_in, OuterCfg cfg)
+{
+    k_outer_next<<<1, 32, 0, s>>>(h, os, norm2, sc_in, cfg);
+}
+
 // ---------------------------------------------------------------------------
 // Mixed precision: FP64 residual of the scaled system, written as the
 // FP32 right-hand side of the next inner solve, and the FP64 correction.
@@ -1810,5 +1875,21 @@ void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e, const
     k_correct<V><<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, e, scale);
 }
 template void launch_correct<float>(cfd_launch_ctx &, long long, double *, const float *, const double *);
+
+__global__ void k_correct_gated(long long n, double *__restrict__ x, const float *__restrict__ e, const double *scale,
+                                const OuterScal *os)
+{
+    if (os->state != OUTER_RUNNING) return;
+    const double sc = scale ? *scale : 1.0;
+    for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
+         row += (long long)gridDim.x * blockDim.x)
+        x[row] += sc * (double)e[row];
+}
+
+void launch_correct_gated(cfd_launch_ctx &c, long long n, double *x, const float *e, const double *scale,
+                          const OuterScal *os)
+{
+    k_correct_gated<<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, e, scale, os);
+}
 
 }  // namespace cfd
