@@ -458,6 +458,13 @@ struct Mg {
     bool cluster = false;  // the coarse levels in one thread-block cluster where they partition;
                            // measured slower than the launches and the small kernel it replaces
     MgTile tile[kMgMaxLevels] = {};  // per grid-wide level: its phases as tiles (tx > 0)
+    // the exact separable solve of the coarsest level (fast diagonalisation,
+    // multigrid.cu): fd_level > 0 is that level, solved in place of the small
+    // levels below it
+    int fd_level = 0;
+    float *fd_v[3] = {};   // per axis: n x n eigenvectors (row i: component i of every mode)
+    float *fd_l[3] = {};   // per axis: the eigenvalues, ascending
+    bool fd_null = false;  // the mode (0, 0, 0) spans the null space (dropped)
     int fuse_from = kMgMaxLevels;  // from this level down, the first pre-sweep from zero and the
                                    // prolongation + first post-colour each in one pass (float4
                                    // levels); off by default

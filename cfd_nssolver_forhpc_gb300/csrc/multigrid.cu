@@ -25,6 +25,7 @@
 // requested colour); the small levels run inside one single-block kernel
 // that performs their whole sub-cycle with block barriers.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -743,6 +744,8 @@ k_mg_prolong4(MgLevel F, MgLevel C, const float *__restrict__ xc, float *__restr
 // for the whole level; the price is the halo recomputation.
 constexpr int kTileThreads = 512;
 constexpr long long kTileCells = 1 << 17;  // levels up to this size run their phases as tiles
+constexpr long long kFdCells = 4096;       // the separable solve takes the first level at most this size
+constexpr size_t kFdSmemMax = 160 * 1024;  // ... whose shared-memory layout fits this
 constexpr int kTileSmemMax = 160 * 1024;  // shared memory of a tile block at most
 
 // x and b of the tile, then its k tables (cm, cp, 1 / w, sum, w as float4
@@ -920,6 +923,92 @@ k_mg_tile(MgLevel L, MgLevel C, MgTile T, float *__restrict__ xout, const int *d
         const int q = ((a + T.h) * T.wy + (bb + T.h)) * T.n4 + kq;
         *reinterpret_cast<float4 *>(xout + ((long long)i * L.ny + j) * L.nz + 4 * kq) = xs[q];
     }
+}
+
+// ---- exact separable solve of the coarsest level ---------------------------
+// The level operator is a sum of Kronecker products, M = Kx (x) Wy (x) Wz +
+// Wx (x) Ky (x) Wz + Wx (x) Wy (x) Kz, with W_a = diag(cell widths) and K_a
+// the symmetric tridiagonal (cyclic for periodic z) face-coefficient
+// operator of axis a.  With K_a v = lambda W_a v solved per axis (V_a^T W_a
+// V_a = I), M = W V L V^T W for V = Vx (x) Vy (x) Vz and L the sums
+// lambda_x + lambda_y + lambda_z, so M^+ = V L^+ V^T: three mode products
+// with the transposed eigenvector matrices, a division by the eigenvalue
+// sums (the all-constant mode, M's null space, dropped), three mode products
+// back (fast diagonalisation; Lynch, Rice and Thomas, 1964).  A fixed
+// symmetric positive semi-definite map, so the V-cycle stays one.
+struct FdDesc {
+    int n[3];             // nx, ny, nz
+    const float *v[3];    // eigenvectors, row-major n x n (row i, column = mode)
+    const float *lam[3];  // eigenvalues
+    int null_mode;        // drop the mode (0, 0, 0)
+};
+
+// One block solves the level in shared memory (the level's cells, two
+// copies, and the three eigenvector matrices with the eigenvalues), six
+// mode products separated by block barriers.  fd_mode forms out[.., p, ..] =
+// sum_q A[p][q] in[.., q, ..] along AX with A = V^T (TR) or V; SCALE divides
+// by the eigenvalue sums (the forward pass's last product, AX = 0, when
+// every axis is in mode space).
+constexpr int kFdThreads = 1024;
+
+template <int AX, bool TR, bool SCALE>
+__device__ __forceinline__ void fd_mode(const FdDesc &D, const float *V, const float *const *lam, const float *in,
+                                        float *out, bool null_mode)
+{
+    const int nx = D.n[0], ny = D.n[1], nz = D.n[2], na = D.n[AX];
+    const int n = nx * ny * nz, stride = AX == 0 ? ny * nz : AX == 1 ? nz : 1;
+    for (int o = threadIdx.x; o < n; o += blockDim.x) {
+        const int k = o % nz, j = (o / nz) % ny, i = o / (ny * nz);
+        const int p = AX == 0 ? i : AX == 1 ? j : k;
+        const float *col = in + (o - p * stride);
+        float acc = 0.f;
+        for (int q = 0; q < na; ++q) acc = fmaf(TR ? V[q * na + p] : V[p * na + q], col[q * stride], acc);
+        if (SCALE) acc = (null_mode && o == 0) ? 0.f : acc / (lam[0][i] + lam[1][j] + lam[2][k]);
+        out[o] = acc;
+    }
+}
+
+__global__ void __launch_bounds__(kFdThreads) k_fd_block(FdDesc D, const float *__restrict__ b, float *__restrict__ x,
+                                                         const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    extern __shared__ float fd_sm[];
+    const int nx = D.n[0], ny = D.n[1], nz = D.n[2], n = nx * ny * nz;
+    float *s0 = fd_sm, *s1 = s0 + n, *v[3], *lam[3];
+    v[0] = s1 + n;
+    v[1] = v[0] + nx * nx;
+    v[2] = v[1] + ny * ny;
+    lam[0] = v[2] + nz * nz;
+    lam[1] = lam[0] + nx;
+    lam[2] = lam[1] + ny;
+    for (int a = 0; a < 3; ++a) {
+        const int na = D.n[a];
+        for (int q = threadIdx.x; q < na * na; q += blockDim.x) v[a][q] = __ldg(D.v[a] + q);
+        for (int q = threadIdx.x; q < na; q += blockDim.x) lam[a][q] = __ldg(D.lam[a] + q);
+    }
+    for (int q = threadIdx.x; q < n; q += blockDim.x) s0[q] = b[q];
+    __syncthreads();
+    const bool nm = D.null_mode != 0;
+    fd_mode<2, true, false>(D, v[2], lam, s0, s1, nm);
+    __syncthreads();
+    fd_mode<1, true, false>(D, v[1], lam, s1, s0, nm);
+    __syncthreads();
+    fd_mode<0, true, true>(D, v[0], lam, s0, s1, nm);
+    __syncthreads();
+    fd_mode<0, false, false>(D, v[0], lam, s1, s0, nm);
+    __syncthreads();
+    fd_mode<1, false, false>(D, v[1], lam, s0, s1, nm);
+    __syncthreads();
+    fd_mode<2, false, false>(D, v[2], lam, s1, x, nm);
+}
+
+// its shared memory: two copies of the level, the eigenvector matrices and
+// the eigenvalues
+__host__ inline size_t fd_smem(int nx, int ny, int nz)
+{
+    return sizeof(float) * (2ull * nx * ny * nz + (size_t)nx * nx + (size_t)ny * ny + (size_t)nz * nz + nx + ny + nz);
 }
 
 // ---- fused red-black sweep (grid-wide levels, nz % 4 == 0) ------------------
@@ -1768,6 +1857,99 @@ int coarse_inverse(cfd_ctx *c, const std::vector<double> (&W)[3], float **out, b
     return CFD_OK;
 }
 
+// eigenvalues (ascending) and eigenvectors (columns of v, row-major n x n)
+// of the symmetric matrix a (destroyed) by cyclic Jacobi rotations, FP64
+static void jacobi_eigen(std::vector<double> &a, int n, std::vector<double> &lam, std::vector<double> &v)
+{
+    v.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) v[(size_t)i * n + i] = 1.0;
+    auto A = [&](int i, int j) -> double & { return a[(size_t)i * n + j]; };
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, tot = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                tot += A(i, j) * A(i, j);
+                if (i != j) off += A(i, j) * A(i, j);
+            }
+        if (off <= 1e-30 * tot) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A(p, q);
+                if (std::fabs(apq) <= 1e-300) continue;
+                // the rotation that zeroes a_pq: t = tan(phi), the smaller root
+                const double theta = (A(q, q) - A(p, p)) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int r = 0; r < n; ++r) {  // columns p, q
+                    const double arp = A(r, p), arq = A(r, q);
+                    A(r, p) = c * arp - sn * arq;
+                    A(r, q) = sn * arp + c * arq;
+                }
+                for (int r = 0; r < n; ++r) {  // rows p, q
+                    const double apr = A(p, r), aqr = A(q, r);
+                    A(p, r) = c * apr - sn * aqr;
+                    A(q, r) = sn * apr + c * aqr;
+                }
+                for (int r = 0; r < n; ++r) {
+                    const double vrp = v[(size_t)r * n + p], vrq = v[(size_t)r * n + q];
+                    v[(size_t)r * n + p] = c * vrp - sn * vrq;
+                    v[(size_t)r * n + q] = sn * vrp + c * vrq;
+                }
+            }
+    }
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return A(x, x) < A(y, y); });
+    lam.resize(n);
+    std::vector<double> vs((size_t)n * n);
+    for (int m = 0; m < n; ++m) {
+        lam[m] = A(order[m], order[m]);
+        for (int r = 0; r < n; ++r) vs[(size_t)r * n + m] = v[(size_t)r * n + order[m]];
+    }
+    v.swap(vs);
+}
+
+// the fast-diagonalisation tables of level G.fd_level from its cell widths:
+// per axis K v = lambda W v through the symmetric S = W^-1/2 K W^-1/2, and
+// V = W^-1/2 U; K has -1 / Ds off the diagonal (Ds the centre distance,
+// both sides when a periodic axis has two cells) and the row sums on it
+int fd_setup(cfd_ctx *c, Mg &G, const std::vector<double> (&W)[3], bool pz)
+{
+    double lam0[3], lmax[3];
+    for (int a = 0; a < 3; ++a) {
+        const int n = (int)W[a].size();
+        std::vector<double> K((size_t)n * n, 0.0);
+        for (int i = 0; i < n; ++i)
+            for (int side = -1; side <= 1; side += 2) {
+                int o = i + side;
+                if (a == 2 && pz) o = (o + n) % n;
+                if (o < 0 || o >= n || o == i) continue;
+                const double cf = 1.0 / (0.5 * (W[a][i] + W[a][o]));
+                K[(size_t)i * n + o] -= cf;
+                K[(size_t)i * n + i] += cf;
+            }
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) K[(size_t)i * n + j] /= std::sqrt(W[a][i] * W[a][j]);
+        std::vector<double> lam, U;
+        jacobi_eigen(K, n, lam, U);
+        std::vector<float> vf((size_t)n * n), lf(n);
+        for (int i = 0; i < n; ++i)
+            for (int m = 0; m < n; ++m) vf[(size_t)i * n + m] = (float)(U[(size_t)i * n + m] / std::sqrt(W[a][i]));
+        for (int m = 0; m < n; ++m) lf[m] = (float)lam[m];
+        lam0[a] = lam[0];
+        lmax[a] = lam[n - 1];
+        CKS(dalloc_t(c, &G.fd_v[a], vf.size()));
+        CKS(dalloc_t(c, &G.fd_l[a], lf.size()));
+        CK(cudaMemcpy(G.fd_v[a], vf.data(), vf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(G.fd_l[a], lf.data(), lf.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    // Neumann or periodic on every axis: constants are the null space
+    G.fd_null = true;
+    for (int a = 0; a < 3; ++a) G.fd_null = G.fd_null && std::fabs(lam0[a]) <= 1e-9 * std::max(lmax[a], 1e-300);
+    CK(cudaFuncSetAttribute(k_fd_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFdSmemMax));
+    return CFD_OK;
+}
+
 // shared-memory layout of the small kernel from level `first` on.  The
 // static image first: the dense inverse (when staged), then per level the
 // per-cell 1 / dV and 1 / diag and the axis tables; after it per level x and
@@ -1851,11 +2033,13 @@ int mg_setup(cfd_ctx *c)
     if (const char *e = std::getenv("CFDGPU_MG_OMEGA")) om = std::max(0.5f, std::min(1.5f, (float)std::atof(e)));
     const FvOp<float> F = fv32(c);
     std::vector<double> W[3];
+    std::vector<std::array<std::vector<double>, 3>> Wl(1);  // the widths of every level
     const int n0[3] = {g.nxc, g.nyc, g.nzc};
     for (int a = 0; a < 3; ++a) {
         W[a].resize(n0[a]);
         for (int i = 0; i < n0[a]; ++i) W[a][i] = c->hraw[3 + a][i + GC];
     }
+    Wl[0] = {W[0], W[1], W[2]};
     MgLevel L0{};
     L0.nx = g.nxc; L0.ny = g.nyc; L0.nz = g.nzc; L0.n = g.n;
     L0.cm[0] = F.A.cxm; L0.cp[0] = F.A.cxp; L0.sum[0] = F.sx; L0.w[0] = F.wx;
@@ -1906,6 +2090,7 @@ int mg_setup(cfd_ctx *c)
         CKS(dalloc_t(c, &L.b, (size_t)L.n));
         set_divs(L);
         G.lev[nl++] = L;
+        Wl.push_back({W[0], W[1], W[2]});
     }
     G.nlev = nl;
     for (int l = 0; l < nl; ++l) {
@@ -1915,9 +2100,36 @@ int mg_setup(cfd_ctx *c)
         // than the shared row loads save
         L.rows2 = G.rows2 && L.quads && L.ny % 2 == 0 && L.om == 1.f && L.n >= (1LL << 21);
     }
+    // the exact separable solve replaces the first level below the finest
+    // of at most kFdCells cells whose tables fit one block's shared memory,
+    // and every coarser one (CFDGPU_MG_FD=0: the small levels in one block
+    // with the dense coarsest solve)
+    bool fd_on = true;
+    long long fd_cells = kFdCells;
+    if (const char *e = std::getenv("CFDGPU_MG_FD")) fd_on = e[0] != '0';
+    if (const char *e = std::getenv("CFDGPU_MG_FD_CELLS")) fd_cells = std::max(1LL, std::atoll(e));
+    G.fd_level = 0;
+    if (const char *e = std::getenv("CFDGPU_MG_CLUSTER")) fd_on = fd_on && e[0] == '0';  // the cluster kernel instead
+    if (fd_on)
+        for (int l = 1; l < nl; ++l) {
+            const MgLevel &L = G.lev[l];
+            if (L.n <= fd_cells && fd_smem(L.nx, L.ny, L.nz) <= kFdSmemMax) {
+                G.fd_level = l;
+                break;
+            }
+        }
+    if (G.fd_level > 0) {
+        nl = G.fd_level + 1;
+        G.nlev = nl;
+        G.usable = true;
+        G.first_small = G.fd_level;
+        G.first_cluster = 0;
+        CKS(fd_setup(c, G, {Wl[nl - 1][0], Wl[nl - 1][1], Wl[nl - 1][2]}, g.pz != 0));
+    }
     const long long ncoarse = G.lev[nl - 1].n;
-    G.usable = nl > 1 && ncoarse <= kMgCoarsest;
+    if (G.fd_level == 0) G.usable = nl > 1 && ncoarse <= kMgCoarsest;
     if (!G.usable) return CFD_OK;
+    if (G.fd_level == 0) {
     CKS(coarse_inverse(c, W, &G.cinv, g.pz != 0));
     // the first small level: at most `small` cells, and all levels from it
     // on fit the small kernel's shared memory; the dense inverse is staged
@@ -1970,6 +2182,7 @@ int mg_setup(cfd_ctx *c)
             }
         }
     }
+    }  // the small levels (no separable solve)
     // fused sweeps on the grid-wide levels with float4 rows: about 128
     // threads a block (TJ rows x nz/4 quads), chunks of CI planes sized for
     // about six blocks per SM, a second x buffer each
@@ -2236,8 +2449,30 @@ static void small_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl 
     else k<<<1, kSmallThreads, G.small_smem, s>>>(small_desc(G, done));
 }
 
+// the separable solve of the coarsest level, b -> x, in one block
+static void fd_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl)
+{
+    const MgLevel &L = G.lev[G.fd_level];
+    FdDesc D{};
+    D.n[0] = L.nx;
+    D.n[1] = L.ny;
+    D.n[2] = L.nz;
+    for (int a = 0; a < 3; ++a) {
+        D.v[a] = G.fd_v[a];
+        D.lam[a] = G.fd_l[a];
+    }
+    D.null_mode = G.fd_null ? 1 : 0;
+    const size_t sm = fd_smem(L.nx, L.ny, L.nz);
+    if (pdl) launch_pdl(k_fd_block, dim3(1), dim3(kFdThreads), sm, s, D, (const float *)L.b, L.x, done);
+    else k_fd_block<<<1, kFdThreads, sm, s>>>(D, L.b, L.x, done);
+}
+
 static void coarse_launch(const Mg &G, const int *done, cudaStream_t s, bool pdl)
 {
+    if (G.fd_level > 0) {
+        fd_launch(G, done, s, pdl);
+        return;
+    }
     if (G.first_cluster == 0) {
         small_launch(G, done, s, pdl);
         return;
@@ -2351,7 +2586,7 @@ void mg_time_part(cfd_ctx *c, int part)
 // kernel launches of one V-cycle
 long long mg_vcycle_launches(const Mg &G)
 {
-    long long n = 1;
+    long long n = 1;  // the coarse solve
     for (int l = 0; l < mg_grid_levels(G); ++l) {
         const MgLevel &L = G.lev[l];
         const long long sw = level_sweeps(G, l), per_sweep = L.sweep_tj > 0 ? 1 : 2;

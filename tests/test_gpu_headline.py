@@ -27,7 +27,7 @@ STEPS = 50
 TOL = 1e-10
 CD_RTOL = 1e-6          # drag, mixed vs FP64
 CL_TOL_OF_CD = 1e-6     # lift difference relative to |drag|
-FIELD_MAX_RTOL = {"U0": 1e-5, "V0": 1e-4, "W0": 1e-3, "P": 1e-4}
+FIELD_MAX_RTOL = {"U0": 1e-5, "V0": 1e-4, "W0": 1e-3, "P": 1e-4}  # measured 7.6e-7, 5.0e-7, 5.0e-7, 4.9e-6
 
 
 def _run(w, **kw):
@@ -55,9 +55,13 @@ def test_mixed_matches_fp64_drag_lift_and_fields_over_50_steps():
     cd_err = np.abs(cd32 / cd64 - 1.0)
     cl_err = np.abs(cl32 - cl64) / np.abs(cd64)
     errs = {}
-    for k in ("P",):  # the pressure is defined up to a constant
-        f64[k] = f64[k] - f64[k].mean()
-        f32[k] = f32[k] - f32[k].mean()
+    # the pressure is defined up to a constant: compare the interior cells
+    # with their mean removed (the edge and corner ghost cells, which no
+    # boundary condition updates, do not follow the solution's constant)
+    gc = 2
+    for f in (f64, f32):
+        p = f["P"].reshape(w.nxc + 2 * gc, w.nyc + 2 * gc, w.nzc + 2 * gc)[gc:-gc, gc:-gc, gc:-gc]
+        f["P"] = p - p.mean()
     for k in f64:
         d = f32[k] - f64[k]
         errs[k] = (float(np.abs(d).max() / np.abs(f64[k]).max()),

@@ -7,9 +7,13 @@
   kernels): the restriction reads the children's rows as float4 quads, the
   prolongation adds to one quad per thread.
 * The coarse levels in one thread-block cluster (CFDGPU_MG_CLUSTER=1, off by
-  default: measured slower; the single-block kernel of the small levels
-  otherwise): a different summation in the coarsest solve, so the runs agree
-  to the solver tolerance rather than bit for bit.
+  default: measured slower), against the single-block kernel of the small
+  levels (CFDGPU_MG_FD=0): a different summation in the coarsest solve, so
+  the runs agree to the solver tolerance rather than bit for bit.
+* The separable solve of the coarsest level (default) against the small
+  levels with the dense coarsest solve (CFDGPU_MG_FD=0): a different
+  preconditioner, so the steps agree to the solver tolerance, and the exact
+  coarse solve needs no more iterations.
 * Two-row colour launches (default on levels of at least 2^21 cells;
   CFDGPU_MG_ROWS2=0 turns them off): a thread updates one quad in each of two
   neighbouring j rows.  c1's levels are below the size, so the test runs a
@@ -41,12 +45,20 @@ from cfd_nssolver_forhpc_gb300.simulation import Simulation
 pytestmark = pytest.mark.gpu
 
 
-def _run_env(w, env, steps=3, **kw):
+def _run_env(w, env, steps=3, sml=False, **kw):
     old = {k: os.environ.get(k) for k in env}
     os.environ.update(env)
     try:
         with Simulation(w, tol=1e-10, **kw) as S:
-            S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
+            if sml:  # the reference's stretched grid instead of the uniform one
+                S.grid_sml()
+                S.init_uniform(1.0, 0.0, 0.0)
+                S.DFIB_CylinderZ(w.cx, w.center_y, w.radius, w.nsub)
+                for nm, a in zip(("U0", "V0", "W0"), initial_velocity(w.nxc, w.nyc, w.nzc)):
+                    S.upload(nm, a)
+                S.start()
+            else:
+                S.setup_cylinder(*initial_velocity(w.nxc, w.nyc, w.nzc))
             hist = [S.step() for _ in range(steps)]
             return hist, {k: S.download(k) for k in ("U0", "V0", "W0", "P")}
     finally:
@@ -101,7 +113,7 @@ def test_two_row_smoother_bitwise(precision, periodic):
 def test_cluster_coarse_levels_match_single_block(name, precision, periodic):
     w = WORKLOADS[name]
     h1, f1 = _run(w, True, "CFDGPU_MG_CLUSTER", precision=precision, periodic_z=periodic)
-    h0, f0 = _run(w, False, "CFDGPU_MG_CLUSTER", precision=precision, periodic_z=periodic)
+    h0, f0 = _run_env(w, {"CFDGPU_MG_CLUSTER": "0", "CFDGPU_MG_FD": "0"}, precision=precision, periodic_z=periodic)
     np.testing.assert_allclose([h["cd"] for h in h1], [h["cd"] for h in h0], rtol=1e-8)
     for a, b in zip(h1, h0):
         assert all(abs(x - y) <= 2 for x, y in zip(a["iters"], b["iters"])), (a["iters"], b["iters"])
@@ -123,3 +135,19 @@ def test_tiled_phases_bitwise(name, precision, periodic, tile_from):
     assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
     for k in f1:
         np.testing.assert_array_equal(f1[k], f0[k], err_msg=k)
+
+
+@pytest.mark.parametrize("name,precision,periodic", [("c1", capi.PREC_MIXED, False), ("c1", capi.PREC_FP64_DC, False),
+                                                     ("c1", capi.PREC_MIXED, True), ("s1", capi.PREC_MIXED, False)])
+def test_separable_coarse_solve_matches_small_levels(name, precision, periodic):
+    w = WORKLOADS[name]
+    kw = dict(precision=precision, periodic_z=periodic, sml=name == "s1")
+    h1, f1 = _run_env(w, {"CFDGPU_MG_FD": "1"}, **kw)
+    h0, f0 = _run_env(w, {"CFDGPU_MG_FD": "0"}, **kw)
+    np.testing.assert_allclose([h["cd"] for h in h1], [h["cd"] for h in h0], rtol=1e-8)
+    for a, b in zip(h1, h0):
+        assert all(r < 1e-10 for r in a["relres"][1:] if r > 0)
+        assert sum(a["iters"]) <= sum(b["iters"]) + 2, (a["iters"], b["iters"])
+    for k in ("U0", "V0", "W0"):
+        d = np.abs(f1[k] - f0[k]).max() / np.abs(f0[k]).max()
+        assert d < 1e-6, (k, d)
