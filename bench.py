@@ -240,7 +240,7 @@ def build_sim(args, w, precision):
     from cfd_nssolver_forhpc_gb300.initial import initial_velocity
     from cfd_nssolver_forhpc_gb300.simulation import Simulation
     solver = {"spe": capi.SOLVER_BICG_SPE, "ell": capi.SOLVER_BICG_ELL, "sor": capi.SOLVER_SOR_RB}[args.solver]
-    prec = capi.PREC_MIXED if precision == "mixed" else capi.PREC_FP64
+    prec = {"mixed": capi.PREC_MIXED, "fp64": capi.PREC_FP64, "fp64_dc": capi.PREC_FP64_DC}[precision]
     maxit = args.fp64_maxit if precision == "fp64" else 5000
     S = Simulation(w, solver=solver, precision=prec, tol=w.tol, check_every=16, maxit=maxit,
                    inner_tol=args.inner_tol)
@@ -329,9 +329,9 @@ def roofline(S, w, infos, precision, ms_step):
         # multigrid-preconditioned CG: one V-cycle per inner iteration and one
         # per inner solve (its start); per V-cycle 4 * sweeps colour passes,
         # one restriction and one prolongation on the finest level and the
-        # single-block kernel of the small levels
+        # coarse solve (the separable solve of the coarsest level)
         v = iters + outer
-        counts = {"mg_smooth": 4 * MG_SWEEPS * v, "mg_restrict": v, "mg_prolong": v, "mg_small": v,
+        counts = {"mg_smooth": 4 * MG_SWEEPS * v, "mg_restrict": v, "mg_prolong": v, "mg_coarse": v,
                   "cg_pq": iters, "mg_upd": iters, "mg_rho": v, "residual64": outer + npass}
         per_row = dict(KERNEL_BYTES_MIXED)
     elif precision == "mixed":
@@ -776,6 +776,25 @@ def main():
                  "roofline": roofline(M, w, minfos, other_prec, msec / K * 1e3),
                  "ratio_mixed_vs_fp64": round(mixed_v / fp64_v, 3)}
         M.close()
+    # FP64 fields with the mixed path's solver (the FP64 defect correction
+    # around the FP32 multigrid CG): what the FP32 fields buy at the same
+    # algorithm, beside what the algorithm buys against FP64 BiCGSTAB
+    same_solver = None
+    if mixed and not args.no_compare and args.solver != "sor":
+        D = build_sim(args, w, "fp64_dc")
+        for _ in range(W):
+            D.step(allow_noconv=True)
+        dsec, dinfos, dlaunch = timed_steps(D, K, dist)
+        dsec = dist.max(dsec)
+        dval = whole_job_rate(w.n_cells, K, dist.world, dsec)
+        same_solver = {"precision": "fp64_dc", "value": round(dval, 4), "unit": UNIT, "dtype": "f64",
+                       "ms_per_step": round(dsec / K * 1e3, 3),
+                       "iters_per_step": [sum(i["iters"]) for i in dinfos],
+                       "outer_per_step": [sum(i["outer"]) for i in dinfos],
+                       "max_relres": max(r for i in dinfos[1:] or dinfos for r in i["relres"]),
+                       "cd_rel_vs_headline": abs(dinfos[-1]["cd"] / cd64 - 1.0), "gpu_launches": dlaunch,
+                       "ratio_mixed_vs_fp64_dc": round(value / dval, 3)}
+        D.close()
     adjoint = None
     if not args.no_adjoint and args.solver != "sor":
         adjoint = adjoint_leg(args, dist)
@@ -803,6 +822,8 @@ def main():
         }
         if mixed:
             line["config"]["inner_tol"] = args.inner_tol
+        if same_solver:
+            line["fp64_dc"] = same_solver
         if other:
             line[other_prec] = other
             line["ratio_mixed_vs_fp64"] = other["ratio_mixed_vs_fp64"]

@@ -23,7 +23,7 @@ PREC_FP64, PREC_MIXED, PREC_FP64_DC = 0, 1, 2
 INNER_CG, INNER_BICGSTAB, INNER_MG = 0, 1, 2
 T0, T1, T3 = 0, 1, 3
 KERNELS = ["bicg_ap", "bicg_s", "bicg_as", "bicg_xr", "bicg_p", "convdiff", "update_uf", "rhs",
-           "sor_sweep", "cg_pq", "cg_upd", "residual64", "mg_smooth", "mg_restrict", "mg_prolong", "mg_small",
+           "sor_sweep", "cg_pq", "cg_upd", "residual64", "mg_smooth", "mg_restrict", "mg_prolong", "mg_coarse",
            "mg_vcycle", "mg_upd", "mg_rho", "mg_sweep", "pass", "update_pass",
            "sor32_sweep"]
 FIELDS = ["U0", "V0", "W0", "U1", "V1", "W1", "U3", "V3", "W3", "P", "ETA", "F", "SRC", "X", "B", "JP", "VIS"]

@@ -1860,7 +1860,7 @@ int cfd_time_kernels(cfd_ctx *c, int reps, double *ms, int nms)
                 CKS(mg_setup(c));
                 if (c->mg.usable) {
                     const int ids[6] = {CFD_KERNEL_MG_SMOOTH, CFD_KERNEL_MG_RESTRICT, CFD_KERNEL_MG_PROLONG,
-                                        CFD_KERNEL_MG_SMALL, CFD_KERNEL_MG_VCYCLE, CFD_KERNEL_MG_SWEEP};
+                                        CFD_KERNEL_MG_COARSE, CFD_KERNEL_MG_VCYCLE, CFD_KERNEL_MG_SWEEP};
                     for (int part = 0; part < 6; ++part)
                         if (!((part < 3 || part == 5) && mg_grid_levels(c->mg) == 0) &&
                             !(part == 5 && c->mg.lev[0].sweep_tj == 0))

@@ -312,7 +312,8 @@ typedef enum {
     CFD_KERNEL_MG_SMOOTH,    /* multigrid: one colour of a Gauss-Seidel sweep on the finest level */
     CFD_KERNEL_MG_RESTRICT,  /* multigrid: residual of the finest level summed to the next */
     CFD_KERNEL_MG_PROLONG,   /* multigrid: coarse correction added to the finest level */
-    CFD_KERNEL_MG_SMALL,     /* multigrid: the single-block sub-cycle of the small levels */
+    CFD_KERNEL_MG_COARSE,    /* multigrid: the coarse solve (the separable solve of the coarsest
+                                level, or the single-block sub-cycle of the small levels) */
     CFD_KERNEL_MG_VCYCLE,    /* multigrid: one whole V-cycle (all its launches) */
     CFD_KERNEL_MG_UPD,       /* multigrid CG: e, h update */
     CFD_KERNEL_MG_RHO,       /* multigrid CG: h.z and the scalar update */
