@@ -408,6 +408,7 @@ struct MgLevel {
     int pz;               // 1: periodic in z (nz even: red-black stays a two-colouring)
     float om;             // smoother relaxation: x += om (x_gs - x); 1 is Gauss-Seidel
     bool rows2;           // colour launches run k_mg_smooth4x2 (two j rows a thread)
+    int march;            // > 0: ... k_mg_smooth4m instead, marching this many x planes a thread
 };
 // A grid-wide level whose smoothing phases run as tiles with a recomputed
 // halo (multigrid.cu, k_mg_tile): tx == 0 where the level runs colour launches

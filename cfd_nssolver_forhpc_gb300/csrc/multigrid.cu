@@ -721,6 +721,86 @@ k_mg_prolong4(MgLevel F, MgLevel C, const float *__restrict__ xc, float *__restr
     }
 }
 
+// The two-row colour pass marching along x: a thread owns the quad pair
+// (j0, j0 + 1; k0) on planes i0 .. i0 + ci - 1 and keeps planes i - 1, i and
+// i + 1 of its two rows in registers, so a plane costs the loads of plane
+// i + 2's rows (issued before the plane's update), b, the two y rows and the
+// k neighbours, against ten quads and the k neighbours in k_mg_smooth4x2.  A
+// colour pass reads only the other colour, which it does not change, so the
+// window's values from before this thread's updates serve the next plane.
+// quad_update's arithmetic: the pass equals k_mg_smooth4x2 bit for bit.
+// Blocks: (quad pairs of a plane / kBlock, planes / ci); 32-bit indices.
+template <bool PZ>
+__global__ void __launch_bounds__(kBlock, 3) k_mg_smooth4m(MgLevel L, const float *__restrict__ b, float *x, int color,
+                                                           int zero_init, int ci, const int *done)
+{
+    pdl_wait();
+    pdl_allow();
+    if (*done) return;
+    const int n4 = L.nz >> 2, np = (L.ny >> 1) * n4;
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= np) return;
+    const int jp = (int)L.fq.div((unsigned)w), k0 = 4 * (w - jp * n4), j0 = 2 * jp;
+    const int i0 = blockIdx.y * ci, i1 = min(i0 + ci, L.nx);
+    const int sx = L.ny * L.nz, sy = L.nz;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto ld = [&](int t) { return *reinterpret_cast<const float4 *>(x + t); };
+    const int tb = (i0 * L.ny + j0) * L.nz + k0;  // row j0 of plane i0
+    float4 m0 = zero, m1 = zero, c0 = zero, c1 = zero, p0 = zero, p1 = zero;
+    if (!zero_init) {
+        if (i0 > 0) {
+            m0 = ld(tb - sx);
+            m1 = ld(tb - sx + sy);
+        }
+        c0 = ld(tb);
+        c1 = ld(tb + sy);
+        if (i0 + 1 < L.nx) {
+            p0 = ld(tb + sx);
+            p1 = ld(tb + sx + sy);
+        }
+    }
+    for (int i = i0; i < i1; ++i) {
+        const int t0 = tb + (i - i0) * sx, t1 = t0 + sy;
+        float4 n0 = zero, n1 = zero;
+        if (!zero_init && i + 1 < i1 && i + 2 < L.nx) {
+            n0 = ld(t0 + 2 * sx);
+            n1 = ld(t1 + 2 * sx);
+        }
+        const float4 b0 = *reinterpret_cast<const float4 *>(b + t0), b1 = *reinterpret_cast<const float4 *>(b + t1);
+        float4 ym = zero, yp = zero;
+        float zl0 = 0.f, zh0 = 0.f, zl1 = 0.f, zh1 = 0.f;
+        if (!zero_init) {
+            if (j0 > 0) ym = ld(t0 - sy);
+            if (j0 + 2 < L.ny) yp = ld(t1 + sy);
+            if (k0 > 0) {
+                zl0 = x[t0 - 1];
+                zl1 = x[t1 - 1];
+            } else if (PZ) {
+                zl0 = x[t0 + (L.nz - 1)];
+                zl1 = x[t1 + (L.nz - 1)];
+            }
+            if (k0 + 4 < L.nz) {
+                zh0 = x[t0 + 4];
+                zh1 = x[t1 + 4];
+            } else if (PZ) {
+                zh0 = x[t0 + 4 - L.nz];
+                zh1 = x[t1 + 4 - L.nz];
+            }
+        }
+        float4 o0, o1;
+        quad_update(L, (unsigned)i, (unsigned)j0, k0, b0, c0, m0, p0, ym, c1, zl0, zh0, color, o0);
+        quad_update(L, (unsigned)i, (unsigned)(j0 + 1), k0, b1, c1, m1, p1, c0, yp, zl1, zh1, color, o1);
+        *reinterpret_cast<float4 *>(x + t0) = o0;
+        *reinterpret_cast<float4 *>(x + t1) = o1;
+        m0 = c0;
+        m1 = c1;
+        c0 = p0;
+        c1 = p1;
+        p0 = n0;
+        p1 = n1;
+    }
+}
+
 // ---- tiled smoothing phases (grid-wide float4 levels) -----------------------
 // One block owns an interior tile of tx x ty columns (all of k) and holds it
 // with a halo of h = 2 s columns on each side (s sweeps) in shared memory, x
@@ -2027,6 +2107,8 @@ int mg_setup(cfd_ctx *c)
     if (const char *e = std::getenv("CFDGPU_MG_TRANSFER4")) G.transfer4 = e[0] != '0';
     if (const char *e = std::getenv("CFDGPU_MG_ROWS2")) G.rows2 = e[0] != '0';
     if (const char *e = std::getenv("CFDGPU_MG_SMALL_SWEEPS")) G.small_sweeps = std::atoi(e) > 0 ? std::atoi(e) : G.sweeps;
+    int march = 0;  // planes a thread of the marching colour pass covers (0: k_mg_smooth4x2)
+    if (const char *e = std::getenv("CFDGPU_MG_MARCH")) march = std::max(0, std::atoi(e));
     long long small = kMgSmall;
     if (const char *e = std::getenv("CFDGPU_MG_SMALL")) small = std::atoll(e);
     float om = 1.f;  // smoother relaxation (1: Gauss-Seidel)
@@ -2099,6 +2181,7 @@ int mg_setup(cfd_ctx *c)
         // at a few hundred blocks the halved thread count costs more latency
         // than the shared row loads save
         L.rows2 = G.rows2 && L.quads && L.ny % 2 == 0 && L.om == 1.f && L.n >= (1LL << 21);
+        L.march = L.rows2 ? march : 0;
     }
     // the exact separable solve replaces the first level below the finest
     // of at most kFdCells cells whose tables fit one block's shared memory,
@@ -2389,6 +2472,13 @@ static void smooth_phase(const Mg &G, int l, bool pre, const int *done, cudaStre
 template <bool PZ>
 static void smooth_launch_t(const MgLevel &L, int color, int zero_init, const int *done, cudaStream_t s)
 {
+    if (L.rows2 && L.march > 0 && L.n + (long long)L.ny * L.nz < (1LL << 31)) {
+        const int np = (L.ny / 2) * (L.nz / 4);
+        const dim3 grid((unsigned)((np + kBlock - 1) / kBlock), (unsigned)((L.nx + L.march - 1) / L.march));
+        launch_pdl(k_mg_smooth4m<PZ>, grid, dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color, zero_init, L.march,
+                   done);
+        return;
+    }
     if (L.rows2 && L.n + (long long)L.ny * L.nz < (1LL << 31)) {
         launch_pdl(k_mg_smooth4x2<int, PZ>, dim3(nblk(L.n / 8)), dim3(kBlock), 0, s, L, (const float *)L.b, L.x, color,
                    zero_init, done);

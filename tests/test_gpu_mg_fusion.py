@@ -18,6 +18,9 @@
   CFDGPU_MG_ROWS2=0 turns them off): a thread updates one quad in each of two
   neighbouring j rows.  c1's levels are below the size, so the test runs a
   512x256x32 grid for one step.
+* The two-row colour pass marching along x (CFDGPU_MG_MARCH=ci planes a
+  thread; off by default): on 512x256x32, with a chunk that divides the 512
+  planes and one that does not.
 * Tiled smoothing phases (default on the grid-wide levels below the finest
   of at most 2^17 cells; CFDGPU_MG_TILE=0 gives the colour launches,
   CFDGPU_MG_TILE_FROM=l tiles every level from l on, l = 0 the finest
@@ -151,3 +154,14 @@ def test_separable_coarse_solve_matches_small_levels(name, precision, periodic):
     for k in ("U0", "V0", "W0"):
         d = np.abs(f1[k] - f0[k]).max() / np.abs(f0[k]).max()
         assert d < 1e-6, (k, d)
+
+
+@pytest.mark.parametrize("march,periodic", [("4", False), ("3", False), ("4", True)])
+def test_marching_colour_pass_bitwise(march, periodic):
+    w = WORKLOADS["c2"]
+    h1, f1 = _run_env(w, {"CFDGPU_MG_MARCH": march}, 2, precision=capi.PREC_MIXED, periodic_z=periodic)
+    h0, f0 = _run_env(w, {"CFDGPU_MG_MARCH": "0"}, 2, precision=capi.PREC_MIXED, periodic_z=periodic)
+    assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
+    assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
+    for k in f1:
+        np.testing.assert_array_equal(f1[k], f0[k], err_msg=k)
