@@ -459,6 +459,8 @@ struct Mg {
     bool cluster = false;  // the coarse levels in one thread-block cluster where they partition;
                            // measured slower than the launches and the small kernel it replaces
     MgTile tile[kMgMaxLevels] = {};  // per grid-wide level: its phases as tiles (tx > 0)
+    MgTile tile_r[kMgMaxLevels] = {};      // ... split phases: the launch that ends with the restriction
+    bool tile_split[kMgMaxLevels] = {};    // ... the phases run one sweep a launch
     // the exact separable solve of the coarsest level (fast diagonalisation,
     // multigrid.cu): fd_level > 0 is that level, solved in place of the small
     // levels below it

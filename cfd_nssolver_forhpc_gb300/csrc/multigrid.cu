@@ -821,9 +821,15 @@ __global__ void __launch_bounds__(kBlock, 3) k_mg_smooth4m(MgLevel L, const floa
 //   buffer (xout = L.xalt), since other blocks still read the halo columns
 //   of this one from L.x; the prolongation into the finer level reads it.
 // One launch replaces the 2 s + 1 launches of the phase, each of which waits
-// for the whole level; the price is the halo recomputation.
+// for the whole level; the price is the halo recomputation.  A phase can also
+// run one sweep a launch (two passes, halo 2, or 3 where the restriction
+// follows), halving the halo's share on larger levels:
+//   ZERO: from x = 0, no transfer;  READ_R: from xin, then the restriction;
+//   READ: from xin (post-smoothing colours).
+enum { kTilePre = 0, kTilePost = 1, kTileZero = 2, kTileReadR = 3, kTileRead = 4 };
 constexpr int kTileThreads = 512;
 constexpr long long kTileCells = 1 << 17;  // levels up to this size run their phases as tiles
+constexpr long long kTileSplitCells = 1 << 20;  // CFDGPU_MG_TILE_SPLIT=1: larger ones up to this, one sweep a launch
 constexpr long long kFdCells = 4096;       // the separable solve takes the first level at most this size
 constexpr size_t kFdSmemMax = 160 * 1024;  // ... whose shared-memory layout fits this
 constexpr int kTileSmemMax = 160 * 1024;  // shared memory of a tile block at most
@@ -835,10 +841,13 @@ __host__ inline size_t tile_smem(const MgTile &T)
     return (2ull * T.wx * T.wy * T.n4 + 5ull * T.n4) * sizeof(float4) + 5ull * (T.wx + T.wy) * sizeof(float);
 }
 
-template <bool PZ, bool PRE>
+template <bool PZ, int MODE>
 __global__ void __launch_bounds__(kTileThreads, 2)
-k_mg_tile(MgLevel L, MgLevel C, MgTile T, float *__restrict__ xout, const int *done)
+k_mg_tile(MgLevel L, MgLevel C, MgTile T, const float *xin, float *__restrict__ xout, const int *done)
 {
+    constexpr bool ZERO_START = MODE == kTilePre || MODE == kTileZero;
+    constexpr bool RESTRICT = MODE == kTilePre || MODE == kTileReadR;
+    constexpr bool PRE = MODE == kTilePre || MODE == kTileZero || MODE == kTileReadR;  // colours 0, 1, ...
     pdl_wait();
     pdl_allow();
     if (*done) return;
@@ -897,8 +906,8 @@ k_mg_tile(MgLevel L, MgLevel C, MgTile T, float *__restrict__ xout, const int *d
         if (i >= 0 && i < L.nx && j >= 0 && j < L.ny) {
             const long long t = ((long long)i * L.ny + j) * L.nz + 4 * kq;
             bv = __ldg(reinterpret_cast<const float4 *>(L.b + t));
-            if (!PRE) {
-                xv = *reinterpret_cast<const float4 *>(L.x + t);
+            if (!ZERO_START) xv = *reinterpret_cast<const float4 *>(xin + t);
+            if (MODE == kTilePost) {
                 const float2 v = __ldg(reinterpret_cast<const float2 *>(
                     C.x + ((long long)(i >> 1) * C.ny + (j >> 1)) * C.nz + 2 * kq));
                 xv.x += v.x;
@@ -913,15 +922,16 @@ k_mg_tile(MgLevel L, MgLevel C, MgTile T, float *__restrict__ xout, const int *d
     __syncthreads();
     const int passes = 2 * T.sweeps;
     for (int p = 0; p < passes; ++p) {
-        // PRE: colours 0, 1, 0, 1 ...; pass p updates the columns at least p
-        // from the tile edge (pass 0, from zero, reads no neighbour), so after
-        // the last pass columns from h - 1 in are exact, as the restriction
-        // of the interior needs.  POST: colours 1, 0, 1, 0 ...; pass p
-        // updates the columns at least p + 1 from the edge.  Every updated
-        // column has its four neighbours inside the tile.
+        // pre-smoothing colours 0, 1, 0, 1 ..., post-smoothing 1, 0, 1, 0 ...
+        // From zero, pass p updates the columns at least p from the tile edge
+        // (pass 0 reads no neighbour), so after 2 s passes columns from
+        // 2 s - 1 = h - 1 in are exact, as the restriction of the interior
+        // needs.  From x, pass p updates the columns at least p + 1 from the
+        // edge (the restriction then needs h = 2 s + 1).  Every updated column
+        // has its four neighbours inside the tile.
         const int color = PRE ? (p & 1) : 1 - (p & 1);
-        const int dmin = PRE ? p : p + 1;
-        const bool zero_pass = PRE && p == 0;
+        const int dmin = ZERO_START ? p : p + 1;
+        const bool zero_pass = ZERO_START && p == 0;
         for (int q = threadIdx.x; q < nq; q += blockDim.x) {
             int a, bb, kq;
             split(q, a, bb, kq);
@@ -942,7 +952,7 @@ k_mg_tile(MgLevel L, MgLevel C, MgTile T, float *__restrict__ xout, const int *d
         }
         __syncthreads();
     }
-    if (PRE) {
+    if (RESTRICT) {
         // k_mg_restrict4 over the interior's coarse cells: one thread per
         // pair of coarse cells along k (the children's quad kq of the four
         // fine columns)
@@ -2303,22 +2313,32 @@ int mg_setup(cfd_ctx *c)
     // stays launches: the CG's rho' is fused into its last colour and the
     // V-cycle's result is its x.  Tiles of 16 x 16 columns where they give a
     // wave of blocks, else 8 x 8; a second x buffer for the post-smoothing.
-    long long tile_cells = kTileCells;
+    long long tile_cells = kTileCells, split_cells = 0;
     int tile_from = kMgMaxLevels, tile_xy = 0;
-    if (const char *e = std::getenv("CFDGPU_MG_TILE")) tile_cells = e[0] != '0' ? tile_cells : 0;
+    if (const char *e = std::getenv("CFDGPU_MG_TILE")) {
+        tile_cells = e[0] != '0' ? tile_cells : 0;
+        split_cells = e[0] != '0' ? split_cells : 0;
+    }
+    if (const char *e = std::getenv("CFDGPU_MG_TILE_SPLIT")) split_cells = e[0] != '0' ? kTileSplitCells : 0;
     if (const char *e = std::getenv("CFDGPU_MG_TILE_FROM")) tile_from = std::max(0, std::atoi(e));
     if (const char *e = std::getenv("CFDGPU_MG_TILE_XY")) tile_xy = std::max(0, std::atoi(e)) & ~1;
     for (int l = 0; l < mg_grid_levels(G); ++l) {
         MgLevel &L = G.lev[l];
-        G.tile[l] = MgTile{};
-        if (l < tile_from && (l == 0 || L.n > tile_cells)) continue;
+        G.tile[l] = G.tile_r[l] = MgTile{};
+        G.tile_split[l] = false;
+        const int sw = level_sweeps(G, l);
+        // one sweep a launch on the levels above tile_cells up to split_cells
+        // (two sweeps a phase; off by default: at 512x256x32 the 524 288-cell
+        // level took 10.82 ms a step so against 10.60 with colour launches)
+        const bool split = l > 0 && l < tile_from && L.n > tile_cells && L.n <= split_cells && sw == 2;
+        if (l < tile_from && (l == 0 || L.n > tile_cells) && !split) continue;
         if (!L.quads || L.om != 1.f || L.sweep_tj > 0 || !transfers4(G, L, G.lev[l + 1])) continue;
-        const int sw = level_sweeps(G, l), h = 2 * sw, n4 = L.nz / 4;
-        auto make = [&](int t) {
+        const int n4 = L.nz / 4;
+        auto make = [&](int t, int sweeps, int h) {
             MgTile T{};
             T.tx = T.ty = t;
             T.h = h;
-            T.sweeps = sw;
+            T.sweeps = sweeps;
             T.wx = t + 2 * h;
             T.wy = t + 2 * h;
             T.n4 = n4;
@@ -2327,16 +2347,23 @@ int mg_setup(cfd_ctx *c)
             T.fwy = FastDiv((unsigned)T.wy);
             return T;
         };
-        auto fits = [&](int t) { return tile_smem(make(t)) <= (size_t)kTileSmemMax; };
+        // a phase in one launch: s sweeps, halo 2 s; split: one sweep, halo 2,
+        // and halo 3 for the launch that ends with the restriction
+        const int ts = split ? 1 : sw, th = split ? 3 : 2 * sw;
+        auto fits = [&](int t) { return tile_smem(make(t, ts, th)) <= (size_t)kTileSmemMax; };
         auto blocks = [&](int t) { return (long long)((L.nx + t - 1) / t) * ((L.ny + t - 1) / t); };
         int t = tile_xy;
         if (t == 0) t = fits(16) && blocks(16) >= sms ? 16 : 8;
         if (t < 2 || !fits(t)) continue;
-        const MgTile T = make(t);
         if (l > 0 && !L.xalt) CKS(dalloc_t(c, &L.xalt, (size_t)L.n));
-        G.tile[l] = T;
+        G.tile[l] = make(t, ts, 2 * ts);
+        if (split) G.tile_r[l] = make(t, 1, 3);
+        G.tile_split[l] = split;
     }
-    for (auto k : {k_mg_tile<false, true>, k_mg_tile<false, false>, k_mg_tile<true, true>, k_mg_tile<true, false>})
+    for (auto k : {k_mg_tile<false, kTilePre>, k_mg_tile<false, kTilePost>, k_mg_tile<false, kTileZero>,
+                   k_mg_tile<false, kTileReadR>, k_mg_tile<false, kTileRead>, k_mg_tile<true, kTilePre>,
+                   k_mg_tile<true, kTilePost>, k_mg_tile<true, kTileZero>, k_mg_tile<true, kTileReadR>,
+                   k_mg_tile<true, kTileRead>})
         CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmemMax));
     CKS(dalloc_t(c, &G.never, 1));
     CK(cudaMemset(G.never, 0, sizeof(int)));
@@ -2589,20 +2616,39 @@ static bool tiled_post(const Mg &G, int l) { return l > 0 && G.tile[l].tx > 0; }
 // into level l - 1 reads)
 static const float *level_out(const Mg &G, int l) { return tiled_post(G, l) ? G.lev[l].xalt : G.lev[l].x; }
 
-// one smoothing phase of level l as tiles (k_mg_tile): PRE with the
-// restriction, or POST with the prolongation
-static void tile_launch(const Mg &G, int l, bool pre, const int *done, cudaStream_t s)
+// one smoothing phase of level l as tiles (k_mg_tile): the pre-smoothing
+// with the restriction, or the post-smoothing with the prolongation; in one
+// launch, or one sweep a launch where the level splits its phases (two
+// sweeps: ZERO to x, READ_R x to xalt; then the prolongation xalt to x and
+// READ x to xalt, so the level ends in xalt either way)
+template <bool PZ>
+static void tile_launch_t(const Mg &G, int l, bool pre, const int *done, cudaStream_t s)
 {
     const MgLevel &L = G.lev[l];
-    const MgTile &T = G.tile[l];
     MgLevel C = G.lev[l + 1];
     if (!pre) C.x = const_cast<float *>(level_out(G, l + 1));
-    float *xout = pre ? L.x : L.xalt;
-    const dim3 grid((unsigned)((L.nx + T.tx - 1) / T.tx * T.tiles_y));
-    const size_t sm = tile_smem(T);
-    auto k = L.pz ? (pre ? k_mg_tile<true, true> : k_mg_tile<true, false>)
-                  : (pre ? k_mg_tile<false, true> : k_mg_tile<false, false>);
-    launch_pdl(k, grid, dim3(kTileThreads), sm, s, L, C, T, xout, done);
+    auto go = [&](auto k, const MgTile &T, const float *xin, float *xout) {
+        const dim3 grid((unsigned)((L.nx + T.tx - 1) / T.tx * T.tiles_y));
+        launch_pdl(k, grid, dim3(kTileThreads), tile_smem(T), s, L, C, T, xin, xout, done);
+    };
+    if (!G.tile_split[l]) {
+        if (pre) go(k_mg_tile<PZ, kTilePre>, G.tile[l], (const float *)L.x, L.x);
+        else go(k_mg_tile<PZ, kTilePost>, G.tile[l], (const float *)L.x, L.xalt);
+        return;
+    }
+    if (pre) {
+        go(k_mg_tile<PZ, kTileZero>, G.tile[l], (const float *)L.x, L.x);
+        go(k_mg_tile<PZ, kTileReadR>, G.tile_r[l], (const float *)L.x, L.xalt);
+    } else {
+        go(k_mg_tile<PZ, kTilePost>, G.tile[l], (const float *)L.xalt, L.x);
+        go(k_mg_tile<PZ, kTileRead>, G.tile[l], (const float *)L.x, L.xalt);
+    }
+}
+
+static void tile_launch(const Mg &G, int l, bool pre, const int *done, cudaStream_t s)
+{
+    if (G.lev[l].pz) tile_launch_t<true>(G, l, pre, done, s);
+    else tile_launch_t<false>(G, l, pre, done, s);
 }
 
 // z = V(h): one V-cycle; every kernel returns at once when *done.  With
@@ -2683,13 +2729,13 @@ long long mg_vcycle_launches(const Mg &G)
         // pre-smoothing and restriction: one tile launch; or 2s - 1 colour
         // launches (the first sweep in one) and the restriction; or s fused
         // sweeps or 2s colours and the restriction
-        if (G.tile[l].tx > 0) n += 1;
+        if (G.tile[l].tx > 0) n += G.tile_split[l] ? 2 : 1;
         else if (fused_ends(G, l)) n += 2 * sw;
         else n += per_sweep * sw + 1;
         // prolongation and post-smoothing: one tile launch; or the
         // prolongation with the first colour and 2s - 1 colours; or the
         // prolongation and the sweeps
-        if (tiled_post(G, l)) n += 1;
+        if (tiled_post(G, l)) n += G.tile_split[l] ? 2 : 1;
         else if (fused_ends(G, l)) n += 2 * sw;
         else n += 1 + per_sweep * sw;
     }

@@ -22,7 +22,8 @@
   thread; off by default): on 512x256x32, with a chunk that divides the 512
   planes and one that does not.
 * Tiled smoothing phases (default on the grid-wide levels below the finest
-  of at most 2^17 cells; CFDGPU_MG_TILE=0 gives the colour launches,
+  of at most 2^17 cells; CFDGPU_MG_TILE_SPLIT=1 adds those up to 2^20 cells
+  one sweep a launch; CFDGPU_MG_TILE=0 gives the colour launches,
   CFDGPU_MG_TILE_FROM=l tiles every level from l on, l = 0 the finest
   level's pre-smoothing too): one launch per phase over tiles with a
   recomputed halo.  The 512x256x32 grid runs with both of its levels below
@@ -128,11 +129,17 @@ def test_cluster_coarse_levels_match_single_block(name, precision, periodic):
 
 @pytest.mark.parametrize("name,precision,periodic,tile_from",
                          [("c2", capi.PREC_MIXED, False, "1"), ("c2", capi.PREC_MIXED, True, "1"),
+                          ("c2", capi.PREC_MIXED, False, None), ("c2", capi.PREC_MIXED, True, None),
+                          ("c2", capi.PREC_MIXED, False, "split"), ("c2", capi.PREC_MIXED, True, "split"),
                           ("c1", capi.PREC_MIXED, False, "0"), ("c1", capi.PREC_FP64_DC, True, "0")])
 def test_tiled_phases_bitwise(name, precision, periodic, tile_from):
+    """tile_from None: the default (the levels of at most 2^17 cells);
+    "split": also the 524 288-cell level of 512x256x32, one sweep a launch."""
     w = WORKLOADS[name]
     steps = 2 if name == "c2" else 3
-    h1, f1 = _run_env(w, {"CFDGPU_MG_TILE_FROM": tile_from}, steps, precision=precision, periodic_z=periodic)
+    env = ({"CFDGPU_MG_TILE": "1"} if tile_from is None else {"CFDGPU_MG_TILE_SPLIT": "1"} if tile_from == "split"
+           else {"CFDGPU_MG_TILE_FROM": tile_from})
+    h1, f1 = _run_env(w, env, steps, precision=precision, periodic_z=periodic)
     h0, f0 = _run_env(w, {"CFDGPU_MG_TILE": "0"}, steps, precision=precision, periodic_z=periodic)
     assert [h["cd"] for h in h1] == [h["cd"] for h in h0]
     assert [h["iters"] for h in h1] == [h["iters"] for h in h0]
