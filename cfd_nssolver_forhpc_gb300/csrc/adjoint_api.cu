@@ -269,6 +269,7 @@ int ck_load(cfd_ctx *c, int slot)
     AdjState &A = *c->adj;
     Checkpoint &k = A.ck[slot];
     if (!k.valid) return fail(CFD_ERR_STATE, "checkpoint slot was never saved");
+    for (int &q : c->warm_n) q = 0;  // a checkpoint holds no warm-start history
     const Geo &g = c->g;
     const size_t fb = (size_t)g.ng * (c->fp32 ? sizeof(float) : sizeof(double));
     for (int sl = 0; sl < 2; ++sl)

@@ -661,6 +661,51 @@ int sor_solve_t(cfd_ctx *c, int si, int *iters, double *err)
     return CFD_OK;
 }
 
+// Warm start of pass k's Poisson solve (mixed and FP64-defect-correction
+// contexts): the reference starts every solve from the previous one's
+// solution (the previous pass's), which at 512x256x32 leaves an initial
+// relative residual of 0.3 to 50; pass k's own solutions of the last two
+// steps, extrapolated linearly in time, start it far closer, so the
+// defect correction needs fewer sweeps.  The converged solution is the same
+// to the solver tolerance.  CFDGPU_WARM=prev keeps the reference's start.
+static bool warm_applies(const cfd_ctx *c)
+{
+    return c->warm_extrap && c->cfg.solver != CFD_SOLVER_SOR_RB &&
+           (c->cfg.precision == CFD_PREC_MIXED || c->cfg.precision == CFD_PREC_FP64_DC);
+}
+
+static int warm_start(cfd_ctx *c, int k)
+{
+    if (!warm_applies(c) || k < 0 || k >= 4) return CFD_OK;
+    const long long n = c->g.n;
+    if (!c->warm_hist[k][0]) {
+        for (int q = 0; q < 2; ++q)
+            if (dalloc_t(c, &c->warm_hist[k][q], (size_t)n) != CFD_OK) {
+                c->warm_extrap = false;  // no room: the reference's start
+                cudaGetLastError();
+                return CFD_OK;
+            }
+        c->warm_n[k] = 0;
+    }
+    if (c->warm_n[k] >= 2) {
+        launch_extrapolate(c->lc, n, c->x, c->warm_hist[k][0], c->warm_hist[k][1]);
+        c->launches += 1;
+        CK(cudaGetLastError());
+    } else if (c->warm_n[k] == 1) {
+        CK(cudaMemcpyAsync(c->x, c->warm_hist[k][1], (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+    }
+    return CFD_OK;
+}
+
+static int warm_store(cfd_ctx *c, int k)
+{
+    if (!warm_applies(c) || k < 0 || k >= 4 || !c->warm_hist[k][0]) return CFD_OK;
+    std::swap(c->warm_hist[k][0], c->warm_hist[k][1]);
+    CK(cudaMemcpyAsync(c->warm_hist[k][1], c->x, (size_t)c->g.n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+    c->warm_n[k] = std::min(2, c->warm_n[k] + 1);
+    return CFD_OK;
+}
+
 // rhs_done: the pass kernel already formed b (and its compatibility projection)
 template <class T>
 int pressure_step(cfd_ctx *c, int si, int *iters, double *relres, int *outer, bool rhs_done = false)
@@ -748,9 +793,11 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
         }
         CK(cudaGetLastError());
         if (c->loop > 1) {
+            if (!rec) CKS(warm_start(c, pass));
             int s2 = pressure_step<T>(c, 1, &loc.iters[pass], &loc.relres[pass], &loc.outer[pass], rhs_done);
             if (s2 != CFD_OK && s2 != CFD_ERR_NOCONV) return s2;
             if (s2 != CFD_OK) st = s2;
+            if (!rec && s2 == CFD_OK) CKS(warm_store(c, pass));
         }
         if (g.pz) {  // the top w face's pressure gradient reads p above it
             launch_sync_z<double>(c->s, g, c->p, nullptr, nullptr);
@@ -1052,6 +1099,7 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (const char *e = std::getenv("CFDGPU_NO_FUSED")) c->fused = !(e[0] == '1');
     if (const char *e = std::getenv("CFDGPU_INNER_ADAPT")) c->inner_adapt = std::max(0.0, std::atof(e));
     if (const char *e = std::getenv("CFDGPU_OUTER_LOOP")) c->outer_graph = std::strcmp(e, "host") != 0;
+    if (const char *e = std::getenv("CFDGPU_WARM")) c->warm_extrap = std::strcmp(e, "prev") != 0;
 
     int st = CFD_OK;
     auto bail = [&](int code) { free_ctx(c); return code; };
@@ -1362,6 +1410,7 @@ int cfd_start(cfd_ctx *c)
     CKS(cfd_bc_main(c, CFD_SLOT_T0));
     CKS(cfd_bc_copy(c, CFD_SLOT_T0, CFD_SLOT_T1));
     c->loop = 1;
+    for (int &k : c->warm_n) k = 0;  // the warm-start history starts over
     c->time = 0.0;
     for (int q = 0; q < 3; ++q) {
         c->run_umax[q] = -1e10;
@@ -1728,6 +1777,7 @@ int cfd_set_clock(cfd_ctx *c, long long loop, double time)
     if (loop < 1 || !std::isfinite(time)) return fail(CFD_ERR_ARG, "loop must be >= 1 and time finite");
     c->loop = loop;
     c->time = time;
+    for (int &k : c->warm_n) k = 0;  // a restored state: no history
     return CFD_OK;
 }
 
