@@ -678,8 +678,9 @@ static int warm_start(cfd_ctx *c, int k)
 {
     if (!warm_applies(c) || k < 0 || k >= 4) return CFD_OK;
     const long long n = c->g.n;
+    const int keep = c->warm_order + 1;  // solutions the extrapolation reads
     if (!c->warm_hist[k][0]) {
-        for (int q = 0; q < 2; ++q)
+        for (int q = 0; q < keep; ++q)
             if (dalloc_t(c, &c->warm_hist[k][q], (size_t)n) != CFD_OK) {
                 c->warm_extrap = false;  // no room: the reference's start
                 cudaGetLastError();
@@ -687,12 +688,17 @@ static int warm_start(cfd_ctx *c, int k)
             }
         c->warm_n[k] = 0;
     }
-    if (c->warm_n[k] >= 2) {
-        launch_extrapolate(c->lc, n, c->x, c->warm_hist[k][0], c->warm_hist[k][1]);
+    double *const *h = c->warm_hist[k];  // the newest is h[keep - 1]
+    if (c->warm_n[k] >= 3 && keep == 3) {
+        launch_extrapolate(c->lc, n, c->x, h[0], h[1], h[2]);
+        c->launches += 1;
+        CK(cudaGetLastError());
+    } else if (c->warm_n[k] >= 2) {
+        launch_extrapolate(c->lc, n, c->x, h[keep - 2], h[keep - 1]);
         c->launches += 1;
         CK(cudaGetLastError());
     } else if (c->warm_n[k] == 1) {
-        CK(cudaMemcpyAsync(c->x, c->warm_hist[k][1], (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+        CK(cudaMemcpyAsync(c->x, h[keep - 1], (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
     }
     return CFD_OK;
 }
@@ -700,9 +706,13 @@ static int warm_start(cfd_ctx *c, int k)
 static int warm_store(cfd_ctx *c, int k)
 {
     if (!warm_applies(c) || k < 0 || k >= 4 || !c->warm_hist[k][0]) return CFD_OK;
-    std::swap(c->warm_hist[k][0], c->warm_hist[k][1]);
-    CK(cudaMemcpyAsync(c->warm_hist[k][1], c->x, (size_t)c->g.n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
-    c->warm_n[k] = std::min(2, c->warm_n[k] + 1);
+    const int keep = c->warm_order + 1;
+    double **h = c->warm_hist[k];
+    double *oldest = h[0];
+    for (int q = 0; q + 1 < keep; ++q) h[q] = h[q + 1];
+    h[keep - 1] = oldest;
+    CK(cudaMemcpyAsync(h[keep - 1], c->x, (size_t)c->g.n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+    c->warm_n[k] = std::min(keep, c->warm_n[k] + 1);
     return CFD_OK;
 }
 
@@ -1099,7 +1109,10 @@ int cfd_create(const cfd_config *cfg, cfd_ctx **out)
     if (const char *e = std::getenv("CFDGPU_NO_FUSED")) c->fused = !(e[0] == '1');
     if (const char *e = std::getenv("CFDGPU_INNER_ADAPT")) c->inner_adapt = std::max(0.0, std::atof(e));
     if (const char *e = std::getenv("CFDGPU_OUTER_LOOP")) c->outer_graph = std::strcmp(e, "host") != 0;
-    if (const char *e = std::getenv("CFDGPU_WARM")) c->warm_extrap = std::strcmp(e, "prev") != 0;
+    if (const char *e = std::getenv("CFDGPU_WARM")) {
+        c->warm_extrap = std::strcmp(e, "prev") != 0;
+        if (std::strcmp(e, "quadratic") == 0) c->warm_order = 2;
+    }
 
     int st = CFD_OK;
     auto bail = [&](int code) { free_ctx(c); return code; };

@@ -124,9 +124,10 @@ struct cfd_ctx {
     // warm start of the defect-correction solves of a step: per pass the
     // solutions of that pass in the last two steps (warm_n of them), from
     // which the next one starts by linear extrapolation in time
-    double *warm_hist[4][2] = {};
+    double *warm_hist[4][3] = {};  // oldest first
     int warm_n[4] = {};
     bool warm_extrap = true;
+    int warm_order = 1;  // 1: linear extrapolation (two steps), 2: quadratic (three)
     // [0] FP64 BiCGSTAB, [1] FP32 inner BiCGSTAB, [2] fused FP32 BiCGSTAB, [3] FP32 CG
     // [4] multigrid-preconditioned CG, [5] red-black SOR, [6] the mixed defect
     // correction around the multigrid CG (outer loop and inner solves) for the

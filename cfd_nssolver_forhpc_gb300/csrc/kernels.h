@@ -213,8 +213,10 @@ void launch_outer_inner_done(cudaStream_t s, OuterScal *os, const BicgScal *sc_i
 // sweep's inner tolerance and the WHILE condition
 void launch_outer_next(cudaStream_t s, cudaGraphConditionalHandle h, OuterScal *os, const double *norm2,
                        BicgScal *sc_in, OuterCfg cfg);
-// x = 2 h1 - h0: the linear extrapolation in time of a pass's solution
-void launch_extrapolate(cfd_launch_ctx &c, long long n, double *x, const double *h0, const double *h1);
+// x = 2 h1 - h0 (h2 null: linear) or 3 h2 - 3 h1 + h0 (quadratic): the
+// extrapolation in time of a pass's solution
+void launch_extrapolate(cfd_launch_ctx &c, long long n, double *x, const double *h0, const double *h1,
+                        const double *h2 = nullptr);
 // x += scale e unless the defect correction has stopped (os->state)
 void launch_correct_gated(cfd_launch_ctx &c, long long n, double *x, const float *e, const double *scale,
                           const OuterScal *os);

@@ -1877,16 +1877,17 @@ void launch_correct(cfd_launch_ctx &c, long long n, double *x, const V *e, const
 template void launch_correct<float>(cfd_launch_ctx &, long long, double *, const float *, const double *);
 
 __global__ void k_extrapolate(long long n, double *__restrict__ x, const double *__restrict__ h0,
-                              const double *__restrict__ h1)
+                              const double *__restrict__ h1, const double *__restrict__ h2)
 {
     for (long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x; row < n;
          row += (long long)gridDim.x * blockDim.x)
-        x[row] = 2.0 * h1[row] - h0[row];
+        x[row] = h2 ? 3.0 * (h2[row] - h1[row]) + h0[row] : 2.0 * h1[row] - h0[row];
 }
 
-void launch_extrapolate(cfd_launch_ctx &c, long long n, double *x, const double *h0, const double *h1)
+void launch_extrapolate(cfd_launch_ctx &c, long long n, double *x, const double *h0, const double *h1,
+                        const double *h2)
 {
-    k_extrapolate<<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, h0, h1);
+    k_extrapolate<<<blocks_for(n, c.grid_cap), kBlock, 0, c.s>>>(n, x, h0, h1, h2);
 }
 
 __global__ void k_correct_gated(long long n, double *__restrict__ x, const float *__restrict__ e, const double *scale,
