@@ -99,7 +99,7 @@ def parse():
     ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="precision of the headline step (the other one is timed beside it)")
-    ap.add_argument("--spinup", type=int, default=40,
+    ap.add_argument("--spinup", type=int, default=60,
                     help="untimed steps from the seeded start before the warm-up (past the impulsive-start "
                          "transient; the comparison legs start from the state they reach)")
     ap.add_argument("--inner-tol", type=float, default=1e-3,

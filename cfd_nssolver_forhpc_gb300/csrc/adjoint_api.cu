@@ -38,6 +38,10 @@ struct AdjState {
     double *ax = nullptr, *ab = nullptr, *aw = nullptr, *bp = nullptr, *zero = nullptr, *pint = nullptr;
     double *af = nullptr, *asrc = nullptr, *aeta = nullptr, *ainflow = nullptr;
     double *red = nullptr;
+    // warm start of the adjoint Poisson solve of pass k: its solutions of the
+    // two steps after this one (the reverse sweep's previous two), extrapolated
+    double *awh[4][2] = {};
+    int awn[4] = {};
     // replay of one step (forward velocity type)
     void *snap[4][3] = {};
     void *rT3[3] = {};
@@ -103,6 +107,7 @@ int zero_adjoint(cfd_ctx *c)
     for (int f = CFD_ADJ_U0; f <= CFD_ADJ_INFLOW; ++f)
         CK(cudaMemsetAsync(adj_ptr(c, f), 0, adj_count(c, f) * sizeof(double), c->s));
     CK(cudaMemsetAsync(A.aw, 0, (size_t)c->g.n * sizeof(double), c->s));
+    for (int &k : A.awn) k = 0;
     A.solve_iters = 0;
     return CFD_OK;
 }
@@ -124,18 +129,39 @@ int alloc_tape(cfd_ctx *c, int len)
     return CFD_OK;
 }
 
-// adjoint Poisson solve: ab = A^-T ax on the range of the operator
-int adj_solve(cfd_ctx *c, int *iters, double *relres)
+// adjoint Poisson solve: ab = A^-T ax on the range of the operator.  pass >= 0:
+// the solve of that pass in the reverse sweep, started from the same pass's
+// solutions of the two steps after this one extrapolated (the forward's warm
+// start run backwards in time; CFDGPU_WARM=prev: the previous solve's)
+int adj_solve(cfd_ctx *c, int *iters, double *relres, int pass = -1)
 {
     AdjState &A = *c->adj;
     const Metrics<double> m = metrics_of<double>(c);
+    const long long n = c->g.n;
     launch_adj_solve_in(c->lc, c->g, m, c->jp, A.ax, A.red, A.bp);
     c->launches += 2;
     CK(cudaGetLastError());
+    const bool warm = pass >= 0 && pass < 4 && c->warm_extrap;
+    if (warm && !A.awh[pass][0]) {
+        for (int q = 0; q < 2; ++q) CKS(dalloc_t(c, &A.awh[pass][q], (size_t)n));
+        A.awn[pass] = 0;
+    }
+    if (warm && A.awn[pass] >= 2) {
+        launch_extrapolate(c->lc, n, A.aw, A.awh[pass][0], A.awh[pass][1]);
+        c->launches += 1;
+        CK(cudaGetLastError());
+    } else if (warm && A.awn[pass] == 1) {
+        CK(cudaMemcpyAsync(A.aw, A.awh[pass][1], (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+    }
     int it = 0, outer = 0;
     double rr = 0.0;
     const int st = linear_solve_cg(c, A.bp, A.aw, A.zero, &it, &rr, &outer);
     if (st != CFD_OK && st != CFD_ERR_NOCONV) return st;
+    if (warm && st == CFD_OK) {
+        std::swap(A.awh[pass][0], A.awh[pass][1]);
+        CK(cudaMemcpyAsync(A.awh[pass][1], A.aw, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, c->s));
+        A.awn[pass] = std::min(2, A.awn[pass] + 1);
+    }
     launch_adj_solve_out(c->lc, c->g, m, c->jp, A.aw, A.red, A.ab);
     c->launches += 2;
     CK(cudaGetLastError());
@@ -216,7 +242,7 @@ int adj_step_t(cfd_ctx *c, int pos, double wcd, double wcl, cfd_adj_step_info *i
         if (k == npass - 1)
             for (int q = 0; q < 3; ++q) CK(cudaMemsetAsync(A.a0[q], 0, (size_t)g.ng * sizeof(double), s));
         if (A.tape_loop[pos] > 1) {  // the pressure was solved in this step (pLoopIni)
-            const int s2 = adj_solve(c, &loc.iters[k], &loc.relres[k]);
+            const int s2 = adj_solve(c, &loc.iters[k], &loc.relres[k], k);
             if (s2 != CFD_OK && s2 != CFD_ERR_NOCONV) return s2;
             if (s2 != CFD_OK) st = s2;
             launch_adj_rhs(c->lc, g, m, 1.0 / dt, c->jp, A.ab, c->cfg.compat_rhs != 0, A.red, A.a1[0], A.a1[1],

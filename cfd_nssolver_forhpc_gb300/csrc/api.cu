@@ -803,11 +803,11 @@ int step_t(cfd_ctx *c, cfd_step_info *info, const StepRecord *rec)
         }
         CK(cudaGetLastError());
         if (c->loop > 1) {
-            if (!rec) CKS(warm_start(c, pass));
+            CKS(warm_start(c, pass));
             int s2 = pressure_step<T>(c, 1, &loc.iters[pass], &loc.relres[pass], &loc.outer[pass], rhs_done);
             if (s2 != CFD_OK && s2 != CFD_ERR_NOCONV) return s2;
             if (s2 != CFD_OK) st = s2;
-            if (!rec && s2 == CFD_OK) CKS(warm_store(c, pass));
+            if (s2 == CFD_OK) CKS(warm_store(c, pass));
         }
         if (g.pz) {  // the top w face's pressure gradient reads p above it
             launch_sync_z<double>(c->s, g, c->p, nullptr, nullptr);
