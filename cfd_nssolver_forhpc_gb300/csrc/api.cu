@@ -504,7 +504,7 @@ int solve_mixed(cfd_ctx *c, const Op64 &A64, const Op32 &A32, const double *b, d
         if (inner == CFD_INNER_MG && c->mg.usable && c->use_graphs && c->device_loops && c->outer_graph &&
             !c->debug) {
             const int st = solve_mixed_graph(c, A64, b, x, iters, relres, outer, zero_x_if_zero_rhs);
-            // a graph the driver cannot build (nested conditional nodes):
+            // where the CUDA runtime cannot build the graph (nested conditional nodes):
             // the host loop from here on
             if (st != CFD_ERR_CUDA || c->graph[(b == c->b && x == c->x) ? 6 : 7]) return st;
             c->outer_graph = false;
