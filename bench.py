@@ -99,9 +99,10 @@ def parse():
     ap.add_argument("--solver", default="spe", choices=["spe", "ell", "sor"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="precision of the headline step (the other one is timed beside it)")
-    ap.add_argument("--spinup", type=int, default=60,
+    ap.add_argument("--spinup", type=int, default=None,
                     help="untimed steps from the seeded start before the warm-up (past the impulsive-start "
-                         "transient; the comparison legs start from the state they reach)")
+                         "transient; the comparison legs start from the state they reach); default 60 for "
+                         "the mixed step, 0 for the FP64 one (seconds a step)")
     ap.add_argument("--inner-tol", type=float, default=1e-3,
                     help="relative tolerance of each FP32 inner solve of the mixed defect correction")
     ap.add_argument("--no-e2e", action="store_true")
@@ -727,6 +728,8 @@ def main():
     build()
     import torch
     torch.cuda.init()
+    if args.spinup is None:
+        args.spinup = 60 if args.precision == "mixed" else 0
     S = build_sim(args, w, args.precision)
     # spin-up: the first ~20 steps from the impulsive start are a transient
     # in which every Poisson solve starts far from its solution; the timed
