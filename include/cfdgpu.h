@@ -193,7 +193,8 @@ int cfd_start(cfd_ctx *ctx);
 /* simuClass::loop and simuClass::time (simuClass.hpp:92-94): the step
    counter (the first step, loop 1, solves no Poisson equation) and the time.
    Setting them restarts a run from fields uploaded from elsewhere (another
-   context, another precision, a Plot3D file). */
+   context, another precision, a Plot3D file), and drops the history the
+   mixed path's warm start extrapolates from (cfd_step). */
 int cfd_set_clock(cfd_ctx *ctx, long long loop, double time);
 int cfd_get_clock(cfd_ctx *ctx, long long *loop, double *time);
 
@@ -242,7 +243,11 @@ int cfd_sync_periodic_z(cfd_ctx *ctx, int slot);
    exact area fraction (nsub == 0, an extension) */
 int cfd_eta_cylinder_z(cfd_ctx *ctx, double cx, double cy, double radius, int nsub);
 /* One iteration of the main loop of the configured driver
-   (RUN_CPU_PC_METHOD.hpp:287-627 or RUN_CPU.hpp:290-462, without IO). */
+   (RUN_CPU_PC_METHOD.hpp:287-627 or RUN_CPU.hpp:290-462, without IO).  The
+   FP64 path starts each Poisson solve from the previous solve's solution, as
+   the reference does; the mixed and FP64-defect-correction paths start pass
+   k from its own solutions of the two previous steps, extrapolated linearly
+   in time (environment CFDGPU_WARM=prev: the reference's start). */
 int cfd_step(cfd_ctx *ctx, cfd_step_info *info);
 /* max |div T[slot]| over interior cells, FP64 */
 int cfd_div_inf(cfd_ctx *ctx, int slot, double *out);
