@@ -99,3 +99,16 @@ def test_build_is_sm103a_only():
     from cfd_nssolver_forhpc_gb300.build import ARCH, _flags
     assert ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
     assert "-lineinfo" in _flags()
+
+
+def test_kernel_timing_names_follow_the_header_enum():
+    """capi.KERNELS names the slots of cfd_time_kernels in the order of the
+    CFD_KERNEL_* enum of include/cfdgpu.h."""
+    import re
+    from pathlib import Path
+
+    from cfd_nssolver_forhpc_gb300 import capi
+    hdr = (Path(__file__).resolve().parent.parent / "include" / "cfdgpu.h").read_text()
+    body = hdr[hdr.index("CFD_KERNEL_BICG_AP"):hdr.index("CFD_KERNEL_COUNT")]
+    names = re.findall(r"CFD_KERNEL_([A-Z0-9_]+)", body)
+    assert [n.lower() for n in names] == capi.KERNELS
